@@ -1,0 +1,149 @@
+/*
+ * qpso.h -- C ABI of the GB300-native Q-PSO pose solver.
+ *
+ * The reference (morpheus1820/Q-PSO) is one executable with no library API;
+ * its in-process boundary is the set of kernels and buffers that main()
+ * drives (main.cu:1301-1780).  Each entry point below names the reference
+ * code it replaces.  Conventions: plain C types only; the caller owns host
+ * memory, which is copied during the call; the library owns device objects
+ * behind integer ids; every function returns a qpso_status; no exception
+ * crosses the boundary; a context is not thread-safe except the
+ * qpso_server_* calls, which lock internally.
+ */
+#ifndef QPSO_H
+#define QPSO_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qpso_context qpso_context;
+typedef int32_t qpso_status;
+
+#define QPSO_OK 0
+#define QPSO_ERR_ARG 1        /* invalid argument */
+#define QPSO_ERR_NOMEM 2      /* device or host allocation failed */
+#define QPSO_ERR_CUDA 3       /* a CUDA call failed; see qpso_last_error */
+#define QPSO_ERR_TIMEOUT 4    /* a bounded device-side wait expired */
+#define QPSO_ERR_BUSY 5       /* admission refused: not enough free memory / slots */
+#define QPSO_ERR_NOT_FOUND 6  /* unknown mesh, frame or request id */
+#define QPSO_ERR_INTERNAL 7   /* a device-side consistency check failed */
+
+/* Pinhole camera.  The reference hard-codes the ACCV intrinsics as double
+ * macros FX/FY/CX/CY and a 640x480 frame (main.h:30-33, 128-129). */
+typedef struct {
+    float fx, fy, cx, cy;
+    int32_t width, height;
+} qpso_camera;
+
+/* One pose solve: QPSOParams_t (main.h:182-204) plus the compile-time
+ * constants of main.h:83-136 as run-time fields.  Defaults from
+ * qpso_solve_desc_init equal the reference's values. */
+typedef struct {
+    uint32_t mesh_id;
+    uint32_t frame_id;
+    int32_t cluster_label;     /* frame label selecting the cluster; -1: depth already masked */
+    int32_t cl_min_x, cl_max_x, cl_min_y, cl_max_y; /* cluster AABB, max exclusive (cv::Rect tl/br) */
+    uint32_t num_points;       /* num_point_SegmentedCluster */
+    float t_lo[3], t_hi[3];    /* translation box x_lo/x_hi (main.cu:1318-1323), metres */
+    uint32_t num_particles;    /* Nparticle_ (main.h:84) */
+    uint32_t iterations;       /* max_steps_ (main.h:99) */
+    float c1, c2;              /* c1_, c2_ */
+    double w;                  /* psoW_ */
+    float vdot;                /* vdot_ */
+    float ang_lo, ang_hi;      /* aminX_ .. amaxZ_ */
+    float qinit[4];            /* InitQPSO qinit (main.cu:128-132) */
+    uint64_t seed;             /* Philox key (replaces the GSL mt19937 table) */
+    uint32_t stream;           /* Philox stream id of this solve */
+} qpso_solve_desc;
+
+typedef struct {
+    float fit;                 /* d_solution_best_fit */
+    float pose[7];             /* d_solution_best_pose: tx,ty,tz (m), q0..q3 */
+    uint32_t flags;            /* device error bits (0 = clean) */
+    uint32_t reserved;
+    uint64_t raster_writes;    /* pixel writes issued by the rasteriser */
+    uint64_t tile_passes;      /* shared-memory tile passes (1 per particle-render when it fits) */
+} qpso_result;
+
+typedef struct {
+    int32_t threads;           /* CTA size, multiple of 32, <= 1024 */
+    int32_t tile_px;           /* int32 depth-tile capacity in pixels, multiple of 8 */
+    int32_t ppb;               /* particles per work item, 1..16 */
+} qpso_launch_config;
+
+const char *qpso_version(void);
+
+/* Context on one GPU (replaces the set-up of main.cu:1301-1574). */
+qpso_status qpso_create(int device, qpso_context **out);
+void qpso_destroy(qpso_context *ctx);
+const char *qpso_last_error(const qpso_context *ctx);
+
+/* Mesh in the loadOBJ3 layout (main.h:620-679): 9*num_faces floats,
+ * [x(v0)|x(v1)|x(v2)|y(v0)|y(v1)|y(v2)|z(v0)|z(v1)|z(v2)], metres.
+ * Replaces loadOBJ3 + cudaMemcpy of d_obj_model (main.cu:1366-1373). */
+qpso_status qpso_mesh_upload(qpso_context *ctx, const float *soa_xyz, uint32_t num_faces,
+                             uint32_t *mesh_id);
+qpso_status qpso_mesh_release(qpso_context *ctx, uint32_t mesh_id);
+
+/* Depth frame (uint16 mm, row-major width*height) with an optional int32
+ * label map (cluster ids).  Replaces the d_depth_kinect upload of the
+ * cluster-masked depth (main.cu:1548-1557). */
+qpso_status qpso_frame_upload(qpso_context *ctx, const uint16_t *depth_mm, const int32_t *labels,
+                              const qpso_camera *cam, uint32_t *frame_id);
+qpso_status qpso_frame_release(qpso_context *ctx, uint32_t frame_id);
+
+/* Reference defaults (main.h:83-136, main.cu:128-132). */
+void qpso_solve_desc_init(qpso_solve_desc *desc);
+/* Translation box from a cluster centroid in mm (main.cu:1285-1323):
+ * c = centroid*0.001f; lo = c - bound; hi = c + bound (bound_z for z). */
+void qpso_box_from_centroid(const float centroid_mm[3], float bound, float bound_z,
+                            float t_lo[3], float t_hi[3]);
+
+qpso_status qpso_set_launch_config(qpso_context *ctx, const qpso_launch_config *plain,
+                                   const qpso_launch_config *batch);
+qpso_status qpso_get_launch_config(const qpso_context *ctx, qpso_launch_config *plain,
+                                   qpso_launch_config *batch);
+
+/* Plain solve: one fused launch per PSO iteration.  Replaces the host loop
+ * main.cu:1601-1727 (InitQPSO, then per iteration 1024 render launches,
+ * the AABB kernel, 1024 fitness launches, thrust::min_element,
+ * UpdatePersonalAndGlobalBest, UpdateParticlesEquationKernel). */
+qpso_status qpso_solve(qpso_context *ctx, const qpso_solve_desc *desc, qpso_result *result);
+
+/* Plain solve that also returns the gbest trace (iterations x 8 floats:
+ * fit, pose) and the final SoA state [7][P] (each pointer may be NULL). */
+qpso_status qpso_solve_traced(qpso_context *ctx, const qpso_solve_desc *desc, qpso_result *result,
+                              float *trace, float *pos, float *vel, float *pbest, float *pbest_fit);
+
+/* Batched solve: every iteration of all n solves in one persistent
+ * cooperative launch (replayed from a CUDA graph when the shape repeats). */
+qpso_status qpso_solve_batch(qpso_context *ctx, const qpso_solve_desc *descs, uint32_t n,
+                             qpso_result *results);
+
+/* Score explicit poses (n x 7 floats) for the cluster/mesh of desc without
+ * touching PSO state: RenderFixedPointKernelAABB +
+ * ComputeAABBFinalReductionKernel + ComputeFitnessKernel (main.cu:305-764)
+ * for arbitrary poses. */
+qpso_status qpso_score_poses(qpso_context *ctx, const qpso_solve_desc *desc, const float *poses,
+                             uint32_t n, float *fit_out);
+
+/* Render one pose of a mesh into a window [x0,x0+w) x [y0,y0+h) of the
+ * raster domain (int32 mm, 60000 where nothing was drawn) and return the
+ * render AABB {minx,maxx,miny,maxy}.  GPU counterpart of RenderCPU
+ * (main.h:2012-2043) for the best-pose render-out. */
+qpso_status qpso_render(qpso_context *ctx, uint32_t mesh_id, const qpso_camera *cam,
+                        const float pose[7], int32_t x0, int32_t y0, int32_t w, int32_t h,
+                        int32_t *depth_out, int32_t box_out[4]);
+
+/* Checks the bounded device wait: a barrier that expects one more CTA
+ * than arrives must expire after timeout_ns and report QPSO_ERR_TIMEOUT.
+ * No counterpart in the reference (which has no device waits). */
+qpso_status qpso_barrier_selftest(qpso_context *ctx, uint64_t timeout_ns, uint32_t *err_bits);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QPSO_H */

@@ -1,0 +1,213 @@
+"""ctypes view of the oracle and of the reference pin library.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline arm, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+NDIM = 7
+DEPTH_BG = 60000
+GUARD = 1024
+
+_f = C.POINTER(C.c_float)
+_i32 = C.POINTER(C.c_int32)
+_u16 = C.POINTER(C.c_uint16)
+
+
+class Camera(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class Params(C.Structure):
+    _fields_ = [("c1", C.c_float), ("c2", C.c_float), ("w", C.c_double), ("vdot", C.c_float),
+                ("ang_lo", C.c_float), ("ang_hi", C.c_float), ("qinit", C.c_float * 4),
+                ("t_lo", C.c_float * 3), ("t_hi", C.c_float * 3),
+                ("cl_min_x", C.c_int32), ("cl_max_x", C.c_int32),
+                ("cl_min_y", C.c_int32), ("cl_max_y", C.c_int32),
+                ("num_points", C.c_uint32), ("num_particles", C.c_uint32),
+                ("iterations", C.c_uint32), ("seed", C.c_uint64), ("stream", C.c_uint32)]
+
+
+class Score(C.Structure):
+    _fields_ = [("n_rendered", C.c_uint32), ("n_no_obs", C.c_uint32),
+                ("n_seg_rendered", C.c_uint32), ("n_seg_not_rendered", C.c_uint32),
+                ("sq_lo", C.c_uint64), ("sq_hi", C.c_uint64),
+                ("r_min_x", C.c_int32), ("r_max_x", C.c_int32),
+                ("r_min_y", C.c_int32), ("r_max_y", C.c_int32),
+                ("w_min_x", C.c_int32), ("w_max_x", C.c_int32),
+                ("w_min_y", C.c_int32), ("w_max_y", C.c_int32),
+                ("partial_len", C.c_int32), ("fit", C.c_float)]
+
+
+class Result(C.Structure):
+    _fields_ = [("gbest_fit", C.c_float), ("gbest", C.c_float * 7), ("raster_writes", C.c_uint64)]
+
+
+_lib = None
+_pin = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = C.CDLL(path)
+        L.qo_uniform.restype = C.c_float
+        L.qo_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
+        for fn in ("qo_sin", "qo_cos", "qo_acos"):
+            getattr(L, fn).restype = C.c_double
+            getattr(L, fn).argtypes = [C.c_double]
+        L.qo_raster_face.restype = C.c_int64
+        L.qo_render.restype = C.c_int64
+        L.qo_fitness_from_counts.restype = C.c_float
+        L.qo_fitness_from_counts.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64,
+                                             C.c_uint64, C.c_uint32]
+        L.qo_fitness_fp64.restype = C.c_double
+        L.qo_domain_w.restype = C.c_int32
+        L.qo_domain_h.restype = C.c_int32
+        L.qo_solve.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def pin():
+    """The reference's main.h helpers compiled for the host (None where the
+    reference sources are absent)."""
+    global _pin
+    if _pin is None:
+        path = _build.build_ref_pin()
+        if path is None:
+            return None
+        _pin = C.CDLL(path)
+    return _pin
+
+
+def ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+def camera(fx=525.0, fy=525.0, cx=319.5, cy=239.5, width=640, height=480) -> Camera:
+    return Camera(fx, fy, cx, cy, width, height)
+
+
+def default_params() -> Params:
+    p = Params()
+    lib().qo_default_params(C.byref(p))
+    return p
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().qo_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def uniform(seed, stream, particle, draw) -> float:
+    return lib().qo_uniform(seed, stream, particle, draw)
+
+
+def zbuf_new(cam: Camera) -> np.ndarray:
+    L = lib()
+    return np.full((L.qo_domain_h(C.byref(cam)), L.qo_domain_w(C.byref(cam))), DEPTH_BG,
+                   dtype=np.int32)
+
+
+def project(s7, v3, cam: Camera):
+    s = np.ascontiguousarray(s7, dtype=np.float32)
+    v = np.ascontiguousarray(v3, dtype=np.float32)
+    o = np.zeros(3, np.float32)
+    lib().qo_project(ptr(s, _f), ptr(v, _f), C.byref(cam), ptr(o, _f))
+    return o
+
+
+def raster_face(v1, v2, v3, cam: Camera, zbuf: np.ndarray, box=None):
+    a = np.ascontiguousarray(v1, np.float32)
+    b = np.ascontiguousarray(v2, np.float32)
+    c = np.ascontiguousarray(v3, np.float32)
+    if box is None:
+        box = np.array([50000, -1, 50000, -1], np.int32)
+    n = lib().qo_raster_face(ptr(a, _f), ptr(b, _f), ptr(c, _f), C.byref(cam),
+                             ptr(zbuf, _i32), ptr(box, _i32))
+    return n, box
+
+
+def render(mesh: np.ndarray, num_faces: int, s7, cam: Camera, zbuf: np.ndarray | None = None):
+    if zbuf is None:
+        zbuf = zbuf_new(cam)
+    s = np.ascontiguousarray(s7, np.float32)
+    box = np.zeros(4, np.int32)
+    m = np.ascontiguousarray(mesh, np.float32)
+    n = lib().qo_render(ptr(m, _f), C.c_uint32(num_faces), ptr(s, _f), C.byref(cam),
+                        ptr(zbuf, _i32), ptr(box, _i32))
+    return zbuf, box, n
+
+
+def score(zbuf: np.ndarray, box: np.ndarray, obs: np.ndarray, cam: Camera, prm: Params) -> Score:
+    sc = Score()
+    o = np.ascontiguousarray(obs, np.uint16)
+    b = np.ascontiguousarray(box, np.int32)
+    lib().qo_score_zbuf(ptr(zbuf, _i32), ptr(b, _i32), ptr(o, _u16), C.byref(cam),
+                        C.byref(prm), C.byref(sc))
+    return sc
+
+
+def fitness_fp64(sc: Score, num_points: int) -> float:
+    return lib().qo_fitness_fp64(C.byref(sc), C.c_uint32(num_points))
+
+
+def init_particle(prm: Params, p: int, pos, vel, pb):
+    lib().qo_init_particle(C.byref(prm), C.c_uint32(p), ptr(pos, _f), ptr(vel, _f), ptr(pb, _f))
+
+
+def update_particle(prm: Params, p: int, it: int, pos, vel, pb, gb):
+    g = np.ascontiguousarray(gb, np.float32)
+    lib().qo_update_particle(C.byref(prm), C.c_uint32(p), C.c_uint32(it), ptr(pos, _f),
+                             ptr(vel, _f), ptr(pb, _f), ptr(g, _f))
+
+
+def solve(mesh: np.ndarray, num_faces: int, obs: np.ndarray, cam: Camera, prm: Params,
+          trace: bool = False):
+    P = prm.num_particles
+    pos = np.zeros((NDIM, P), np.float32)
+    vel = np.zeros((NDIM, P), np.float32)
+    pb = np.zeros((NDIM, P), np.float32)
+    pbf = np.zeros(P, np.float32)
+    res = Result()
+    tg = np.zeros((prm.iterations, 8), np.float32) if trace else None
+    tf = np.zeros((prm.iterations, P), np.float32) if trace else None
+    m = np.ascontiguousarray(mesh, np.float32)
+    o = np.ascontiguousarray(obs, np.uint16)
+    rc = lib().qo_solve(ptr(m, _f), C.c_uint32(num_faces), ptr(o, _u16), C.byref(cam),
+                        C.byref(prm), ptr(pos, _f), ptr(vel, _f), ptr(pb, _f), ptr(pbf, _f),
+                        C.byref(res), ptr(tg, _f) if trace else None,
+                        ptr(tf, _f) if trace else None)
+    if rc != 0:
+        raise RuntimeError("qo_solve failed: %d" % rc)
+    out = {"fit": res.gbest_fit, "pose": np.array(res.gbest[:], np.float32), "pos": pos,
+           "vel": vel, "pbest": pb, "pbest_fit": pbf, "raster_writes": res.raster_writes}
+    if trace:
+        out["trace_gbest"] = tg
+        out["trace_fit"] = tf
+    return out
+
+
+def sin(x):
+    return lib().qo_sin(x)
+
+
+def cos(x):
+    return lib().qo_cos(x)
+
+
+def acos(x):
+    return lib().qo_acos(x)

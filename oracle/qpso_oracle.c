@@ -1,0 +1,740 @@
+/*
+ * qpso_oracle.c -- scalar CPU restatement of the Q-PSO pose-solve hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker; see qpso_oracle.h for the parity
+ * status and the arithmetic contract).  Build with -ffp-contract=off.
+ *
+ * Every function cites the reference file:line it restates.  Where the
+ * reference is racy, undefined or launch-shape dependent, the restatement
+ * fixes one deterministic meaning; each such point is marked DEVIATION.
+ */
+#include "qpso_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* Philox4x32-10, Salmon, Moraes, Dror, Shaw, "Parallel random numbers:
+ * as easy as 1, 2, 3", SC'11.  Replaces the GSL mt19937 table of
+ * main.cu:1337-1352 (capped at 512 draws per particle). */
+void qo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* Draw number `draw` of particle `particle` in stream `stream`: counter
+ * (draw/4, particle, stream, 0), key (seed lo, seed hi), lane draw%4,
+ * top 24 bits scaled to [0, 1). */
+float qo_uniform(uint64_t seed, uint32_t stream, uint32_t particle, uint32_t draw)
+{
+    uint32_t ctr[4] = {draw >> 2, particle, stream, 0u};
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t o[4];
+    qo_philox4x32_10(ctr, key, o);
+    return (float)(o[draw & 3u] >> 8) * 0x1p-24f;
+}
+
+/* ------------------------------------------------------------------ */
+/* sin/cos/acos.  The reference calls CUDA's cosf/sinf/acosf under
+ * -use_fast_math (main.h:287-294, 391-399; main.cu:946,970); those differ
+ * between CUDA and libm, so both sides of this build use the same
+ * double-precision series instead: Cody-Waite reduction by pi/2 (3-part
+ * split, 30 bits per part) and Taylor polynomials on [-pi/4, pi/4]
+ * (truncation < 1e-19); acos via asin's Taylor series on [0, 1/2] and
+ * acos(x) = 2 asin(sqrt((1-x)/2)) above 1/2. */
+static const double QO_PIO2_1 = 1.5707963276654482;
+static const double QO_PIO2_2 = -8.705515692000731e-10;
+static const double QO_PIO2_3 = -3.50343439808993e-19;
+static const double QO_2OPI = 0.6366197723675814;
+static const double QO_PI = 3.141592653589793;
+static const double QO_PIO2 = 1.5707963267948966;
+
+static double qo_sin_kernel(double r)
+{
+    double r2 = r * r;
+    double p = 2.8114572543455206e-15;
+    p = p * r2 + -7.647163731819816e-13;
+    p = p * r2 + 1.6059043836821613e-10;
+    p = p * r2 + -2.505210838544172e-08;
+    p = p * r2 + 2.7557319223985893e-06;
+    p = p * r2 + -0.0001984126984126984;
+    p = p * r2 + 0.008333333333333333;
+    p = p * r2 + -0.16666666666666666;
+    return r + r * (r2 * p);
+}
+
+static double qo_cos_kernel(double r)
+{
+    double r2 = r * r;
+    double p = -1.5619206968586225e-16;
+    p = p * r2 + 4.779477332387385e-14;
+    p = p * r2 + -1.1470745597729725e-11;
+    p = p * r2 + 2.08767569878681e-09;
+    p = p * r2 + -2.755731922398589e-07;
+    p = p * r2 + 2.48015873015873e-05;
+    p = p * r2 + -0.001388888888888889;
+    p = p * r2 + 0.041666666666666664;
+    p = p * r2 + -0.5;
+    return 1.0 + r2 * p;
+}
+
+/* Reduce x to r in [-pi/4, pi/4] and quadrant q = k mod 4. */
+static double qo_reduce(double x, int *q)
+{
+    double ax = fabs(x);
+    if (ax > 1.0e6) {
+        /* outside any argument this solver produces; fmod is exact on both
+         * sides, so the result is still deterministic */
+        x = fmod(x, 2.0 * QO_PI);
+    }
+    double k = rint(x * QO_2OPI);
+    double r = x - k * QO_PIO2_1;
+    r = r - k * QO_PIO2_2;
+    r = r - k * QO_PIO2_3;
+    long long ki = (long long)k;
+    *q = (int)(ki & 3);
+    return r;
+}
+
+double qo_sin(double x)
+{
+    if (x != x || isinf(x)) return x - x;
+    int q;
+    double r = qo_reduce(x, &q);
+    switch (q) {
+    case 0: return qo_sin_kernel(r);
+    case 1: return qo_cos_kernel(r);
+    case 2: return -qo_sin_kernel(r);
+    default: return -qo_cos_kernel(r);
+    }
+}
+
+double qo_cos(double x)
+{
+    if (x != x || isinf(x)) return x - x;
+    int q;
+    double r = qo_reduce(x, &q);
+    switch (q) {
+    case 0: return qo_cos_kernel(r);
+    case 1: return -qo_sin_kernel(r);
+    case 2: return -qo_cos_kernel(r);
+    default: return qo_sin_kernel(r);
+    }
+}
+
+static const double QO_ASIN_C[27] = {
+    0.16666666666666666, 0.075, 0.044642857142857144, 0.030381944444444444,
+    0.022372159090909092, 0.017352764423076924, 0.01396484375,
+    0.011551800896139705, 0.009761609529194078, 0.008390335809616815,
+    0.0073125258735988454, 0.006447210311889649, 0.005740037670841924,
+    0.005153309682319905, 0.004660143486915096, 0.004240907093679363,
+    0.003880964558837669, 0.0035692053938259347, 0.003297059503473485,
+    0.0030578216492580306, 0.002846178401108942, 0.00265787063820729,
+    0.0024894486782468836, 0.002338091892111975, 0.0022014739737101384,
+    0.0020776610325181676, 0.0019650336162772837};
+
+/* asin on [-1/2, 1/2] */
+static double qo_asin_kernel(double x)
+{
+    double x2 = x * x;
+    double p = QO_ASIN_C[26];
+    for (int i = 25; i >= 0; --i) p = p * x2 + QO_ASIN_C[i];
+    return x + x * (x2 * p);
+}
+
+double qo_acos(double x)
+{
+    if (x != x) return x;
+    if (x > 1.0) x = 1.0;
+    if (x < -1.0) x = -1.0;
+    if (x > 0.5) return 2.0 * qo_asin_kernel(sqrt((1.0 - x) * 0.5));
+    if (x < -0.5) return QO_PI - 2.0 * qo_asin_kernel(sqrt((1.0 + x) * 0.5));
+    return QO_PIO2 - qo_asin_kernel(x);
+}
+
+static float qo_sinf(float x) { return (float)qo_sin((double)x); }
+static float qo_cosf(float x) { return (float)qo_cos((double)x); }
+static float qo_acosf(float x) { return (float)qo_acos((double)x); }
+
+/* ------------------------------------------------------------------ */
+/* Quaternion helpers.  State vectors are [tx,ty,tz,q0,q1,q2,q3]
+ * (main.h:88-94). */
+#define TX 0
+#define TY 1
+#define TZ 2
+#define Q0 3
+#define Q1 4
+#define Q2 5
+#define Q3 6
+#define QO_MIN_NORM 1.0e-7f /* MIN_NORM_, main.h:95 */
+
+/* QuatProd_pqPSOstateVect, main.h:248-254 (p, q are 7-vectors) */
+void qo_quat_prod(const float *p, const float *q, float *o)
+{
+    o[0] = p[Q0] * q[Q0] - p[Q1] * q[Q1] - p[Q2] * q[Q2] - p[Q3] * q[Q3];
+    o[1] = p[Q1] * q[Q0] + p[Q0] * q[Q1] + p[Q2] * q[Q3] - p[Q3] * q[Q2];
+    o[2] = p[Q2] * q[Q0] + p[Q0] * q[Q2] + p[Q3] * q[Q1] - p[Q1] * q[Q3];
+    o[3] = p[Q3] * q[Q0] + p[Q0] * q[Q3] + p[Q1] * q[Q2] - p[Q2] * q[Q1];
+}
+
+/* QuatProd_pq_1PSOstateVect, main.h:256-264: p * conj(q) */
+void qo_quat_prod_conj(const float *p, const float *q, float *o)
+{
+    o[0] = p[Q0] * q[Q0] + p[Q1] * q[Q1] + p[Q2] * q[Q2] + p[Q3] * q[Q3];
+    o[1] = p[Q1] * q[Q0] - p[Q0] * q[Q1] - p[Q2] * q[Q3] + p[Q3] * q[Q2];
+    o[2] = p[Q2] * q[Q0] - p[Q0] * q[Q2] - p[Q3] * q[Q1] + p[Q1] * q[Q3];
+    o[3] = p[Q3] * q[Q0] - p[Q0] * q[Q3] - p[Q1] * q[Q2] + p[Q2] * q[Q1];
+}
+
+/* NormalizeQuaternionPSOstateVect, main.h:209-221 (__frcp_rn == 1/x) */
+void qo_normalize_quat(float *s)
+{
+    const float den = sqrtf(s[Q0] * s[Q0] + s[Q1] * s[Q1] + s[Q2] * s[Q2] + s[Q3] * s[Q3]);
+    if (den > QO_MIN_NORM) {
+        const float r = 1.0f / den;
+        s[Q0] = s[Q0] * r;
+        s[Q1] = s[Q1] * r;
+        s[Q2] = s[Q2] * r;
+        s[Q3] = s[Q3] * r;
+    }
+}
+
+/* Cast2TopHalfHypersphere, main.h:236-246 (4-vector) */
+void qo_cast_top_half(float *q)
+{
+    if (q[0] < 0.0f) {
+        q[0] = -q[0]; q[1] = -q[1]; q[2] = -q[2]; q[3] = -q[3];
+    }
+}
+
+static void qo_cast_top_half_state(float *s) /* main.h:223-234 */
+{
+    if (s[Q0] < 0.0f) {
+        s[Q0] = -s[Q0]; s[Q1] = -s[Q1]; s[Q2] = -s[Q2]; s[Q3] = -s[Q3];
+    }
+}
+
+/* Exponential-map step shared by QuatKinematicsPSOStateVectWithInit
+ * (main.h:266-307) and QuatKinematicsPSOStateVect (main.h:373-413):
+ * q <- cos(|w Ts|/2) q0 + 1/2 sinc (q0 (x) (0, w Ts)), renormalised and cast
+ * to the top half.  mTs_ = 0.5 (main.h:96) scales exactly. */
+static void qo_kinematics(const float *q_from, float *s, const float *w)
+{
+    float wt[7] = {0, 0, 0, 0, 0, 0, 0};
+    wt[Q1] = w[Q1] * 0.5f;
+    wt[Q2] = w[Q2] * 0.5f;
+    wt[Q3] = w[Q3] * 0.5f;
+    const float nrm = sqrtf(wt[Q1] * wt[Q1] + wt[Q2] * wt[Q2] + wt[Q3] * wt[Q3]);
+    const float dom = nrm * 0.5f;
+    const float cosw = qo_cosf(dom);
+    float sinw;
+    if (dom < QO_MIN_NORM) {
+        sinw = 1.0f;
+    } else {
+        const float r = 1.0f / dom;
+        sinw = qo_sinf(dom) * r;
+    }
+    float qxw[4];
+    qo_quat_prod(q_from, wt, qxw);
+    float qn[4];
+    for (int i = 0; i < 4; ++i) qn[i] = cosw * q_from[Q0 + i] + 0.5f * sinw * qxw[i];
+    for (int i = 0; i < 4; ++i) s[Q0 + i] = qn[i];
+    qo_normalize_quat(s);
+    qo_cast_top_half_state(s);
+}
+
+void qo_quat_kinematics(float *s, const float *w)
+{
+    float from[7];
+    memcpy(from, s, sizeof(from));
+    qo_kinematics(from, s, w);
+}
+
+void qo_quat_kinematics_init(const float *qinit7, float *s, const float *w)
+{
+    qo_kinematics(qinit7, s, w);
+}
+
+/* quatVectRotationPSOstateVect, main.h:328-347: t = 2 q.xyz x v;
+ * v' = v + q.w t + q.xyz x t (cross product as in main.h:309-326). */
+void qo_rotate(const float *s, const float v[3], float o[3])
+{
+    float t[3], k[3];
+    t[0] = s[Q2] * v[2] - s[Q3] * v[1];
+    t[1] = -(s[Q1] * v[2] - s[Q3] * v[0]);
+    t[2] = s[Q1] * v[1] - s[Q2] * v[0];
+    t[0] = 2.0f * t[0]; t[1] = 2.0f * t[1]; t[2] = 2.0f * t[2];
+    k[0] = s[Q2] * t[2] - s[Q3] * t[1];
+    k[1] = -(s[Q1] * t[2] - s[Q3] * t[0]);
+    k[2] = s[Q1] * t[1] - s[Q2] * t[0];
+    o[0] = v[0] + s[Q0] * t[0] + k[0];
+    o[1] = v[1] + s[Q0] * t[1] + k[1];
+    o[2] = v[2] + s[Q0] * t[2] + k[2];
+}
+
+/* projectModelPointsToPixels(const float*, const float4&, float4&),
+ * main.h:513-545: rotate, translate, u = cx + fx x/z, v = cy + fy y/z with
+ * x/z = x * rcp_rn(z), z in mm.  DEVIATION: the reference's intrinsics are
+ * double macros, so it evaluates cx + fx*(x/z) in double; this build takes
+ * fp32 intrinsics at run time and evaluates it as one fp32 fma. */
+void qo_project(const float *s, const float v[3], const qo_camera *cam, float o[3])
+{
+    float p[3];
+    qo_rotate(s, v, p);
+    p[0] = p[0] + s[TX];
+    p[1] = p[1] + s[TY];
+    p[2] = p[2] + s[TZ];
+    const float rz = 1.0f / p[2];
+    o[0] = fmaf(cam->fx, p[0] * rz, cam->cx);
+    o[1] = fmaf(cam->fy, p[1] * rz, cam->cy);
+    o[2] = 1000.0f * p[2];
+}
+
+/* ------------------------------------------------------------------ */
+/* Fixed-point raster.  Integer helpers give the wrap-around, arithmetic
+ * shift and saturating round-to-nearest-even conversion that the reference
+ * gets from CUDA (int32 arithmetic, >> on int, __float2int_rn). */
+static inline int32_t w_add(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+static inline int32_t w_sub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+static inline int32_t w_mul(int32_t a, int32_t b) { return (int32_t)((uint32_t)a * (uint32_t)b); }
+static inline int32_t w_shl(int32_t a, int s) { return (int32_t)((uint32_t)a << s); }
+static inline int32_t asr(int32_t a, int s) { return a >> s; } /* gcc: arithmetic */
+static inline int32_t imin(int32_t a, int32_t b) { return a < b ? a : b; }
+static inline int32_t imax(int32_t a, int32_t b) { return a > b ? a : b; }
+
+static inline int32_t f2i_rn(float f)
+{
+    if (f != f) return 0;
+    if (f >= 2147483648.0f) return INT32_MAX;
+    if (f <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)nearbyintf(f); /* default rounding mode: half to even */
+}
+
+int32_t qo_domain_w(const qo_camera *cam) { return cam->width + 2 * QO_GUARD; }
+int32_t qo_domain_h(const qo_camera *cam) { return cam->height + 2 * QO_GUARD; }
+
+void qo_zbuf_reset(int32_t *zbuf, const qo_camera *cam)
+{
+    size_t n = (size_t)qo_domain_w(cam) * (size_t)qo_domain_h(cam);
+    for (size_t i = 0; i < n; ++i) zbuf[i] = QO_DEPTH_BG;
+}
+
+/* renderFixedPointAABB, main.h:1306-1491, for one face.
+ *
+ * Quirks kept exactly: the inside test is a no-op (the mask of main.h:1440
+ * is 0 or 1 and the guard of main.h:1473 tests its sign bit), so every pixel
+ * of the face's integer bounding rectangle is written; depth is
+ * z1 + cx2*(z2-z1)/A + cx3*(z3-z1)/A with cx = (E+15)>>8 (main.h:1421-1448).
+ * The render AABB takes every face, culled or not, before culling
+ * (main.h:1348-1359 then 1371-1378), and starts from 50000 / -1.
+ *
+ * DEVIATION: writes outside the raster domain (the image grown by QO_GUARD
+ * px) are dropped.  The reference writes every pixel through the linear
+ * index y*640+x with no clipping (main.h:1442), which aliases columns
+ * outside [0,640) into neighbouring rows and rows outside [0,480) into other
+ * particles' buffers or past the allocation. */
+int64_t qo_raster_face(const float v1[3], const float v2[3], const float v3[3],
+                       const qo_camera *cam, int32_t *zbuf, int32_t box[4])
+{
+    const int32_t Y1 = f2i_rn(16.0f * v1[1]);
+    const int32_t Y2 = f2i_rn(16.0f * v2[1]);
+    const int32_t Y3 = f2i_rn(16.0f * v3[1]);
+    const int32_t X1 = f2i_rn(16.0f * v1[0]);
+    const int32_t X2 = f2i_rn(16.0f * v2[0]);
+    const int32_t X3 = f2i_rn(16.0f * v3[0]);
+
+    const int32_t minx = asr(w_add(imin(imin(X1, X2), X3), 0xF), 4);
+    const int32_t maxx = asr(w_add(imax(imax(X1, X2), X3), 0xF), 4);
+    const int32_t miny = asr(w_add(imin(imin(Y1, Y2), Y3), 0xF), 4);
+    const int32_t maxy = asr(w_add(imax(imax(Y1, Y2), Y3), 0xF), 4);
+
+    box[0] = imin(box[0], minx);
+    box[1] = imax(box[1], maxx);
+    box[2] = imin(box[2], miny);
+    box[3] = imax(box[3], maxy);
+
+    const int32_t DX12 = w_sub(X1, X2), DX23 = w_sub(X2, X3), DX31 = w_sub(X3, X1);
+    const int32_t DY12 = w_sub(Y1, Y2), DY23 = w_sub(Y2, Y3), DY31 = w_sub(Y3, Y1);
+
+    const int32_t tri_area = w_sub(w_mul(DX12, DY31), w_mul(DX31, DY12));
+    if (tri_area <= 0) return 0;
+    if (w_sub(maxx, minx) <= 0 || w_sub(maxy, miny) <= 0) return 0;
+
+    const float rA = 1.0f / (float)tri_area; /* overA_ == 1 (main.h:155) */
+
+    const int32_t FDX23 = w_shl(DX23, 4), FDX31 = w_shl(DX31, 4);
+    const int32_t FDY23 = w_shl(DY23, 4), FDY31 = w_shl(DY31, 4);
+
+    int32_t C2 = w_sub(w_mul(DY23, X2), w_mul(DX23, Y2));
+    int32_t C3 = w_sub(w_mul(DY31, X3), w_mul(DX31, Y3));
+    C2 = w_add(C2, (DY23 < 0 || (DY23 == 0 && DX23 > 0)) ? 1 : 0);
+    C3 = w_add(C3, (DY31 < 0 || (DY31 == 0 && DX31 > 0)) ? 1 : 0);
+
+    const int32_t MINY = w_shl(miny, 4), MINX = w_shl(minx, 4);
+    const int32_t CY2 = w_sub(w_add(C2, w_mul(DX23, MINY)), w_mul(DY23, MINX));
+    const int32_t CY3 = w_sub(w_add(C3, w_mul(DX31, MINY)), w_mul(DY31, MINX));
+
+    const float z1 = v1[2];
+    const float z2 = (v2[2] - v1[2]) * rA;
+    const float z3 = (v3[2] - v1[2]) * rA;
+
+    /* loop bounds: [minx, maxx) x [miny, maxy), clipped to the domain; the
+     * true extents are < 2^31 because the wrapped differences are > 0 */
+    const int64_t dx0 = -QO_GUARD, dx1 = (int64_t)cam->width + QO_GUARD;
+    const int64_t dy0 = -QO_GUARD, dy1 = (int64_t)cam->height + QO_GUARD;
+    const int64_t ext_x = (int64_t)(uint32_t)w_sub(maxx, minx);
+    const int64_t ext_y = (int64_t)(uint32_t)w_sub(maxy, miny);
+    int64_t xa = minx, xb = (int64_t)minx + ext_x;
+    int64_t ya = miny, yb = (int64_t)miny + ext_y;
+    if (xa < dx0) xa = dx0;
+    if (xb > dx1) xb = dx1;
+    if (ya < dy0) ya = dy0;
+    if (yb > dy1) yb = dy1;
+    if (xa >= xb || ya >= yb) return 0;
+
+    const int32_t dw = qo_domain_w(cam);
+    int64_t writes = 0;
+    for (int64_t y = ya; y < yb; ++y) {
+        const int32_t ry = (int32_t)(y - (int64_t)miny); /* rows since miny */
+        for (int64_t x = xa; x < xb; ++x) {
+            const int32_t rx = (int32_t)(x - (int64_t)minx);
+            const int32_t CX2 = w_sub(w_add(CY2, w_mul(ry, FDX23)), w_mul(rx, FDY23));
+            const int32_t CX3 = w_sub(w_add(CY3, w_mul(ry, FDX31)), w_mul(rx, FDY31));
+            const int32_t cx2 = asr(w_add(CX2, 0xF), 8);
+            const int32_t cx3 = asr(w_add(CX3, 0xF), 8);
+            float depth = z1;
+            depth = depth + (float)cx2 * z2;
+            depth = depth + (float)cx3 * z3;
+            const int32_t d = f2i_rn(depth);
+            int32_t *px = &zbuf[(size_t)(y + QO_GUARD) * (size_t)dw + (size_t)(x + QO_GUARD)];
+            if (d < *px) *px = d;
+            ++writes;
+        }
+    }
+    return writes;
+}
+
+/* RenderFixedPointKernelAABB, main.cu:305-419: one face per thread, vertices
+ * read from the loadOBJ3 SoA layout (main.h:620-679, index f + j*F + c*3F). */
+int64_t qo_render(const float *mesh, uint32_t F, const float *s, const qo_camera *cam,
+                  int32_t *zbuf, int32_t box[4])
+{
+    box[0] = QO_AABB_INIT_MIN; box[1] = QO_AABB_INIT_MAX;
+    box[2] = QO_AABB_INIT_MIN; box[3] = QO_AABB_INIT_MAX;
+    int64_t writes = 0;
+    for (uint32_t f = 0; f < F; ++f) {
+        float v[3][3], uvz[3][3];
+        for (int j = 0; j < 3; ++j) {
+            v[j][0] = mesh[f + (size_t)j * F];
+            v[j][1] = mesh[f + 3 * (size_t)F + (size_t)j * F];
+            v[j][2] = mesh[f + 6 * (size_t)F + (size_t)j * F];
+            qo_project(s, v[j], cam, uvz[j]);
+        }
+        writes += qo_raster_face(uvz[0], uvz[1], uvz[2], cam, zbuf, box);
+    }
+    return writes;
+}
+
+/* ------------------------------------------------------------------ */
+/* ComputeFitnessKernel, main.cu:550-764.
+ *
+ * Window = union of the render AABB and the cluster AABB (main.cu:596-622);
+ * the reference walks t = 0 .. ceil(Area/1024)*1024-1 with x = t % W,
+ * y = t / W and keeps y <= maxY (main.cu:624-640), so it visits the rows
+ * [minY, maxY) fully plus the first min(W, pad) pixels of row maxY, where
+ * pad = ceil(Area/1024)*1024 - Area.  That tail is kept.
+ *
+ * DEVIATION: the reference computes y with a float reciprocal of W
+ * (main.cu:628), which for 137 of the first 1024 widths puts some x = 0
+ * pixels on the previous row: those pixels are visited twice by racing
+ * threads and their neighbours never, and the never-visited pixels are not
+ * reset, so their depth leaks into the particle's next render.  This build
+ * visits each window pixel exactly once.  The reference also converts Area
+ * to float (exact below 2^24 px) and overflows int32 for windows above
+ * 2^31 px; here Area is an exact 64-bit integer.
+ *
+ * Observed depth outside the image reads as 0.  The rendered depth of a
+ * pixel outside the raster domain is the background value. */
+void qo_score_zbuf(const int32_t *zbuf, const int32_t box[4], const uint16_t *obs,
+                   const qo_camera *cam, const qo_params *prm, qo_score *out)
+{
+    memset(out, 0, sizeof(*out));
+    out->r_min_x = box[0]; out->r_max_x = box[1];
+    out->r_min_y = box[2]; out->r_max_y = box[3];
+    const int32_t minX = imin(box[0], prm->cl_min_x);
+    const int32_t maxX = imax(box[1], prm->cl_max_x);
+    const int32_t minY = imin(box[2], prm->cl_min_y);
+    const int32_t maxY = imax(box[3], prm->cl_max_y);
+    out->w_min_x = minX; out->w_max_x = maxX; out->w_min_y = minY; out->w_max_y = maxY;
+    const int64_t W = (int64_t)maxX - minX, H = (int64_t)maxY - minY;
+    int64_t L = 0;
+    if (W > 0 && H > 0) {
+        const int64_t area = W * H;
+        const int64_t pad = (1024 - area % 1024) % 1024;
+        L = pad < W ? pad : W;
+    }
+    out->partial_len = (int32_t)L;
+    if (W <= 0 || H <= 0) {
+        out->fit = qo_fitness_from_counts(0, 0, 0, 0, 0, prm->num_points);
+        return;
+    }
+    const int32_t dw = qo_domain_w(cam);
+    uint32_t nR = 0, nNo = 0, nSegR = 0, nSNR = 0;
+    uint64_t lo = 0, hi = 0;
+    for (int64_t y = minY; y <= maxY; ++y) {
+        const int64_t xe = (y < maxY) ? (int64_t)maxX : (int64_t)minX + L;
+        for (int64_t x = minX; x < xe; ++x) {
+            int32_t zr = QO_DEPTH_BG;
+            if (x >= -QO_GUARD && x < cam->width + QO_GUARD &&
+                y >= -QO_GUARD && y < cam->height + QO_GUARD)
+                zr = zbuf[(size_t)(y + QO_GUARD) * (size_t)dw + (size_t)(x + QO_GUARD)];
+            int32_t zk = 0;
+            if (x >= 0 && x < cam->width && y >= 0 && y < cam->height)
+                zk = obs[(size_t)y * (size_t)cam->width + (size_t)x];
+            if (zk != 0 && zr == QO_DEPTH_BG) ++nSNR;
+            if (zr != QO_DEPTH_BG) {
+                ++nR;
+                if (zk == 0) {
+                    ++nNo;
+                } else {
+                    const int32_t d = w_sub(zr, zk);
+                    const uint64_t sq = (uint64_t)((int64_t)d * (int64_t)d);
+                    lo += sq;
+                    if (lo < sq) ++hi;
+                    ++nSegR;
+                }
+            }
+        }
+    }
+    out->n_rendered = nR;
+    out->n_no_obs = nNo;
+    out->n_seg_rendered = nSegR;
+    out->n_seg_not_rendered = nSNR;
+    out->sq_lo = lo;
+    out->sq_hi = hi;
+    out->fit = qo_fitness_from_counts(nSNR, nR, nNo, lo, hi, prm->num_points);
+}
+
+/* main.cu:743-760.  The reference sums float((zr-zk)*0.001)^2 in float;
+ * here the sum of squares is an exact integer (mm^2), converted once.
+ * DEVIATION: with no rendered pixel the reference computes 0 * rcp(0) =
+ * NaN; here the fitness is +inf (never a best, as NaN never was). */
+float qo_fitness_from_counts(uint32_t nSNR, uint32_t nR, uint32_t nNo, uint64_t lo,
+                             uint64_t hi, uint32_t num_points)
+{
+    if (nR == 0) return INFINITY;
+    const double S = (hi != 0) ? (double)hi * 18446744073709551616.0 + (double)lo : (double)lo;
+    const float ratio = (float)nSNR * (1.0f / (float)num_points);
+    const float rR = 1.0f / (float)nR;
+    const float ratioT = (float)nNo * rR;
+    const float zerr = (float)(S * 1.0e-6) * rR;
+    return (float)((double)(ratio + ratioT) * 0.05 + (double)zerr);
+}
+
+/* FP64 recomputation of the fitness from the integer counts, for the
+ * 1e-5 relative agreement check. */
+double qo_fitness_fp64(const qo_score *sc, uint32_t num_points)
+{
+    if (sc->n_rendered == 0) return INFINITY;
+    const double S = (double)sc->sq_hi * 18446744073709551616.0 + (double)sc->sq_lo;
+    return 0.05 * ((double)sc->n_seg_not_rendered / (double)num_points +
+                   (double)sc->n_no_obs / (double)sc->n_rendered) +
+           S * 1.0e-6 / (double)sc->n_rendered;
+}
+
+/* ------------------------------------------------------------------ */
+/* InitQPSO, main.cu:72-198.  Draws 0..11 of the particle's stream. */
+void qo_init_particle(const qo_params *prm, uint32_t p, float *pos, float *vel, float *pb)
+{
+    const uint32_t P = prm->num_particles;
+    uint32_t k = 0;
+#define U() qo_uniform(prm->seed, prm->stream, p, k++)
+    float s[7], v[7];
+    for (int d = 0; d < 3; ++d) {
+        s[d] = prm->t_lo[d] + (prm->t_hi[d] - prm->t_lo[d]) * U();
+        v[d] = -prm->vdot + (2.0f * prm->vdot) * U();
+    }
+    float qinit[7] = {0.f, 0.f, 0.f, prm->qinit[0], prm->qinit[1], prm->qinit[2], prm->qinit[3]};
+    float wpert[7] = {0, 0, 0, 0, 0, 0, 0};
+    const float span = prm->ang_hi - prm->ang_lo;
+    wpert[Q1] = prm->ang_lo + span * U();
+    wpert[Q2] = prm->ang_lo + span * U();
+    wpert[Q3] = prm->ang_lo + span * U();
+    qo_quat_kinematics_init(qinit, s, wpert);
+    v[Q0] = 0.0f;
+    v[Q1] = prm->ang_lo + span * U();
+    v[Q2] = prm->ang_lo + span * U();
+    v[Q3] = prm->ang_lo + span * U();
+#undef U
+    for (int d = 0; d < 7; ++d) {
+        pos[p + (size_t)d * P] = s[d];
+        vel[p + (size_t)d * P] = v[d];
+        pb[p + (size_t)d * P] = s[d];
+    }
+}
+
+/* UpdateParticlesEquationKernel, main.cu:858-1060.  Iteration `iter` (>= 1)
+ * uses draws 12*iter .. 12*iter+11. */
+void qo_update_particle(const qo_params *prm, uint32_t p, uint32_t iter, float *pos,
+                        float *vel, const float *pbv, const float *gb)
+{
+    const uint32_t P = prm->num_particles;
+    uint32_t k = 12u * iter;
+#define U() qo_uniform(prm->seed, prm->stream, p, k++)
+    float s[7], v[7], b[7], g[7];
+    for (int d = 0; d < 7; ++d) {
+        s[d] = pos[p + (size_t)d * P];
+        v[d] = vel[p + (size_t)d * P];
+        b[d] = pbv[p + (size_t)d * P];
+        g[d] = gb[d];
+    }
+    for (int d = 0; d < 3; ++d) {
+        const float r1 = prm->c1 * U();
+        const float r2 = prm->c2 * U();
+        const float iV = (float)(prm->w * (double)v[d]);
+        const float cV = r1 * (b[d] - s[d]);
+        const float sV = r2 * (g[d] - s[d]);
+        v[d] = iV + cV + sV;
+        s[d] = s[d] + v[d];
+        if (s[d] < prm->t_lo[d]) {
+            s[d] = prm->t_lo[d];
+            v[d] = 0.0f;
+        } else if (s[d] > prm->t_hi[d]) {
+            s[d] = prm->t_hi[d];
+            v[d] = 0.0f;
+        }
+    }
+    float qc[4], qs[4], wc[3] = {0, 0, 0}, ws[3] = {0, 0, 0};
+    qo_quat_prod_conj(b, s, qc);
+    qo_cast_top_half(qc);
+    const float nc = sqrtf(qc[1] * qc[1] + qc[2] * qc[2] + qc[3] * qc[3]);
+    if (nc > QO_MIN_NORM) {
+        const float rn = 1.0f / nc;
+        const float a = 2.0f * qo_acosf(qc[0]) * rn;
+        wc[0] = qc[1] * a; wc[1] = qc[2] * a; wc[2] = qc[3] * a;
+    }
+    qo_quat_prod_conj(g, s, qs);
+    qo_cast_top_half(qs);
+    const float ns = sqrtf(qs[1] * qs[1] + qs[2] * qs[2] + qs[3] * qs[3]);
+    if (ns > QO_MIN_NORM) {
+        const float rn = 1.0f / ns;
+        const float a = 2.0f * qo_acosf(qs[0]) * rn;
+        ws[0] = qs[1] * a; ws[1] = qs[2] * a; ws[2] = qs[3] * a;
+    }
+    v[Q0] = 0.0f;
+    for (int i = 1; i < 4; ++i) {
+        const float r1 = prm->c1 * U();
+        const float r2 = prm->c2 * U();
+        const float iW = (float)(prm->w * (double)v[Q0 + i]);
+        const float cW = r1 * wc[i - 1];
+        const float sW = r2 * ws[i - 1];
+        v[Q0 + i] = iW + cW + sW;
+    }
+#undef U
+    qo_quat_kinematics(s, v);
+    for (int d = 0; d < 7; ++d) {
+        pos[p + (size_t)d * P] = s[d];
+        vel[p + (size_t)d * P] = v[d];
+    }
+}
+
+/* ------------------------------------------------------------------ */
+void qo_default_params(qo_params *prm)
+{
+    memset(prm, 0, sizeof(*prm));
+    prm->c1 = 1.0f;
+    prm->c2 = 1.0f;
+    prm->w = 0.3;
+    prm->vdot = 3.0f;
+    prm->ang_lo = -10.0f;
+    prm->ang_hi = 10.0f;
+    prm->qinit[0] = 0.7071f; prm->qinit[1] = 0.7071f; prm->qinit[2] = 0.f; prm->qinit[3] = 0.f;
+    prm->num_particles = 64;
+    prm->iterations = 50;
+}
+
+/* Host loop main.cu:1601-1727: init, then per iteration render + score every
+ * particle, personal/global best update (main.cu:768-855, argmin with the
+ * first minimum like thrust::min_element), then the particle update. */
+int qo_solve(const float *mesh, uint32_t F, const uint16_t *obs, const qo_camera *cam,
+             const qo_params *prm, float *pos, float *vel, float *pbest, float *pbest_fit,
+             qo_result *res, float *trace_gbest, float *trace_fit)
+{
+    const uint32_t P = prm->num_particles;
+    if (P == 0 || F == 0 || prm->num_points == 0) return -1;
+    const size_t dn = (size_t)qo_domain_w(cam) * (size_t)qo_domain_h(cam);
+    int32_t *zbuf = (int32_t *)malloc(dn * sizeof(int32_t));
+    float *fit = (float *)malloc(P * sizeof(float));
+    if (!zbuf || !fit) { free(zbuf); free(fit); return -2; }
+    qo_zbuf_reset(zbuf, cam);
+    const int32_t dw = qo_domain_w(cam);
+
+    float gfit = 1.0e10f; /* max_best_fit_, main.h:100 */
+    float g[7] = {0, 0, 0, 0, 0, 0, 0};
+    uint64_t writes = 0;
+    for (uint32_t p = 0; p < P; ++p) {
+        qo_init_particle(prm, p, pos, vel, pbest);
+        pbest_fit[p] = 1.0e10f;
+    }
+    for (uint32_t it = 0; it < prm->iterations; ++it) {
+        if (it > 0)
+            for (uint32_t p = 0; p < P; ++p) qo_update_particle(prm, p, it, pos, vel, pbest, g);
+        for (uint32_t p = 0; p < P; ++p) {
+            float s[7];
+            for (int d = 0; d < 7; ++d) s[d] = pos[p + (size_t)d * P];
+            int32_t box[4];
+            writes += (uint64_t)qo_render(mesh, F, s, cam, zbuf, box);
+            qo_score sc;
+            qo_score_zbuf(zbuf, box, obs, cam, prm, &sc);
+            fit[p] = sc.fit;
+            /* reset the touched rows of the render box (the reference's
+             * fitness kernel resets the pixels it visits) */
+            int64_t x0 = box[0], x1 = box[1], y0 = box[2], y1 = box[3];
+            if (x0 < -QO_GUARD) x0 = -QO_GUARD;
+            if (y0 < -QO_GUARD) y0 = -QO_GUARD;
+            if (x1 > cam->width + QO_GUARD) x1 = cam->width + QO_GUARD;
+            if (y1 > cam->height + QO_GUARD) y1 = cam->height + QO_GUARD;
+            for (int64_t y = y0; y < y1; ++y)
+                for (int64_t x = x0; x < x1; ++x)
+                    zbuf[(size_t)(y + QO_GUARD) * (size_t)dw + (size_t)(x + QO_GUARD)] = QO_DEPTH_BG;
+        }
+        uint32_t best = 0;
+        for (uint32_t p = 0; p < P; ++p) {
+            if (fit[p] < pbest_fit[p]) {
+                pbest_fit[p] = fit[p];
+                for (int d = 0; d < 7; ++d) pbest[p + (size_t)d * P] = pos[p + (size_t)d * P];
+            }
+            if (fit[p] < fit[best]) best = p;
+        }
+        if (fit[best] < gfit) {
+            gfit = fit[best];
+            for (int d = 0; d < 7; ++d) g[d] = pos[best + (size_t)d * P];
+        }
+        if (trace_gbest) {
+            trace_gbest[(size_t)it * 8] = gfit;
+            for (int d = 0; d < 7; ++d) trace_gbest[(size_t)it * 8 + 1 + d] = g[d];
+        }
+        if (trace_fit)
+            for (uint32_t p = 0; p < P; ++p) trace_fit[(size_t)it * P + p] = fit[p];
+    }
+    res->gbest_fit = gfit;
+    for (int d = 0; d < 7; ++d) res->gbest[d] = g[d];
+    res->raster_writes = writes;
+    free(zbuf);
+    free(fit);
+    return 0;
+}

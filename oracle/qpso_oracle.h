@@ -1,0 +1,148 @@
+/*
+ * qpso_oracle.h -- scalar CPU restatement of the Q-PSO pose-solve hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path in
+ * q-pso_gb300/csrc: only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline arm may load it.  The product path never calls it and has no CPU
+ * fallback.
+ *
+ * Parity status: partially pinned.  The reference ships no tests, fixtures or
+ * golden vectors.  The quaternion helpers, the vertex rotation and the
+ * fixed-point rasteriser of the reference's main.h are compiled from the
+ * reference sources by oracle/ref_pin (stub headers for OpenCV/assimp, one
+ * emulated thread) and their outputs are committed as tests/golden fixtures;
+ * this restatement is checked against them.  The fitness, best-update and
+ * particle-update kernels live in main.cu, which cannot be compiled here
+ * (OpenCV 2.4, GSL and a missing header), so those parts are restated from
+ * the source and are unpinned beyond the helpers they call.
+ *
+ * Arithmetic contract shared with the CUDA kernels (both sides must agree
+ * bit for bit):
+ *   - every float expression is evaluated in source order with one IEEE
+ *     rounding per operation (no contraction: gcc -ffp-contract=off, nvcc
+ *     --fmad=false), except the projection u = cx + fx*(x/z), which the
+ *     reference evaluates in double (its intrinsics are double macros) and
+ *     which both sides evaluate as one fp32 fused multiply-add;
+ *   - int32 edge arithmetic wraps modulo 2^32, right shifts are arithmetic,
+ *     float->int conversion rounds half to even and saturates (NaN -> 0),
+ *     exactly like cvt.rni.s32.f32;
+ *   - sin, cos and acos are this project's own double-precision series
+ *     (qo_sin/qo_cos/qo_acos) rounded to float, not libm or CUDA's;
+ *   - random numbers come from Philox4x32-10 (Salmon et al., SC'11).
+ */
+#ifndef QPSO_ORACLE_H
+#define QPSO_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QO_NDIM 7
+#define QO_DEPTH_BG 60000         /* maxVal_depthBufferInt, main.h:157 */
+#define QO_AABB_INIT_MIN 50000    /* max_AABB_, main.h:159 */
+#define QO_AABB_INIT_MAX (-1)     /* min_AABB_, main.h:160 */
+#define QO_GUARD 1024             /* raster domain = image grown by this many px per side */
+
+typedef struct {
+    float fx, fy, cx, cy;
+    int32_t width, height;
+} qo_camera;
+
+/* Per-solve constants: QPSOParams_t (main.h:182-204) plus the compile-time
+ * macros of main.h:83-136 that this build makes runtime parameters. */
+typedef struct {
+    float c1, c2;                 /* c1_, c2_ (main.h:104-105) */
+    double w;                     /* psoW_ 0.3 (main.h:106), applied in double */
+    float vdot;                   /* vdot_ 3 (main.h:126) */
+    float ang_lo, ang_hi;         /* aminX_/amaxX_ -10/10 (main.h:118-123) */
+    float qinit[4];               /* InitQPSO qinit (main.cu:128-132) */
+    float t_lo[3], t_hi[3];       /* x_lo, x_hi (main.cu:1318-1323) */
+    int32_t cl_min_x, cl_max_x, cl_min_y, cl_max_y; /* cluster AABB, br() exclusive */
+    uint32_t num_points;          /* num_point_SegmentedCluster */
+    uint32_t num_particles;
+    uint32_t iterations;
+    uint64_t seed;
+    uint32_t stream;              /* Philox stream id of this solve instance */
+} qo_params;
+
+typedef struct {
+    uint32_t n_rendered;          /* sNrenderedPointsWarpBallot total */
+    uint32_t n_no_obs;            /* sNumRenderedDepthWoutValid3dClusterPixel */
+    uint32_t n_seg_rendered;      /* rendered pixels with observed depth */
+    uint32_t n_seg_not_rendered;  /* sNumSegDepthWoutValid3dModelPixel */
+    uint64_t sq_lo, sq_hi;        /* sum of (z_r - z_k)^2 in mm^2, 128 bit */
+    int32_t r_min_x, r_max_x, r_min_y, r_max_y;   /* render AABB */
+    int32_t w_min_x, w_max_x, w_min_y, w_max_y;   /* fitness window */
+    int32_t partial_len;          /* pixels visited on row w_max_y */
+    float fit;
+} qo_score;
+
+/* ---- RNG ---- */
+void qo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+float qo_uniform(uint64_t seed, uint32_t stream, uint32_t particle, uint32_t draw);
+
+/* ---- math ---- */
+double qo_sin(double x);
+double qo_cos(double x);
+double qo_acos(double x);
+
+/* ---- quaternion helpers (7-float PSO state vectors) ---- */
+void qo_quat_prod(const float *p, const float *q, float *out);
+void qo_quat_prod_conj(const float *p, const float *q, float *out);
+void qo_normalize_quat(float *s);
+void qo_cast_top_half(float *q4);
+void qo_quat_kinematics(float *s, const float *w);
+void qo_quat_kinematics_init(const float *qinit7, float *s, const float *w);
+void qo_rotate(const float *s, const float v[3], float out[3]);
+void qo_project(const float *s, const float v[3], const qo_camera *cam, float out[3]);
+
+/* ---- raster ---- */
+/* z-buffer over the raster domain [-QO_GUARD, width+QO_GUARD) x
+ * [-QO_GUARD, height+QO_GUARD), row-major, initialised to QO_DEPTH_BG. */
+int32_t qo_domain_w(const qo_camera *cam);
+int32_t qo_domain_h(const qo_camera *cam);
+void qo_zbuf_reset(int32_t *zbuf, const qo_camera *cam);
+/* Rasterise one face given its three projected vertices (u, v, z_mm).
+ * Updates the render AABB in box[4] = {minx,maxx,miny,maxy}.  Returns the
+ * number of pixel writes issued inside the domain. */
+int64_t qo_raster_face(const float v1[3], const float v2[3], const float v3[3],
+                       const qo_camera *cam, int32_t *zbuf, int32_t box[4]);
+/* Render a whole mesh (loadOBJ3 SoA layout, 9*F floats) at pose s. */
+int64_t qo_render(const float *mesh, uint32_t num_faces, const float *s,
+                  const qo_camera *cam, int32_t *zbuf, int32_t box[4]);
+
+/* ---- fitness ---- */
+void qo_score_zbuf(const int32_t *zbuf, const int32_t box[4], const uint16_t *obs,
+                   const qo_camera *cam, const qo_params *prm, qo_score *out);
+float qo_fitness_from_counts(uint32_t n_seg_not_rendered, uint32_t n_rendered,
+                             uint32_t n_no_obs, uint64_t sq_lo, uint64_t sq_hi,
+                             uint32_t num_points);
+double qo_fitness_fp64(const qo_score *sc, uint32_t num_points);
+
+/* ---- PSO ---- */
+void qo_init_particle(const qo_params *prm, uint32_t p, float *pos, float *vel, float *pbest);
+void qo_update_particle(const qo_params *prm, uint32_t p, uint32_t iter,
+                        float *pos, float *vel, const float *pbest, const float *gbest);
+
+/* Full solve.  Arrays are SoA [7][P] (index p + d*P) like main.cu:1389-1465.
+ * trace_gbest (optional) receives iterations x 8 floats (fit, pose[7]) after
+ * each best update; trace_fit (optional) receives iterations x P fitness. */
+typedef struct {
+    float gbest_fit;
+    float gbest[QO_NDIM];
+    uint64_t raster_writes;
+} qo_result;
+
+int qo_solve(const float *mesh, uint32_t num_faces, const uint16_t *obs,
+             const qo_camera *cam, const qo_params *prm,
+             float *pos, float *vel, float *pbest, float *pbest_fit,
+             qo_result *res, float *trace_gbest, float *trace_fit);
+
+void qo_default_params(qo_params *prm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,734 @@
+// qpso_api.cu -- host runtime behind the C ABI of include/qpso.h.
+//
+// The reference's host program (main.cu:1301-1780) allocates a 1.26 GB
+// per-particle render buffer, 16 streams and ~2k launches per iteration.
+// This runtime keeps meshes and frames resident behind integer ids, lays
+// every solve's state out in one grow-only device workspace, stages its
+// metadata through one pinned buffer (one H2D copy, one D2H copy per solve)
+// and runs the fused kernels of qpso_kernels.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "qpso.h"
+#include "qpso_internal.cuh"
+
+using namespace qpso;
+
+namespace {
+
+struct MeshObj {
+  float* d = nullptr;
+  uint32_t F = 0;
+  float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+struct FrameObj {
+  uint16_t* depth = nullptr;
+  int32_t* labels = nullptr;
+  qpso_camera cam{};
+};
+
+struct Buf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+// Offsets of one solve batch inside the device workspace and the pinned
+// staging buffer.  The metadata block (instances, headers, prep jobs, work
+// items) is contiguous so that one copy uploads it.
+struct Header {  // per instance, 64 bytes: result + counters read back once
+  float gbest[8];
+  uint32_t done;
+  uint32_t err;
+  unsigned long long stats[2];
+  uint32_t pad[2];
+};
+static_assert(sizeof(Header) == 64, "header layout");
+
+struct Layout {
+  size_t inst = 0, hdr = 0, prep = 0, items = 0, claim = 0, bar = 0, berr = 0, meta_end = 0;
+  size_t total = 0;
+  std::vector<size_t> obs, sat, pos, vel, pbest, pbf, fit, trace;
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct qpso_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  int smem_optin = 0;
+  std::string err;
+  std::unordered_map<uint32_t, MeshObj> meshes;
+  std::unordered_map<uint32_t, FrameObj> frames;
+  uint32_t next_id = 1;
+  TileConfig plain{256, 16384, 1};
+  TileConfig batch{256, 16384, 1};
+  Buf ws;    // device workspace
+  Buf pin;   // pinned host staging
+  // batched-launch graph cache
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<uint64_t> gkey;
+  std::mutex mu;
+};
+
+namespace {
+
+qpso_status fail(qpso_context* ctx, qpso_status st, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return st;
+}
+
+qpso_status cuda_fail(qpso_context* ctx, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(ctx, e == cudaErrorMemoryAllocation ? QPSO_ERR_NOMEM : QPSO_ERR_CUDA, m);
+}
+
+#define QPSO_CUDA(ctx, call)                                  \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
+  } while (0)
+
+qpso_status ensure_ws(qpso_context* ctx, size_t bytes) {
+  if (bytes <= ctx->ws.cap) return QPSO_OK;
+  if (ctx->ws.p) {
+    QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->ws.p);
+    ctx->ws.p = nullptr;
+    ctx->ws.cap = 0;
+  }
+  const size_t cap = align_up(bytes + bytes / 4, 1 << 20);
+  QPSO_CUDA(ctx, cudaMalloc(&ctx->ws.p, cap));
+  ctx->ws.cap = cap;
+  return QPSO_OK;
+}
+
+qpso_status ensure_pin(qpso_context* ctx, size_t bytes) {
+  if (bytes <= ctx->pin.cap) return QPSO_OK;
+  if (ctx->pin.p) {
+    QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFreeHost(ctx->pin.p);
+    ctx->pin.p = nullptr;
+    ctx->pin.cap = 0;
+  }
+  const size_t cap = align_up(bytes + bytes / 4, 1 << 16);
+  QPSO_CUDA(ctx, cudaMallocHost(&ctx->pin.p, cap));
+  ctx->pin.cap = cap;
+  return QPSO_OK;
+}
+
+bool valid_cfg(const qpso_launch_config& c, int smem_optin) {
+  return c.threads >= 32 && c.threads <= 1024 && c.threads % 32 == 0 && c.tile_px >= 64 &&
+         c.tile_px % 8 == 0 && (size_t)c.tile_px * 4 <= (size_t)smem_optin && c.ppb >= 1 &&
+         c.ppb <= 16;
+}
+
+qpso_status check_desc(qpso_context* ctx, const qpso_solve_desc& d, const MeshObj** m,
+                       const FrameObj** f) {
+  auto mi = ctx->meshes.find(d.mesh_id);
+  if (mi == ctx->meshes.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown mesh id");
+  auto fi = ctx->frames.find(d.frame_id);
+  if (fi == ctx->frames.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown frame id");
+  if (d.num_particles == 0 || d.num_particles > (1u << 20))
+    return fail(ctx, QPSO_ERR_ARG, "num_particles must be in [1, 2^20]");
+  if (d.iterations == 0 || d.iterations > (1u << 20))
+    return fail(ctx, QPSO_ERR_ARG, "iterations must be in [1, 2^20]");
+  if (d.num_points == 0) return fail(ctx, QPSO_ERR_ARG, "num_points must be > 0");
+  if (!(d.cl_min_x < d.cl_max_x && d.cl_min_y < d.cl_max_y))
+    return fail(ctx, QPSO_ERR_ARG, "cluster AABB must be non-empty (min < max)");
+  const qpso_camera& c = fi->second.cam;
+  if (d.cl_min_x < -kGuard || d.cl_max_x > c.width + kGuard || d.cl_min_y < -kGuard ||
+      d.cl_max_y > c.height + kGuard)
+    return fail(ctx, QPSO_ERR_ARG, "cluster AABB outside the raster domain");
+  if (d.cluster_label < 0 && d.cluster_label != -1)
+    return fail(ctx, QPSO_ERR_ARG, "cluster_label must be >= 0 or -1");
+  if (d.cluster_label >= 0 && fi->second.labels == nullptr)
+    return fail(ctx, QPSO_ERR_ARG, "frame has no label map");
+  for (int k = 0; k < 3; ++k)
+    if (!(d.t_lo[k] <= d.t_hi[k])) return fail(ctx, QPSO_ERR_ARG, "t_lo must be <= t_hi");
+  *m = &mi->second;
+  *f = &fi->second;
+  return QPSO_OK;
+}
+
+SolveParams to_params(const qpso_solve_desc& d) {
+  SolveParams p;
+  p.c1 = d.c1;
+  p.c2 = d.c2;
+  p.w = d.w;
+  p.vdot = d.vdot;
+  p.ang_lo = d.ang_lo;
+  p.ang_hi = d.ang_hi;
+  for (int k = 0; k < 4; ++k) p.qinit[k] = d.qinit[k];
+  for (int k = 0; k < 3; ++k) {
+    p.t_lo[k] = d.t_lo[k];
+    p.t_hi[k] = d.t_hi[k];
+  }
+  p.cl_min_x = d.cl_min_x;
+  p.cl_max_x = d.cl_max_x;
+  p.cl_min_y = d.cl_min_y;
+  p.cl_max_y = d.cl_max_y;
+  p.num_points = d.num_points;
+  p.num_particles = d.num_particles;
+  p.iterations = d.iterations;
+  p.seed = d.seed;
+  p.stream = d.stream;
+  return p;
+}
+
+Layout make_layout(const std::vector<const qpso_solve_desc*>& ds,
+                   const std::vector<const FrameObj*>& frames, uint32_t n_items, uint32_t max_iters,
+                   bool trace) {
+  Layout L;
+  const size_t n = ds.size();
+  size_t o = 0;
+  L.inst = o;
+  o = align_up(o + n * sizeof(Instance), 256);
+  L.hdr = o;
+  o = align_up(o + n * sizeof(Header), 256);
+  L.prep = o;
+  o = align_up(o + n * sizeof(PrepDesc), 256);
+  L.items = o;
+  o = align_up(o + (size_t)n_items * sizeof(WorkItem), 256);
+  L.claim = o;
+  o = align_up(o + (size_t)max_iters * sizeof(uint32_t), 256);
+  L.bar = o;
+  o = align_up(o + 2 * sizeof(uint32_t), 256);
+  L.berr = o;
+  o = align_up(o + sizeof(uint32_t), 256);
+  L.meta_end = o;
+  for (size_t i = 0; i < n; ++i) {
+    const qpso_camera& c = frames[i]->cam;
+    const size_t P = ds[i]->num_particles;
+    L.obs.push_back(o);
+    o = align_up(o + (size_t)c.width * c.height * sizeof(uint16_t), 256);
+    L.sat.push_back(o);
+    o = align_up(o + (size_t)(c.width + 1) * (c.height + 1) * sizeof(int32_t), 256);
+    L.pos.push_back(o);
+    o = align_up(o + 7 * P * sizeof(float), 256);
+    L.vel.push_back(o);
+    o = align_up(o + 7 * P * sizeof(float), 256);
+    L.pbest.push_back(o);
+    o = align_up(o + 7 * P * sizeof(float), 256);
+    L.pbf.push_back(o);
+    o = align_up(o + P * sizeof(float), 256);
+    L.fit.push_back(o);
+    o = align_up(o + P * sizeof(float), 256);
+    L.trace.push_back(o);
+    if (trace) o = align_up(o + (size_t)ds[i]->iterations * 8 * sizeof(float), 256);
+  }
+  L.total = o;
+  return L;
+}
+
+// Fill the pinned metadata block for a batch laid out by L.
+void fill_meta(qpso_context* ctx, const Layout& L, const std::vector<const qpso_solve_desc*>& ds,
+               const std::vector<const MeshObj*>& meshes, const std::vector<const FrameObj*>& frames,
+               const std::vector<WorkItem>& items, uint32_t ppb, bool trace) {
+  char* h = static_cast<char*>(ctx->pin.p);
+  char* d = static_cast<char*>(ctx->ws.p);
+  std::memset(h, 0, L.meta_end);
+  Instance* hi = reinterpret_cast<Instance*>(h + L.inst);
+  Header* hh = reinterpret_cast<Header*>(h + L.hdr);
+  PrepDesc* hp = reinterpret_cast<PrepDesc*>(h + L.prep);
+  for (size_t i = 0; i < ds.size(); ++i) {
+    const qpso_solve_desc& s = *ds[i];
+    const MeshObj& m = *meshes[i];
+    const FrameObj& f = *frames[i];
+    Instance& I = hi[i];
+    I.mesh = m.d;
+    I.F = m.F;
+    for (int k = 0; k < 3; ++k) {
+      I.mesh_lo[k] = m.lo[k];
+      I.mesh_hi[k] = m.hi[k];
+    }
+    I.obs = reinterpret_cast<const uint16_t*>(d + L.obs[i]);
+    I.sat = reinterpret_cast<const int32_t*>(d + L.sat[i]);
+    I.cam = Camera{f.cam.fx, f.cam.fy, f.cam.cx, f.cam.cy, f.cam.width, f.cam.height};
+    I.prm = to_params(s);
+    I.pos = reinterpret_cast<float*>(d + L.pos[i]);
+    I.vel = reinterpret_cast<float*>(d + L.vel[i]);
+    I.pbest = reinterpret_cast<float*>(d + L.pbest[i]);
+    I.pbest_fit = reinterpret_cast<float*>(d + L.pbf[i]);
+    I.fit = reinterpret_cast<float*>(d + L.fit[i]);
+    Header* dh = reinterpret_cast<Header*>(d + L.hdr) + i;
+    I.gbest = dh->gbest;
+    I.done = &dh->done;
+    I.err = &dh->err;
+    I.stats = dh->stats;
+    I.trace = trace ? reinterpret_cast<float*>(d + L.trace[i]) : nullptr;
+    I.ppb = ppb;
+    I.chunks = (s.num_particles + ppb - 1) / ppb;
+    hh[i].gbest[0] = kBestInit;
+    PrepDesc& p = hp[i];
+    p.depth = f.depth;
+    p.labels = (s.cluster_label >= 0) ? f.labels : nullptr;
+    p.label = s.cluster_label;
+    p.width = f.cam.width;
+    p.height = f.cam.height;
+    p.obs = reinterpret_cast<uint16_t*>(d + L.obs[i]);
+    p.sat = reinterpret_cast<int32_t*>(d + L.sat[i]);
+  }
+  if (!items.empty()) std::memcpy(h + L.items, items.data(), items.size() * sizeof(WorkItem));
+}
+
+qpso_status gather_descs(qpso_context* ctx, const qpso_solve_desc* descs, uint32_t n,
+                         std::vector<const qpso_solve_desc*>& ds, std::vector<const MeshObj*>& ms,
+                         std::vector<const FrameObj*>& fs) {
+  for (uint32_t i = 0; i < n; ++i) {
+    const MeshObj* m;
+    const FrameObj* f;
+    qpso_status st = check_desc(ctx, descs[i], &m, &f);
+    if (st != QPSO_OK) return st;
+    ds.push_back(&descs[i]);
+    ms.push_back(m);
+    fs.push_back(f);
+  }
+  return QPSO_OK;
+}
+
+void read_result(const Header& h, qpso_result* r) {
+  r->fit = h.gbest[0];
+  for (int k = 0; k < 7; ++k) r->pose[k] = h.gbest[1 + k];
+  r->flags = h.err;
+  r->reserved = 0;
+  r->raster_writes = h.stats[0];
+  r->tile_passes = h.stats[1];
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* qpso_version(void) { return "qpso-gb300 0.1 (sm_103a)"; }
+
+qpso_status qpso_create(int device, qpso_context** out) {
+  if (!out) return QPSO_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || device < 0 || device >= n) return QPSO_ERR_CUDA;
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return QPSO_ERR_CUDA;
+  qpso_context* ctx = new (std::nothrow) qpso_context();
+  if (!ctx) return QPSO_ERR_NOMEM;
+  ctx->device = device;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return QPSO_ERR_CUDA;
+  }
+  if (prop.major * 10 + prop.minor < 100) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return QPSO_ERR_CUDA;  // the kernels are built for sm_103a only
+  }
+  ctx->num_sms = prop.multiProcessorCount;
+  ctx->smem_optin = (int)prop.sharedMemPerBlockOptin - (int)smem_ctl_bytes() - 1024;
+  *out = ctx;
+  return QPSO_OK;
+}
+
+void qpso_destroy(qpso_context* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& kv : ctx->meshes) cudaFree(kv.second.d);
+  for (auto& kv : ctx->frames) {
+    cudaFree(kv.second.depth);
+    cudaFree(kv.second.labels);
+  }
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  if (ctx->ws.p) cudaFree(ctx->ws.p);
+  if (ctx->pin.p) cudaFreeHost(ctx->pin.p);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* qpso_last_error(const qpso_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+qpso_status qpso_mesh_upload(qpso_context* ctx, const float* soa, uint32_t F, uint32_t* mesh_id) {
+  if (!ctx || !soa || !mesh_id || F == 0 || F > (1u << 26)) return fail(ctx, QPSO_ERR_ARG, "bad mesh");
+  for (size_t i = 0; i < 9 * (size_t)F; ++i)
+    if (!std::isfinite(soa[i])) return fail(ctx, QPSO_ERR_ARG, "mesh has a non-finite coordinate");
+  cudaSetDevice(ctx->device);
+  MeshObj m;
+  m.F = F;
+  QPSO_CUDA(ctx, cudaMalloc(&m.d, 9 * (size_t)F * sizeof(float) + 32));
+  float* dbox = m.d + 9 * (size_t)F;
+  cudaError_t e = cudaMemcpyAsync(m.d, soa, 9 * (size_t)F * sizeof(float), cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  if (e == cudaSuccess) e = launch_mesh_aabb(m.d, F, dbox, ctx->stream);
+  float box[6];
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(box, dbox, sizeof(box), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(m.d);
+    return cuda_fail(ctx, e, "mesh upload");
+  }
+  for (int k = 0; k < 3; ++k) {
+    m.lo[k] = box[k];
+    m.hi[k] = box[3 + k];
+  }
+  std::lock_guard<std::mutex> g(ctx->mu);
+  *mesh_id = ctx->next_id++;
+  ctx->meshes[*mesh_id] = m;
+  return QPSO_OK;
+}
+
+qpso_status qpso_mesh_release(qpso_context* ctx, uint32_t id) {
+  if (!ctx) return QPSO_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  auto it = ctx->meshes.find(id);
+  if (it == ctx->meshes.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown mesh id");
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(it->second.d);
+  ctx->meshes.erase(it);
+  return QPSO_OK;
+}
+
+qpso_status qpso_frame_upload(qpso_context* ctx, const uint16_t* depth, const int32_t* labels,
+                              const qpso_camera* cam, uint32_t* frame_id) {
+  if (!ctx || !depth || !cam || !frame_id) return fail(ctx, QPSO_ERR_ARG, "null argument");
+  if (cam->width <= 0 || cam->height <= 0 || cam->width > 8192 || cam->height > 8192)
+    return fail(ctx, QPSO_ERR_ARG, "frame size must be in [1, 8192]");
+  if (!(std::isfinite(cam->fx) && std::isfinite(cam->fy) && std::isfinite(cam->cx) &&
+        std::isfinite(cam->cy)))
+    return fail(ctx, QPSO_ERR_ARG, "non-finite intrinsics");
+  cudaSetDevice(ctx->device);
+  FrameObj f;
+  f.cam = *cam;
+  const size_t npx = (size_t)cam->width * cam->height;
+  QPSO_CUDA(ctx, cudaMalloc(&f.depth, npx * sizeof(uint16_t)));
+  cudaError_t e = cudaMemcpyAsync(f.depth, depth, npx * sizeof(uint16_t), cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  if (e == cudaSuccess && labels) {
+    e = cudaMalloc(&f.labels, npx * sizeof(int32_t));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(f.labels, labels, npx * sizeof(int32_t), cudaMemcpyHostToDevice,
+                          ctx->stream);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(f.depth);
+    if (f.labels) cudaFree(f.labels);
+    return cuda_fail(ctx, e, "frame upload");
+  }
+  std::lock_guard<std::mutex> g(ctx->mu);
+  *frame_id = ctx->next_id++;
+  ctx->frames[*frame_id] = f;
+  return QPSO_OK;
+}
+
+qpso_status qpso_frame_release(qpso_context* ctx, uint32_t id) {
+  if (!ctx) return QPSO_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  auto it = ctx->frames.find(id);
+  if (it == ctx->frames.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown frame id");
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(it->second.depth);
+  if (it->second.labels) cudaFree(it->second.labels);
+  ctx->frames.erase(it);
+  return QPSO_OK;
+}
+
+void qpso_solve_desc_init(qpso_solve_desc* d) {
+  if (!d) return;
+  std::memset(d, 0, sizeof(*d));
+  d->cluster_label = -1;
+  d->num_particles = 1024;  // Nparticle_, main.h:84
+  d->iterations = 20;       // max_steps_, main.h:99
+  d->c1 = 1.0f;             // c1_, main.h:104
+  d->c2 = 1.0f;             // c2_, main.h:105
+  d->w = 0.3;               // psoW_, main.h:106
+  d->vdot = 3.0f;           // vdot_, main.h:126
+  d->ang_lo = -10.0f;       // aminX_, main.h:118
+  d->ang_hi = 10.0f;        // amaxX_, main.h:119
+  d->qinit[0] = 0.7071f;    // main.cu:130
+  d->qinit[1] = 0.7071f;
+  d->qinit[2] = 0.0f;
+  d->qinit[3] = 0.0f;
+}
+
+void qpso_box_from_centroid(const float c_mm[3], float bound, float bound_z, float lo[3],
+                            float hi[3]) {
+  for (int k = 0; k < 3; ++k) {
+    const float c = c_mm[k] * 0.001f;
+    const float b = (k == 2) ? bound_z : bound;
+    lo[k] = c - b;
+    hi[k] = c + b;
+  }
+}
+
+qpso_status qpso_set_launch_config(qpso_context* ctx, const qpso_launch_config* plain,
+                                   const qpso_launch_config* batch) {
+  if (!ctx) return QPSO_ERR_ARG;
+  if (plain && !valid_cfg(*plain, ctx->smem_optin)) return fail(ctx, QPSO_ERR_ARG, "bad plain launch config");
+  if (batch && !valid_cfg(*batch, ctx->smem_optin)) return fail(ctx, QPSO_ERR_ARG, "bad batch launch config");
+  if (plain) ctx->plain = TileConfig{plain->threads, plain->tile_px, plain->ppb};
+  if (batch) ctx->batch = TileConfig{batch->threads, batch->tile_px, batch->ppb};
+  return QPSO_OK;
+}
+
+qpso_status qpso_get_launch_config(const qpso_context* ctx, qpso_launch_config* plain,
+                                   qpso_launch_config* batch) {
+  if (!ctx) return QPSO_ERR_ARG;
+  if (plain) *plain = qpso_launch_config{ctx->plain.threads, ctx->plain.tile_px, ctx->plain.ppb};
+  if (batch) *batch = qpso_launch_config{ctx->batch.threads, ctx->batch.tile_px, ctx->batch.ppb};
+  return QPSO_OK;
+}
+
+qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qpso_result* result,
+                              float* trace, float* pos, float* vel, float* pbest, float* pbest_fit) {
+  if (!ctx || !desc || !result) return fail(ctx, QPSO_ERR_ARG, "null argument");
+  cudaSetDevice(ctx->device);
+  std::vector<const qpso_solve_desc*> ds;
+  std::vector<const MeshObj*> ms;
+  std::vector<const FrameObj*> fs;
+  qpso_status st = gather_descs(ctx, desc, 1, ds, ms, fs);
+  if (st != QPSO_OK) return st;
+  const TileConfig cfg = ctx->plain;
+  const bool want_trace = trace != nullptr;
+  Layout L = make_layout(ds, fs, 0, 0, want_trace);
+  if ((st = ensure_ws(ctx, L.total)) != QPSO_OK) return st;
+  if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
+  fill_meta(ctx, L, ds, ms, fs, {}, (uint32_t)cfg.ppb, want_trace);
+  char* d = static_cast<char*>(ctx->ws.p);
+  char* h = static_cast<char*>(ctx->pin.p);
+  cudaStream_t s = ctx->stream;
+  QPSO_CUDA(ctx, cudaMemcpyAsync(d, h, L.meta_end, cudaMemcpyHostToDevice, s));
+  QPSO_CUDA(ctx, launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), 1, fs[0]->cam.width,
+                             fs[0]->cam.height, s));
+  const Instance* dinst = reinterpret_cast<const Instance*>(d + L.inst);
+  const uint32_t chunks = (desc->num_particles + cfg.ppb - 1) / cfg.ppb;
+  for (uint32_t it = 0; it < desc->iterations; ++it)
+    QPSO_CUDA(ctx, launch_step(dinst, it, chunks, cfg, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
+  const size_t P = desc->num_particles;
+  if (trace)
+    QPSO_CUDA(ctx, cudaMemcpyAsync(trace, d + L.trace[0], desc->iterations * 8 * sizeof(float),
+                                   cudaMemcpyDeviceToHost, s));
+  if (pos) QPSO_CUDA(ctx, cudaMemcpyAsync(pos, d + L.pos[0], 7 * P * 4, cudaMemcpyDeviceToHost, s));
+  if (vel) QPSO_CUDA(ctx, cudaMemcpyAsync(vel, d + L.vel[0], 7 * P * 4, cudaMemcpyDeviceToHost, s));
+  if (pbest)
+    QPSO_CUDA(ctx, cudaMemcpyAsync(pbest, d + L.pbest[0], 7 * P * 4, cudaMemcpyDeviceToHost, s));
+  if (pbest_fit)
+    QPSO_CUDA(ctx, cudaMemcpyAsync(pbest_fit, d + L.pbf[0], P * 4, cudaMemcpyDeviceToHost, s));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  const Header& hd = *reinterpret_cast<const Header*>(h + L.hdr);
+  read_result(hd, result);
+  if (hd.err & kErrBound) return fail(ctx, QPSO_ERR_INTERNAL, "raster bound violated");
+  return QPSO_OK;
+}
+
+qpso_status qpso_solve(qpso_context* ctx, const qpso_solve_desc* desc, qpso_result* result) {
+  return qpso_solve_traced(ctx, desc, result, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, uint32_t n,
+                             qpso_result* results) {
+  if (!ctx || !descs || !results || n == 0) return fail(ctx, QPSO_ERR_ARG, "bad batch arguments");
+  cudaSetDevice(ctx->device);
+  std::vector<const qpso_solve_desc*> ds;
+  std::vector<const MeshObj*> ms;
+  std::vector<const FrameObj*> fs;
+  qpso_status st = gather_descs(ctx, descs, n, ds, ms, fs);
+  if (st != QPSO_OK) return st;
+  const TileConfig cfg = ctx->batch;
+  // work items: every chunk of every instance, most expensive first
+  std::vector<uint32_t> order(n);
+  std::vector<double> cost(n);
+  uint32_t max_iters = 0, max_w = 0, max_h = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    order[i] = i;
+    const double area = (double)(ds[i]->cl_max_x - ds[i]->cl_min_x) * (ds[i]->cl_max_y - ds[i]->cl_min_y);
+    cost[i] = (double)ms[i]->F * 3.0 + area;
+    max_iters = std::max(max_iters, ds[i]->iterations);
+    max_w = std::max(max_w, (uint32_t)fs[i]->cam.width);
+    max_h = std::max(max_h, (uint32_t)fs[i]->cam.height);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+  std::vector<WorkItem> items;
+  for (uint32_t i : order) {
+    const uint32_t chunks = (ds[i]->num_particles + cfg.ppb - 1) / cfg.ppb;
+    for (uint32_t c = 0; c < chunks; ++c) items.push_back(WorkItem{i, c});
+  }
+  Layout L = make_layout(ds, fs, (uint32_t)items.size(), max_iters, false);
+  if ((st = ensure_ws(ctx, L.total)) != QPSO_OK) return st;
+  if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
+  int per_sm = 0;
+  QPSO_CUDA(ctx, batch_max_grid(cfg, &per_sm));
+  if (per_sm <= 0) return fail(ctx, QPSO_ERR_ARG, "batch launch config does not fit on an SM");
+  const int grid = (int)std::min<size_t>(items.size(), (size_t)per_sm * ctx->num_sms);
+  // wait before touching pinned staging that an earlier graph may read
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  fill_meta(ctx, L, ds, ms, fs, items, (uint32_t)cfg.ppb, false);
+  char* d = static_cast<char*>(ctx->ws.p);
+  char* h = static_cast<char*>(ctx->pin.p);
+  cudaStream_t s = ctx->stream;
+  std::vector<uint64_t> key = {(uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)h, L.total, L.meta_end,
+                               n, items.size(), max_iters, (uint64_t)grid, (uint64_t)cfg.threads,
+                               (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h};
+  if (!ctx->gexec || key != ctx->gkey) {
+    if (ctx->gexec) {
+      cudaGraphExecDestroy(ctx->gexec);
+      ctx->gexec = nullptr;
+    }
+    BatchArgs A;
+    A.inst = reinterpret_cast<Instance*>(d + L.inst);
+    A.items = reinterpret_cast<const WorkItem*>(d + L.items);
+    A.n_items = (uint32_t)items.size();
+    A.step_claim = reinterpret_cast<uint32_t*>(d + L.claim);
+    A.barrier = reinterpret_cast<uint32_t*>(d + L.bar);
+    A.err = reinterpret_cast<uint32_t*>(d + L.berr);
+    A.max_iters = max_iters;
+    A.timeout_ns = 20ull * 1000 * 1000 * 1000;  // 20 s per barrier
+    cudaGraph_t graph;
+    QPSO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemcpyAsync(d, h, L.meta_end, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), (int)n, (int)max_w, (int)max_h, s);
+    if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h + L.hdr, d + L.hdr, n * sizeof(Header), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h + L.berr, d + L.berr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batch capture");
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "batch capture end");
+    e = cudaGraphInstantiate(&ctx->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      ctx->gexec = nullptr;
+      return cuda_fail(ctx, e, "graph instantiate");
+    }
+    ctx->gkey = key;
+  }
+  QPSO_CUDA(ctx, cudaGraphLaunch(ctx->gexec, s));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  const Header* hh = reinterpret_cast<const Header*>(h + L.hdr);
+  bool bad = false;
+  for (uint32_t i = 0; i < n; ++i) {
+    read_result(hh[i], &results[i]);
+    bad = bad || (hh[i].err & kErrBound);
+  }
+  const uint32_t berr = *reinterpret_cast<const uint32_t*>(h + L.berr);
+  if (berr & kErrTimeout) return fail(ctx, QPSO_ERR_TIMEOUT, "batch barrier timed out");
+  if (bad) return fail(ctx, QPSO_ERR_INTERNAL, "raster bound violated");
+  return QPSO_OK;
+}
+
+qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, const float* poses,
+                             uint32_t n, float* fit_out) {
+  if (!ctx || !desc || !poses || !fit_out || n == 0) return fail(ctx, QPSO_ERR_ARG, "null argument");
+  cudaSetDevice(ctx->device);
+  std::vector<const qpso_solve_desc*> ds;
+  std::vector<const MeshObj*> ms;
+  std::vector<const FrameObj*> fs;
+  qpso_status st = gather_descs(ctx, desc, 1, ds, ms, fs);
+  if (st != QPSO_OK) return st;
+  Layout L = make_layout(ds, fs, 0, 0, false);
+  const size_t pose_off = align_up(L.total, 256);
+  const size_t fit_off = align_up(pose_off + (size_t)n * 7 * sizeof(float), 256);
+  const size_t total = align_up(fit_off + (size_t)n * sizeof(float), 256);
+  if ((st = ensure_ws(ctx, total)) != QPSO_OK) return st;
+  if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  fill_meta(ctx, L, ds, ms, fs, {}, 1, false);
+  char* d = static_cast<char*>(ctx->ws.p);
+  char* h = static_cast<char*>(ctx->pin.p);
+  cudaStream_t s = ctx->stream;
+  QPSO_CUDA(ctx, cudaMemcpyAsync(d, h, L.meta_end, cudaMemcpyHostToDevice, s));
+  QPSO_CUDA(ctx, launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), 1, fs[0]->cam.width,
+                             fs[0]->cam.height, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(d + pose_off, poses, (size_t)n * 7 * sizeof(float),
+                                 cudaMemcpyHostToDevice, s));
+  const int grid = (int)std::min<uint32_t>(n, (uint32_t)ctx->num_sms * 4);
+  QPSO_CUDA(ctx, launch_score(reinterpret_cast<const Instance*>(d + L.inst),
+                              reinterpret_cast<const float*>(d + pose_off), n,
+                              reinterpret_cast<float*>(d + fit_off), ctx->plain, grid, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(fit_out, d + fit_off, (size_t)n * sizeof(float),
+                                 cudaMemcpyDeviceToHost, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  const Header& hd = *reinterpret_cast<const Header*>(h + L.hdr);
+  if (hd.err & kErrBound) return fail(ctx, QPSO_ERR_INTERNAL, "raster bound violated");
+  return QPSO_OK;
+}
+
+qpso_status qpso_render(qpso_context* ctx, uint32_t mesh_id, const qpso_camera* cam,
+                        const float pose[7], int32_t x0, int32_t y0, int32_t w, int32_t h,
+                        int32_t* depth_out, int32_t box_out[4]) {
+  if (!ctx || !cam || !pose || !depth_out || !box_out || w <= 0 || h <= 0 || w % 4 != 0)
+    return fail(ctx, QPSO_ERR_ARG, "bad render arguments (w must be a positive multiple of 4)");
+  if ((size_t)w * h * 4 > (size_t)ctx->smem_optin)
+    return fail(ctx, QPSO_ERR_ARG, "render window exceeds one CTA's shared memory");
+  auto mi = ctx->meshes.find(mesh_id);
+  if (mi == ctx->meshes.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown mesh id");
+  cudaSetDevice(ctx->device);
+  const MeshObj& m = mi->second;
+  const size_t inst_off = 0, pose_off = 256, box_off = 512, out_off = 1024;
+  const size_t total = out_off + (size_t)w * h * 4;
+  qpso_status st;
+  if ((st = ensure_ws(ctx, total)) != QPSO_OK) return st;
+  if ((st = ensure_pin(ctx, 1024)) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  char* d = static_cast<char*>(ctx->ws.p);
+  char* hp = static_cast<char*>(ctx->pin.p);
+  std::memset(hp, 0, 1024);
+  Instance& I = *reinterpret_cast<Instance*>(hp + inst_off);
+  I.mesh = m.d;
+  I.F = m.F;
+  for (int k = 0; k < 3; ++k) {
+    I.mesh_lo[k] = m.lo[k];
+    I.mesh_hi[k] = m.hi[k];
+  }
+  I.cam = Camera{cam->fx, cam->fy, cam->cx, cam->cy, cam->width, cam->height};
+  std::memcpy(hp + pose_off, pose, 7 * sizeof(float));
+  cudaStream_t s = ctx->stream;
+  QPSO_CUDA(ctx, cudaMemcpyAsync(d, hp, 1024, cudaMemcpyHostToDevice, s));
+  QPSO_CUDA(ctx, launch_render_window(reinterpret_cast<const Instance*>(d + inst_off),
+                                      reinterpret_cast<const float*>(d + pose_off), x0, y0, w, h,
+                                      reinterpret_cast<int32_t*>(d + out_off),
+                                      reinterpret_cast<int32_t*>(d + box_off), 256, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(depth_out, d + out_off, (size_t)w * h * 4, cudaMemcpyDeviceToHost, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(box_out, d + box_off, 16, cudaMemcpyDeviceToHost, s));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  return QPSO_OK;
+}
+
+qpso_status qpso_barrier_selftest(qpso_context* ctx, uint64_t timeout_ns, uint32_t* err_bits) {
+  if (!ctx || !err_bits || timeout_ns == 0 || timeout_ns > 10ull * 1000 * 1000 * 1000)
+    return fail(ctx, QPSO_ERR_ARG, "timeout must be in (0, 10 s]");
+  cudaSetDevice(ctx->device);
+  qpso_status st;
+  if ((st = ensure_ws(ctx, 256)) != QPSO_OK) return st;
+  if ((st = ensure_pin(ctx, 16)) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  uint32_t* d = static_cast<uint32_t*>(ctx->ws.p);
+  cudaStream_t s = ctx->stream;
+  QPSO_CUDA(ctx, cudaMemsetAsync(d, 0, 16, s));
+  // two CTAs arrive, three are expected: both waits must expire
+  QPSO_CUDA(ctx, launch_barrier_probe(d, d + 2, 2, 3, timeout_ns, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(ctx->pin.p, d + 2, 4, cudaMemcpyDeviceToHost, s));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  *err_bits = *static_cast<uint32_t*>(ctx->pin.p);
+  return (*err_bits & kErrTimeout) ? QPSO_ERR_TIMEOUT : QPSO_OK;
+}
+
+}  // extern "C"

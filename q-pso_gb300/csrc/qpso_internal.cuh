@@ -1,0 +1,95 @@
+// qpso_internal.cuh -- device-resident instance layout shared by the kernels
+// (qpso_kernels.cu) and the host runtime (qpso_api.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "qpso_device.cuh"
+
+namespace qpso {
+
+// Error bits reported through Instance::err.
+enum : uint32_t {
+  kErrBound = 1u << 0,     // a face wrote outside its conservative tile bound
+  kErrTimeout = 1u << 1,   // a bounded inter-CTA wait gave up
+  kErrArg = 1u << 2,       // bad launch arguments detected on the device
+};
+
+// One solve instance as the kernels see it (one cluster x mesh x swarm).
+// Particle state is SoA [7][P] (index p + d*P), like main.cu:1389-1465.
+struct Instance {
+  const float* mesh;        // loadOBJ3 layout, 9*F floats (main.h:620-679)
+  uint32_t F;
+  float mesh_lo[3], mesh_hi[3];
+  const uint16_t* obs;      // cluster-masked observed depth (mm), width*height
+  const int32_t* sat;       // (height+1) x (width+1) counts of obs != 0
+  Camera cam;
+  SolveParams prm;
+  float* pos;
+  float* vel;
+  float* pbest;
+  float* pbest_fit;         // [P]
+  float* fit;               // [P] fitness of the current iteration
+  float* gbest;             // [8]: fitness, pose[7]
+  uint32_t* done;           // CTAs finished in the current iteration
+  uint32_t* err;            // error bits
+  unsigned long long* stats;  // [0] raster pixel writes, [1] tile passes
+  float* trace;             // optional [iterations][8] gbest after each iteration
+  uint32_t chunks;          // CTAs (work items) per iteration
+  uint32_t ppb;             // particles per work item
+};
+
+// Launch-shape knobs chosen by the tuner.
+struct TileConfig {
+  int threads;      // CTA size
+  int tile_px;      // int32 depth tile capacity (pixels); a multiple of 8
+  int ppb;          // particles per work item
+};
+
+// Work item of the persistent batched kernel: one chunk of one instance.
+struct WorkItem {
+  uint32_t inst;
+  uint32_t chunk;
+};
+
+// Per-instance preparation job: mask the frame to the cluster and build
+// the summed-area table of observed pixels.
+struct PrepDesc {
+  const uint16_t* depth;
+  const int32_t* labels;    // nullable: depth is already masked
+  int32_t label;
+  int32_t width, height;
+  uint16_t* obs;
+  int32_t* sat;
+};
+
+struct BatchArgs {
+  Instance* inst;           // device array of instances
+  const WorkItem* items;    // every chunk of every instance, largest first
+  uint32_t n_items;
+  uint32_t* step_claim;     // [max_iters] work-claim counters (zeroed)
+  uint32_t* barrier;        // [2] arrival counter, generation (zeroed)
+  uint32_t* err;            // batch-level error bits (zeroed)
+  uint32_t max_iters;
+  unsigned long long timeout_ns;
+};
+
+// Host-side launch wrappers (defined in qpso_kernels.cu).
+cudaError_t launch_prep(const PrepDesc* jobs, int n, int max_w, int max_h, cudaStream_t st);
+cudaError_t launch_mesh_aabb(const float* mesh, uint32_t F, float* out, cudaStream_t st);
+cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, const TileConfig& cfg,
+                        cudaStream_t st);
+cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st);
+cudaError_t batch_max_grid(const TileConfig& cfg, int* blocks_per_sm);
+cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
+                         const TileConfig& cfg, int grid, cudaStream_t st);
+cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_t x0, int32_t y0,
+                                 int32_t w, int32_t h, int32_t* out, int32_t* box, int threads,
+                                 cudaStream_t st);
+cudaError_t launch_barrier_probe(uint32_t* bar, uint32_t* err, uint32_t grid, uint32_t expected,
+                                 unsigned long long timeout_ns, cudaStream_t st);
+size_t smem_ctl_bytes();
+
+}  // namespace qpso

@@ -1,0 +1,824 @@
+// qpso_kernels.cu -- the fused Q-PSO iteration on sm_103a.
+//
+// One work item = one chunk of `ppb` particles of one solve instance, run by
+// one CTA.  Per item: the PSO step (InitQPSO main.cu:72-198 on the first
+// iteration, UpdateParticlesEquationKernel main.cu:858-1060 afterwards),
+// then per particle the transform + fixed-point raster into an int32 depth
+// tile in shared memory (RenderFixedPointKernelAABB main.cu:305-419,
+// renderFixedPointAABB main.h:1306-1491, smem atomicMin instead of global
+// atomics into a 1.2 MB-per-particle buffer), the render AABB
+// (ComputeAABBFinalReductionKernel main.cu:423-546, here a warp-shuffle
+// reduction), the fitness (ComputeFitnessKernel main.cu:550-764) and the
+// personal best.  The CTA that finishes an instance's last chunk of an
+// iteration does the argmin and the global best (thrust::min_element +
+// UpdatePersonalAndGlobalBest, main.cu:1691-1704, 768-855).
+//
+// Fitness counting.  The reference walks every pixel of the window
+// (render AABB union cluster AABB) and counts, per pixel, rendered /
+// observed combinations.  Pixels outside the render AABB are never
+// rendered, so their only contribution is "observed but not rendered".
+// Here the number of observed pixels in the window comes from a
+// summed-area table of (obs != 0) in O(1), and only the tile pixels (a
+// conservative superset of the rendered ones) are scanned:
+//   n_seg_not_rendered = observed(window) - observed_and_rendered.
+// Every count is an exact integer, so the result equals the direct walk.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "qpso_internal.cuh"
+
+namespace qpso {
+
+constexpr int kMaxPpb = 16;
+constexpr int kMaxThreads = 1024;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void add128(uint64_t& lo, uint64_t& hi, uint64_t v) {
+  lo += v;
+  hi += (lo < v) ? 1ull : 0ull;
+}
+
+struct Partial {
+  uint32_t nR, nNo, nSegR;
+  uint64_t lo, hi;
+  int32_t rminx, rmaxx, rminy, rmaxy;
+  unsigned long long writes;
+};
+
+__device__ __forceinline__ void warp_reduce(Partial& a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a.nR += __shfl_xor_sync(0xffffffffu, a.nR, o);
+    a.nNo += __shfl_xor_sync(0xffffffffu, a.nNo, o);
+    a.nSegR += __shfl_xor_sync(0xffffffffu, a.nSegR, o);
+    const uint64_t lo = __shfl_xor_sync(0xffffffffu, a.lo, o);
+    const uint64_t hi = __shfl_xor_sync(0xffffffffu, a.hi, o);
+    a.hi += hi;
+    add128(a.lo, a.hi, lo);
+    a.rminx = min(a.rminx, __shfl_xor_sync(0xffffffffu, a.rminx, o));
+    a.rmaxx = max(a.rmaxx, __shfl_xor_sync(0xffffffffu, a.rmaxx, o));
+    a.rminy = min(a.rminy, __shfl_xor_sync(0xffffffffu, a.rminy, o));
+    a.rmaxy = max(a.rmaxy, __shfl_xor_sync(0xffffffffu, a.rmaxy, o));
+    a.writes += __shfl_xor_sync(0xffffffffu, a.writes, o);
+  }
+}
+
+// Observed pixels (obs != 0) in [x0,x1) x [y0,y1), clipped to the image.
+__device__ __forceinline__ uint32_t sat_count(const int32_t* sat, int32_t w, int32_t h, int64_t x0,
+                                              int64_t x1, int64_t y0, int64_t y1) {
+  x0 = x0 < 0 ? 0 : (x0 > w ? w : x0);
+  x1 = x1 < 0 ? 0 : (x1 > w ? w : x1);
+  y0 = y0 < 0 ? 0 : (y0 > h ? h : y0);
+  y1 = y1 < 0 ? 0 : (y1 > h ? h : y1);
+  if (x0 >= x1 || y0 >= y1) return 0;
+  const int64_t W1 = (int64_t)w + 1;
+  const int32_t a = __ldg(sat + y1 * W1 + x1), b = __ldg(sat + y0 * W1 + x1);
+  const int32_t c = __ldg(sat + y1 * W1 + x0), d = __ldg(sat + y0 * W1 + x0);
+  return (uint32_t)(a - b - c + d);
+}
+
+struct SmemCtl {
+  float pose[kMaxPpb][8];
+  int32_t bound[4];
+  uint32_t claim;
+  int last;
+  Partial warp[kMaxThreads / 32];
+  float argv[kMaxThreads / 32];
+  uint32_t argi[kMaxThreads / 32];
+};
+
+// Conservative pixel bound of every face's raster rectangle at pose s: the
+// mesh AABB's eight corners, projected (all at least 5 cm in front of the
+// camera, so float error stays far below the 1 px margin), bound every
+// projected vertex because x/z is linear-fractional.  Falls back to the
+// whole raster domain.
+__device__ void pose_bound(const Instance& I, const float* s, int32_t b[4]) {
+  const int32_t dx0 = -kGuard, dx1 = I.cam.width + kGuard;
+  const int32_t dy0 = -kGuard, dy1 = I.cam.height + kGuard;
+  float ulo = 3.0e38f, uhi = -3.0e38f, vlo = 3.0e38f, vhi = -3.0e38f;
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const float x = (c & 1) ? I.mesh_hi[0] : I.mesh_lo[0];
+    const float y = (c & 2) ? I.mesh_hi[1] : I.mesh_lo[1];
+    const float z = (c & 4) ? I.mesh_hi[2] : I.mesh_lo[2];
+    float u, v, zz;
+    project(s, x, y, z, I.cam, u, v, zz);
+    ok = ok && (zz >= 50.0f);  // 50 mm
+    ulo = fminf(ulo, u);
+    uhi = fmaxf(uhi, u);
+    vlo = fminf(vlo, v);
+    vhi = fmaxf(vhi, v);
+  }
+  if (!ok || !(ulo == ulo) || !(vlo == vlo) || !(uhi == uhi) || !(vhi == vhi)) {
+    b[0] = dx0; b[1] = dx1; b[2] = dy0; b[3] = dy1;
+    return;
+  }
+  const float fx0 = fmaxf(floorf(ulo) - 1.0f, (float)dx0), fx1 = fminf(floorf(uhi) + 2.0f, (float)dx1);
+  const float fy0 = fmaxf(floorf(vlo) - 1.0f, (float)dy0), fy1 = fminf(floorf(vhi) + 2.0f, (float)dy1);
+  b[0] = (int32_t)fx0;
+  b[1] = (int32_t)fx1;
+  b[2] = (int32_t)fy0;
+  b[3] = (int32_t)fy1;
+  if (b[1] < b[0]) b[1] = b[0];
+  if (b[3] < b[2]) b[3] = b[2];
+}
+
+// Render + score one particle whose pose sits in shared memory.  All
+// threads of the CTA call this.  Returns the fitness on thread 0.
+__device__ float render_score(const Instance& I, const float* s, int32_t* tile, int tile_px,
+                              SmemCtl& ctl) {
+  const int tid = threadIdx.x, T = blockDim.x;
+  const int32_t W = I.cam.width, H = I.cam.height;
+  const int32_t dx0 = -kGuard, dx1 = W + kGuard, dy0 = -kGuard, dy1 = H + kGuard;
+  if (tid == 0) pose_bound(I, s, ctl.bound);
+  __syncthreads();
+  const int32_t bx0 = ctl.bound[0], bx1 = ctl.bound[1], by0 = ctl.bound[2], by1 = ctl.bound[3];
+
+  // tiling of the bound: columns in chunks of cw (multiple of 8), rows in
+  // bands of th so that cw * th <= tile_px
+  const int32_t tx0 = bx0 & ~7;  // floor to a multiple of 8 (two's complement)
+  const int32_t tw = ((bx1 - tx0) + 7) & ~7;
+  const int32_t bh = by1 - by0;
+  int32_t cw = tw < tile_px ? tw : (tile_px & ~7);
+  if (cw < 8) cw = 8;
+  const int32_t th = tile_px / cw;
+  const int32_t ncol = tw > 0 ? (tw + cw - 1) / cw : 0;
+  const int32_t nrow = (bh > 0 && th > 0) ? (bh + th - 1) / th : 0;
+  const int32_t npass = (ncol * nrow) > 0 ? ncol * nrow : 1;  // >= 1 pass for the AABB
+
+  Partial acc;
+  acc.nR = acc.nNo = acc.nSegR = 0;
+  acc.lo = acc.hi = 0;
+  acc.rminx = kAabbInitMin;
+  acc.rmaxx = kAabbInitMax;
+  acc.rminy = kAabbInitMin;
+  acc.rmaxy = kAabbInitMax;
+  acc.writes = 0;
+  bool bound_violation = false;
+
+  const uint32_t F = I.F;
+  const float* __restrict__ mesh = I.mesh;
+  const uint16_t* __restrict__ obs = I.obs;
+  const bool vec_obs = (W & 3) == 0;
+
+  for (int32_t pass = 0; pass < npass; ++pass) {
+    int32_t x0 = 0, y0 = 0, cwp = 0, thp = 0;
+    if (ncol * nrow > 0) {
+      const int32_t pr = pass / ncol, pc = pass - pr * ncol;
+      x0 = tx0 + pc * cw;
+      y0 = by0 + pr * th;
+      cwp = min(cw, tx0 + tw - x0);
+      thp = min(th, by1 - y0);
+    }
+    const int32_t npx = cwp * thp;
+    // fill with the background depth, 16 bytes per store
+    {
+      int4* t4 = reinterpret_cast<int4*>(tile);
+      const int4 bg = make_int4(kDepthBg, kDepthBg, kDepthBg, kDepthBg);
+      for (int i = tid; i < (npx >> 2); i += T) t4[i] = bg;
+    }
+    __syncthreads();
+    for (uint32_t f = tid; f < F; f += T) {
+      float u[3], v[3], z[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float mx = __ldg(mesh + f + (size_t)j * F);
+        const float my = __ldg(mesh + f + (size_t)(3 + j) * F);
+        const float mz = __ldg(mesh + f + (size_t)(6 + j) * F);
+        project(s, mx, my, mz, I.cam, u[j], v[j], z[j]);
+      }
+      FaceSetup fs;
+      setup_face(u[0], v[0], z[0], u[1], v[1], z[1], u[2], v[2], z[2], fs);
+      if (pass == 0) {
+        acc.rminx = min(acc.rminx, fs.minx);
+        acc.rmaxx = max(acc.rmaxx, fs.maxx);
+        acc.rminy = min(acc.rminy, fs.miny);
+        acc.rmaxy = max(acc.rmaxy, fs.maxy);
+      }
+      if (!fs.live) continue;
+      if (pass == 0) {
+        // the rectangle inside the domain must lie inside the bound
+        const int32_t ca = max(fs.minx, dx0), cb = min(fs.maxx, dx1);
+        const int32_t ra = max(fs.miny, dy0), rb = min(fs.maxy, dy1);
+        if (ca < cb && ra < rb && (ca < bx0 || cb > bx1 || ra < by0 || rb > by1))
+          bound_violation = true;
+      }
+      const int32_t xa = max(fs.minx, x0), xb = min(fs.maxx, x0 + cwp);
+      const int32_t ya = max(fs.miny, y0), yb = min(fs.maxy, y0 + thp);
+      if (xa >= xb || ya >= yb) continue;
+      acc.writes += (unsigned long long)(xb - xa) * (unsigned long long)(yb - ya);
+      const int32_t rx0 = xa - fs.minx;
+      for (int32_t y = ya; y < yb; ++y) {
+        const int32_t ry = y - fs.miny;
+        int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
+        int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
+        int32_t* row = tile + (y - y0) * cwp - x0;
+        for (int32_t x = xa; x < xb; ++x) {
+          const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+          const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+          float depth = fs.z1;
+          depth = depth + (float)cx2 * fs.z2;
+          depth = depth + (float)cx3 * fs.z3;
+          const int32_t d = __float2int_rn(depth);
+          if (d < kDepthBg) atomicMin(row + x, d);
+          CX2 = wsub(CX2, fs.fdy23);
+          CX3 = wsub(CX3, fs.fdy31);
+        }
+      }
+    }
+    __syncthreads();
+    // scan the tile: rendered pixels only, 4 pixels per step
+    if (npx > 0) {
+      const int32_t gpr = cwp >> 2;
+      const int32_t ng = gpr * thp;
+      for (int32_t g = tid; g < ng; g += T) {
+        const int32_t r = g / gpr;
+        const int32_t c = (g - r * gpr) << 2;
+        const int4 zz = *reinterpret_cast<const int4*>(tile + r * cwp + c);
+        if (zz.x >= kDepthBg && zz.y >= kDepthBg && zz.z >= kDepthBg && zz.w >= kDepthBg) continue;
+        const int32_t y = y0 + r, x = x0 + c;
+        uint32_t k[4] = {0u, 0u, 0u, 0u};
+        if (y >= 0 && y < H) {
+          const uint16_t* orow = obs + (size_t)y * (size_t)W;
+          if (vec_obs && x >= 0 && x + 3 < W) {
+            const uint2 q = __ldg(reinterpret_cast<const uint2*>(orow + x));
+            k[0] = q.x & 0xffffu;
+            k[1] = q.x >> 16;
+            k[2] = q.y & 0xffffu;
+            k[3] = q.y >> 16;
+          } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if (x + e >= 0 && x + e < W) k[e] = __ldg(orow + x + e);
+          }
+        }
+        const int32_t zr[4] = {zz.x, zz.y, zz.z, zz.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (zr[e] < kDepthBg) {
+            acc.nR += 1;
+            if (k[e] == 0u) {
+              acc.nNo += 1;
+            } else {
+              const int32_t dd = wsub(zr[e], (int32_t)k[e]);
+              const int64_t d64 = dd;
+              add128(acc.lo, acc.hi, (uint64_t)(d64 * d64));
+              acc.nSegR += 1;
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (bound_violation) atomicOr(I.err, kErrBound);
+
+  // block reduction
+  warp_reduce(acc);
+  const int wid = tid >> 5, lane = tid & 31, nw = T >> 5;
+  if (lane == 0) ctl.warp[wid] = acc;
+  __syncthreads();
+  float fitv = 0.f;
+  if (tid == 0) {
+    Partial t = ctl.warp[0];
+    for (int i = 1; i < nw; ++i) {
+      const Partial& o = ctl.warp[i];
+      t.nR += o.nR;
+      t.nNo += o.nNo;
+      t.nSegR += o.nSegR;
+      t.hi += o.hi;
+      add128(t.lo, t.hi, o.lo);
+      t.rminx = min(t.rminx, o.rminx);
+      t.rmaxx = max(t.rmaxx, o.rmaxx);
+      t.rminy = min(t.rminy, o.rminy);
+      t.rmaxy = max(t.rmaxy, o.rmaxy);
+      t.writes += o.writes;
+    }
+    const SolveParams& prm = I.prm;
+    const int32_t minX = min(t.rminx, prm.cl_min_x), maxX = max(t.rmaxx, prm.cl_max_x);
+    const int32_t minY = min(t.rminy, prm.cl_min_y), maxY = max(t.rmaxy, prm.cl_max_y);
+    const int64_t Ww = (int64_t)maxX - minX, Hh = (int64_t)maxY - minY;
+    uint32_t observed = 0;
+    if (Ww > 0 && Hh > 0) {
+      const int64_t area = Ww * Hh;
+      const int64_t pad = (1024 - area % 1024) % 1024;
+      const int64_t L = pad < Ww ? pad : Ww;
+      observed = sat_count(I.sat, W, H, minX, maxX, minY, maxY) +
+                 sat_count(I.sat, W, H, minX, (int64_t)minX + L, maxY, (int64_t)maxY + 1);
+    }
+    const uint32_t nSNR = observed - t.nSegR;
+    fitv = fitness_from_counts(nSNR, t.nR, t.nNo, t.lo, t.hi, prm.num_points);
+    atomicAdd(I.stats, t.writes);
+    atomicAdd(I.stats + 1, (unsigned long long)npass);
+  }
+  return fitv;
+}
+
+// PSO step + render + score + personal best for one work item.
+__device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, int32_t* tile,
+                             int tile_px, SmemCtl& ctl) {
+  const int tid = threadIdx.x;
+  const uint32_t P = I.prm.num_particles;
+  const uint32_t p0 = chunk * I.ppb;
+  const uint32_t np = min(I.ppb, P - p0);
+  if (tid < (int)np) {
+    const uint32_t p = p0 + tid;
+    float s[7], v[7];
+    if (iter == 0) {
+      init_particle(I.prm, p, s, v);
+#pragma unroll
+      for (int d = 0; d < 7; ++d) I.pbest[p + (size_t)d * P] = s[d];
+      I.pbest_fit[p] = kBestInit;
+    } else {
+      float b[7], g[7];
+#pragma unroll
+      for (int d = 0; d < 7; ++d) {
+        s[d] = __ldcg(I.pos + p + (size_t)d * P);
+        v[d] = __ldcg(I.vel + p + (size_t)d * P);
+        b[d] = __ldcg(I.pbest + p + (size_t)d * P);
+        g[d] = __ldcg(I.gbest + 1 + d);
+      }
+      update_particle(I.prm, p, iter, s, v, b, g);
+    }
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+      I.pos[p + (size_t)d * P] = s[d];
+      I.vel[p + (size_t)d * P] = v[d];
+      ctl.pose[tid][d] = s[d];
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = 0; i < np; ++i) {
+    const float fv = render_score(I, ctl.pose[i], tile, tile_px, ctl);
+    if (tid == 0) {
+      const uint32_t p = p0 + i;
+      I.fit[p] = fv;
+      if (fv < __ldcg(I.pbest_fit + p)) {
+        I.pbest_fit[p] = fv;
+#pragma unroll
+        for (int d = 0; d < 7; ++d) I.pbest[p + (size_t)d * P] = ctl.pose[i][d];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// After a work item: the CTA that completes the instance's last chunk of the
+// iteration takes the first minimum of the fitness and updates the global
+// best (main.cu:1691-1704 and 826-852).
+__device__ void instance_epilogue(const Instance& I, uint32_t iter, SmemCtl& ctl) {
+  const int tid = threadIdx.x, T = blockDim.x;
+  if (tid == 0) {
+    __threadfence();
+    const uint32_t t = atomicAdd(I.done, 1u);
+    ctl.last = (t == I.chunks - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!ctl.last) return;
+  __threadfence();
+  const uint32_t P = I.prm.num_particles;
+  float bv = __int_as_float(0x7f800000);
+  uint32_t bi = 0xffffffffu;
+  for (uint32_t p = tid; p < P; p += T) {
+    const float f = __ldcg(I.fit + p);
+    if (bi == 0xffffffffu || f < bv) {
+      bv = f;
+      bi = p;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+    const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (oi != 0xffffffffu && (bi == 0xffffffffu || ov < bv || (!(bv < ov) && oi < bi))) {
+      bv = ov;
+      bi = oi;
+    }
+  }
+  const int wid = tid >> 5, lane = tid & 31, nw = T >> 5;
+  if (lane == 0) {
+    ctl.argv[wid] = bv;
+    ctl.argi[wid] = bi;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    bv = ctl.argv[0];
+    bi = ctl.argi[0];
+    for (int i = 1; i < nw; ++i) {
+      const float ov = ctl.argv[i];
+      const uint32_t oi = ctl.argi[i];
+      if (oi != 0xffffffffu && (bi == 0xffffffffu || ov < bv || (!(bv < ov) && oi < bi))) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    const float gf = __ldcg(I.gbest);
+    if (bi != 0xffffffffu && bv < gf) {
+      I.gbest[0] = bv;
+#pragma unroll
+      for (int d = 0; d < 7; ++d) I.gbest[1 + d] = __ldcg(I.pos + bi + (size_t)d * P);
+    }
+    if (I.trace) {
+      float* tr = I.trace + (size_t)iter * 8;
+#pragma unroll
+      for (int d = 0; d < 8; ++d) tr[d] = __ldcg(I.gbest + d);
+    }
+    *I.done = 0u;
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+// Plain form: one launch per iteration of one instance, one CTA per chunk.
+__global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* __restrict__ inst,
+                                                                uint32_t iter, int tile_px) {
+  extern __shared__ int4 dyn_smem[];
+  __shared__ SmemCtl ctl;
+  int32_t* tile = reinterpret_cast<int32_t*>(dyn_smem);
+  const Instance& I = *inst;
+  process_item(I, blockIdx.x, iter, tile, tile_px, ctl);
+  instance_epilogue(I, iter, ctl);
+}
+
+// Grid-wide barrier for the cooperative persistent launch.  Waits are
+// bounded by timeout_ns of wall time; on expiry the CTA records kErrTimeout
+// and every CTA leaves at its next barrier.
+__device__ bool grid_barrier(uint32_t* bar, uint32_t* err, unsigned long long timeout_ns) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile uint32_t* gen = bar + 1;
+    const uint32_t my = *gen;
+    __threadfence();
+    const uint32_t arrived = atomicAdd(bar, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (*gen == my) {
+        if (*(volatile uint32_t*)err != 0u) {
+          ok = 0;
+          break;
+        }
+        if (global_ns() - t0 > timeout_ns) {
+          atomicOr(err, kErrTimeout);
+          ok = 0;
+          break;
+        }
+        __nanosleep(256);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Batched form: every iteration of every instance in one cooperative
+// launch.  Step s runs the s-th iteration of all instances that have one;
+// CTAs claim work items (largest first) from a per-step counter, and the
+// last chunk of an instance updates its global best before the barrier.
+__global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, int tile_px) {
+  extern __shared__ int4 dyn_smem[];
+  __shared__ SmemCtl ctl;
+  int32_t* tile = reinterpret_cast<int32_t*>(dyn_smem);
+  for (uint32_t s = 0; s < A.max_iters; ++s) {
+    while (true) {
+      if (threadIdx.x == 0) ctl.claim = atomicAdd(A.step_claim + s, 1u);
+      __syncthreads();
+      const uint32_t k = ctl.claim;
+      __syncthreads();
+      if (k >= A.n_items) break;
+      const WorkItem it = A.items[k];
+      const Instance& I = A.inst[it.inst];
+      if (s >= I.prm.iterations) continue;
+      process_item(I, it.chunk, s, tile, tile_px, ctl);
+      instance_epilogue(I, s, ctl);
+    }
+    if (s + 1 < A.max_iters && !grid_barrier(A.barrier, A.err, A.timeout_ns)) return;
+  }
+}
+
+// Wait-expiry check for the bounded barrier: `expected` CTAs are awaited
+// but only gridDim.x arrive, so every waiter runs out its limit and the
+// kernel returns with kErrTimeout set; nothing else is touched.
+__global__ void qpso_barrier_probe_kernel(uint32_t* bar, uint32_t* err, uint32_t expected,
+                                          unsigned long long timeout_ns) {
+  if (threadIdx.x != 0) return;
+  volatile uint32_t* gen = bar + 1;
+  const uint32_t my = *gen;
+  const uint32_t arrived = atomicAdd(bar, 1u);
+  if (arrived == expected - 1) {
+    atomicAdd(bar + 1, 1u);
+    return;
+  }
+  const unsigned long long t0 = global_ns();
+  while (*gen == my) {
+    if (global_ns() - t0 > timeout_ns) {
+      atomicOr(err, kErrTimeout);
+      return;
+    }
+    __nanosleep(1000);
+  }
+}
+
+// ------------------------------------------------------------------------
+// Per-solve preparation.
+
+// Cluster-masked observed depth (main.cu:1548-1557 builds it from
+// GraphCannySeg's clusterDepth): depth where label == cluster, else 0.
+// blockIdx.y selects the preparation job.
+__global__ void mask_depth_kernel(const PrepDesc* __restrict__ jobs) {
+  const PrepDesc J = jobs[blockIdx.y];
+  const int32_t n = J.width * J.height;
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint16_t d = J.depth[i];
+    J.obs[i] = (J.labels == nullptr || J.labels[i] == J.label) ? d : (uint16_t)0;
+  }
+}
+
+// Summed-area table of (obs != 0): sat[y][x] = #{(i,j): i<y, j<x, obs!=0}.
+// Pass 1: one warp per row, inclusive scan of the row into sat[y+1][1..w].
+__global__ void sat_rows_kernel(const PrepDesc* __restrict__ jobs) {
+  const PrepDesc J = jobs[blockIdx.y];
+  const int32_t w = J.width, h = J.height;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t W1 = (int64_t)w + 1;
+  if (warp == 0)
+    for (int32_t x = lane; x <= w; x += 32) J.sat[x] = 0;
+  for (int32_t y = warp; y < h; y += (gridDim.x * blockDim.x) >> 5) {
+    int32_t carry = 0;
+    int32_t* out = J.sat + (int64_t)(y + 1) * W1;
+    if (lane == 0) out[0] = 0;
+    for (int32_t x0 = 0; x0 < w; x0 += 32) {
+      const int32_t x = x0 + lane;
+      int32_t v = (x < w && J.obs[(int64_t)y * w + x] != 0) ? 1 : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+      }
+      if (x < w) out[x + 1] = carry + v;
+      carry += __shfl_sync(0xffffffffu, v, 31);
+    }
+  }
+}
+
+// Pass 2: one thread per column, running sum down the rows.
+__global__ void sat_cols_kernel(const PrepDesc* __restrict__ jobs) {
+  const PrepDesc J = jobs[blockIdx.y];
+  const int32_t w = J.width, h = J.height;
+  const int64_t W1 = (int64_t)w + 1;
+  for (int32_t x = blockIdx.x * blockDim.x + threadIdx.x; x <= w; x += gridDim.x * blockDim.x) {
+    int32_t run = 0;
+    for (int32_t y = 1; y <= h; ++y) {
+      run += J.sat[y * W1 + x];
+      J.sat[y * W1 + x] = run;
+    }
+  }
+}
+
+// Mesh AABB over all 3F vertices (min/max of each coordinate).
+__global__ void mesh_aabb_kernel(const float* __restrict__ mesh, uint32_t F, float* __restrict__ out) {
+  __shared__ float red[6][32];
+  float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+  const size_t n = 3 * (size_t)F;
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float v = mesh[i + c * n];
+      lo[c] = fminf(lo[c], v);
+      hi[c] = fmaxf(hi[c], v);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+  }
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int c = 0; c < 3; ++c) {
+      red[c][wid] = lo[c];
+      red[3 + c][wid] = hi[c];
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int c = 0; c < 3; ++c) {
+      float a = red[c][0], b = red[3 + c][0];
+      for (int i = 1; i < nw; ++i) {
+        a = fminf(a, red[c][i]);
+        b = fmaxf(b, red[3 + c][i]);
+      }
+      out[c] = a;
+      out[3 + c] = b;
+    }
+  }
+}
+
+// Render one pose into a caller window of the raster domain (for parity
+// tests and the best-pose render-out): window [x0, x0+ww) x [y0, y0+wh),
+// ww*wh <= tile_px, int32 depth with the background value where nothing
+// was written.  box receives the render AABB.  One CTA.
+__global__ void render_window_kernel(const Instance* __restrict__ inst, const float* __restrict__ pose,
+                                     int32_t x0, int32_t y0, int32_t ww, int32_t wh,
+                                     int32_t* __restrict__ out, int32_t* __restrict__ box) {
+  extern __shared__ int4 dyn_smem[];
+  int32_t* tile = reinterpret_cast<int32_t*>(dyn_smem);
+  __shared__ float s[8];
+  __shared__ int32_t red[4][32];
+  const Instance& I = *inst;
+  const int tid = threadIdx.x, T = blockDim.x;
+  if (tid < 7) s[tid] = pose[tid];
+  const int32_t n = ww * wh;
+  for (int i = tid; i < n; i += T) tile[i] = kDepthBg;
+  __syncthreads();
+  const int32_t dx0 = -kGuard, dx1 = I.cam.width + kGuard, dy0 = -kGuard, dy1 = I.cam.height + kGuard;
+  int32_t b0 = kAabbInitMin, b1 = kAabbInitMax, b2 = kAabbInitMin, b3 = kAabbInitMax;
+  for (uint32_t f = tid; f < I.F; f += T) {
+    float u[3], v[3], z[3];
+    for (int j = 0; j < 3; ++j)
+      project(s, I.mesh[f + (size_t)j * I.F], I.mesh[f + (size_t)(3 + j) * I.F],
+              I.mesh[f + (size_t)(6 + j) * I.F], I.cam, u[j], v[j], z[j]);
+    FaceSetup fs;
+    setup_face(u[0], v[0], z[0], u[1], v[1], z[1], u[2], v[2], z[2], fs);
+    b0 = min(b0, fs.minx);
+    b1 = max(b1, fs.maxx);
+    b2 = min(b2, fs.miny);
+    b3 = max(b3, fs.maxy);
+    if (!fs.live) continue;
+    const int32_t xa = max(max(fs.minx, x0), dx0), xb = min(min(fs.maxx, x0 + ww), dx1);
+    const int32_t ya = max(max(fs.miny, y0), dy0), yb = min(min(fs.maxy, y0 + wh), dy1);
+    for (int32_t y = ya; y < yb; ++y) {
+      const int32_t ry = y - fs.miny;
+      int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(xa - fs.minx, fs.fdy23));
+      int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(xa - fs.minx, fs.fdy31));
+      for (int32_t x = xa; x < xb; ++x) {
+        const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+        const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+        float depth = fs.z1;
+        depth = depth + (float)cx2 * fs.z2;
+        depth = depth + (float)cx3 * fs.z3;
+        atomicMin(tile + (y - y0) * ww + (x - x0), __float2int_rn(depth));
+        CX2 = wsub(CX2, fs.fdy23);
+        CX3 = wsub(CX3, fs.fdy31);
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    b0 = min(b0, __shfl_xor_sync(0xffffffffu, b0, o));
+    b1 = max(b1, __shfl_xor_sync(0xffffffffu, b1, o));
+    b2 = min(b2, __shfl_xor_sync(0xffffffffu, b2, o));
+    b3 = max(b3, __shfl_xor_sync(0xffffffffu, b3, o));
+  }
+  const int wid = tid >> 5, lane = tid & 31;
+  if (lane == 0) {
+    red[0][wid] = b0;
+    red[1][wid] = b1;
+    red[2][wid] = b2;
+    red[3][wid] = b3;
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += T) out[i] = tile[i];
+  if (tid == 0) {
+    for (int i = 1; i < (T >> 5); ++i) {
+      b0 = min(b0, red[0][i]);
+      b1 = max(b1, red[1][i]);
+      b2 = min(b2, red[2][i]);
+      b3 = max(b3, red[3][i]);
+    }
+    b0 = min(b0, red[0][0]);
+    b1 = max(b1, red[1][0]);
+    b2 = min(b2, red[2][0]);
+    b3 = max(b3, red[3][0]);
+    box[0] = b0;
+    box[1] = b1;
+    box[2] = b2;
+    box[3] = b3;
+  }
+}
+
+// Score explicit poses of one instance (no PSO state change): pose k goes
+// to fit_out[k] and its integer counts to counts_out[k*8 ..].
+__global__ void __launch_bounds__(kMaxThreads) score_poses_kernel(const Instance* __restrict__ inst,
+                                                                  const float* __restrict__ poses,
+                                                                  uint32_t n, int tile_px,
+                                                                  float* __restrict__ fit_out) {
+  extern __shared__ int4 dyn_smem[];
+  __shared__ SmemCtl ctl;
+  int32_t* tile = reinterpret_cast<int32_t*>(dyn_smem);
+  for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
+    if (threadIdx.x < 7) ctl.pose[0][threadIdx.x] = poses[(size_t)k * 7 + threadIdx.x];
+    __syncthreads();
+    const float fv = render_score(*inst, ctl.pose[0], tile, tile_px, ctl);
+    if (threadIdx.x == 0) fit_out[k] = fv;
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------
+// Host launch wrappers.
+
+size_t smem_ctl_bytes() { return sizeof(SmemCtl); }
+
+// Opt in to more than 48 KB of dynamic shared memory (per kernel, current
+// device; the call is cheap and idempotent).
+template <typename K>
+static cudaError_t ensure_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t launch_prep(const PrepDesc* jobs, int n, int max_w, int max_h, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int npx = max_w * max_h;
+  dim3 g1((npx + 255) / 256 < 512 ? (npx + 255) / 256 : 512, n);
+  mask_depth_kernel<<<g1, 256, 0, st>>>(jobs);
+  dim3 g2((max_h * 32 + 255) / 256, n);
+  sat_rows_kernel<<<g2, 256, 0, st>>>(jobs);
+  dim3 g3((max_w + 1 + 127) / 128, n);
+  sat_cols_kernel<<<g3, 128, 0, st>>>(jobs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_aabb(const float* mesh, uint32_t F, float* out, cudaStream_t st) {
+  mesh_aabb_kernel<<<1, 1024, 0, st>>>(mesh, F, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, const TileConfig& cfg,
+                        cudaStream_t st) {
+  const size_t smem = (size_t)cfg.tile_px * sizeof(int32_t);
+  cudaError_t e = ensure_smem(qpso_step_kernel, smem);
+  if (e != cudaSuccess) return e;
+  qpso_step_kernel<<<chunks, cfg.threads, smem, st>>>(inst, iter, cfg.tile_px);
+  return cudaGetLastError();
+}
+
+cudaError_t batch_max_grid(const TileConfig& cfg, int* blocks_per_sm) {
+  const size_t smem = (size_t)cfg.tile_px * sizeof(int32_t);
+  cudaError_t e = ensure_smem(qpso_batch_kernel, smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, qpso_batch_kernel, cfg.threads, smem);
+}
+
+cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st) {
+  const size_t smem = (size_t)cfg.tile_px * sizeof(int32_t);
+  cudaError_t e = ensure_smem(qpso_batch_kernel, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(grid);
+  lc.blockDim = dim3(cfg.threads);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, qpso_batch_kernel, args, cfg.tile_px);
+}
+
+cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
+                         const TileConfig& cfg, int grid, cudaStream_t st) {
+  const size_t smem = (size_t)cfg.tile_px * sizeof(int32_t);
+  cudaError_t e = ensure_smem(score_poses_kernel, smem);
+  if (e != cudaSuccess) return e;
+  score_poses_kernel<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_t x0, int32_t y0,
+                                 int32_t w, int32_t h, int32_t* out, int32_t* box, int threads,
+                                 cudaStream_t st) {
+  const size_t smem = (size_t)w * (size_t)h * sizeof(int32_t);
+  cudaError_t e = ensure_smem(render_window_kernel, smem < 16 ? 16 : smem);
+  if (e != cudaSuccess) return e;
+  render_window_kernel<<<1, threads, smem < 16 ? 16 : smem, st>>>(inst, pose, x0, y0, w, h, out, box);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_barrier_probe(uint32_t* bar, uint32_t* err, uint32_t grid, uint32_t expected,
+                                 unsigned long long timeout_ns, cudaStream_t st) {
+  qpso_barrier_probe_kernel<<<grid, 32, 0, st>>>(bar, err, expected, timeout_ns);
+  return cudaGetLastError();
+}
+
+}  // namespace qpso

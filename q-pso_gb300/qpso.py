@@ -1,0 +1,252 @@
+"""Python view of the C ABI in include/qpso.h (ctypes over the in-tree
+``_build/libqpso_gb300.so``).
+
+This mirrors the reference's host-side workflow (main.cu:1198-1780): upload
+the mesh (loadOBJ3 layout) and the observed depth, describe the cluster and
+the PSO constants, solve, read back the global best.  Every call goes to the
+sm_103a library; there is no CPU path, and loading fails loudly when the
+library is missing or no GB300-class GPU is present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libqpso_gb300.so")
+
+OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_TIMEOUT, ERR_BUSY, ERR_NOT_FOUND, ERR_INTERNAL = range(8)
+STATUS_NAMES = ["OK", "ERR_ARG", "ERR_NOMEM", "ERR_CUDA", "ERR_TIMEOUT", "ERR_BUSY",
+                "ERR_NOT_FOUND", "ERR_INTERNAL"]
+ERR_BIT_BOUND, ERR_BIT_TIMEOUT, ERR_BIT_ARG = 1, 2, 4
+
+# Functions declared in include/qpso.h (checked by the CPU test suite).
+EXPORTS = [
+    "qpso_version", "qpso_create", "qpso_destroy", "qpso_last_error", "qpso_mesh_upload",
+    "qpso_mesh_release", "qpso_frame_upload", "qpso_frame_release", "qpso_solve_desc_init",
+    "qpso_box_from_centroid", "qpso_set_launch_config", "qpso_get_launch_config", "qpso_solve",
+    "qpso_solve_traced", "qpso_solve_batch", "qpso_score_poses", "qpso_render",
+    "qpso_barrier_selftest",
+]
+
+
+class Camera(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class SolveDesc(C.Structure):
+    _fields_ = [("mesh_id", C.c_uint32), ("frame_id", C.c_uint32), ("cluster_label", C.c_int32),
+                ("cl_min_x", C.c_int32), ("cl_max_x", C.c_int32), ("cl_min_y", C.c_int32),
+                ("cl_max_y", C.c_int32), ("num_points", C.c_uint32), ("t_lo", C.c_float * 3),
+                ("t_hi", C.c_float * 3), ("num_particles", C.c_uint32), ("iterations", C.c_uint32),
+                ("c1", C.c_float), ("c2", C.c_float), ("w", C.c_double), ("vdot", C.c_float),
+                ("ang_lo", C.c_float), ("ang_hi", C.c_float), ("qinit", C.c_float * 4),
+                ("seed", C.c_uint64), ("stream", C.c_uint32)]
+
+
+class Result(C.Structure):
+    _fields_ = [("fit", C.c_float), ("pose", C.c_float * 7), ("flags", C.c_uint32),
+                ("reserved", C.c_uint32), ("raster_writes", C.c_uint64),
+                ("tile_passes", C.c_uint64)]
+
+
+class LaunchConfig(C.Structure):
+    _fields_ = [("threads", C.c_int32), ("tile_px", C.c_int32), ("ppb", C.c_int32)]
+
+
+class QpsoError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES[status] if 0 <= status < 8 else status, msg))
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("qpso CUDA library not built: %s (run __graft_entry__.build())" % path)
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.qpso_version.restype = C.c_char_p
+    L.qpso_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.qpso_destroy.argtypes = [vp]
+    L.qpso_destroy.restype = None
+    L.qpso_last_error.argtypes = [vp]
+    L.qpso_last_error.restype = C.c_char_p
+    L.qpso_mesh_upload.argtypes = [vp, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]
+    L.qpso_mesh_release.argtypes = [vp, C.c_uint32]
+    L.qpso_frame_upload.argtypes = [vp, C.c_void_p, C.c_void_p, C.POINTER(Camera),
+                                    C.POINTER(C.c_uint32)]
+    L.qpso_frame_release.argtypes = [vp, C.c_uint32]
+    L.qpso_solve_desc_init.argtypes = [C.POINTER(SolveDesc)]
+    L.qpso_solve_desc_init.restype = None
+    L.qpso_box_from_centroid.argtypes = [C.POINTER(C.c_float), C.c_float, C.c_float,
+                                         C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.qpso_box_from_centroid.restype = None
+    L.qpso_set_launch_config.argtypes = [vp, C.POINTER(LaunchConfig), C.POINTER(LaunchConfig)]
+    L.qpso_get_launch_config.argtypes = [vp, C.POINTER(LaunchConfig), C.POINTER(LaunchConfig)]
+    L.qpso_solve.argtypes = [vp, C.POINTER(SolveDesc), C.POINTER(Result)]
+    L.qpso_solve_traced.argtypes = [vp, C.POINTER(SolveDesc), C.POINTER(Result), C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.qpso_solve_batch.argtypes = [vp, C.POINTER(SolveDesc), C.c_uint32, C.POINTER(Result)]
+    L.qpso_score_poses.argtypes = [vp, C.POINTER(SolveDesc), C.c_void_p, C.c_uint32, C.c_void_p]
+    L.qpso_render.argtypes = [vp, C.c_uint32, C.POINTER(Camera), C.c_void_p, C.c_int32,
+                              C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
+    L.qpso_barrier_selftest.argtypes = [vp, C.c_uint64, C.POINTER(C.c_uint32)]
+    for fn in EXPORTS:
+        if fn not in ("qpso_version", "qpso_destroy", "qpso_last_error", "qpso_solve_desc_init",
+                      "qpso_box_from_centroid"):
+            getattr(L, fn).restype = C.c_int32
+    _lib = L
+    return L
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def solve_desc(**kw) -> SolveDesc:
+    """A descriptor with the reference's defaults, fields overridden by kw."""
+    d = SolveDesc()
+    load_library().qpso_solve_desc_init(C.byref(d))
+    for k, v in kw.items():
+        if k in ("t_lo", "t_hi"):
+            setattr(d, k, (C.c_float * 3)(*v))
+        elif k == "qinit":
+            setattr(d, k, (C.c_float * 4)(*v))
+        else:
+            setattr(d, k, v)
+    return d
+
+
+def box_from_centroid(centroid_mm, bound=0.3, bound_z=0.3):
+    c = (C.c_float * 3)(*centroid_mm)
+    lo = (C.c_float * 3)()
+    hi = (C.c_float * 3)()
+    load_library().qpso_box_from_centroid(c, bound, bound_z, lo, hi)
+    return list(lo), list(hi)
+
+
+class Context:
+    """One GPU context (qpso_create / qpso_destroy)."""
+
+    def __init__(self, device: int = 0):
+        self.L = load_library()
+        self.h = C.c_void_p()
+        st = self.L.qpso_create(device, C.byref(self.h))
+        if st != OK:
+            raise QpsoError(st, "qpso_create(device=%d) failed (no sm_100+ GPU?)" % device)
+
+    def close(self):
+        if self.h:
+            self.L.qpso_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != OK:
+            raise QpsoError(st, self.L.qpso_last_error(self.h).decode())
+
+    def mesh_upload(self, soa: np.ndarray, num_faces: int) -> int:
+        a = _f32(soa)
+        if a.size != 9 * num_faces:
+            raise ValueError("mesh must hold 9*num_faces floats")
+        mid = C.c_uint32()
+        self._check(self.L.qpso_mesh_upload(self.h, a.ctypes.data, num_faces, C.byref(mid)))
+        return mid.value
+
+    def mesh_release(self, mid: int):
+        self._check(self.L.qpso_mesh_release(self.h, mid))
+
+    def frame_upload(self, depth_mm: np.ndarray, cam: Camera, labels: np.ndarray | None = None) -> int:
+        d = np.ascontiguousarray(depth_mm, dtype=np.uint16)
+        lab = None if labels is None else np.ascontiguousarray(labels, dtype=np.int32)
+        if d.shape != (cam.height, cam.width):
+            raise ValueError("depth shape must be (height, width)")
+        fid = C.c_uint32()
+        self._check(self.L.qpso_frame_upload(self.h, d.ctypes.data,
+                                             None if lab is None else lab.ctypes.data,
+                                             C.byref(cam), C.byref(fid)))
+        return fid.value
+
+    def frame_release(self, fid: int):
+        self._check(self.L.qpso_frame_release(self.h, fid))
+
+    def set_launch_config(self, plain=None, batch=None):
+        p = None if plain is None else C.byref(LaunchConfig(*plain))
+        b = None if batch is None else C.byref(LaunchConfig(*batch))
+        self._check(self.L.qpso_set_launch_config(self.h, p, b))
+
+    def get_launch_config(self):
+        p, b = LaunchConfig(), LaunchConfig()
+        self._check(self.L.qpso_get_launch_config(self.h, C.byref(p), C.byref(b)))
+        return (p.threads, p.tile_px, p.ppb), (b.threads, b.tile_px, b.ppb)
+
+    def solve(self, desc: SolveDesc) -> Result:
+        r = Result()
+        self._check(self.L.qpso_solve(self.h, C.byref(desc), C.byref(r)))
+        return r
+
+    def solve_traced(self, desc: SolveDesc):
+        P, it = desc.num_particles, desc.iterations
+        trace = np.zeros((it, 8), np.float32)
+        pos = np.zeros((7, P), np.float32)
+        vel = np.zeros((7, P), np.float32)
+        pb = np.zeros((7, P), np.float32)
+        pbf = np.zeros(P, np.float32)
+        r = Result()
+        self._check(self.L.qpso_solve_traced(self.h, C.byref(desc), C.byref(r), trace.ctypes.data,
+                                             pos.ctypes.data, vel.ctypes.data, pb.ctypes.data,
+                                             pbf.ctypes.data))
+        return r, {"trace_gbest": trace, "pos": pos, "vel": vel, "pbest": pb, "pbest_fit": pbf}
+
+    def solve_batch(self, descs) -> list:
+        n = len(descs)
+        arr = (SolveDesc * n)(*descs)
+        res = (Result * n)()
+        self._check(self.L.qpso_solve_batch(self.h, arr, n, res))
+        return list(res)
+
+    def score_poses(self, desc: SolveDesc, poses: np.ndarray) -> np.ndarray:
+        p = _f32(poses).reshape(-1, 7)
+        out = np.zeros(p.shape[0], np.float32)
+        self._check(self.L.qpso_score_poses(self.h, C.byref(desc), p.ctypes.data, p.shape[0],
+                                            out.ctypes.data))
+        return out
+
+    def render(self, mesh_id: int, cam: Camera, pose, x0: int, y0: int, w: int, h: int):
+        out = np.zeros((h, w), np.int32)
+        box = np.zeros(4, np.int32)
+        p = _f32(pose)
+        self._check(self.L.qpso_render(self.h, mesh_id, C.byref(cam), p.ctypes.data, x0, y0, w, h,
+                                       out.ctypes.data, box.ctypes.data))
+        return out, box
+
+    def barrier_selftest(self, timeout_ns: int):
+        bits = C.c_uint32()
+        st = self.L.qpso_barrier_selftest(self.h, timeout_ns, C.byref(bits))
+        return st, bits.value
+
+
+def result_dict(r: Result) -> dict:
+    return {"fit": r.fit, "pose": np.array(r.pose[:], np.float32), "flags": r.flags,
+            "raster_writes": r.raster_writes, "tile_passes": r.tile_passes}

@@ -1,0 +1,249 @@
+"""Parity of the sm_103a path (through the C ABI) with the oracle.
+
+Bar: depth tiles, render AABBs and integer fitness counts bit-exact; the
+fitness and the whole PSO trajectory bit-exact as well (both sides follow
+the same arithmetic contract), which is stricter than the 0.5 deg / 1 mm
+pose tolerance; float fitness within 1e-5 relative of an FP64
+recomputation from the integer counts.
+"""
+import numpy as np
+import pytest
+
+import scene
+from oracle import pyoracle as po
+from tests.helpers import gpu_camera, gpu_desc, oracle_obs, oracle_params, rot_err_deg, upload_workload
+
+pytestmark = pytest.mark.gpu
+
+FIT_RTOL_FP64 = 1e-5
+POSE_TOL_DEG = 0.5
+POSE_TOL_M = 1e-3
+
+
+@pytest.fixture(scope="module")
+def c1_gpu(gpu_ctx, c1):
+    mids, fids = upload_workload(gpu_ctx, c1)
+    return c1, mids, fids
+
+
+def random_poses(rng, s, n, spread=1.0):
+    f = scene.solve_fields(s)
+    lo, hi = np.array(f["t_lo"]), np.array(f["t_hi"])
+    c = (lo + hi) / 2
+    t = c + (rng.uniform(-1, 1, (n, 3)) * (hi - lo) / 2 * spread)
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q[q[:, 0] < 0] *= -1
+    return np.concatenate([t, q], 1).astype(np.float32)
+
+
+def test_render_tiles_bit_exact(gpu_ctx, c1_gpu):
+    w, mids, _ = c1_gpu
+    soa, F = w["meshes"][0]
+    s = w["solves"][0]
+    rng = np.random.default_rng(1)
+    poses = np.concatenate([s["gt_pose"][None], random_poses(rng, s, 24, 0.4)])
+    cam_o, cam_g = po.camera(), gpu_camera()
+    for pose in poses:
+        zb, box, _ = po.render(soa, F, pose, cam_o)
+        x0, x1, y0, y1 = box
+        x0 = max(int(x0), -po.GUARD) & ~3
+        y0 = max(int(y0), -po.GUARD)
+        ww = min(((min(int(x1), 640 + po.GUARD) - x0 + 3) & ~3), 200)
+        hh = min(min(int(y1), 480 + po.GUARD) - y0, 200)
+        if ww <= 0 or hh <= 0:
+            continue
+        tile, gbox = gpu_ctx.render(mids[0], cam_g, pose, x0, y0, ww, hh)
+        np.testing.assert_array_equal(gbox, box)
+        want = zb[y0 + po.GUARD:y0 + po.GUARD + hh, x0 + po.GUARD:x0 + po.GUARD + ww]
+        np.testing.assert_array_equal(tile, want)
+
+
+def _oracle_scores(w, s, poses, **over):
+    soa, F = w["meshes"][s["mesh"]]
+    prm = oracle_params(s, **over)
+    obs = oracle_obs(w, s)
+    cam = po.camera()
+    out = []
+    for pose in poses:
+        zb, box, _ = po.render(soa, F, pose, cam)
+        out.append(po.score(zb, box, obs, cam, prm))
+    return out, prm
+
+
+def test_fitness_bit_exact_and_fp64(gpu_ctx, c1_gpu):
+    w, mids, fids = c1_gpu
+    s = w["solves"][0]
+    rng = np.random.default_rng(2)
+    poses = np.concatenate([s["gt_pose"][None], random_poses(rng, s, 200, 1.0)])
+    got = gpu_ctx.score_poses(gpu_desc(s, mids[0], fids[0]), poses)
+    scores, prm = _oracle_scores(w, s, poses)
+    want = np.array([sc.fit for sc in scores], np.float32)
+    np.testing.assert_array_equal(got, want)
+    for sc in scores:
+        if sc.n_rendered:
+            ref = po.fitness_fp64(sc, prm.num_points)
+            assert abs(sc.fit - ref) <= FIT_RTOL_FP64 * abs(ref)
+
+
+def test_fitness_full_frame_window_and_partial_row(gpu_ctx, c1_gpu):
+    """Cluster AABB = the whole frame (the stress configuration's window)
+    and odd windows whose area leaves a partial last row."""
+    w, mids, fids = c1_gpu
+    s = w["solves"][0]
+    rng = np.random.default_rng(3)
+    poses = random_poses(rng, s, 40, 0.8)
+    for aabb in [(0, 640, 0, 480), (300, 371, 90, 153), (310, 313, 100, 400)]:
+        over = dict(cl_min_x=aabb[0], cl_max_x=aabb[1], cl_min_y=aabb[2], cl_max_y=aabb[3])
+        got = gpu_ctx.score_poses(gpu_desc(s, mids[0], fids[0], **over), poses)
+        scores, _ = _oracle_scores(w, s, poses, **over)
+        np.testing.assert_array_equal(got, np.array([sc.fit for sc in scores], np.float32))
+        assert any(sc.partial_len > 0 for sc in scores) or aabb == (0, 640, 0, 480)
+
+
+def test_fitness_off_screen_and_behind_camera(gpu_ctx, c1_gpu):
+    """Poses whose render leaves the image, leaves the raster domain, or
+    puts vertices behind the camera (no conservative bound: banded passes)."""
+    w, mids, fids = c1_gpu
+    s = w["solves"][0]
+    gt = s["gt_pose"].copy()
+    poses = []
+    for dx, dy, dz in [(0.25, 0, 0), (-0.3, 0.1, 0), (0, 0.25, -0.2), (0.9, 0, -0.5), (0, 0, -0.66),
+                       (0, 0, -0.69), (0, 0, -0.75), (3.0, 0, 0), (0, 0, 0.5)]:
+        p = gt.copy()
+        p[:3] += np.float32([dx, dy, dz])
+        poses.append(p)
+    poses = np.array(poses, np.float32)
+    got = gpu_ctx.score_poses(gpu_desc(s, mids[0], fids[0]), poses)
+    scores, _ = _oracle_scores(w, s, poses)
+    np.testing.assert_array_equal(got, np.array([sc.fit for sc in scores], np.float32))
+
+
+def test_small_tiles_force_multipass(gpu_ctx, c1_gpu):
+    """A tile capacity far below the render bound makes every particle-render
+    take several row/column passes; the fitness must not change."""
+    w, mids, fids = c1_gpu
+    s = w["solves"][0]
+    rng = np.random.default_rng(4)
+    poses = random_poses(rng, s, 32, 0.5)
+    base = gpu_ctx.score_poses(gpu_desc(s, mids[0], fids[0]), poses)
+    old = gpu_ctx.get_launch_config()
+    try:
+        gpu_ctx.set_launch_config(plain=(128, 256, 1))
+        small = gpu_ctx.score_poses(gpu_desc(s, mids[0], fids[0]), poses)
+    finally:
+        gpu_ctx.set_launch_config(plain=old[0], batch=old[1])
+    np.testing.assert_array_equal(small, base)
+
+
+def test_plain_solve_trace_bit_exact(gpu_ctx, c1_gpu):
+    """C1 (64 particles x 50 iterations, Philox seed 0): the global-best
+    trace of every iteration and the final swarm equal the oracle's."""
+    w, mids, fids = c1_gpu
+    s = w["solves"][0]
+    soa, F = w["meshes"][0]
+    want = po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s), trace=True)
+    r, st = gpu_ctx.solve_traced(gpu_desc(s, mids[0], fids[0]))
+    assert r.flags == 0
+    np.testing.assert_array_equal(st["trace_gbest"], want["trace_gbest"])
+    np.testing.assert_array_equal(st["pos"], want["pos"])
+    np.testing.assert_array_equal(st["vel"], want["vel"])
+    np.testing.assert_array_equal(st["pbest"], want["pbest"])
+    np.testing.assert_array_equal(st["pbest_fit"], want["pbest_fit"])
+    pose = np.array(r.pose[:], np.float32)
+    assert np.abs(pose[:3] - want["pose"][:3]).max() <= POSE_TOL_M
+    assert rot_err_deg(pose[3:], want["pose"][3:]) <= POSE_TOL_DEG
+    g = np.load("tests/golden/oracle_c1.npz")
+    np.testing.assert_array_equal(st["trace_gbest"], g["trace_gbest"])
+
+
+@pytest.mark.parametrize("cfg", [(256, 16384, 1), (128, 4096, 4), (512, 32768, 3)])
+def test_plain_launch_shapes_agree(gpu_ctx, c1_gpu, cfg):
+    w, mids, fids = c1_gpu
+    s = dict(w["solves"][0], particles=40, iterations=12, seed=5, stream=9)
+    soa, F = w["meshes"][0]
+    want = po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s), trace=True)
+    old = gpu_ctx.get_launch_config()
+    try:
+        gpu_ctx.set_launch_config(plain=cfg)
+        r, st = gpu_ctx.solve_traced(gpu_desc(s, mids[0], fids[0]))
+    finally:
+        gpu_ctx.set_launch_config(plain=old[0], batch=old[1])
+    np.testing.assert_array_equal(st["trace_gbest"], want["trace_gbest"])
+
+
+def test_batch_equals_plain_and_oracle(gpu_ctx, c1_gpu):
+    """Uneven instances (particle counts, iteration counts, seeds, cluster
+    windows) in one persistent launch give the same results as their own
+    plain solves and as the oracle."""
+    w, mids, fids = c1_gpu
+    base = w["solves"][0]
+    soa, F = w["meshes"][0]
+    variants = [dict(particles=64, iterations=20, seed=0, stream=0),
+                dict(particles=37, iterations=9, seed=1, stream=1),
+                dict(particles=128, iterations=15, seed=2, stream=2),
+                dict(particles=5, iterations=25, seed=3, stream=3),
+                dict(particles=96, iterations=1, seed=4, stream=4)]
+    solves = [dict(base, **v) for v in variants]
+    descs = [gpu_desc(s, mids[0], fids[0]) for s in solves]
+    for cfg in [(256, 16384, 1), (256, 8192, 2)]:
+        old = gpu_ctx.get_launch_config()
+        try:
+            gpu_ctx.set_launch_config(batch=cfg)
+            res = gpu_ctx.solve_batch(descs)
+            res2 = gpu_ctx.solve_batch(descs)  # graph replay
+        finally:
+            gpu_ctx.set_launch_config(plain=old[0], batch=old[1])
+        for s, d, r, r2 in zip(solves, descs, res, res2):
+            plain = gpu_ctx.solve(d)
+            want = po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s))
+            assert r.flags == 0
+            assert r.fit == plain.fit == want["fit"] == r2.fit
+            np.testing.assert_array_equal(np.array(r.pose[:], np.float32), want["pose"])
+            np.testing.assert_array_equal(np.array(r2.pose[:], np.float32), want["pose"])
+
+
+def test_solution_near_ground_truth(gpu_ctx, c1_gpu):
+    """Sanity of the whole solve: the best fitness is at most a little above
+    the fitness of the ground-truth pose (the ellipsoid is nearly symmetric,
+    so the pose itself may be a symmetric twin)."""
+    w, mids, fids = c1_gpu
+    s = w["solves"][0]
+    r = gpu_ctx.solve(gpu_desc(s, mids[0], fids[0]))
+    gt_fit = gpu_ctx.score_poses(gpu_desc(s, mids[0], fids[0]), s["gt_pose"][None])[0]
+    assert r.fit <= 2.0 * gt_fit
+    assert np.abs(np.array(r.pose[:3]) - s["gt_pose"][:3]).max() < 0.03
+
+
+def test_bounded_wait_expires(gpu_ctx):
+    import qpso
+
+    st, bits = gpu_ctx.barrier_selftest(50_000_000)
+    assert st == qpso.ERR_TIMEOUT and bits & qpso.ERR_BIT_TIMEOUT
+    # the context is still usable afterwards
+    st2, _ = gpu_ctx.barrier_selftest(10_000_000)
+    assert st2 == qpso.ERR_TIMEOUT
+
+
+def test_argument_errors(gpu_ctx, c1_gpu):
+    import qpso
+
+    w, mids, fids = c1_gpu
+    s = w["solves"][0]
+    with pytest.raises(qpso.QpsoError) as e:
+        gpu_ctx.solve(gpu_desc(s, 9999, fids[0]))
+    assert e.value.status == qpso.ERR_NOT_FOUND
+    with pytest.raises(qpso.QpsoError) as e:
+        gpu_ctx.solve(gpu_desc(s, mids[0], fids[0], num_particles=0))
+    assert e.value.status == qpso.ERR_ARG
+    with pytest.raises(qpso.QpsoError) as e:
+        gpu_ctx.solve(gpu_desc(s, mids[0], fids[0], cl_min_x=10, cl_max_x=10))
+    assert e.value.status == qpso.ERR_ARG
+    with pytest.raises(qpso.QpsoError) as e:
+        gpu_ctx.solve(gpu_desc(s, mids[0], fids[0], num_points=0))
+    assert e.value.status == qpso.ERR_ARG
+    with pytest.raises(qpso.QpsoError) as e:
+        gpu_ctx.set_launch_config(plain=(100, 16384, 1))
+    assert e.value.status == qpso.ERR_ARG
+    with pytest.raises(qpso.QpsoError):
+        gpu_ctx.mesh_upload(np.full(9, np.nan, np.float32), 1)
