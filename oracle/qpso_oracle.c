@@ -495,9 +495,14 @@ void qo_score_zbuf(const int32_t *zbuf, const int32_t box[4], const uint16_t *ob
     const int32_t dw = qo_domain_w(cam);
     uint32_t nR = 0, nNo = 0, nSegR = 0, nSNR = 0;
     uint64_t lo = 0, hi = 0;
-    for (int64_t y = minY; y <= maxY; ++y) {
-        const int64_t xe = (y < maxY) ? (int64_t)maxX : (int64_t)minX + L;
-        for (int64_t x = minX; x < xe; ++x) {
+    /* Visited pixels outside the raster domain have neither a rendered nor
+     * an observed depth and add nothing, so the walk is clipped to it. */
+    const int64_t cx0 = -QO_GUARD, cx1 = (int64_t)cam->width + QO_GUARD;
+    const int64_t cy0 = -QO_GUARD, cy1 = (int64_t)cam->height + QO_GUARD;
+    for (int64_t y = (minY > cy0 ? minY : cy0); y <= maxY && y < cy1; ++y) {
+        int64_t xe = (y < maxY) ? (int64_t)maxX : (int64_t)minX + L;
+        if (xe > cx1) xe = cx1;
+        for (int64_t x = (minX > cx0 ? minX : cx0); x < xe; ++x) {
             int32_t zr = QO_DEPTH_BG;
             if (x >= -QO_GUARD && x < cam->width + QO_GUARD &&
                 y >= -QO_GUARD && y < cam->height + QO_GUARD)

@@ -186,6 +186,8 @@ def test_batch_equals_plain_and_oracle(gpu_ctx, c1_gpu):
                 dict(particles=96, iterations=1, seed=4, stream=4)]
     solves = [dict(base, **v) for v in variants]
     descs = [gpu_desc(s, mids[0], fids[0]) for s in solves]
+    wants = [po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s)) for s in solves]
+    plains = [gpu_ctx.solve(d) for d in descs]
     for cfg in [(256, 16384, 1), (256, 8192, 2)]:
         old = gpu_ctx.get_launch_config()
         try:
@@ -194,9 +196,7 @@ def test_batch_equals_plain_and_oracle(gpu_ctx, c1_gpu):
             res2 = gpu_ctx.solve_batch(descs)  # graph replay
         finally:
             gpu_ctx.set_launch_config(plain=old[0], batch=old[1])
-        for s, d, r, r2 in zip(solves, descs, res, res2):
-            plain = gpu_ctx.solve(d)
-            want = po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s))
+        for r, r2, plain, want in zip(res, res2, plains, wants):
             assert r.flags == 0
             assert r.fit == plain.fit == want["fit"] == r2.fit
             np.testing.assert_array_equal(np.array(r.pose[:], np.float32), want["pose"])
