@@ -1,0 +1,396 @@
+"""Benchmark of the Q-PSO pose solve on one GB300 (or N replicas).
+
+Default workload: the plain method at production size -- one synthetic
+640x480 RGB-D frame with 8 non-overlapping objects drawn from 4 procedural
+meshes (~5k faces, 50-200 mm), each cluster solved by its own plain solve
+(one fused launch per iteration), 256 particles x 100 iterations, fp32.  A
+step is one frame: 8 pose solves.  `value` is pose solves/s with meshes and
+frame resident in HBM; `e2e` re-uploads the frame (depth + labels) from
+page-locked host memory every step and reads every result back.  The same
+workload through the batched persistent kernel is reported under
+`batched`.  Inputs are far smaller than L2, so L2 is scrubbed (256 MB
+written) before every timed step.
+
+Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                        [--workload c2|c1|c3|c5]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "q-pso_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "pose solves/sec (particle-renders/sec alongside), plain vs batched"
+L2_SCRUB_BYTES = 256 << 20
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for N replicas (gloo, host scalars)."""
+
+    def __init__(self, ws):
+        self.ws = ws
+        self.dist = None
+        if ws > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device),
+                                          "--query-gpu=" + self.FIELDS, "--format=csv,noheader",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                smax.append(float(parts[2].split()[0]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.remove(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_workload(name: str):
+    import scene
+
+    if name == "c1":
+        return scene.workload_c1(), "c1: plain single solve, 1280-face ellipsoid, 64 particles x 50 iterations"
+    if name == "c2":
+        return scene.workload_c2(), ("c2: plain method at production size, 8 clusters per frame, "
+                                     "4 meshes ~5k faces (50-200 mm), 256 particles x 100 iterations")
+    if name == "c3":
+        return scene.workload_c3(), ("c3: 64 clusters from 8 frames, meshes log-uniform 1k-50k faces, "
+                                     "windows 40-300 px, particles in {128..1024} x 100 iterations")
+    if name == "c5":
+        return scene.workload_c5(), ("c5: one level-7 icosphere (327,680 faces, 250 mm), "
+                                     "4096 particles x 200 iterations, full 640x480 window")
+    raise SystemExit("unknown workload " + name)
+
+
+def algorithmic_bytes(w) -> tuple[float, float]:
+    """Per particle-render: 36 F (mesh, loadOBJ3 layout) + 2 A (uint16
+    observed window, A = cluster AABB area) + 96 (pose/velocity/best state
+    read and written).  Returns (bytes summed over all renders of one pass of
+    every solve, renders of that pass)."""
+    tot, n = 0.0, 0
+    for s in w["solves"]:
+        F = w["meshes"][s["mesh"]][1]
+        x0, x1, y0, y1 = s["cluster"]["aabb"]
+        per = 36.0 * F + 2.0 * (x1 - x0) * (y1 - y0) + 96.0
+        tot += per * s["particles"]
+        n += s["particles"]
+    return tot, n
+
+
+def traffic_per_launch(workload: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/step_kernel_<workload>.md, line 'dram_bytes_per_launch:')."""
+    p = os.path.join(ROOT, "profiles", "step_kernel_%s.md" % workload)
+    try:
+        for line in open(p):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(w, budget_s: float = 12.0):
+    """The oracle (scalar C restatement) with every host thread on a bounded
+    sample of the workload: whole cluster solves until ~budget_s of CPU time."""
+    import scene
+    from oracle import pyoracle as po
+    from tests.helpers import oracle_obs, oracle_params
+
+    threads = os.cpu_count() or 1
+    done, renders, t0 = 0, 0, time.perf_counter()
+    for s in w["solves"]:
+        soa, F = w["meshes"][s["mesh"]]
+        po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s), threads=threads)
+        done += 1
+        renders += s["particles"] * s["iterations"]
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": "%d whole cluster solve(s) of the workload (%d particle-renders) in %.1f s"
+                      % (done, renders, dt),
+            "particle_renders_per_s": renders / dt}
+
+
+def run_reference(args, ws, rank):
+    """Reference arm: the oracle port on the host cores (the reference's own
+    code needs OpenCV 2.4, assimp, GSL and a missing header and cannot be
+    built), each step a bounded sample: one whole cluster solve."""
+    if rank != 0:
+        return
+    w, desc = load_workload(args.workload)
+    import scene  # noqa: F401
+    from oracle import pyoracle as po
+    from tests.helpers import oracle_obs, oracle_params
+
+    threads = os.cpu_count() or 1
+    solves = w["solves"]
+
+    def step(i):
+        s = solves[i % len(solves)]
+        soa, F = w["meshes"][s["mesh"]]
+        po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s), threads=threads)
+        return s["particles"] * s["iterations"]
+
+    for i in range(args.warmup):
+        step(i)
+    t0 = time.perf_counter()
+    renders = 0
+    for i in range(args.steps):
+        renders += step(i)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1000 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "sample": "one whole cluster solve per step"},
+            "particle_renders_per_s": renders / dt,
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": "%d whole cluster solves" % args.steps},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, ws, rank, local):
+    import qpso
+    import build as pkg_build
+    import scene
+
+    pkg_build.build()
+    d = Dist(ws)
+    w, desc = load_workload(args.workload)
+    ctx = qpso.Context(local)
+    cam = qpso.Camera(*scene.camera_tuple())
+    mids = [ctx.mesh_upload(soa, F) for soa, F in w["meshes"]]
+    fids = [ctx.frame_upload(dep, cam, labels=lab) for dep, lab, _ in w["frames"]]
+    descs = []
+    for s in w["solves"]:
+        f = scene.solve_fields(s)
+        descs.append(qpso.solve_desc(mesh_id=mids[s["mesh"]], frame_id=fids[s["frame"]], **f))
+    n_solves = len(descs)
+    renders_per_step = sum(s["particles"] * s["iterations"] for s in w["solves"])
+    iters_per_step = sum(s["iterations"] for s in w["solves"])
+    batched_default = args.workload == "c3"
+
+    # pinned host copies of the frames for the end-to-end arm
+    pinned = []
+    for dep, lab, _ in w["frames"]:
+        pd = qpso.PinnedArray(dep.shape, np.uint16)
+        pl = qpso.PinnedArray(lab.shape, np.int32)
+        pd.array[...] = dep
+        pl.array[...] = lab
+        pinned.append((pd, pl))
+    h2d = sum(pd.nbytes + pl.nbytes for pd, pl in pinned) + n_solves * qpso.C.sizeof(qpso.SolveDesc)
+    d2h = n_solves * qpso.C.sizeof(qpso.Result)
+
+    def step_plain(e2e=False):
+        if e2e:
+            for fid, (pd, pl) in zip(fids, pinned):
+                ctx.frame_update(fid, pd.array, pl.array)
+        return [ctx.solve(x) for x in descs]
+
+    def step_batch(e2e=False):
+        if e2e:
+            for fid, (pd, pl) in zip(fids, pinned):
+                ctx.frame_update(fid, pd.array, pl.array)
+        return ctx.solve_batch(descs)
+
+    def timed(fn, steps, e2e=False, prof=False):
+        ctx.set_profiling(prof)
+        ctx.profile(reset=True)
+        total = 0.0
+        for _ in range(steps):
+            ctx.scrub_l2(L2_SCRUB_BYTES)
+            ctx.timer_record(0)
+            fn(e2e)
+            ctx.timer_record(1)
+            total += ctx.timer_elapsed_ms(0, 1)
+        ctx.set_profiling(False)
+        return total, ctx.profile(reset=True)
+
+    main_fn, alt_fn = (step_batch, step_plain) if batched_default else (step_plain, step_batch)
+    for _ in range(args.warmup):
+        main_fn()
+        alt_fn()
+    # correctness of what is timed: plain and batched agree bit for bit
+    r_main, r_alt = main_fn(), alt_fn()
+    agree = all(a.fit == b.fit and list(a.pose) == list(b.pose) for a, b in zip(r_main, r_alt))
+    flags = max(r.flags for r in r_main)
+
+    sampler = ClockSampler(local)
+    d.barrier()
+    sampler.start()
+    ms_main, prof = timed(main_fn, args.steps, prof=True)
+    clocks = sampler.stop()
+    ms_main = d.max(ms_main)
+    d.barrier()
+    ms_e2e, _ = timed(main_fn, args.steps, e2e=True)
+    ms_e2e = d.max(ms_e2e)
+    alt_steps = max(1, args.steps if not batched_default else min(args.steps, 2))
+    ms_alt, prof_alt = timed(alt_fn, alt_steps, prof=True)
+    ms_alt = d.max(ms_alt)
+
+    value = ws * n_solves * args.steps / (ms_main / 1000.0)
+    e2e = ws * n_solves * args.steps / (ms_e2e / 1000.0)
+    alt = ws * n_solves * alt_steps / (ms_alt / 1000.0)
+    plain_v, batch_v = (alt, value) if batched_default else (value, alt)
+
+    # roofline of the dominant kernel (fused per-iteration kernel on the plain
+    # path, the persistent kernel on the batched path)
+    bytes_pass, renders_pass = algorithmic_bytes(w)
+    hbm, peak_kind = peaks()
+    if batched_default:
+        launches = max(1, prof["batch_launches"])
+        kern_ms = prof["batch_ms"] / launches
+        bytes_launch = bytes_pass * (iters_per_step / n_solves)
+        kname = "qpso_batch_kernel"
+        gpu_launches = prof["batch_launches"] + prof["prep_launches"]
+    else:
+        launches = max(1, prof["step_launches"])
+        kern_ms = prof["step_ms"] / launches
+        bytes_launch = bytes_pass / n_solves
+        kname = "qpso_step_kernel"
+        gpu_launches = prof["step_launches"] + prof["prep_launches"]
+    achieved = bytes_launch / (kern_ms / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_main / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "path": "batched" if batched_default else "plain",
+                   "solves_per_step": n_solves, "l2": "scrubbed (256 MB write) before every step",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "particle_renders_per_s": value * renders_per_step / n_solves,
+        "plain": {"value": plain_v, "unit": "solves/s"},
+        "batched": {"value": batch_v, "unit": "solves/s", "speedup_vs_plain": batch_v / plain_v},
+        "plain_batched_bit_identical": bool(agree), "device_error_bits": int(flags),
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(gpu_launches),
+        "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_kind,
+                     "traffic": traffic_per_launch(args.workload),
+                     "bytes_per_launch": bytes_launch, "avg_launch_ms": kern_ms,
+                     "model": "36F + 2A + 96 bytes per particle-render"},
+        "clocks": clocks,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w)
+    if rank == 0:
+        print(json.dumps(line))
+    for pd, pl in pinned:
+        pd.close()
+        pl.close()
+    ctx.close()
+    d.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c5"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

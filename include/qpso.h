@@ -95,6 +95,41 @@ qpso_status qpso_frame_upload(qpso_context *ctx, const uint16_t *depth_mm, const
                               const qpso_camera *cam, uint32_t *frame_id);
 qpso_status qpso_frame_release(qpso_context *ctx, uint32_t frame_id);
 
+/* Overwrite a resident frame's depth (and labels, if it has a label map)
+ * in place, without allocating: the per-frame input of a serving loop.
+ * Same role as qpso_frame_upload for a frame that is already resident. */
+qpso_status qpso_frame_update(qpso_context *ctx, uint32_t frame_id, const uint16_t *depth_mm,
+                              const int32_t *labels);
+
+/* Page-locked host buffers for fast uploads (cudaMallocHost).  No
+ * counterpart in the reference, which copies from pageable memory. */
+void *qpso_host_alloc(uint64_t bytes);
+void qpso_host_free(void *ptr);
+
+/* The CUDA stream (cudaStream_t) every call of this context runs on. */
+void *qpso_get_stream(const qpso_context *ctx);
+
+/* Device-time accounting of the solver kernels with CUDA events on the
+ * context stream (off by default).  No counterpart in the reference, whose
+ * timers are host gettimeofday (myTimer.h). */
+typedef struct {
+    uint64_t step_launches;    /* fused per-iteration kernels (plain path) */
+    double step_ms;            /* their summed device time */
+    uint64_t batch_launches;   /* persistent batched kernels */
+    double batch_ms;
+    uint64_t prep_launches;    /* mask / summed-area-table kernels */
+} qpso_profile;
+qpso_status qpso_set_profiling(qpso_context *ctx, int enable);
+qpso_status qpso_get_profile(qpso_context *ctx, qpso_profile *out, int reset);
+
+/* CUDA events on the context stream for timing whole calls on the device:
+ * record slot (0..63); elapsed waits for slot b and returns b - a in ms. */
+qpso_status qpso_timer_record(qpso_context *ctx, uint32_t slot);
+qpso_status qpso_timer_elapsed(qpso_context *ctx, uint32_t a, uint32_t b, float *ms);
+/* Write `bytes` of scratch device memory on the context stream so that the
+ * next call starts with a cold L2 (benchmark hygiene). */
+qpso_status qpso_scrub_l2(qpso_context *ctx, uint64_t bytes);
+
 /* Reference defaults (main.h:83-136, main.cu:128-132). */
 void qpso_solve_desc_init(qpso_solve_desc *desc);
 /* Translation box from a cluster centroid in mm (main.cu:1285-1323):

@@ -74,6 +74,7 @@ def lib():
         L.qo_domain_w.restype = C.c_int32
         L.qo_domain_h.restype = C.c_int32
         L.qo_solve.restype = C.c_int
+        L.qo_solve_mt.restype = C.c_int
         _lib = L
     return _lib
 
@@ -176,7 +177,7 @@ def update_particle(prm: Params, p: int, it: int, pos, vel, pb, gb):
 
 
 def solve(mesh: np.ndarray, num_faces: int, obs: np.ndarray, cam: Camera, prm: Params,
-          trace: bool = False):
+          trace: bool = False, threads: int = 1):
     P = prm.num_particles
     pos = np.zeros((NDIM, P), np.float32)
     vel = np.zeros((NDIM, P), np.float32)
@@ -187,10 +188,10 @@ def solve(mesh: np.ndarray, num_faces: int, obs: np.ndarray, cam: Camera, prm: P
     tf = np.zeros((prm.iterations, P), np.float32) if trace else None
     m = np.ascontiguousarray(mesh, np.float32)
     o = np.ascontiguousarray(obs, np.uint16)
-    rc = lib().qo_solve(ptr(m, _f), C.c_uint32(num_faces), ptr(o, _u16), C.byref(cam),
-                        C.byref(prm), ptr(pos, _f), ptr(vel, _f), ptr(pb, _f), ptr(pbf, _f),
-                        C.byref(res), ptr(tg, _f) if trace else None,
-                        ptr(tf, _f) if trace else None)
+    rc = lib().qo_solve_mt(ptr(m, _f), C.c_uint32(num_faces), ptr(o, _u16), C.byref(cam),
+                           C.byref(prm), ptr(pos, _f), ptr(vel, _f), ptr(pb, _f), ptr(pbf, _f),
+                           C.byref(res), ptr(tg, _f) if trace else None,
+                           ptr(tf, _f) if trace else None, C.c_int(threads))
     if rc != 0:
         raise RuntimeError("qo_solve failed: %d" % rc)
     out = {"fit": res.gbest_fit, "pose": np.array(res.gbest[:], np.float32), "pos": pos,

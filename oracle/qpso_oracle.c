@@ -11,6 +11,9 @@
 #include "qpso_oracle.h"
 
 #include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stdlib.h>
 #include <string.h>
 
@@ -672,20 +675,29 @@ void qo_default_params(qo_params *prm)
     prm->iterations = 50;
 }
 
-/* Host loop main.cu:1601-1727: init, then per iteration render + score every
- * particle, personal/global best update (main.cu:768-855, argmin with the
- * first minimum like thrust::min_element), then the particle update. */
-int qo_solve(const float *mesh, uint32_t F, const uint16_t *obs, const qo_camera *cam,
-             const qo_params *prm, float *pos, float *vel, float *pbest, float *pbest_fit,
-             qo_result *res, float *trace_gbest, float *trace_fit)
+/* Multi-threaded form of qo_solve: particles are rendered and scored in
+ * parallel (one z-buffer per thread); every result is identical. */
+int qo_solve_mt(const float *mesh, uint32_t F, const uint16_t *obs, const qo_camera *cam,
+                const qo_params *prm, float *pos, float *vel, float *pbest, float *pbest_fit,
+                qo_result *res, float *trace_gbest, float *trace_fit, int threads)
 {
     const uint32_t P = prm->num_particles;
     if (P == 0 || F == 0 || prm->num_points == 0) return -1;
+    if (threads < 1) threads = 1;
+    if ((uint32_t)threads > P) threads = (int)P;
     const size_t dn = (size_t)qo_domain_w(cam) * (size_t)qo_domain_h(cam);
-    int32_t *zbuf = (int32_t *)malloc(dn * sizeof(int32_t));
+    int32_t **zb = (int32_t **)calloc((size_t)threads, sizeof(int32_t *));
     float *fit = (float *)malloc(P * sizeof(float));
-    if (!zbuf || !fit) { free(zbuf); free(fit); return -2; }
-    qo_zbuf_reset(zbuf, cam);
+    int ok = zb && fit;
+    for (int t = 0; ok && t < threads; ++t) {
+        zb[t] = (int32_t *)malloc(dn * sizeof(int32_t));
+        if (!zb[t]) ok = 0; else qo_zbuf_reset(zb[t], cam);
+    }
+    if (!ok) {
+        if (zb) for (int t = 0; t < threads; ++t) free(zb[t]);
+        free(zb); free(fit);
+        return -2;
+    }
     const int32_t dw = qo_domain_w(cam);
 
     float gfit = 1.0e10f; /* max_best_fit_, main.h:100 */
@@ -696,18 +708,29 @@ int qo_solve(const float *mesh, uint32_t F, const uint16_t *obs, const qo_camera
         pbest_fit[p] = 1.0e10f;
     }
     for (uint32_t it = 0; it < prm->iterations; ++it) {
-        if (it > 0)
-            for (uint32_t p = 0; p < P; ++p) qo_update_particle(prm, p, it, pos, vel, pbest, g);
-        for (uint32_t p = 0; p < P; ++p) {
+        if (it > 0) {
+#pragma omp parallel for num_threads(threads) schedule(static)
+            for (int64_t p = 0; p < (int64_t)P; ++p)
+                qo_update_particle(prm, (uint32_t)p, it, pos, vel, pbest, g);
+        }
+        uint64_t wsum = 0;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1) reduction(+ : wsum)
+        for (int64_t pp = 0; pp < (int64_t)P; ++pp) {
+#ifdef _OPENMP
+            int32_t *zbuf = zb[omp_get_thread_num()];
+#else
+            int32_t *zbuf = zb[0];
+#endif
+            const uint32_t p = (uint32_t)pp;
             float s[7];
             for (int d = 0; d < 7; ++d) s[d] = pos[p + (size_t)d * P];
             int32_t box[4];
-            writes += (uint64_t)qo_render(mesh, F, s, cam, zbuf, box);
+            wsum += (uint64_t)qo_render(mesh, F, s, cam, zbuf, box);
             qo_score sc;
             qo_score_zbuf(zbuf, box, obs, cam, prm, &sc);
             fit[p] = sc.fit;
-            /* reset the touched rows of the render box (the reference's
-             * fitness kernel resets the pixels it visits) */
+            /* reset the touched part of the z-buffer (the reference's fitness
+             * kernel resets the pixels it visits) */
             int64_t x0 = box[0], x1 = box[1], y0 = box[2], y1 = box[3];
             if (x0 < -QO_GUARD) x0 = -QO_GUARD;
             if (y0 < -QO_GUARD) y0 = -QO_GUARD;
@@ -717,6 +740,7 @@ int qo_solve(const float *mesh, uint32_t F, const uint16_t *obs, const qo_camera
                 for (int64_t x = x0; x < x1; ++x)
                     zbuf[(size_t)(y + QO_GUARD) * (size_t)dw + (size_t)(x + QO_GUARD)] = QO_DEPTH_BG;
         }
+        writes += wsum;
         uint32_t best = 0;
         for (uint32_t p = 0; p < P; ++p) {
             if (fit[p] < pbest_fit[p]) {
@@ -739,7 +763,19 @@ int qo_solve(const float *mesh, uint32_t F, const uint16_t *obs, const qo_camera
     res->gbest_fit = gfit;
     for (int d = 0; d < 7; ++d) res->gbest[d] = g[d];
     res->raster_writes = writes;
-    free(zbuf);
+    for (int t = 0; t < threads; ++t) free(zb[t]);
+    free(zb);
     free(fit);
     return 0;
+}
+
+/* Host loop main.cu:1601-1727: init, then per iteration render + score every
+ * particle, personal/global best update (main.cu:768-855, argmin with the
+ * first minimum like thrust::min_element), then the particle update. */
+int qo_solve(const float *mesh, uint32_t F, const uint16_t *obs, const qo_camera *cam,
+             const qo_params *prm, float *pos, float *vel, float *pbest, float *pbest_fit,
+             qo_result *res, float *trace_gbest, float *trace_fit)
+{
+    return qo_solve_mt(mesh, F, obs, cam, prm, pos, vel, pbest, pbest_fit, res, trace_gbest,
+                       trace_fit, 1);
 }

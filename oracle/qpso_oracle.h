@@ -140,6 +140,11 @@ int qo_solve(const float *mesh, uint32_t num_faces, const uint16_t *obs,
              float *pos, float *vel, float *pbest, float *pbest_fit,
              qo_result *res, float *trace_gbest, float *trace_fit);
 
+int qo_solve_mt(const float *mesh, uint32_t num_faces, const uint16_t *obs,
+                const qo_camera *cam, const qo_params *prm,
+                float *pos, float *vel, float *pbest, float *pbest_fit,
+                qo_result *res, float *trace_gbest, float *trace_fit, int threads);
+
 void qo_default_params(qo_params *prm);
 
 #ifdef __cplusplus

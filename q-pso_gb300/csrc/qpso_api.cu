@@ -80,6 +80,13 @@ struct qpso_context {
   // batched-launch graph cache
   cudaGraphExec_t gexec = nullptr;
   std::vector<uint64_t> gkey;
+  // device-time accounting
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev;   // pool of timing events
+  cudaEvent_t gev[2] = {nullptr, nullptr};  // around the batched kernel in the graph
+  qpso_profile prof{};
+  cudaEvent_t timers[64] = {};
+  Buf scrub;
   std::mutex mu;
 };
 
@@ -127,6 +134,25 @@ qpso_status ensure_pin(qpso_context* ctx, size_t bytes) {
   QPSO_CUDA(ctx, cudaMallocHost(&ctx->pin.p, cap));
   ctx->pin.cap = cap;
   return QPSO_OK;
+}
+
+qpso_status ensure_events(qpso_context* ctx, size_t n) {
+  while (ctx->ev.size() < n) {
+    cudaEvent_t e;
+    QPSO_CUDA(ctx, cudaEventCreate(&e));
+    ctx->ev.push_back(e);
+  }
+  return QPSO_OK;
+}
+
+// Sum the device time between event pairs (2i, 2i+1), i < pairs.
+double event_pairs_ms(qpso_context* ctx, size_t pairs) {
+  double ms = 0.0;
+  for (size_t i = 0; i < pairs; ++i) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, ctx->ev[2 * i], ctx->ev[2 * i + 1]) == cudaSuccess) ms += t;
+  }
+  return ms;
 }
 
 bool valid_cfg(const qpso_launch_config& c, int smem_optin) {
@@ -353,6 +379,12 @@ void qpso_destroy(qpso_context* ctx) {
     cudaFree(kv.second.labels);
   }
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->timers)
+    if (e) cudaEventDestroy(e);
+  if (ctx->scrub.p) cudaFree(ctx->scrub.p);
+  for (cudaEvent_t e : ctx->gev)
+    if (e) cudaEventDestroy(e);
   if (ctx->ws.p) cudaFree(ctx->ws.p);
   if (ctx->pin.p) cudaFreeHost(ctx->pin.p);
   cudaStreamDestroy(ctx->stream);
@@ -447,6 +479,82 @@ qpso_status qpso_frame_release(qpso_context* ctx, uint32_t id) {
   return QPSO_OK;
 }
 
+qpso_status qpso_frame_update(qpso_context* ctx, uint32_t id, const uint16_t* depth,
+                              const int32_t* labels) {
+  if (!ctx || !depth) return fail(ctx, QPSO_ERR_ARG, "null argument");
+  auto it = ctx->frames.find(id);
+  if (it == ctx->frames.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown frame id");
+  FrameObj& f = it->second;
+  if (labels && !f.labels) return fail(ctx, QPSO_ERR_ARG, "frame was uploaded without labels");
+  cudaSetDevice(ctx->device);
+  const size_t npx = (size_t)f.cam.width * f.cam.height;
+  QPSO_CUDA(ctx, cudaMemcpyAsync(f.depth, depth, npx * 2, cudaMemcpyHostToDevice, ctx->stream));
+  if (labels)
+    QPSO_CUDA(ctx, cudaMemcpyAsync(f.labels, labels, npx * 4, cudaMemcpyHostToDevice, ctx->stream));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return QPSO_OK;
+}
+
+void* qpso_host_alloc(uint64_t bytes) {
+  void* p = nullptr;
+  if (bytes == 0 || cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void qpso_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+void* qpso_get_stream(const qpso_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+qpso_status qpso_set_profiling(qpso_context* ctx, int enable) {
+  if (!ctx) return QPSO_ERR_ARG;
+  ctx->profiling = enable != 0;
+  return QPSO_OK;
+}
+
+qpso_status qpso_get_profile(qpso_context* ctx, qpso_profile* out, int reset) {
+  if (!ctx || !out) return QPSO_ERR_ARG;
+  *out = ctx->prof;
+  if (reset) ctx->prof = qpso_profile{};
+  return QPSO_OK;
+}
+
+qpso_status qpso_timer_record(qpso_context* ctx, uint32_t slot) {
+  if (!ctx || slot >= 64) return fail(ctx, QPSO_ERR_ARG, "timer slot must be < 64");
+  cudaSetDevice(ctx->device);
+  if (!ctx->timers[slot]) QPSO_CUDA(ctx, cudaEventCreate(&ctx->timers[slot]));
+  QPSO_CUDA(ctx, cudaEventRecord(ctx->timers[slot], ctx->stream));
+  return QPSO_OK;
+}
+
+qpso_status qpso_timer_elapsed(qpso_context* ctx, uint32_t a, uint32_t b, float* ms) {
+  if (!ctx || !ms || a >= 64 || b >= 64 || !ctx->timers[a] || !ctx->timers[b])
+    return fail(ctx, QPSO_ERR_ARG, "timer slots not recorded");
+  QPSO_CUDA(ctx, cudaEventSynchronize(ctx->timers[b]));
+  QPSO_CUDA(ctx, cudaEventElapsedTime(ms, ctx->timers[a], ctx->timers[b]));
+  return QPSO_OK;
+}
+
+qpso_status qpso_scrub_l2(qpso_context* ctx, uint64_t bytes) {
+  if (!ctx || bytes == 0 || bytes > (8ull << 30)) return fail(ctx, QPSO_ERR_ARG, "scrub size");
+  cudaSetDevice(ctx->device);
+  if (ctx->scrub.cap < bytes) {
+    if (ctx->scrub.p) {
+      QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      cudaFree(ctx->scrub.p);
+      ctx->scrub.p = nullptr;
+      ctx->scrub.cap = 0;
+    }
+    QPSO_CUDA(ctx, cudaMalloc(&ctx->scrub.p, bytes));
+    ctx->scrub.cap = bytes;
+  }
+  static uint8_t flip = 0;
+  flip ^= 0x5a;
+  QPSO_CUDA(ctx, cudaMemsetAsync(ctx->scrub.p, flip, bytes, ctx->stream));
+  return QPSO_OK;
+}
+
 void qpso_solve_desc_init(qpso_solve_desc* d) {
   if (!d) return;
   std::memset(d, 0, sizeof(*d));
@@ -516,8 +624,13 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
                              fs[0]->cam.height, s));
   const Instance* dinst = reinterpret_cast<const Instance*>(d + L.inst);
   const uint32_t chunks = (desc->num_particles + cfg.ppb - 1) / cfg.ppb;
-  for (uint32_t it = 0; it < desc->iterations; ++it)
+  const bool prof = ctx->profiling;
+  if (prof && (st = ensure_events(ctx, 2 * (size_t)desc->iterations)) != QPSO_OK) return st;
+  for (uint32_t it = 0; it < desc->iterations; ++it) {
+    if (prof) QPSO_CUDA(ctx, cudaEventRecord(ctx->ev[2 * it], s));
     QPSO_CUDA(ctx, launch_step(dinst, it, chunks, cfg, s));
+    if (prof) QPSO_CUDA(ctx, cudaEventRecord(ctx->ev[2 * it + 1], s));
+  }
   QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
   const size_t P = desc->num_particles;
   if (trace)
@@ -530,6 +643,11 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
   if (pbest_fit)
     QPSO_CUDA(ctx, cudaMemcpyAsync(pbest_fit, d + L.pbf[0], P * 4, cudaMemcpyDeviceToHost, s));
   QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  if (prof) {
+    ctx->prof.step_launches += desc->iterations;
+    ctx->prof.step_ms += event_pairs_ms(ctx, desc->iterations);
+    ctx->prof.prep_launches += 3;
+  }
   const Header& hd = *reinterpret_cast<const Header*>(h + L.hdr);
   read_result(hd, result);
   if (hd.err & kErrBound) return fail(ctx, QPSO_ERR_INTERNAL, "raster bound violated");
@@ -581,6 +699,10 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   char* d = static_cast<char*>(ctx->ws.p);
   char* h = static_cast<char*>(ctx->pin.p);
   cudaStream_t s = ctx->stream;
+  if (!ctx->gev[0]) {
+    QPSO_CUDA(ctx, cudaEventCreate(&ctx->gev[0]));
+    QPSO_CUDA(ctx, cudaEventCreate(&ctx->gev[1]));
+  }
   std::vector<uint64_t> key = {(uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)h, L.total, L.meta_end,
                                n, items.size(), max_iters, (uint64_t)grid, (uint64_t)cfg.threads,
                                (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h};
@@ -603,7 +725,9 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     cudaError_t e = cudaMemcpyAsync(d, h, L.meta_end, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
       e = launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), (int)n, (int)max_w, (int)max_h, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->gev[0], s);
     if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->gev[1], s);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h + L.hdr, d + L.hdr, n * sizeof(Header), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
@@ -621,6 +745,12 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   }
   QPSO_CUDA(ctx, cudaGraphLaunch(ctx->gexec, s));
   QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  if (ctx->profiling) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, ctx->gev[0], ctx->gev[1]) == cudaSuccess) ctx->prof.batch_ms += t;
+    ctx->prof.batch_launches += 1;
+    ctx->prof.prep_launches += 3;
+  }
   const Header* hh = reinterpret_cast<const Header*>(h + L.hdr);
   bool bad = false;
   for (uint32_t i = 0; i < n; ++i) {

@@ -28,7 +28,9 @@ EXPORTS = [
     "qpso_mesh_release", "qpso_frame_upload", "qpso_frame_release", "qpso_solve_desc_init",
     "qpso_box_from_centroid", "qpso_set_launch_config", "qpso_get_launch_config", "qpso_solve",
     "qpso_solve_traced", "qpso_solve_batch", "qpso_score_poses", "qpso_render",
-    "qpso_barrier_selftest",
+    "qpso_barrier_selftest", "qpso_frame_update", "qpso_host_alloc", "qpso_host_free",
+    "qpso_get_stream", "qpso_set_profiling", "qpso_get_profile", "qpso_timer_record",
+    "qpso_timer_elapsed", "qpso_scrub_l2",
 ]
 
 
@@ -55,6 +57,12 @@ class Result(C.Structure):
 
 class LaunchConfig(C.Structure):
     _fields_ = [("threads", C.c_int32), ("tile_px", C.c_int32), ("ppb", C.c_int32)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("step_launches", C.c_uint64), ("step_ms", C.c_double),
+                ("batch_launches", C.c_uint64), ("batch_ms", C.c_double),
+                ("prep_launches", C.c_uint64)]
 
 
 class QpsoError(RuntimeError):
@@ -101,9 +109,22 @@ def load_library(path: str = LIB_PATH):
     L.qpso_render.argtypes = [vp, C.c_uint32, C.POINTER(Camera), C.c_void_p, C.c_int32,
                               C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
     L.qpso_barrier_selftest.argtypes = [vp, C.c_uint64, C.POINTER(C.c_uint32)]
+    L.qpso_frame_update.argtypes = [vp, C.c_uint32, C.c_void_p, C.c_void_p]
+    L.qpso_host_alloc.argtypes = [C.c_uint64]
+    L.qpso_host_alloc.restype = C.c_void_p
+    L.qpso_host_free.argtypes = [C.c_void_p]
+    L.qpso_host_free.restype = None
+    L.qpso_get_stream.argtypes = [vp]
+    L.qpso_get_stream.restype = C.c_void_p
+    L.qpso_set_profiling.argtypes = [vp, C.c_int]
+    L.qpso_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
+    L.qpso_timer_record.argtypes = [vp, C.c_uint32]
+    L.qpso_timer_elapsed.argtypes = [vp, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]
+    L.qpso_scrub_l2.argtypes = [vp, C.c_uint64]
     for fn in EXPORTS:
         if fn not in ("qpso_version", "qpso_destroy", "qpso_last_error", "qpso_solve_desc_init",
-                      "qpso_box_from_centroid"):
+                      "qpso_box_from_centroid", "qpso_host_alloc", "qpso_host_free",
+                      "qpso_get_stream"):
             getattr(L, fn).restype = C.c_int32
     _lib = L
     return L
@@ -241,10 +262,61 @@ class Context:
                                        out.ctypes.data, box.ctypes.data))
         return out, box
 
+    def frame_update(self, fid: int, depth_mm: np.ndarray, labels: np.ndarray | None = None):
+        self._check(self.L.qpso_frame_update(self.h, fid, depth_mm.ctypes.data,
+                                             None if labels is None else labels.ctypes.data))
+
+    def stream_handle(self) -> int:
+        return self.L.qpso_get_stream(self.h) or 0
+
+    def set_profiling(self, on: bool):
+        self._check(self.L.qpso_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self, reset: bool = False) -> dict:
+        p = Profile()
+        self._check(self.L.qpso_get_profile(self.h, C.byref(p), 1 if reset else 0))
+        return {k: getattr(p, k) for k, _ in Profile._fields_}
+
+    def timer_record(self, slot: int):
+        self._check(self.L.qpso_timer_record(self.h, slot))
+
+    def timer_elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        self._check(self.L.qpso_timer_elapsed(self.h, a, b, C.byref(ms)))
+        return ms.value
+
+    def scrub_l2(self, nbytes: int = 256 << 20):
+        self._check(self.L.qpso_scrub_l2(self.h, nbytes))
+
     def barrier_selftest(self, timeout_ns: int):
         bits = C.c_uint32()
         st = self.L.qpso_barrier_selftest(self.h, timeout_ns, C.byref(bits))
         return st, bits.value
+
+
+class PinnedArray:
+    """numpy view of a page-locked host buffer (qpso_host_alloc)."""
+
+    def __init__(self, shape, dtype):
+        L = load_library()
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.ptr = L.qpso_host_alloc(self.nbytes)
+        if not self.ptr:
+            raise MemoryError("qpso_host_alloc(%d) failed" % self.nbytes)
+        buf = (C.c_char * self.nbytes).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def close(self):
+        if self.ptr:
+            self.array = None
+            load_library().qpso_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def result_dict(r: Result) -> dict:

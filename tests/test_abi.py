@@ -25,7 +25,7 @@ def lib():
 def declared_functions():
     txt = open(HDR).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(qpso_[a-z_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(qpso_[a-z0-9_]+)\s*\(", txt)))
 
 
 def test_header_and_binding_agree():
@@ -40,15 +40,6 @@ def test_every_declared_symbol_is_exported(lib):
     exported = set(re.findall(r" T (qpso_\w+)", out))
     missing = [f for f in declared_functions() if f not in exported]
     assert not missing, missing
-
-
-def test_library_is_sm103a_only(lib):
-    out = subprocess.run(["/usr/local/cuda/bin/cuobjdump", "--list-elf", lib._name],
-                         capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    arches = set(re.findall(r"sm_(\d+a?)", out.stdout))
-    assert arches == {"103a"}, arches
 
 
 def test_struct_layout_matches_header(tmp_path):
