@@ -165,6 +165,33 @@ qpso_status qpso_solve_batch(qpso_context *ctx, const qpso_solve_desc *descs, ui
 qpso_status qpso_score_poses(qpso_context *ctx, const qpso_solve_desc *desc, const float *poses,
                              uint32_t n, float *fit_out);
 
+/* Pose scoring that allocates nothing (no counterpart in the reference).
+ * For callers that cannot let a library call cudaMalloc: applications whose
+ * device memory is owned by their own pool or caching allocator with a fixed
+ * budget, and real-time loops where cudaMalloc's implicit synchronisation
+ * and latency are not acceptable.  Same results as qpso_score_poses.
+ * Inputs and outputs are device pointers the caller owns: the mesh
+ * (loadOBJ3 layout, 9*num_faces floats), the depth frame (uint16 mm,
+ * cam->width*cam->height) and, when desc->cluster_label >= 0, its int32
+ * label map; n poses (n x 7 floats); fit_out (n floats); flags_out
+ * (optional, one uint32 of device error bits).  From desc only the cluster
+ * fields (label, AABB, num_points) are read; mesh_id and frame_id are
+ * ignored.  Work is queued on `stream` (a cudaStream_t, NULL for the legacy
+ * default stream) on the current device; results are ready when the stream
+ * is synchronised.  Intermediate buffers live in one 4 MiB device array
+ * fixed at load time (held by every GPU that loads the library until
+ * exit): frames above about 690,000 pixels (640x480 and 960x720 fit) are
+ * rejected with QPSO_ERR_ARG.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress), so make it before any
+ * stream capture.  All calls on a device share the array and leave their
+ * contents in it; calls that overlap on the GPU race, so issue them on one
+ * stream. */
+qpso_status qpso_score_poses_noalloc(const float *d_mesh_soa, uint32_t num_faces,
+                                     const uint16_t *d_depth_mm, const int32_t *d_labels,
+                                     const qpso_camera *cam, const qpso_solve_desc *desc,
+                                     const float *d_poses, uint32_t n, float *d_fit_out,
+                                     uint32_t *d_flags_out, void *stream);
+
 /* Render one pose of a mesh into a window [x0,x0+w) x [y0,y0+h) of the
  * raster domain (int32 mm, 60000 where nothing was drawn) and return the
  * render AABB {minx,maxx,miny,maxy}.  GPU counterpart of RenderCPU

@@ -90,6 +90,9 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
                                  cudaStream_t st);
 cudaError_t launch_barrier_probe(uint32_t* bar, uint32_t* err, uint32_t grid, uint32_t expected,
                                  unsigned long long timeout_ns, cudaStream_t st);
+cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* di, PrepDesc* dj,
+                                cudaStream_t st);
+cudaError_t launch_copy_flags(const uint32_t* src, uint32_t* dst, cudaStream_t st);
 size_t smem_ctl_bytes();
 
 }  // namespace qpso

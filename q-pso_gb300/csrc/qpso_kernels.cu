@@ -733,6 +733,24 @@ __global__ void __launch_bounds__(kMaxThreads) score_poses_kernel(const Instance
   }
 }
 
+// Writes the instance and preparation records of a scoring call into
+// caller-independent scratch and clears its header words (error bits,
+// counters), so nothing is copied from the host.
+__global__ void noalloc_init_kernel(Instance I, PrepDesc J, Instance* di, PrepDesc* dj) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  *di = I;
+  *dj = J;
+  for (int d = 0; d < 8; ++d) I.gbest[d] = 0.f;
+  *I.done = 0u;
+  *I.err = 0u;
+  I.stats[0] = 0ull;
+  I.stats[1] = 0ull;
+}
+
+__global__ void copy_flags_kernel(const uint32_t* src, uint32_t* dst) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
+}
+
 // ------------------------------------------------------------------------
 // Host launch wrappers.
 
@@ -812,6 +830,17 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
   cudaError_t e = ensure_smem(render_window_kernel, smem < 16 ? 16 : smem);
   if (e != cudaSuccess) return e;
   render_window_kernel<<<1, threads, smem < 16 ? 16 : smem, st>>>(inst, pose, x0, y0, w, h, out, box);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* di, PrepDesc* dj,
+                                cudaStream_t st) {
+  noalloc_init_kernel<<<1, 32, 0, st>>>(I, J, di, dj);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_flags(const uint32_t* src, uint32_t* dst, cudaStream_t st) {
+  copy_flags_kernel<<<1, 32, 0, st>>>(src, dst);
   return cudaGetLastError();
 }
 

@@ -30,7 +30,7 @@ EXPORTS = [
     "qpso_solve_traced", "qpso_solve_batch", "qpso_score_poses", "qpso_render",
     "qpso_barrier_selftest", "qpso_frame_update", "qpso_host_alloc", "qpso_host_free",
     "qpso_get_stream", "qpso_set_profiling", "qpso_get_profile", "qpso_timer_record",
-    "qpso_timer_elapsed", "qpso_scrub_l2",
+    "qpso_timer_elapsed", "qpso_scrub_l2", "qpso_score_poses_noalloc",
 ]
 
 
@@ -121,6 +121,9 @@ def load_library(path: str = LIB_PATH):
     L.qpso_timer_record.argtypes = [vp, C.c_uint32]
     L.qpso_timer_elapsed.argtypes = [vp, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]
     L.qpso_scrub_l2.argtypes = [vp, C.c_uint64]
+    L.qpso_score_poses_noalloc.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
+                                           C.POINTER(Camera), C.POINTER(SolveDesc), C.c_void_p,
+                                           C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
     for fn in EXPORTS:
         if fn not in ("qpso_version", "qpso_destroy", "qpso_last_error", "qpso_solve_desc_init",
                       "qpso_box_from_centroid", "qpso_host_alloc", "qpso_host_free",
