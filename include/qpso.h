@@ -142,6 +142,16 @@ qpso_status qpso_set_launch_config(qpso_context *ctx, const qpso_launch_config *
 qpso_status qpso_get_launch_config(const qpso_context *ctx, qpso_launch_config *plain,
                                    qpso_launch_config *batch);
 
+/* Autotuner (no counterpart in the reference, whose launch shape is the
+ * fixed 6x512 / 1x1024 of main.cu:1639,1674).  Times a short run (at most
+ * tune_iters iterations) of the given solves for every valid candidate
+ * (threads 128/256/512, tile 4K..32K px, 1/2/4 particles per work item)
+ * on the plain path (batched = 0) or the batched path (batched = 1),
+ * installs the fastest in the context and returns it.  Results do not
+ * depend on the launch shape, only the speed does. */
+qpso_status qpso_autotune(qpso_context *ctx, const qpso_solve_desc *descs, uint32_t n, int batched,
+                          uint32_t tune_iters, qpso_launch_config *best, float *best_ms);
+
 /* Plain solve: one fused launch per PSO iteration.  Replaces the host loop
  * main.cu:1601-1727 (InitQPSO, then per iteration 1024 render launches,
  * the AABB kernel, 1024 fitness launches, thrust::min_element,

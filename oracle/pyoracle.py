@@ -65,6 +65,9 @@ def lib():
         for fn in ("qo_sin", "qo_cos", "qo_acos"):
             getattr(L, fn).restype = C.c_double
             getattr(L, fn).argtypes = [C.c_double]
+        for fn in ("qo_sinf", "qo_cosf", "qo_acosf"):
+            getattr(L, fn).restype = C.c_float
+            getattr(L, fn).argtypes = [C.c_float]
         L.qo_raster_face.restype = C.c_int64
         L.qo_render.restype = C.c_int64
         L.qo_fitness_from_counts.restype = C.c_float
@@ -212,3 +215,15 @@ def cos(x):
 
 def acos(x):
     return lib().qo_acos(x)
+
+
+def sinf(x):
+    return lib().qo_sinf(x)
+
+
+def cosf(x):
+    return lib().qo_cosf(x)
+
+
+def acosf(x):
+    return lib().qo_acosf(x)

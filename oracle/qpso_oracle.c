@@ -54,11 +54,12 @@ float qo_uniform(uint64_t seed, uint32_t stream, uint32_t particle, uint32_t dra
 /* ------------------------------------------------------------------ */
 /* sin/cos/acos.  The reference calls CUDA's cosf/sinf/acosf under
  * -use_fast_math (main.h:287-294, 391-399; main.cu:946,970); those differ
- * between CUDA and libm, so both sides of this build use the same
- * double-precision series instead: Cody-Waite reduction by pi/2 (3-part
- * split, 30 bits per part) and Taylor polynomials on [-pi/4, pi/4]
- * (truncation < 1e-19); acos via asin's Taylor series on [0, 1/2] and
- * acos(x) = 2 asin(sqrt((1-x)/2)) above 1/2. */
+ * between CUDA and libm, so both sides of this build use the same series
+ * instead.  The double forms (Cody-Waite reduction by pi/2 in three 30-bit
+ * parts, Taylor polynomials on [-pi/4, pi/4], truncation < 1e-19; acos via
+ * asin's Taylor series on [0, 1/2] and acos(x) = 2 asin(sqrt((1-x)/2))
+ * above 1/2) serve as the reference and as the fallback of the fp32 forms
+ * below for arguments beyond 4096. */
 static const double QO_PIO2_1 = 1.5707963276654482;
 static const double QO_PIO2_2 = -8.705515692000731e-10;
 static const double QO_PIO2_3 = -3.50343439808993e-19;
@@ -169,9 +170,104 @@ double qo_acos(double x)
     return QO_PIO2 - qo_asin_kernel(x);
 }
 
-static float qo_sinf(float x) { return (float)qo_sin((double)x); }
-static float qo_cosf(float x) { return (float)qo_cos((double)x); }
-static float qo_acosf(float x) { return (float)qo_acos((double)x); }
+/* fp32 forms used by the PSO step: Cody-Waite reduction by pi/2 split in
+ * three parts of 12, 12 and 24 bits (k*P1 and k*P2 exact for |x| <= 4096,
+ * larger arguments fall back to the double routines), Taylor polynomials
+ * on [-pi/4, pi/4] (truncation < 7e-12), asin's Taylor series to x^23 on
+ * [0, 1/2] (truncation < 5e-10), all in fp32 with one rounding per
+ * operation.  GB300's fp64 pipe is narrow, so the step stays in fp32. */
+static const float QF_P1 = 1.57080078125f;
+static const float QF_P2 = -4.453584551811218e-06f;
+static const float QF_P3 = -8.705515752716053e-10f;
+static const float QF_2OPI = 0.6366197466850281f;
+static const float QF_PI = 3.1415927410125732f;
+static const float QF_PIO2 = 1.5707963705062866f;
+
+static float qf_sin_kernel(float r)
+{
+    const float r2 = r * r;
+    float p = -2.5052107943679403e-08f;
+    p = p * r2 + 2.7557318844628753e-06f;
+    p = p * r2 + -0.00019841270113829523f;
+    p = p * r2 + 0.008333333767950535f;
+    p = p * r2 + -0.1666666716337204f;
+    return r + r * (r2 * p);
+}
+
+static float qf_cos_kernel(float r)
+{
+    const float r2 = r * r;
+    float p = 2.0876755879584152e-09f;
+    p = p * r2 + -2.755731998149713e-07f;
+    p = p * r2 + 2.4801587642286904e-05f;
+    p = p * r2 + -0.0013888889225199819f;
+    p = p * r2 + 0.0416666679084301f;
+    p = p * r2 + -0.5f;
+    return 1.0f + r2 * p;
+}
+
+static float qf_reduce(float x, int *q)
+{
+    const float k = rintf(x * QF_2OPI);
+    float r = x - k * QF_P1;
+    r = r - k * QF_P2;
+    r = r - k * QF_P3;
+    *q = (int)((long)k & 3);
+    return r;
+}
+
+float qo_sinf(float x)
+{
+    if (x != x || isinf(x)) return x - x;
+    if (fabsf(x) > 4096.0f) return (float)qo_sin((double)x);
+    int q;
+    const float r = qf_reduce(x, &q);
+    switch (q) {
+    case 0: return qf_sin_kernel(r);
+    case 1: return qf_cos_kernel(r);
+    case 2: return -qf_sin_kernel(r);
+    default: return -qf_cos_kernel(r);
+    }
+}
+
+float qo_cosf(float x)
+{
+    if (x != x || isinf(x)) return x - x;
+    if (fabsf(x) > 4096.0f) return (float)qo_cos((double)x);
+    int q;
+    const float r = qf_reduce(x, &q);
+    switch (q) {
+    case 0: return qf_cos_kernel(r);
+    case 1: return -qf_sin_kernel(r);
+    case 2: return -qf_cos_kernel(r);
+    default: return qf_sin_kernel(r);
+    }
+}
+
+static const float QF_ASIN_C[11] = {
+    0.1666666716337204f, 0.07500000298023224f, 0.0446428582072258f, 0.0303819440305233f,
+    0.022372158244252205f, 0.017352763563394547f, 0.013964843936264515f, 0.01155180111527443f,
+    0.009761609137058258f, 0.008390335366129875f, 0.007312525995075703f};
+
+static float qf_asin_kernel(float x)
+{
+    const float x2 = x * x;
+    float p = QF_ASIN_C[10];
+    for (int i = 9; i >= 0; --i) p = p * x2 + QF_ASIN_C[i];
+    return x + x * (x2 * p);
+}
+
+/* acos with the argument clamped to [-1, 1] (DEVIATION: the reference's
+ * acosf of a dot product that rounds to 1 + ulp is NaN). */
+float qo_acosf(float x)
+{
+    if (x != x) return x;
+    if (x > 1.0f) x = 1.0f;
+    if (x < -1.0f) x = -1.0f;
+    if (x > 0.5f) return 2.0f * qf_asin_kernel(sqrtf((1.0f - x) * 0.5f));
+    if (x < -0.5f) return QF_PI - 2.0f * qf_asin_kernel(sqrtf((1.0f + x) * 0.5f));
+    return QF_PIO2 - qf_asin_kernel(x);
+}
 
 /* ------------------------------------------------------------------ */
 /* Quaternion helpers.  State vectors are [tx,ty,tz,q0,q1,q2,q3]

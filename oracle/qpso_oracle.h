@@ -26,8 +26,8 @@
  *   - int32 edge arithmetic wraps modulo 2^32, right shifts are arithmetic,
  *     float->int conversion rounds half to even and saturates (NaN -> 0),
  *     exactly like cvt.rni.s32.f32;
- *   - sin, cos and acos are this project's own double-precision series
- *     (qo_sin/qo_cos/qo_acos) rounded to float, not libm or CUDA's;
+ *   - sin, cos and acos are this project's own fp32 series
+ *     (qo_sinf/qo_cosf/qo_acosf), not libm or CUDA's;
  *   - random numbers come from Philox4x32-10 (Salmon et al., SC'11).
  */
 #ifndef QPSO_ORACLE_H
@@ -87,6 +87,9 @@ float qo_uniform(uint64_t seed, uint32_t stream, uint32_t particle, uint32_t dra
 double qo_sin(double x);
 double qo_cos(double x);
 double qo_acos(double x);
+float qo_sinf(float x);
+float qo_cosf(float x);
+float qo_acosf(float x);
 
 /* ---- quaternion helpers (7-float PSO state vectors) ---- */
 void qo_quat_prod(const float *p, const float *q, float *out);

@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "--fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-I", INCLUDE, "-I", CSRC]
 UNITS = ["qpso_kernels.cu", "qpso_api.cu", "qpso_noalloc.cu"]
-HEADERS = ["qpso_device.cuh", "qpso_internal.cuh"]
+HEADERS = ["qpso_device.cuh", "qpso_internal.cuh", "meshlets.h"]
 
 
 def _sources():

@@ -18,6 +18,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "meshlets.h"
 #include "qpso.h"
 #include "qpso_internal.cuh"
 
@@ -25,10 +26,15 @@ using namespace qpso;
 
 namespace {
 
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
 struct MeshObj {
   float* d = nullptr;
   uint32_t F = 0;
   float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  MeshletHdr* mlets = nullptr;       // device
+  unsigned char* blob = nullptr;     // device
+  uint32_t n_mlets = 0;
 };
 
 struct FrameObj {
@@ -59,8 +65,6 @@ struct Layout {
   size_t total = 0;
   std::vector<size_t> obs, sat, pos, vel, pbest, pbf, fit, trace;
 };
-
-size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 }  // namespace
 
@@ -157,8 +161,8 @@ double event_pairs_ms(qpso_context* ctx, size_t pairs) {
 
 bool valid_cfg(const qpso_launch_config& c, int smem_optin) {
   return c.threads >= 32 && c.threads <= 1024 && c.threads % 32 == 0 && c.tile_px >= 64 &&
-         c.tile_px % 8 == 0 && (size_t)c.tile_px * 4 <= (size_t)smem_optin && c.ppb >= 1 &&
-         c.ppb <= 16;
+         c.tile_px % 8 == 0 && c.ppb >= 1 && c.ppb <= 16 && c.threads >= 8 * c.ppb &&
+         fused_smem_bytes(c.threads, c.ppb, c.tile_px) <= (size_t)smem_optin;
 }
 
 qpso_status check_desc(qpso_context* ctx, const qpso_solve_desc& d, const MeshObj** m,
@@ -276,6 +280,9 @@ void fill_meta(qpso_context* ctx, const Layout& L, const std::vector<const qpso_
     Instance& I = hi[i];
     I.mesh = m.d;
     I.F = m.F;
+    I.mlets = m.mlets;
+    I.mlet_blob = m.blob;
+    I.n_mlets = m.n_mlets;
     for (int k = 0; k < 3; ++k) {
       I.mesh_lo[k] = m.lo[k];
       I.mesh_hi[k] = m.hi[k];
@@ -365,6 +372,8 @@ qpso_status qpso_create(int device, qpso_context** out) {
   }
   ctx->num_sms = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin - (int)smem_ctl_bytes() - 1024;
+  ctx->plain = TileConfig{256, 8192, 1};
+  ctx->batch = TileConfig{256, 8192, 1};
   *out = ctx;
   return QPSO_OK;
 }
@@ -373,7 +382,11 @@ void qpso_destroy(qpso_context* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  for (auto& kv : ctx->meshes) cudaFree(kv.second.d);
+  for (auto& kv : ctx->meshes) {
+    cudaFree(kv.second.d);
+    cudaFree(kv.second.mlets);
+    cudaFree(kv.second.blob);
+  }
   for (auto& kv : ctx->frames) {
     cudaFree(kv.second.depth);
     cudaFree(kv.second.labels);
@@ -398,12 +411,23 @@ qpso_status qpso_mesh_upload(qpso_context* ctx, const float* soa, uint32_t F, ui
   for (size_t i = 0; i < 9 * (size_t)F; ++i)
     if (!std::isfinite(soa[i])) return fail(ctx, QPSO_ERR_ARG, "mesh has a non-finite coordinate");
   cudaSetDevice(ctx->device);
+  std::vector<MeshletHdr> hdr;
+  std::vector<unsigned char> blob;
+  build_meshlets(soa, F, hdr, blob);
   MeshObj m;
   m.F = F;
+  m.n_mlets = (uint32_t)hdr.size();
   QPSO_CUDA(ctx, cudaMalloc(&m.d, 9 * (size_t)F * sizeof(float) + 32));
+  cudaError_t e = cudaMalloc(&m.mlets, hdr.size() * sizeof(MeshletHdr));
+  if (e == cudaSuccess) e = cudaMalloc(&m.blob, blob.size());
   float* dbox = m.d + 9 * (size_t)F;
-  cudaError_t e = cudaMemcpyAsync(m.d, soa, 9 * (size_t)F * sizeof(float), cudaMemcpyHostToDevice,
-                                  ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(m.d, soa, 9 * (size_t)F * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(m.mlets, hdr.data(), hdr.size() * sizeof(MeshletHdr), cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(m.blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = launch_mesh_aabb(m.d, F, dbox, ctx->stream);
   float box[6];
   if (e == cudaSuccess)
@@ -411,6 +435,8 @@ qpso_status qpso_mesh_upload(qpso_context* ctx, const float* soa, uint32_t F, ui
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     cudaFree(m.d);
+    if (m.mlets) cudaFree(m.mlets);
+    if (m.blob) cudaFree(m.blob);
     return cuda_fail(ctx, e, "mesh upload");
   }
   for (int k = 0; k < 3; ++k) {
@@ -430,6 +456,8 @@ qpso_status qpso_mesh_release(qpso_context* ctx, uint32_t id) {
   if (it == ctx->meshes.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown mesh id");
   cudaStreamSynchronize(ctx->stream);
   cudaFree(it->second.d);
+  cudaFree(it->second.mlets);
+  cudaFree(it->second.blob);
   ctx->meshes.erase(it);
   return QPSO_OK;
 }
@@ -725,9 +753,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     cudaError_t e = cudaMemcpyAsync(d, h, L.meta_end, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
       e = launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), (int)n, (int)max_w, (int)max_h, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->gev[0], s);
     if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->gev[1], s);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h + L.hdr, d + L.hdr, n * sizeof(Header), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
@@ -743,7 +769,11 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     }
     ctx->gkey = key;
   }
+  // device time of the replayed graph: metadata upload, preparation, the
+  // persistent kernel and the result read-back (the kernel dominates)
+  if (ctx->profiling) QPSO_CUDA(ctx, cudaEventRecord(ctx->gev[0], s));
   QPSO_CUDA(ctx, cudaGraphLaunch(ctx->gexec, s));
+  if (ctx->profiling) QPSO_CUDA(ctx, cudaEventRecord(ctx->gev[1], s));
   QPSO_CUDA(ctx, cudaStreamSynchronize(s));
   if (ctx->profiling) {
     float t = 0.f;
@@ -763,6 +793,61 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   return QPSO_OK;
 }
 
+qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint32_t n, int batched,
+                          uint32_t tune_iters, qpso_launch_config* best, float* best_ms) {
+  if (!ctx || !descs || n == 0 || tune_iters == 0) return fail(ctx, QPSO_ERR_ARG, "bad autotune arguments");
+  std::vector<qpso_solve_desc> ds(descs, descs + n);
+  for (auto& d : ds) d.iterations = std::min(d.iterations, tune_iters);
+  const TileConfig saved = batched ? ctx->batch : ctx->plain;
+  TileConfig win = saved;
+  float win_ms = 3.0e38f;
+  std::vector<qpso_result> res(n);
+  qpso_status st = QPSO_OK;
+  if (!ctx->timers[0]) QPSO_CUDA(ctx, cudaEventCreate(&ctx->timers[0]));
+  if (!ctx->timers[1]) QPSO_CUDA(ctx, cudaEventCreate(&ctx->timers[1]));
+  const int threads[] = {128, 256, 512};
+  const int tiles[] = {4096, 8192, 16384, 32768};
+  const int ppbs[] = {1, 2, 4};
+  for (int th : threads)
+    for (int tp : tiles)
+      for (int pb : ppbs) {
+        const qpso_launch_config c{th, tp, pb};
+        if (!valid_cfg(c, ctx->smem_optin)) continue;
+        const TileConfig tc{th, tp, pb};
+        if (batched) {
+          int per_sm = 0;
+          if (batch_max_grid(tc, &per_sm) != cudaSuccess || per_sm <= 0) continue;
+          ctx->batch = tc;
+        } else {
+          ctx->plain = tc;
+        }
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && st == QPSO_OK; ++rep) {  // rep 0 warms up (graph capture)
+          QPSO_CUDA(ctx, cudaEventRecord(ctx->timers[0], ctx->stream));
+          if (batched) {
+            st = qpso_solve_batch(ctx, ds.data(), n, res.data());
+          } else {
+            for (uint32_t i = 0; i < n && st == QPSO_OK; ++i) st = qpso_solve(ctx, &ds[i], &res[i]);
+          }
+          QPSO_CUDA(ctx, cudaEventRecord(ctx->timers[1], ctx->stream));
+          QPSO_CUDA(ctx, cudaEventSynchronize(ctx->timers[1]));
+          QPSO_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->timers[0], ctx->timers[1]));
+        }
+        if (st != QPSO_OK) {
+          if (batched) ctx->batch = saved; else ctx->plain = saved;
+          return st;
+        }
+        if (ms < win_ms) {
+          win_ms = ms;
+          win = tc;
+        }
+      }
+  if (batched) ctx->batch = win; else ctx->plain = win;
+  if (best) *best = qpso_launch_config{win.threads, win.tile_px, win.ppb};
+  if (best_ms) *best_ms = win_ms;
+  return QPSO_OK;
+}
+
 qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, const float* poses,
                              uint32_t n, float* fit_out) {
   if (!ctx || !desc || !poses || !fit_out || n == 0) return fail(ctx, QPSO_ERR_ARG, "null argument");
@@ -779,7 +864,8 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   if ((st = ensure_ws(ctx, total)) != QPSO_OK) return st;
   if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
   QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  fill_meta(ctx, L, ds, ms, fs, {}, 1, false);
+  const TileConfig cfg = ctx->plain;
+  fill_meta(ctx, L, ds, ms, fs, {}, (uint32_t)cfg.ppb, false);
   char* d = static_cast<char*>(ctx->ws.p);
   char* h = static_cast<char*>(ctx->pin.p);
   cudaStream_t s = ctx->stream;
@@ -788,10 +874,11 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
                              fs[0]->cam.height, s));
   QPSO_CUDA(ctx, cudaMemcpyAsync(d + pose_off, poses, (size_t)n * 7 * sizeof(float),
                                  cudaMemcpyHostToDevice, s));
-  const int grid = (int)std::min<uint32_t>(n, (uint32_t)ctx->num_sms * 4);
-  QPSO_CUDA(ctx, launch_score(reinterpret_cast<const Instance*>(d + L.inst),
-                              reinterpret_cast<const float*>(d + pose_off), n,
-                              reinterpret_cast<float*>(d + fit_off), ctx->plain, grid, s));
+  const uint32_t groups = (n + cfg.ppb - 1) / cfg.ppb;
+  const int grid = (int)std::min<uint32_t>(groups, (uint32_t)ctx->num_sms * 4);
+  QPSO_CUDA(ctx, launch_score_mlets(reinterpret_cast<const Instance*>(d + L.inst),
+                                    reinterpret_cast<const float*>(d + pose_off), n,
+                                    reinterpret_cast<float*>(d + fit_off), cfg, grid, s));
   QPSO_CUDA(ctx, cudaMemcpyAsync(fit_out, d + fit_off, (size_t)n * sizeof(float),
                                  cudaMemcpyDeviceToHost, s));
   QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));

@@ -8,9 +8,9 @@
 //     main.h:30-33,538-540);
 //   * int32 edge arithmetic wraps modulo 2^32 (done in uint32), right shifts
 //     are arithmetic, float->int is cvt.rni (half-even, saturating);
-//   * sin, cos and acos are this project's double-precision series, not
-//     CUDA's math library (the reference's fast-math cosf/sinf/acosf differ
-//     from any host libm);
+//   * sin, cos and acos are this project's fp32 series, not CUDA's math
+//     library (the reference's fast-math cosf/sinf/acosf differ from any
+//     host libm);
 //   * random numbers are Philox4x32-10 (Salmon et al., SC'11) keyed by
 //     (seed) with counter (draw/4, particle, stream, 0).
 #pragma once
@@ -157,6 +157,89 @@ __device__ __forceinline__ double dacos(double x) {
   return 1.5707963267948966 - asin_kernel(x);
 }
 
+// fp32 forms used by the PSO step (the double forms above are their
+// fallback beyond |x| = 4096): Cody-Waite reduction with pi/2 split in 12 +
+// 12 + 24 bits, Taylor polynomials on [-pi/4, pi/4], asin's Taylor series
+// to x^23 on [0, 1/2].  GB300's fp64 pipe is narrow, so the step stays fp32.
+__device__ __forceinline__ float fsin_kernel(float r) {
+  const float r2 = r * r;
+  float p = -2.5052107943679403e-08f;
+  p = p * r2 + 2.7557318844628753e-06f;
+  p = p * r2 + -0.00019841270113829523f;
+  p = p * r2 + 0.008333333767950535f;
+  p = p * r2 + -0.1666666716337204f;
+  return r + r * (r2 * p);
+}
+
+__device__ __forceinline__ float fcos_kernel(float r) {
+  const float r2 = r * r;
+  float p = 2.0876755879584152e-09f;
+  p = p * r2 + -2.755731998149713e-07f;
+  p = p * r2 + 2.4801587642286904e-05f;
+  p = p * r2 + -0.0013888889225199819f;
+  p = p * r2 + 0.0416666679084301f;
+  p = p * r2 + -0.5f;
+  return 1.0f + r2 * p;
+}
+
+__device__ __forceinline__ float freduce(float x, int* q) {
+  const float k = rintf(x * 0.6366197466850281f);
+  float r = x - k * 1.57080078125f;
+  r = r - k * -4.453584551811218e-06f;
+  r = r - k * -8.705515752716053e-10f;
+  *q = (int)((long long)k & 3);
+  return r;
+}
+
+__device__ __forceinline__ float fsin(float x) {
+  if (x != x || isinf(x)) return x - x;
+  if (fabsf(x) > 4096.0f) return (float)dsin((double)x);
+  int q;
+  const float r = freduce(x, &q);
+  switch (q) {
+    case 0: return fsin_kernel(r);
+    case 1: return fcos_kernel(r);
+    case 2: return -fsin_kernel(r);
+    default: return -fcos_kernel(r);
+  }
+}
+
+__device__ __forceinline__ float fcos(float x) {
+  if (x != x || isinf(x)) return x - x;
+  if (fabsf(x) > 4096.0f) return (float)dcos((double)x);
+  int q;
+  const float r = freduce(x, &q);
+  switch (q) {
+    case 0: return fcos_kernel(r);
+    case 1: return -fsin_kernel(r);
+    case 2: return -fcos_kernel(r);
+    default: return fsin_kernel(r);
+  }
+}
+
+__device__ __forceinline__ float fasin_kernel(float x) {
+  const float c[11] = {0.1666666716337204f,   0.07500000298023224f,  0.0446428582072258f,
+                       0.0303819440305233f,   0.022372158244252205f, 0.017352763563394547f,
+                       0.013964843936264515f, 0.01155180111527443f,  0.009761609137058258f,
+                       0.008390335366129875f, 0.007312525995075703f};
+  const float x2 = x * x;
+  float p = c[10];
+#pragma unroll
+  for (int i = 9; i >= 0; --i) p = p * x2 + c[i];
+  return x + x * (x2 * p);
+}
+
+// acos with its argument clamped to [-1, 1] (the reference's acosf of a
+// dot product that rounds to 1 + ulp is NaN and kills the particle).
+__device__ __forceinline__ float facos(float x) {
+  if (x != x) return x;
+  if (x > 1.0f) x = 1.0f;
+  if (x < -1.0f) x = -1.0f;
+  if (x > 0.5f) return 2.0f * fasin_kernel(sqrtf((1.0f - x) * 0.5f));
+  if (x < -0.5f) return 3.1415927410125732f - 2.0f * fasin_kernel(sqrtf((1.0f + x) * 0.5f));
+  return 1.5707963705062866f - fasin_kernel(x);
+}
+
 // ------------------------------------------------------------------------
 // Quaternion algebra on 7-float state vectors [tx,ty,tz,q0,q1,q2,q3].
 
@@ -207,13 +290,13 @@ __device__ __forceinline__ void kinematics(const float* from, float* s, const fl
   wt[kQ3] = w[kQ3] * 0.5f;
   const float nrm = sqrtf(wt[kQ1] * wt[kQ1] + wt[kQ2] * wt[kQ2] + wt[kQ3] * wt[kQ3]);
   const float dom = nrm * 0.5f;
-  const float cosw = (float)dcos((double)dom);
+  const float cosw = fcos(dom);
   float sinw;
   if (dom < kMinNorm) {
     sinw = 1.0f;
   } else {
     const float r = 1.0f / dom;
-    sinw = (float)dsin((double)dom) * r;
+    sinw = fsin(dom) * r;
   }
   float qxw[4];
   quat_prod(from, wt, qxw);
@@ -302,7 +385,7 @@ __device__ __forceinline__ void update_particle(const SolveParams& prm, uint32_t
   const float nc = sqrtf(qc[1] * qc[1] + qc[2] * qc[2] + qc[3] * qc[3]);
   if (nc > kMinNorm) {
     const float rn = 1.0f / nc;
-    const float a = 2.0f * (float)dacos((double)qc[0]) * rn;
+    const float a = 2.0f * facos(qc[0]) * rn;
     wc[0] = qc[1] * a;
     wc[1] = qc[2] * a;
     wc[2] = qc[3] * a;
@@ -312,7 +395,7 @@ __device__ __forceinline__ void update_particle(const SolveParams& prm, uint32_t
   const float ns = sqrtf(qs[1] * qs[1] + qs[2] * qs[2] + qs[3] * qs[3]);
   if (ns > kMinNorm) {
     const float rn = 1.0f / ns;
-    const float a = 2.0f * (float)dacos((double)qs[0]) * rn;
+    const float a = 2.0f * facos(qs[0]) * rn;
     ws[0] = qs[1] * a;
     ws[1] = qs[2] * a;
     ws[2] = qs[3] * a;
@@ -386,14 +469,11 @@ struct FaceSetup {
   bool live;                  // front-facing with a non-empty rectangle
 };
 
-__device__ __forceinline__ void setup_face(float u1, float v1, float w1, float u2, float v2,
-                                           float w2, float u3, float v3, float w3, FaceSetup& f) {
-  const int32_t Y1 = __float2int_rn(16.0f * v1);
-  const int32_t Y2 = __float2int_rn(16.0f * v2);
-  const int32_t Y3 = __float2int_rn(16.0f * v3);
-  const int32_t X1 = __float2int_rn(16.0f * u1);
-  const int32_t X2 = __float2int_rn(16.0f * u2);
-  const int32_t X3 = __float2int_rn(16.0f * u3);
+// Set-up from the snapped 28.4 vertex coordinates X = rn(16 u), Y = rn(16 v)
+// (main.h:1333-1338) and the vertex depths in mm.
+__device__ __forceinline__ void setup_face_fixed(int32_t X1, int32_t Y1, float w1, int32_t X2, int32_t Y2,
+                                                 float w2, int32_t X3, int32_t Y3, float w3,
+                                                 FaceSetup& f) {
   f.minx = wadd(min(min(X1, X2), X3), 0xF) >> 4;
   f.maxx = wadd(max(max(X1, X2), X3), 0xF) >> 4;
   f.miny = wadd(min(min(Y1, Y2), Y3), 0xF) >> 4;
@@ -418,6 +498,13 @@ __device__ __forceinline__ void setup_face(float u1, float v1, float w1, float u
   f.z1 = w1;
   f.z2 = (w2 - w1) * rA;
   f.z3 = (w3 - w1) * rA;
+}
+
+__device__ __forceinline__ void setup_face(float u1, float v1, float w1, float u2, float v2,
+                                           float w2, float u3, float v3, float w3, FaceSetup& f) {
+  setup_face_fixed(__float2int_rn(16.0f * u1), __float2int_rn(16.0f * v1), w1,
+                   __float2int_rn(16.0f * u2), __float2int_rn(16.0f * v2), w2,
+                   __float2int_rn(16.0f * u3), __float2int_rn(16.0f * v3), w3, f);
 }
 
 // Depth written at pixel (minx+rx, miny+ry) of a live face (main.h:1432-1448):

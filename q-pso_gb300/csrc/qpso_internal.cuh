@@ -6,6 +6,7 @@
 
 #include <cstdint>
 
+#include "meshlets.h"
 #include "qpso_device.cuh"
 
 namespace qpso {
@@ -22,6 +23,9 @@ enum : uint32_t {
 struct Instance {
   const float* mesh;        // loadOBJ3 layout, 9*F floats (main.h:620-679)
   uint32_t F;
+  const MeshletHdr* mlets;  // meshlets of the same faces (the fused kernels read these)
+  const unsigned char* mlet_blob;
+  uint32_t n_mlets;
   float mesh_lo[3], mesh_hi[3];
   const uint16_t* obs;      // cluster-masked observed depth (mm), width*height
   const int32_t* sat;       // (height+1) x (width+1) counts of obs != 0
@@ -85,6 +89,9 @@ cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg,
 cudaError_t batch_max_grid(const TileConfig& cfg, int* blocks_per_sm);
 cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
                          const TileConfig& cfg, int grid, cudaStream_t st);
+cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
+                               const TileConfig& cfg, int grid, cudaStream_t st);
+size_t fused_smem_bytes(int threads, int ppb, int tile_px);
 cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_t x0, int32_t y0,
                                  int32_t w, int32_t h, int32_t* out, int32_t* box, int threads,
                                  cudaStream_t st);

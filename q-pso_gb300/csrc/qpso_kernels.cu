@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "qpso_internal.cuh"
 
@@ -84,14 +86,36 @@ __device__ __forceinline__ uint32_t sat_count(const int32_t* sat, int32_t w, int
   return (uint32_t)(a - b - c + d);
 }
 
+// Per-particle bookkeeping of the meshlet path.
+struct PartCtl {
+  int32_t bound[4];                 // conservative pixel bound (domain-clipped)
+  int32_t tx0, tw, cw, th, ncol, nrow, npass;
+  int32_t x0, y0, cwp, thp;         // current band
+  int32_t box[4];                   // render AABB (shared-memory atomics)
+  uint32_t nR, nNo, nSegR;
+  uint64_t lo, hi;
+};
+
+constexpr int kCullCap = 512;  // meshlets whose per-particle rectangles are kept
+
+// Dynamic shared memory of the fused kernels.
+struct FusedSmem {
+  int4* vcache;          // [warps][kMletVerts] snapped X, Y and depth bits, per warp
+  int4* mbox;            // [ppb][kCullCap] meshlet rectangles (minx, maxx, miny, maxy)
+  int32_t* tiles;        // [ppb][tile_px] depth tiles
+};
+
 struct SmemCtl {
   float pose[kMaxPpb][8];
   int32_t bound[4];
   uint32_t claim;
   int last;
+  int maxpass;
   Partial warp[kMaxThreads / 32];
   float argv[kMaxThreads / 32];
   uint32_t argi[kMaxThreads / 32];
+  PartCtl part[kMaxPpb];
+  float corner[kMaxPpb][8][3];
 };
 
 // Conservative pixel bound of every face's raster rectangle at pose s: the
@@ -322,8 +346,357 @@ __device__ float render_score(const Instance& I, const float* s, int32_t* tile, 
   return fitv;
 }
 
+// ------------------------------------------------------------------------
+// Meshlet path: the fused kernels' render + score of up to kMaxPpb
+// particles at once.  Warps work independently on (particle, meshlet)
+// items: every unique vertex of the meshlet is transformed once into the
+// warp's vertex cache (28.4 snapped X, Y and depth z), the faces are set up
+// from the cache and rasterised into the particle's int32 tile in shared
+// memory; the CTA synchronises only between passes.  The tile is scanned
+// over the exact render AABB only.
+
+// Exact i / d for i < 2^16 and 1 <= d <= 2^10 through a float reciprocal:
+// (i + 0.5) / d is at least 1/(2d) away from the next integer.
+__device__ __forceinline__ int32_t small_div(int32_t i, float rd) {
+  return __float2int_rz(((float)i + 0.5f) * rd);
+}
+
+struct BlockSums {
+  uint32_t nR, nNo, nSegR;
+  uint64_t lo, hi;
+};
+
+// Per-particle tiling of its conservative bound (same rule as render_score).
+__device__ __forceinline__ void plan_tiles(PartCtl& pc, int tile_px) {
+  const int32_t bx0 = pc.bound[0], bx1 = pc.bound[1], by0 = pc.bound[2], by1 = pc.bound[3];
+  pc.tx0 = bx0 & ~7;
+  pc.tw = ((bx1 - pc.tx0) + 7) & ~7;
+  const int32_t bh = by1 - by0;
+  int32_t cw = pc.tw < tile_px ? pc.tw : (tile_px & ~7);
+  if (cw < 8) cw = 8;
+  pc.cw = cw;
+  pc.th = tile_px / cw;
+  pc.ncol = pc.tw > 0 ? (pc.tw + cw - 1) / cw : 0;
+  pc.nrow = (bh > 0 && pc.th > 0) ? (bh + pc.th - 1) / pc.th : 0;
+  pc.npass = (pc.ncol * pc.nrow) > 0 ? pc.ncol * pc.nrow : 1;
+}
+
+__device__ __forceinline__ FusedSmem carve_smem(unsigned char* dyn, int ppb) {
+  FusedSmem sm;
+  size_t o = 0;
+  sm.vcache = reinterpret_cast<int4*>(dyn + o);
+  o += (size_t)(blockDim.x >> 5) * kMletVerts * 16;
+  sm.mbox = reinterpret_cast<int4*>(dyn + o);
+  o += (size_t)ppb * kCullCap * 16;
+  sm.tiles = reinterpret_cast<int32_t*>(dyn + o);
+  return sm;
+}
+
+// Half-open rectangle overlap test (face rectangles are [min, max)).
+__device__ __forceinline__ bool rect_overlaps(const int4& b, const PartCtl& pc) {
+  return pc.cwp > 0 && pc.thp > 0 && b.x < pc.x0 + pc.cwp && b.y > pc.x0 && b.z < pc.y0 + pc.thp &&
+         b.w > pc.y0;
+}
+
+// Render + score particles 0..np-1 whose poses are in ctl.pose.  All
+// threads call this; fitness k is returned in fit_out[k] (shared memory).
+// When a particle's conservative bound needs several tile passes, pass 0
+// records every meshlet's screen rectangle per particle and later passes
+// load and transform only the meshlets that overlap a live band.
+__device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& sm, int tile_px,
+                                   SmemCtl& ctl, float* fit_out) {
+  const int tid = threadIdx.x, T = blockDim.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = T >> 5;
+  const int32_t W = I.cam.width, H = I.cam.height;
+  const int32_t dx0 = -kGuard, dx1 = W + kGuard, dy0 = -kGuard, dy1 = H + kGuard;
+  const uint32_t nm = I.n_mlets;
+  const bool cull_ok = nm <= (uint32_t)kCullCap;
+  int32_t* tiles = sm.tiles;
+  int4* vcache = sm.vcache;
+  int4* mbox = sm.mbox;
+
+  // 1. conservative bounds: one thread per (particle, mesh-AABB corner)
+  if (tid < np * 8) {
+    const int k = tid >> 3, c = tid & 7;
+    const float x = (c & 1) ? I.mesh_hi[0] : I.mesh_lo[0];
+    const float y = (c & 2) ? I.mesh_hi[1] : I.mesh_lo[1];
+    const float z = (c & 4) ? I.mesh_hi[2] : I.mesh_lo[2];
+    float u, v, zz;
+    project(ctl.pose[k], x, y, z, I.cam, u, v, zz);
+    ctl.corner[k][c][0] = u;
+    ctl.corner[k][c][1] = v;
+    ctl.corner[k][c][2] = (zz >= 50.0f && u == u && v == v) ? 1.f : 0.f;
+  }
+  if (cull_ok)
+    for (int i = tid; i < np * (int)nm; i += T)
+      mbox[(i / nm) * kCullCap + (i % nm)] = make_int4(kAabbInitMin, kAabbInitMax, kAabbInitMin, kAabbInitMax);
+  __syncthreads();
+  if (tid < np) {
+    PartCtl& pc = ctl.part[tid];
+    float ulo = 3.0e38f, uhi = -3.0e38f, vlo = 3.0e38f, vhi = -3.0e38f;
+    bool ok = true;
+    for (int c = 0; c < 8; ++c) {
+      ok = ok && ctl.corner[tid][c][2] != 0.f;
+      ulo = fminf(ulo, ctl.corner[tid][c][0]);
+      uhi = fmaxf(uhi, ctl.corner[tid][c][0]);
+      vlo = fminf(vlo, ctl.corner[tid][c][1]);
+      vhi = fmaxf(vhi, ctl.corner[tid][c][1]);
+    }
+    if (!ok) {
+      pc.bound[0] = dx0; pc.bound[1] = dx1; pc.bound[2] = dy0; pc.bound[3] = dy1;
+    } else {
+      pc.bound[0] = (int32_t)fmaxf(floorf(ulo) - 1.0f, (float)dx0);
+      pc.bound[1] = (int32_t)fminf(floorf(uhi) + 2.0f, (float)dx1);
+      pc.bound[2] = (int32_t)fmaxf(floorf(vlo) - 1.0f, (float)dy0);
+      pc.bound[3] = (int32_t)fminf(floorf(vhi) + 2.0f, (float)dy1);
+      if (pc.bound[1] < pc.bound[0]) pc.bound[1] = pc.bound[0];
+      if (pc.bound[3] < pc.bound[2]) pc.bound[3] = pc.bound[2];
+    }
+    plan_tiles(pc, tile_px);
+    pc.box[0] = kAabbInitMin;
+    pc.box[1] = kAabbInitMax;
+    pc.box[2] = kAabbInitMin;
+    pc.box[3] = kAabbInitMax;
+    pc.nR = pc.nNo = pc.nSegR = 0;
+    pc.lo = pc.hi = 0;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int mp = 1;
+    for (int k = 0; k < np; ++k) mp = max(mp, ctl.part[k].npass);
+    ctl.maxpass = mp;
+  }
+  __syncthreads();
+  const int maxpass = ctl.maxpass;
+  unsigned long long writes = 0;
+  bool violation = false;
+
+  for (int pass = 0; pass < maxpass; ++pass) {
+    // 2a. band of every particle still active in this pass
+    if (tid < np) {
+      PartCtl& pc = ctl.part[tid];
+      pc.x0 = pc.y0 = pc.cwp = pc.thp = 0;
+      if (pass < pc.npass && pc.ncol * pc.nrow > 0) {
+        const int32_t pr = pass / pc.ncol, pcol = pass - pr * pc.ncol;
+        pc.x0 = pc.tx0 + pcol * pc.cw;
+        pc.y0 = pc.bound[2] + pr * pc.th;
+        pc.cwp = min(pc.cw, pc.tx0 + pc.tw - pc.x0);
+        pc.thp = min(pc.th, pc.bound[3] - pc.y0);
+      }
+    }
+    __syncthreads();
+    // 2b. clear the tiles of the active particles
+    for (int k = 0; k < np; ++k) {
+      const PartCtl& pc = ctl.part[k];
+      int4* t4 = reinterpret_cast<int4*>(tiles + (size_t)k * tile_px);
+      const int4 bg = make_int4(kDepthBg, kDepthBg, kDepthBg, kDepthBg);
+      const int n4 = (pc.cwp * pc.thp) >> 2;
+      for (int i = tid; i < n4; i += T) t4[i] = bg;
+    }
+    __syncthreads();
+    // 2c. every warp takes (particle, meshlet) items on its own: vertices
+    //     into its private cache, then the faces into the particle's tile.
+    //     In passes after the first, meshlets whose rectangle misses the
+    //     particle's band are skipped.
+    const bool cull = pass > 0 && cull_ok;
+    int4* vc = vcache + wid * kMletVerts;
+    for (uint32_t item = wid; item < (uint32_t)np * nm; item += nw) {
+      const int k = (int)(item / nm);
+      const uint32_t m = item - (uint32_t)k * nm;
+      PartCtl& pc = ctl.part[k];
+      if (pass >= pc.npass || (cull && !rect_overlaps(mbox[k * kCullCap + m], pc))) continue;
+      const uint2 hw = __ldg(reinterpret_cast<const uint2*>(I.mlets + m));
+      MeshletHdr h;
+      h.off = hw.x;
+      h.nv = (uint16_t)(hw.y & 0xffffu);
+      h.nf = (uint16_t)(hw.y >> 16);
+      const int nv = h.nv, nf = h.nf;
+      const float4* gv = reinterpret_cast<const float4*>(I.mlet_blob + h.off);
+      const uint32_t* gf = reinterpret_cast<const uint32_t*>(I.mlet_blob + h.off + nv * 16);
+      const float* pose = ctl.pose[k];
+      for (int v = lane; v < nv; v += 32) {
+        const float4 qv = __ldg(gv + v);
+        float u, vv, z;
+        project(pose, qv.x, qv.y, qv.z, I.cam, u, vv, z);
+        vc[v] = make_int4(__float2int_rn(16.0f * u), __float2int_rn(16.0f * vv), __float_as_int(z), 0);
+      }
+      __syncwarp();
+      int32_t bminx = kAabbInitMin, bmaxx = kAabbInitMax, bminy = kAabbInitMin, bmaxy = kAabbInitMax;
+      int32_t* tile = tiles + (size_t)k * tile_px;
+      const int32_t x0 = pc.x0, y0 = pc.y0, cwp = pc.cwp, thp = pc.thp;
+      for (int f = lane; f < nf; f += 32) {
+        const uint32_t fi = __ldg(gf + f);
+        const int4 a = vc[fi & 1023u], bb = vc[(fi >> 10) & 1023u], c = vc[(fi >> 20) & 1023u];
+        FaceSetup fs;
+        setup_face_fixed(a.x, a.y, __int_as_float(a.z), bb.x, bb.y, __int_as_float(bb.z), c.x, c.y,
+                         __int_as_float(c.z), fs);
+        bminx = min(bminx, fs.minx);
+        bmaxx = max(bmaxx, fs.maxx);
+        bminy = min(bminy, fs.miny);
+        bmaxy = max(bmaxy, fs.maxy);
+        if (!fs.live) continue;
+        if (pass == 0) {
+          const int32_t ca = max(fs.minx, dx0), cb = min(fs.maxx, dx1);
+          const int32_t ra = max(fs.miny, dy0), rb = min(fs.maxy, dy1);
+          if (ca < cb && ra < rb &&
+              (ca < pc.bound[0] || cb > pc.bound[1] || ra < pc.bound[2] || rb > pc.bound[3]))
+            violation = true;
+        }
+        const int32_t xa = max(fs.minx, x0), xb = min(fs.maxx, x0 + cwp);
+        const int32_t ya = max(fs.miny, y0), yb = min(fs.maxy, y0 + thp);
+        if (xa >= xb || ya >= yb) continue;
+        writes += (unsigned long long)(xb - xa) * (unsigned long long)(yb - ya);
+        const int32_t rx0 = xa - fs.minx;
+        for (int32_t y = ya; y < yb; ++y) {
+          const int32_t ry = y - fs.miny;
+          int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
+          int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
+          int32_t* row = tile + (y - y0) * cwp - x0;
+          for (int32_t x = xa; x < xb; ++x) {
+            const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+            const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+            float depth = fs.z1;
+            depth = depth + (float)cx2 * fs.z2;
+            depth = depth + (float)cx3 * fs.z3;
+            const int32_t d = __float2int_rn(depth);
+            if (d < kDepthBg) atomicMin(row + x, d);
+            CX2 = wsub(CX2, fs.fdy23);
+            CX3 = wsub(CX3, fs.fdy31);
+          }
+        }
+      }
+      if (pass == 0) {
+        bminx = __reduce_min_sync(0xffffffffu, bminx);
+        bmaxx = __reduce_max_sync(0xffffffffu, bmaxx);
+        bminy = __reduce_min_sync(0xffffffffu, bminy);
+        bmaxy = __reduce_max_sync(0xffffffffu, bmaxy);
+        if (lane == 0) {
+          atomicMin(&pc.box[0], bminx);
+          atomicMax(&pc.box[1], bmaxx);
+          atomicMin(&pc.box[2], bminy);
+          atomicMax(&pc.box[3], bmaxy);
+          if (cull_ok) {
+            int4* mb = mbox + k * kCullCap + m;
+            mb->x = max(bminx, dx0);
+            mb->y = min(bmaxx, dx1);
+            mb->z = max(bminy, dy0);
+            mb->w = min(bmaxy, dy1);
+          }
+        }
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    // 2e. scan every active particle's tile over its render AABB
+    for (int k = 0; k < np; ++k) {
+      PartCtl& pc = ctl.part[k];
+      if (pass >= pc.npass) continue;  // CTA-uniform
+      const int32_t x0 = pc.x0, y0 = pc.y0, cwp = pc.cwp;
+      const int32_t sx0 = max(pc.box[0], x0), sx1 = min(pc.box[1], x0 + cwp);
+      const int32_t sy0 = max(pc.box[2], y0), sy1 = min(pc.box[3], y0 + pc.thp);
+      BlockSums acc = {0u, 0u, 0u, 0, 0};
+      if (sx0 < sx1 && sy0 < sy1) {
+        const int32_t gx0 = x0 + ((sx0 - x0) & ~3);
+        const int32_t gpr = (sx1 - gx0 + 3) >> 2;
+        const int32_t ng = gpr * (sy1 - sy0);
+        const float rg = 1.0f / (float)gpr;
+        const int32_t* tile = tiles + (size_t)k * tile_px;
+        const uint16_t* __restrict__ obs = I.obs;
+        const bool vec_obs = (W & 3) == 0;
+        for (int32_t gi = tid; gi < ng; gi += T) {
+          const int32_t r = small_div(gi, rg);
+          const int32_t x = gx0 + ((gi - r * gpr) << 2);
+          const int32_t y = sy0 + r;
+          const int4 zz = *reinterpret_cast<const int4*>(tile + (y - y0) * cwp + (x - x0));
+          if (zz.x >= kDepthBg && zz.y >= kDepthBg && zz.z >= kDepthBg && zz.w >= kDepthBg) continue;
+          uint32_t kk[4] = {0u, 0u, 0u, 0u};
+          if (y >= 0 && y < H) {
+            const uint16_t* orow = obs + (size_t)y * (size_t)W;
+            if (vec_obs && x >= 0 && x + 3 < W) {
+              const uint2 qo = __ldg(reinterpret_cast<const uint2*>(orow + x));
+              kk[0] = qo.x & 0xffffu;
+              kk[1] = qo.x >> 16;
+              kk[2] = qo.y & 0xffffu;
+              kk[3] = qo.y >> 16;
+            } else {
+#pragma unroll
+              for (int e = 0; e < 4; ++e)
+                if (x + e >= 0 && x + e < W) kk[e] = __ldg(orow + x + e);
+            }
+          }
+          const int32_t zr[4] = {zz.x, zz.y, zz.z, zz.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            if (zr[e] < kDepthBg) {
+              acc.nR += 1;
+              if (kk[e] == 0u) {
+                acc.nNo += 1;
+              } else {
+                const int64_t d64 = wsub(zr[e], (int32_t)kk[e]);
+                add128(acc.lo, acc.hi, (uint64_t)(d64 * d64));
+                acc.nSegR += 1;
+              }
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        acc.nR += __shfl_xor_sync(0xffffffffu, acc.nR, o);
+        acc.nNo += __shfl_xor_sync(0xffffffffu, acc.nNo, o);
+        acc.nSegR += __shfl_xor_sync(0xffffffffu, acc.nSegR, o);
+        const uint64_t lo = __shfl_xor_sync(0xffffffffu, acc.lo, o);
+        const uint64_t hi = __shfl_xor_sync(0xffffffffu, acc.hi, o);
+        acc.hi += hi;
+        add128(acc.lo, acc.hi, lo);
+      }
+      if (lane == 0) {
+        ctl.warp[wid].nR = acc.nR;
+        ctl.warp[wid].nNo = acc.nNo;
+        ctl.warp[wid].nSegR = acc.nSegR;
+        ctl.warp[wid].lo = acc.lo;
+        ctl.warp[wid].hi = acc.hi;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        for (int i = 0; i < nw; ++i) {
+          pc.nR += ctl.warp[i].nR;
+          pc.nNo += ctl.warp[i].nNo;
+          pc.nSegR += ctl.warp[i].nSegR;
+          pc.hi += ctl.warp[i].hi;
+          add128(pc.lo, pc.hi, ctl.warp[i].lo);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (violation) atomicOr(I.err, kErrBound);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) writes += __shfl_xor_sync(0xffffffffu, writes, o);
+  if (lane == 0 && writes) atomicAdd(I.stats, writes);
+  // 3. window, observed count from the summed-area table, fitness
+  if (tid < np) {
+    const PartCtl& pc = ctl.part[tid];
+    const SolveParams& prm = I.prm;
+    const int32_t minX = min(pc.box[0], prm.cl_min_x), maxX = max(pc.box[1], prm.cl_max_x);
+    const int32_t minY = min(pc.box[2], prm.cl_min_y), maxY = max(pc.box[3], prm.cl_max_y);
+    const int64_t Ww = (int64_t)maxX - minX, Hh = (int64_t)maxY - minY;
+    uint32_t observed = 0;
+    if (Ww > 0 && Hh > 0) {
+      const int64_t area = Ww * Hh;
+      const int64_t pad = (1024 - area % 1024) % 1024;
+      const int64_t L = pad < Ww ? pad : Ww;
+      observed = sat_count(I.sat, W, H, minX, maxX, minY, maxY) +
+                 sat_count(I.sat, W, H, minX, (int64_t)minX + L, maxY, (int64_t)maxY + 1);
+    }
+    fit_out[tid] = fitness_from_counts(observed - pc.nSegR, pc.nR, pc.nNo, pc.lo, pc.hi, prm.num_points);
+    atomicAdd(I.stats + 1, (unsigned long long)pc.npass);
+  }
+  __syncthreads();
+}
+
 // PSO step + render + score + personal best for one work item.
-__device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, int32_t* tile,
+__device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, unsigned char* dyn,
                              int tile_px, SmemCtl& ctl) {
   const int tid = threadIdx.x;
   const uint32_t P = I.prm.num_particles;
@@ -356,19 +729,25 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, i
     }
   }
   __syncthreads();
-  for (uint32_t i = 0; i < np; ++i) {
-    const float fv = render_score(I, ctl.pose[i], tile, tile_px, ctl);
-    if (tid == 0) {
-      const uint32_t p = p0 + i;
-      I.fit[p] = fv;
-      if (fv < __ldcg(I.pbest_fit + p)) {
-        I.pbest_fit[p] = fv;
+  render_score_mlets(I, (int)np, carve_smem(dyn, (int)I.ppb), tile_px, ctl, ctl.argv);
+  if (tid < (int)np) {
+    const uint32_t p = p0 + tid;
+    const float fv = ctl.argv[tid];
+    I.fit[p] = fv;
+    if (fv < __ldcg(I.pbest_fit + p)) {
+      I.pbest_fit[p] = fv;
 #pragma unroll
-        for (int d = 0; d < 7; ++d) I.pbest[p + (size_t)d * P] = ctl.pose[i][d];
-      }
+      for (int d = 0; d < 7; ++d) I.pbest[p + (size_t)d * P] = ctl.pose[tid][d];
     }
-    __syncthreads();
   }
+  __syncthreads();
+}
+
+// Shared memory of the fused kernels: one vertex cache per warp, ppb
+// meshlet-rectangle tables, ppb depth tiles.
+size_t fused_smem_bytes(int threads, int ppb, int tile_px) {
+  return (size_t)(threads / 32) * kMletVerts * 16 + (size_t)ppb * kCullCap * 16 +
+         (size_t)ppb * tile_px * 4;
 }
 
 // After a work item: the CTA that completes the instance's last chunk of the
@@ -442,9 +821,8 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* 
                                                                 uint32_t iter, int tile_px) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
-  int32_t* tile = reinterpret_cast<int32_t*>(dyn_smem);
   const Instance& I = *inst;
-  process_item(I, blockIdx.x, iter, tile, tile_px, ctl);
+  process_item(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
   instance_epilogue(I, iter, ctl);
 }
 
@@ -492,7 +870,6 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t* err, unsigned long long ti
 __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, int tile_px) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
-  int32_t* tile = reinterpret_cast<int32_t*>(dyn_smem);
   for (uint32_t s = 0; s < A.max_iters; ++s) {
     while (true) {
       if (threadIdx.x == 0) ctl.claim = atomicAdd(A.step_claim + s, 1u);
@@ -503,7 +880,7 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, in
       const WorkItem it = A.items[k];
       const Instance& I = A.inst[it.inst];
       if (s >= I.prm.iterations) continue;
-      process_item(I, it.chunk, s, tile, tile_px, ctl);
+      process_item(I, it.chunk, s, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
       instance_epilogue(I, s, ctl);
     }
     if (s + 1 < A.max_iters && !grid_barrier(A.barrier, A.err, A.timeout_ns)) return;
@@ -733,6 +1110,28 @@ __global__ void __launch_bounds__(kMaxThreads) score_poses_kernel(const Instance
   }
 }
 
+// Score explicit poses with the meshlet path, ppb poses per CTA pass.
+__global__ void __launch_bounds__(kMaxThreads) score_poses_mlet_kernel(const Instance* __restrict__ inst,
+                                                                       const float* __restrict__ poses,
+                                                                       uint32_t n, int tile_px,
+                                                                       float* __restrict__ fit_out) {
+  extern __shared__ int4 dyn_smem[];
+  __shared__ SmemCtl ctl;
+  const Instance& I = *inst;
+  unsigned char* dyn = reinterpret_cast<unsigned char*>(dyn_smem);
+  const FusedSmem sm = carve_smem(dyn, (int)I.ppb);
+  const uint32_t groups = (n + I.ppb - 1) / I.ppb;
+  for (uint32_t gi = blockIdx.x; gi < groups; gi += gridDim.x) {
+    const uint32_t k0 = gi * I.ppb;
+    const int np = (int)min(I.ppb, n - k0);
+    if ((int)threadIdx.x < np * 7) ctl.pose[threadIdx.x / 7][threadIdx.x % 7] = poses[(size_t)k0 * 7 + threadIdx.x];
+    __syncthreads();
+    render_score_mlets(I, np, sm, tile_px, ctl, ctl.argv);
+    if ((int)threadIdx.x < np) fit_out[k0 + threadIdx.x] = ctl.argv[threadIdx.x];
+    __syncthreads();
+  }
+}
+
 // Writes the instance and preparation records of a scoring call into
 // caller-independent scratch and clears its header words (error bits,
 // counters), so nothing is copied from the host.
@@ -756,12 +1155,35 @@ __global__ void copy_flags_kernel(const uint32_t* src, uint32_t* dst) {
 
 size_t smem_ctl_bytes() { return sizeof(SmemCtl); }
 
-// Opt in to more than 48 KB of dynamic shared memory (per kernel, current
-// device; the call is cheap and idempotent).
+// Opt in to more than 48 KB of dynamic shared memory.  The attribute is
+// set once per kernel, device and size: calling cudaFuncSetAttribute on
+// every launch costs host time that starves back-to-back iteration launches.
 template <typename K>
 static cudaError_t ensure_smem(K kernel, size_t bytes) {
   if (bytes <= 48 * 1024) return cudaSuccess;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  struct Entry {
+    const void* fn;
+    int dev;
+    size_t bytes;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> g(mu);
+  for (const Entry& x : done)
+    if (x.fn == (const void*)kernel && x.dev == dev && x.bytes >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) {
+    for (Entry& x : done)
+      if (x.fn == (const void*)kernel && x.dev == dev) {
+        x.bytes = bytes;
+        return e;
+      }
+    done.push_back(Entry{(const void*)kernel, dev, bytes});
+  }
+  return e;
 }
 
 cudaError_t launch_prep(const PrepDesc* jobs, int n, int max_w, int max_h, cudaStream_t st) {
@@ -783,7 +1205,7 @@ cudaError_t launch_mesh_aabb(const float* mesh, uint32_t F, float* out, cudaStre
 
 cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, const TileConfig& cfg,
                         cudaStream_t st) {
-  const size_t smem = (size_t)cfg.tile_px * sizeof(int32_t);
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
   cudaError_t e = ensure_smem(qpso_step_kernel, smem);
   if (e != cudaSuccess) return e;
   qpso_step_kernel<<<chunks, cfg.threads, smem, st>>>(inst, iter, cfg.tile_px);
@@ -791,14 +1213,14 @@ cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, co
 }
 
 cudaError_t batch_max_grid(const TileConfig& cfg, int* blocks_per_sm) {
-  const size_t smem = (size_t)cfg.tile_px * sizeof(int32_t);
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
   cudaError_t e = ensure_smem(qpso_batch_kernel, smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, qpso_batch_kernel, cfg.threads, smem);
 }
 
 cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st) {
-  const size_t smem = (size_t)cfg.tile_px * sizeof(int32_t);
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
   cudaError_t e = ensure_smem(qpso_batch_kernel, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t lc = {};
@@ -820,6 +1242,15 @@ cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, f
   cudaError_t e = ensure_smem(score_poses_kernel, smem);
   if (e != cudaSuccess) return e;
   score_poses_kernel<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
+                               const TileConfig& cfg, int grid, cudaStream_t st) {
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
+  cudaError_t e = ensure_smem(score_poses_mlet_kernel, smem);
+  if (e != cudaSuccess) return e;
+  score_poses_mlet_kernel<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out);
   return cudaGetLastError();
 }
 

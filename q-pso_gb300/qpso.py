@@ -30,7 +30,7 @@ EXPORTS = [
     "qpso_solve_traced", "qpso_solve_batch", "qpso_score_poses", "qpso_render",
     "qpso_barrier_selftest", "qpso_frame_update", "qpso_host_alloc", "qpso_host_free",
     "qpso_get_stream", "qpso_set_profiling", "qpso_get_profile", "qpso_timer_record",
-    "qpso_timer_elapsed", "qpso_scrub_l2", "qpso_score_poses_noalloc",
+    "qpso_timer_elapsed", "qpso_scrub_l2", "qpso_score_poses_noalloc", "qpso_autotune",
 ]
 
 
@@ -121,6 +121,8 @@ def load_library(path: str = LIB_PATH):
     L.qpso_timer_record.argtypes = [vp, C.c_uint32]
     L.qpso_timer_elapsed.argtypes = [vp, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]
     L.qpso_scrub_l2.argtypes = [vp, C.c_uint64]
+    L.qpso_autotune.argtypes = [vp, C.POINTER(SolveDesc), C.c_uint32, C.c_int, C.c_uint32,
+                                C.POINTER(LaunchConfig), C.POINTER(C.c_float)]
     L.qpso_score_poses_noalloc.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                            C.POINTER(Camera), C.POINTER(SolveDesc), C.c_void_p,
                                            C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -224,6 +226,17 @@ class Context:
         p, b = LaunchConfig(), LaunchConfig()
         self._check(self.L.qpso_get_launch_config(self.h, C.byref(p), C.byref(b)))
         return (p.threads, p.tile_px, p.ppb), (b.threads, b.tile_px, b.ppb)
+
+    def autotune(self, descs, batched: bool, tune_iters: int = 3):
+        """Pick the fastest launch shape for these solves (installed in the
+        context); returns ((threads, tile_px, ppb), ms of the tuning run)."""
+        n = len(descs)
+        arr = (SolveDesc * n)(*descs)
+        best = LaunchConfig()
+        ms = C.c_float()
+        self._check(self.L.qpso_autotune(self.h, arr, n, 1 if batched else 0, tune_iters,
+                                         C.byref(best), C.byref(ms)))
+        return (best.threads, best.tile_px, best.ppb), ms.value
 
     def solve(self, desc: SolveDesc) -> Result:
         r = Result()

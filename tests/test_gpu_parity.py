@@ -157,7 +157,7 @@ def test_plain_solve_trace_bit_exact(gpu_ctx, c1_gpu):
     np.testing.assert_array_equal(st["trace_gbest"], g["trace_gbest"])
 
 
-@pytest.mark.parametrize("cfg", [(256, 16384, 1), (128, 4096, 4), (512, 32768, 3)])
+@pytest.mark.parametrize("cfg", [(256, 16384, 1), (128, 4096, 4), (512, 8192, 3), (256, 512, 5), (256, 1024, 10)])
 def test_plain_launch_shapes_agree(gpu_ctx, c1_gpu, cfg):
     w, mids, fids = c1_gpu
     s = dict(w["solves"][0], particles=40, iterations=12, seed=5, stream=9)
@@ -201,6 +201,28 @@ def test_batch_equals_plain_and_oracle(gpu_ctx, c1_gpu):
             assert r.fit == plain.fit == want["fit"] == r2.fit
             np.testing.assert_array_equal(np.array(r.pose[:], np.float32), want["pose"])
             np.testing.assert_array_equal(np.array(r2.pose[:], np.float32), want["pose"])
+
+
+def test_autotune_keeps_results(gpu_ctx, c1_gpu):
+    """The autotuner only changes speed: after tuning either path, solves
+    still equal the oracle bit for bit."""
+    w, mids, fids = c1_gpu
+    soa, F = w["meshes"][0]
+    solves = [dict(w["solves"][0], particles=48, iterations=6, seed=21, stream=s) for s in range(3)]
+    descs = [gpu_desc(s, mids[0], fids[0]) for s in solves]
+    old = gpu_ctx.get_launch_config()
+    try:
+        cfg_p, ms_p = gpu_ctx.autotune(descs, batched=False, tune_iters=2)
+        cfg_b, ms_b = gpu_ctx.autotune(descs, batched=True, tune_iters=2)
+        assert gpu_ctx.get_launch_config() == (cfg_p, cfg_b)
+        assert ms_p > 0 and ms_b > 0
+        res = gpu_ctx.solve_batch(descs)
+        for s, d, r in zip(solves, descs, res):
+            want = po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s))
+            assert r.fit == want["fit"] and gpu_ctx.solve(d).fit == want["fit"]
+            np.testing.assert_array_equal(np.array(r.pose[:], np.float32), want["pose"])
+    finally:
+        gpu_ctx.set_launch_config(plain=old[0], batch=old[1])
 
 
 def test_solution_near_ground_truth(gpu_ctx, c1_gpu):

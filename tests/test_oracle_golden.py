@@ -44,6 +44,18 @@ def test_series_math_accuracy():
     assert po.acos(1.0000001) == 0.0 and abs(po.acos(-1.5) - math.pi) < 1e-15
 
 
+def test_fp32_series_accuracy():
+    """The fp32 sin/cos/acos of the PSO step stay within a few float ulps of
+    the true functions (both sides of the arithmetic contract use them)."""
+    xs = np.float32(np.linspace(-30, 30, 6001))
+    assert max(abs(po.sinf(float(x)) - math.sin(float(x))) for x in xs) < 4e-7
+    assert max(abs(po.cosf(float(x)) - math.cos(float(x))) for x in xs) < 4e-7
+    for x in np.float32(np.linspace(-1, 1, 6001)):
+        assert abs(po.acosf(float(x)) - math.acos(float(x))) <= 1e-6 * max(1.0, math.acos(float(x)))
+    assert po.acosf(1.0000001) == 0.0
+    assert abs(po.sinf(5000.0) - math.sin(5000.0)) < 1e-6
+
+
 def test_raster_matches_reference_render(ref):
     """renderFixedPointAABB (main.h:1306-1491) compiled from the reference:
     every depth of every face's rectangle and the AABB are bit-exact."""
