@@ -145,6 +145,10 @@ def load_workload(name: str):
     if name == "c3":
         return scene.workload_c3(), ("c3: 64 clusters from 8 frames, meshes log-uniform 1k-50k faces, "
                                      "windows 40-300 px, particles in {128..1024} x 100 iterations")
+    if name == "c4":
+        return scene.workload_c4(), ("c4: serving, Poisson arrivals over 16 resident meshes "
+                                     "(2k-100k faces) and 32 resident 640x480 frames, 256 or 1024 "
+                                     "particles x 100 iterations")
     if name == "c5":
         return scene.workload_c5(), ("c5: one level-7 icosphere (327,680 faces, 250 mm), "
                                      "4096 particles x 200 iterations, full 640x480 window")
@@ -312,9 +316,12 @@ def run_ours(args, ws, rank, local):
         ctx.set_profiling(False)
         return total, ctx.profile(reset=True)
 
-    # launch shapes chosen by the autotuner on a 3-iteration run of this workload
-    plain_cfg, _ = ctx.autotune(descs, batched=False, tune_iters=3)
-    batch_cfg, _ = ctx.autotune(descs, batched=True, tune_iters=3)
+    # launch shapes chosen by the autotuner on 30-iteration runs of up to 16
+    # solves spread over the workload (the first iterations, with the swarm
+    # still spread out, render larger than the converged ones)
+    tune = descs[::max(1, len(descs) // 16)][:16]
+    plain_cfg, _ = ctx.autotune(tune[:4], batched=False, tune_iters=30)
+    batch_cfg, _ = ctx.autotune(tune, batched=True, tune_iters=30)
 
     main_fn, alt_fn = (step_batch, step_plain) if batched_default else (step_plain, step_batch)
     for _ in range(args.warmup):
@@ -395,16 +402,82 @@ def run_ours(args, ws, rank, local):
     d.close()
 
 
+def run_serving(args, ws, rank, local):
+    """C4: continuous-batching server under Poisson arrivals.  For each rate
+    the same number of requests (drawn from every (frame, cluster) pair) is
+    submitted on the arrival schedule; latency is submit -> completion on the
+    host clock, throughput is completed requests / makespan."""
+    import qpso
+    import build as pkg_build
+    import scene
+
+    pkg_build.build()
+    w, desc = load_workload("c4")
+    ctx = qpso.Context(local)
+    cam = qpso.Camera(*scene.camera_tuple())
+    mids = [ctx.mesh_upload(soa, F) for soa, F in w["meshes"]]
+    fids = [ctx.frame_upload(dep, cam, labels=lab) for dep, lab, _ in w["frames"]]
+    pool = [qpso.solve_desc(mesh_id=mids[s["mesh"]], frame_id=fids[s["frame"]], **scene.solve_fields(s))
+            for s in w["solves"]]
+    rng = np.random.default_rng(17)
+    cfg, _ = ctx.autotune(pool[:16], batched=True, tune_iters=6)
+    rates = [float(r) for r in args.rates.split(",")]
+    per_rate = args.requests
+    results = []
+    renders = {id(d): d.num_particles * d.iterations for d in pool}
+    sampler = ClockSampler(local)
+    sampler.start()
+    for rate in rates:
+        picks = [pool[int(i)] for i in rng.integers(0, len(pool), per_rate)]
+        gaps = rng.exponential(1.0 / rate, per_rate)
+        with qpso.Server(ctx, max_slots=args.slots, iters_per_epoch=args.epoch_iters) as srv:
+            ids = []
+            t0 = time.perf_counter()
+            due = t0
+            for d, g in zip(picks, gaps):
+                due += g
+                while time.perf_counter() < due:
+                    pass
+                ids.append(srv.submit(d))
+            lats = [srv.wait(rid)[1] for rid in ids]
+            span = time.perf_counter() - t0
+            st = srv.stats()
+        lats = np.array(lats)
+        results.append({"rate_req_s": rate, "requests": per_rate,
+                        "p50_ms": float(np.percentile(lats, 50)), "p99_ms": float(np.percentile(lats, 99)),
+                        "solves_per_s": per_rate / span,
+                        "particle_renders_per_s": sum(d.num_particles * d.iterations for d in picks) / span,
+                        "peak_active": st["peak_active"], "epochs": st["epochs"]})
+    clocks = sampler.stop()
+    best = max(results, key=lambda r: r["solves_per_s"])
+    line = {"metric": "pose solves/sec at sustained load with p50/p99 latency (serving)",
+            "value": best["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": len(rates),
+            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "slots": args.slots, "iters_per_epoch": args.epoch_iters,
+                       "launch_batched": {"threads": cfg[0], "tile_px": cfg[1], "ppb": cfg[2]}},
+            "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "sweep": results, "clocks": clocks}
+    print(json.dumps(line))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rates", default="5,20,100,1000,20000", help="c4: arrival rates (req/s)")
+    ap.add_argument("--requests", type=int, default=48, help="c4: requests per rate")
+    ap.add_argument("--slots", type=int, default=64, help="c4: server slots")
+    ap.add_argument("--epoch-iters", type=int, default=4, help="c4: iterations per epoch")
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "c4" and args.impl != "reference":
+        run_serving(args, ws, rank, local)
+        return
     if args.impl == "reference":
         run_reference(args, ws, rank)
     else:

@@ -210,6 +210,45 @@ qpso_status qpso_render(qpso_context *ctx, uint32_t mesh_id, const qpso_camera *
                         const float pose[7], int32_t x0, int32_t y0, int32_t w, int32_t h,
                         int32_t *depth_out, int32_t box_out[4]);
 
+/* ---- serving: continuous batching of solve requests ----
+ * No counterpart in the reference (one solve per process).  A scheduler
+ * thread admits submitted requests into free slots while the slot count and
+ * the HBM budget allow (their swarm state, masked depth and summed-area
+ * table are allocated on admission from the server's own memory pool and
+ * stay resident until the request completes), and runs epochs: each epoch
+ * launches the multi-request iteration kernel, which advances every active
+ * request by one iteration at its own iteration number, up to
+ * iters_per_epoch times; finished requests leave and queued ones join
+ * between epochs.  Meshes and frames are the context's resident objects
+ * and must stay uploaded while requests use them.  A request's result is
+ * bit-identical to qpso_solve of the same descriptor, whatever else runs. */
+typedef struct qpso_server qpso_server;
+typedef struct {
+    uint32_t max_slots;        /* requests on the GPU at once (>= 1) */
+    uint64_t hbm_budget_bytes; /* request memory cap; 0 = half of free HBM at start */
+    uint32_t iters_per_epoch;  /* iterations per scheduling epoch (>= 1) */
+} qpso_server_config;
+typedef struct {
+    uint64_t submitted, admitted, completed, failed;
+    uint32_t pending, active, peak_active;
+    uint64_t bytes_in_use, peak_bytes, budget_bytes;
+    uint64_t epochs, launches;
+} qpso_server_stats;
+qpso_status qpso_server_start(qpso_context *ctx, const qpso_server_config *cfg, qpso_server **out);
+/* Queue a request; QPSO_ERR_BUSY if it could never fit the budget. */
+qpso_status qpso_server_submit(qpso_server *srv, const qpso_solve_desc *desc, uint64_t *request_id);
+/* Non-blocking query; *done = 1 once finished (result and latency set).
+ * A finished request's result is handed out once (by poll or wait); its id
+ * is unknown afterwards. */
+qpso_status qpso_server_poll(qpso_server *srv, uint64_t request_id, int *done, qpso_result *result,
+                             double *latency_ms);
+/* Block until the request finishes or timeout_ms passes (QPSO_ERR_TIMEOUT). */
+qpso_status qpso_server_wait(qpso_server *srv, uint64_t request_id, uint64_t timeout_ms,
+                             qpso_result *result, double *latency_ms);
+qpso_status qpso_server_stats_get(qpso_server *srv, qpso_server_stats *out);
+/* Finish every queued and active request, then stop the scheduler. */
+qpso_status qpso_server_stop(qpso_server *srv);
+
 /* Checks the bounded device wait: a barrier that expects one more CTA
  * than arrives must expire after timeout_ns and report QPSO_ERR_TIMEOUT.
  * No counterpart in the reference (which has no device waits). */

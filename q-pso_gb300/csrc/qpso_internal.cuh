@@ -43,6 +43,7 @@ struct Instance {
   float* trace;             // optional [iterations][8] gbest after each iteration
   uint32_t chunks;          // CTAs (work items) per iteration
   uint32_t ppb;             // particles per work item
+  uint32_t cur_iter;        // serving: next iteration to run (advanced by the last CTA)
 };
 
 // Launch-shape knobs chosen by the tuner.
@@ -97,6 +98,8 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
                                  cudaStream_t st);
 cudaError_t launch_barrier_probe(uint32_t* bar, uint32_t* err, uint32_t grid, uint32_t expected,
                                  unsigned long long timeout_ns, cudaStream_t st);
+cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
+                              const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* di, PrepDesc* dj,
                                 cudaStream_t st);
 cudaError_t launch_copy_flags(const uint32_t* src, uint32_t* dst, cudaStream_t st);

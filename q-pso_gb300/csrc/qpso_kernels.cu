@@ -826,6 +826,24 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* 
   instance_epilogue(I, iter, ctl);
 }
 
+// Serving form: one launch advances every active request by one
+// iteration, each at its own iteration number (continuous batching: the
+// set of requests changes between launches).  CTA b runs work item b; the
+// CTA finishing an instance's last chunk updates its global best and
+// advances its iteration counter for the next launch.
+__global__ void __launch_bounds__(kMaxThreads) qpso_multi_step_kernel(Instance* __restrict__ slots,
+                                                                      const WorkItem* __restrict__ items,
+                                                                      int tile_px) {
+  extern __shared__ int4 dyn_smem[];
+  __shared__ SmemCtl ctl;
+  const WorkItem it = items[blockIdx.x];
+  Instance& I = slots[it.inst];
+  const uint32_t iter = __ldcg(&I.cur_iter);
+  process_item(I, it.chunk, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
+  instance_epilogue(I, iter, ctl);
+  if (ctl.last && threadIdx.x == 0) I.cur_iter = iter + 1;
+}
+
 // Grid-wide barrier for the cooperative persistent launch.  Waits are
 // bounded by timeout_ns of wall time; on expiry the CTA records kErrTimeout
 // and every CTA leaves at its next barrier.
@@ -953,16 +971,24 @@ __global__ void sat_rows_kernel(const PrepDesc* __restrict__ jobs) {
   }
 }
 
-// Pass 2: one thread per column, running sum down the rows.
+// Pass 2: one thread per column, running sum down the rows, 16 rows per
+// step so that the loads of a step are in flight together.
 __global__ void sat_cols_kernel(const PrepDesc* __restrict__ jobs) {
   const PrepDesc J = jobs[blockIdx.y];
   const int32_t w = J.width, h = J.height;
   const int64_t W1 = (int64_t)w + 1;
   for (int32_t x = blockIdx.x * blockDim.x + threadIdx.x; x <= w; x += gridDim.x * blockDim.x) {
     int32_t run = 0;
-    for (int32_t y = 1; y <= h; ++y) {
-      run += J.sat[y * W1 + x];
-      J.sat[y * W1 + x] = run;
+    int32_t* col = J.sat + x;
+    for (int32_t y0 = 1; y0 <= h; y0 += 16) {
+      int32_t v[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = (y0 + i <= h) ? col[(y0 + i) * W1] : 0;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        run += v[i];
+        if (y0 + i <= h) col[(y0 + i) * W1] = run;
+      }
     }
   }
 }
@@ -1261,6 +1287,16 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
   cudaError_t e = ensure_smem(render_window_kernel, smem < 16 ? 16 : smem);
   if (e != cudaSuccess) return e;
   render_window_kernel<<<1, threads, smem < 16 ? 16 : smem, st>>>(inst, pose, x0, y0, w, h, out, box);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
+                              const TileConfig& cfg, cudaStream_t st) {
+  if (n_items == 0) return cudaSuccess;
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
+  cudaError_t e = ensure_smem(qpso_multi_step_kernel, smem);
+  if (e != cudaSuccess) return e;
+  qpso_multi_step_kernel<<<n_items, cfg.threads, smem, st>>>(slots, items, cfg.tile_px);
   return cudaGetLastError();
 }
 

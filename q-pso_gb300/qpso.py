@@ -31,6 +31,8 @@ EXPORTS = [
     "qpso_barrier_selftest", "qpso_frame_update", "qpso_host_alloc", "qpso_host_free",
     "qpso_get_stream", "qpso_set_profiling", "qpso_get_profile", "qpso_timer_record",
     "qpso_timer_elapsed", "qpso_scrub_l2", "qpso_score_poses_noalloc", "qpso_autotune",
+    "qpso_server_start", "qpso_server_submit", "qpso_server_poll", "qpso_server_wait",
+    "qpso_server_stats_get", "qpso_server_stop",
 ]
 
 
@@ -63,6 +65,18 @@ class Profile(C.Structure):
     _fields_ = [("step_launches", C.c_uint64), ("step_ms", C.c_double),
                 ("batch_launches", C.c_uint64), ("batch_ms", C.c_double),
                 ("prep_launches", C.c_uint64)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("max_slots", C.c_uint32), ("hbm_budget_bytes", C.c_uint64),
+                ("iters_per_epoch", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("failed", C.c_uint64), ("pending", C.c_uint32), ("active", C.c_uint32),
+                ("peak_active", C.c_uint32), ("bytes_in_use", C.c_uint64), ("peak_bytes", C.c_uint64),
+                ("budget_bytes", C.c_uint64), ("epochs", C.c_uint64), ("launches", C.c_uint64)]
 
 
 class QpsoError(RuntimeError):
@@ -121,6 +135,14 @@ def load_library(path: str = LIB_PATH):
     L.qpso_timer_record.argtypes = [vp, C.c_uint32]
     L.qpso_timer_elapsed.argtypes = [vp, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]
     L.qpso_scrub_l2.argtypes = [vp, C.c_uint64]
+    L.qpso_server_start.argtypes = [vp, C.POINTER(ServerConfig), C.POINTER(vp)]
+    L.qpso_server_submit.argtypes = [vp, C.POINTER(SolveDesc), C.POINTER(C.c_uint64)]
+    L.qpso_server_poll.argtypes = [vp, C.c_uint64, C.POINTER(C.c_int), C.POINTER(Result),
+                                   C.POINTER(C.c_double)]
+    L.qpso_server_wait.argtypes = [vp, C.c_uint64, C.c_uint64, C.POINTER(Result),
+                                   C.POINTER(C.c_double)]
+    L.qpso_server_stats_get.argtypes = [vp, C.POINTER(ServerStats)]
+    L.qpso_server_stop.argtypes = [vp]
     L.qpso_autotune.argtypes = [vp, C.POINTER(SolveDesc), C.c_uint32, C.c_int, C.c_uint32,
                                 C.POINTER(LaunchConfig), C.POINTER(C.c_float)]
     L.qpso_score_poses_noalloc.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
@@ -308,6 +330,59 @@ class Context:
         bits = C.c_uint32()
         st = self.L.qpso_barrier_selftest(self.h, timeout_ns, C.byref(bits))
         return st, bits.value
+
+
+class Server:
+    """Continuous-batching request loop on a context (qpso_server_*)."""
+
+    def __init__(self, ctx: Context, max_slots: int = 64, hbm_budget_bytes: int = 0,
+                 iters_per_epoch: int = 4):
+        self.L = ctx.L
+        self.h = C.c_void_p()
+        cfg = ServerConfig(max_slots, hbm_budget_bytes, iters_per_epoch)
+        st = self.L.qpso_server_start(ctx.h, C.byref(cfg), C.byref(self.h))
+        if st != OK:
+            raise QpsoError(st, ctx.L.qpso_last_error(ctx.h).decode())
+
+    def submit(self, desc: SolveDesc) -> int:
+        rid = C.c_uint64()
+        st = self.L.qpso_server_submit(self.h, C.byref(desc), C.byref(rid))
+        if st != OK:
+            raise QpsoError(st, "submit refused")
+        return rid.value
+
+    def poll(self, rid: int):
+        done = C.c_int()
+        r = Result()
+        lat = C.c_double()
+        st = self.L.qpso_server_poll(self.h, rid, C.byref(done), C.byref(r), C.byref(lat))
+        if st != OK:
+            raise QpsoError(st, "request %d failed" % rid)
+        return (r, lat.value) if done.value else None
+
+    def wait(self, rid: int, timeout_ms: int = 600000):
+        r = Result()
+        lat = C.c_double()
+        st = self.L.qpso_server_wait(self.h, rid, timeout_ms, C.byref(r), C.byref(lat))
+        if st != OK:
+            raise QpsoError(st, "request %d" % rid)
+        return r, lat.value
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        self.L.qpso_server_stats_get(self.h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def stop(self):
+        if self.h:
+            self.L.qpso_server_stop(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.stop()
 
 
 class PinnedArray:

@@ -431,6 +431,42 @@ def workload_c3(seed: int = 0, n_frames: int = 8, per_frame: int = 8, iterations
     return {"meshes": meshes, "frames": fr, "solves": solves}
 
 
+def workload_c4(seed: int = 0, n_meshes: int = 16, n_frames: int = 32, per_frame: int = 4,
+                iterations: int = 100, particle_choices=(256, 1024)):
+    """Serving pool: 16 resident procedural meshes (log-uniform 2k-100k
+    faces, 50-200 mm) and 32 resident 640x480 frames, each showing
+    `per_frame` objects drawn from the pool.  Every (frame, cluster) pair is
+    a possible request, solved with the mesh that made the cluster."""
+    rng = np.random.default_rng(9000 + seed)
+    kinds = ["ellipsoid", "box", "cylinder"]
+    meshes = []
+    for i in range(n_meshes):
+        nf = int(round(math.exp(rng.uniform(math.log(2000), math.log(100000)))))
+        meshes.append(make_mesh(kinds[i % 3], nf, rng.uniform(50, 200), seed * 100 + i))
+    fr, solves = [], []
+    for fi in range(n_frames):
+        taken, objs, mids = [], [], []
+        while len(objs) < per_frame:
+            mi = int(rng.integers(0, n_meshes))
+            soa, F = meshes[mi]
+            try:
+                pose = place_pose(rng, soa, F, margin_px=2, taken=taken, tries=400)
+            except RuntimeError:
+                continue
+            objs.append((soa, F, pose))
+            mids.append(mi)
+        depth, labels, _ = compose_frame(objs, seed=9500 + seed * 100 + fi)
+        fr.append((depth, labels, None))
+        for j in range(per_frame):
+            info = cluster_info(depth, labels, j)
+            if info is None:
+                continue
+            solves.append(dict(mesh=mids[j], frame=fi, cluster=info,
+                               particles=int(rng.choice(particle_choices)), iterations=iterations,
+                               seed=seed, stream=len(solves), gt_pose=objs[j][2]))
+    return {"meshes": meshes, "frames": fr, "solves": solves}
+
+
 def workload_c5(seed: int = 0, particles: int = 4096, iterations: int = 200, level: int = 7):
     """Stress: one noise-displaced level-7 icosphere (250 mm extent) and a
     full 640x480 fitness window (cluster AABB = the frame)."""
