@@ -97,6 +97,7 @@ struct PartCtl {
 };
 
 constexpr int kCullCap = 512;  // meshlets whose per-particle rectangles are kept
+constexpr int kLaneRasterMax = 32;  // larger face rectangles are rasterised by the whole warp
 
 // Dynamic shared memory of the fused kernels.
 struct FusedSmem {
@@ -524,44 +525,98 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
       int32_t bminx = kAabbInitMin, bmaxx = kAabbInitMax, bminy = kAabbInitMin, bmaxy = kAabbInitMax;
       int32_t* tile = tiles + (size_t)k * tile_px;
       const int32_t x0 = pc.x0, y0 = pc.y0, cwp = pc.cwp, thp = pc.thp;
-      for (int f = lane; f < nf; f += 32) {
-        const uint32_t fi = __ldg(gf + f);
-        const int4 a = vc[fi & 1023u], bb = vc[(fi >> 10) & 1023u], c = vc[(fi >> 20) & 1023u];
+      // faces: a lane rasterises its own face when the clipped rectangle has
+      // at most kLaneRasterMax pixels; larger rectangles are rasterised by the
+      // whole warp (set-up broadcast by shuffles, pixels strided over lanes)
+      for (int base = 0; base < nf; base += 32) {
+        const int f = base + lane;
         FaceSetup fs;
-        setup_face_fixed(a.x, a.y, __int_as_float(a.z), bb.x, bb.y, __int_as_float(bb.z), c.x, c.y,
-                         __int_as_float(c.z), fs);
-        bminx = min(bminx, fs.minx);
-        bmaxx = max(bmaxx, fs.maxx);
-        bminy = min(bminy, fs.miny);
-        bmaxy = max(bmaxy, fs.maxy);
-        if (!fs.live) continue;
-        if (pass == 0) {
-          const int32_t ca = max(fs.minx, dx0), cb = min(fs.maxx, dx1);
-          const int32_t ra = max(fs.miny, dy0), rb = min(fs.maxy, dy1);
-          if (ca < cb && ra < rb &&
-              (ca < pc.bound[0] || cb > pc.bound[1] || ra < pc.bound[2] || rb > pc.bound[3]))
-            violation = true;
+        int32_t xa = 0, xb = 0, ya = 0, yb = 0;
+        bool big = false;
+        if (f < nf) {
+          const uint32_t fi = __ldg(gf + f);
+          const int4 a = vc[fi & 1023u], bb = vc[(fi >> 10) & 1023u], c = vc[(fi >> 20) & 1023u];
+          setup_face_fixed(a.x, a.y, __int_as_float(a.z), bb.x, bb.y, __int_as_float(bb.z), c.x, c.y,
+                           __int_as_float(c.z), fs);
+          bminx = min(bminx, fs.minx);
+          bmaxx = max(bmaxx, fs.maxx);
+          bminy = min(bminy, fs.miny);
+          bmaxy = max(bmaxy, fs.maxy);
+          if (fs.live) {
+            if (pass == 0) {
+              const int32_t ca = max(fs.minx, dx0), cb = min(fs.maxx, dx1);
+              const int32_t ra = max(fs.miny, dy0), rb = min(fs.maxy, dy1);
+              if (ca < cb && ra < rb &&
+                  (ca < pc.bound[0] || cb > pc.bound[1] || ra < pc.bound[2] || rb > pc.bound[3]))
+                violation = true;
+            }
+            xa = max(fs.minx, x0);
+            xb = min(fs.maxx, x0 + cwp);
+            ya = max(fs.miny, y0);
+            yb = min(fs.maxy, y0 + thp);
+            if (xa < xb && ya < yb) {
+              const int32_t n = (xb - xa) * (yb - ya);
+              writes += (unsigned long long)n;
+              if (n > kLaneRasterMax) {
+                big = true;
+              } else {
+                const int32_t rx0 = xa - fs.minx;
+                for (int32_t y = ya; y < yb; ++y) {
+                  const int32_t ry = y - fs.miny;
+                  int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
+                  int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
+                  int32_t* row = tile + (y - y0) * cwp - x0;
+                  for (int32_t x = xa; x < xb; ++x) {
+                    const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+                    const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+                    float depth = fs.z1;
+                    depth = depth + (float)cx2 * fs.z2;
+                    depth = depth + (float)cx3 * fs.z3;
+                    const int32_t d = __float2int_rn(depth);
+                    if (d < kDepthBg) atomicMin(row + x, d);
+                    CX2 = wsub(CX2, fs.fdy23);
+                    CX3 = wsub(CX3, fs.fdy31);
+                  }
+                }
+              }
+            }
+          }
         }
-        const int32_t xa = max(fs.minx, x0), xb = min(fs.maxx, x0 + cwp);
-        const int32_t ya = max(fs.miny, y0), yb = min(fs.maxy, y0 + thp);
-        if (xa >= xb || ya >= yb) continue;
-        writes += (unsigned long long)(xb - xa) * (unsigned long long)(yb - ya);
-        const int32_t rx0 = xa - fs.minx;
-        for (int32_t y = ya; y < yb; ++y) {
-          const int32_t ry = y - fs.miny;
-          int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
-          int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
-          int32_t* row = tile + (y - y0) * cwp - x0;
-          for (int32_t x = xa; x < xb; ++x) {
+        unsigned bigmask = __ballot_sync(0xffffffffu, big);
+        while (bigmask) {
+          const int src = __ffs(bigmask) - 1;
+          bigmask &= bigmask - 1;
+          const int32_t fminx = __shfl_sync(0xffffffffu, fs.minx, src);
+          const int32_t fminy = __shfl_sync(0xffffffffu, fs.miny, src);
+          const int32_t cy2 = __shfl_sync(0xffffffffu, fs.cy2, src);
+          const int32_t cy3 = __shfl_sync(0xffffffffu, fs.cy3, src);
+          const int32_t fdx23 = __shfl_sync(0xffffffffu, fs.fdx23, src);
+          const int32_t fdx31 = __shfl_sync(0xffffffffu, fs.fdx31, src);
+          const int32_t fdy23 = __shfl_sync(0xffffffffu, fs.fdy23, src);
+          const int32_t fdy31 = __shfl_sync(0xffffffffu, fs.fdy31, src);
+          const float z1 = __shfl_sync(0xffffffffu, fs.z1, src);
+          const float z2 = __shfl_sync(0xffffffffu, fs.z2, src);
+          const float z3 = __shfl_sync(0xffffffffu, fs.z3, src);
+          const int32_t bxa = __shfl_sync(0xffffffffu, xa, src);
+          const int32_t bxb = __shfl_sync(0xffffffffu, xb, src);
+          const int32_t bya = __shfl_sync(0xffffffffu, ya, src);
+          const int32_t byb = __shfl_sync(0xffffffffu, yb, src);
+          const int32_t w = bxb - bxa;
+          const int32_t n = w * (byb - bya);
+          const float rw = 1.0f / (float)w;
+          for (int32_t pix = lane; pix < n; pix += 32) {
+            const int32_t r = small_div(pix, rw);
+            const int32_t x = bxa + (pix - r * w), y = bya + r;
+            const int32_t ry = y - fminy, rx = x - fminx;
+            const int32_t CX2 = wsub(wadd(cy2, wmul(ry, fdx23)), wmul(rx, fdy23));
+            const int32_t CX3 = wsub(wadd(cy3, wmul(ry, fdx31)), wmul(rx, fdy31));
             const int32_t cx2 = wadd(CX2, 0xF) >> 8;
             const int32_t cx3 = wadd(CX3, 0xF) >> 8;
-            float depth = fs.z1;
-            depth = depth + (float)cx2 * fs.z2;
-            depth = depth + (float)cx3 * fs.z3;
+            float depth = z1;
+            depth = depth + (float)cx2 * z2;
+            depth = depth + (float)cx3 * z3;
             const int32_t d = __float2int_rn(depth);
-            if (d < kDepthBg) atomicMin(row + x, d);
-            CX2 = wsub(CX2, fs.fdy23);
-            CX3 = wsub(CX3, fs.fdy31);
+            if (d < kDepthBg) atomicMin(tile + (y - y0) * cwp + (x - x0), d);
           }
         }
       }

@@ -119,6 +119,36 @@ def test_fitness_off_screen_and_behind_camera(gpu_ctx, c1_gpu):
     np.testing.assert_array_equal(got, np.array([sc.fit for sc in scores], np.float32))
 
 
+@pytest.mark.parametrize("kind,n,extent", [("box", 12, 150.0), ("icosphere", 80, 220.0),
+                                           ("cylinder", 40, 180.0)])
+def test_low_poly_meshes_large_faces(gpu_ctx, c1_gpu, kind, n, extent):
+    """Few large faces (rectangles of hundreds of pixels): the warp-wide
+    raster path must match the oracle as exactly as the per-lane path."""
+    w, _, fids = c1_gpu
+    s = w["solves"][0]
+    soa, F = scene.make_mesh(kind, n, extent, seed=4, bump_mm=0.0)
+    mid = gpu_ctx.mesh_upload(soa, F)
+    rng = np.random.default_rng(6)
+    poses = random_poses(rng, s, 48, 0.7)
+    got = gpu_ctx.score_poses(gpu_desc(s, mid, fids[0]), poses)
+    prm = oracle_params(s)
+    obs = oracle_obs(w, s)
+    cam = po.camera()
+    want = []
+    for pose in poses:
+        zb, box, _ = po.render(soa, F, pose, cam)
+        want.append(po.score(zb, box, obs, cam, prm).fit)
+    np.testing.assert_array_equal(got, np.array(want, np.float32))
+    # a short solve with this mesh, batched and plain
+    s2 = dict(s, particles=24, iterations=6, seed=9, stream=3)
+    want = po.solve(soa, F, obs, cam, oracle_params(s2), trace=True)
+    r, st = gpu_ctx.solve_traced(gpu_desc(s2, mid, fids[0]))
+    np.testing.assert_array_equal(st["trace_gbest"], want["trace_gbest"])
+    rb = gpu_ctx.solve_batch([gpu_desc(s2, mid, fids[0])])[0]
+    assert rb.fit == want["fit"]
+    gpu_ctx.mesh_release(mid)
+
+
 def test_small_tiles_force_multipass(gpu_ctx, c1_gpu):
     """A tile capacity far below the render bound makes every particle-render
     take several row/column passes; the fitness must not change."""
