@@ -319,9 +319,15 @@ def run_ours(args, ws, rank, local):
     # launch shapes chosen by the autotuner on 30-iteration runs of up to 16
     # solves spread over the workload (the first iterations, with the swarm
     # still spread out, render larger than the converged ones)
-    tune = descs[::max(1, len(descs) // 16)][:16]
-    plain_cfg, _ = ctx.autotune(tune[:4], batched=False, tune_iters=30)
-    batch_cfg, _ = ctx.autotune(tune, batched=True, tune_iters=30)
+    # (--launch fixes both shapes instead, e.g. to profile one shape)
+    if args.launch:
+        plain_cfg = batch_cfg = tuple(int(x) for x in args.launch.split(","))
+        ctx.set_launch_config(plain=plain_cfg, batch=batch_cfg)
+    else:
+        tune = descs[::max(1, len(descs) // 16)][:16]
+        tune_iters = 4 if args.workload == "c5" else 30
+        plain_cfg, _ = ctx.autotune(tune[:4], batched=False, tune_iters=tune_iters)
+        batch_cfg, _ = ctx.autotune(tune, batched=True, tune_iters=tune_iters)
 
     main_fn, alt_fn = (step_batch, step_plain) if batched_default else (step_plain, step_batch)
     for _ in range(args.warmup):
@@ -329,6 +335,7 @@ def run_ours(args, ws, rank, local):
         alt_fn()
     # correctness of what is timed: plain and batched agree bit for bit
     r_main, r_alt = main_fn(), alt_fn()
+    writes_per_step = sum(r.raster_writes for r in r_main)
     agree = all(a.fit == b.fit and list(a.pose) == list(b.pose) for a, b in zip(r_main, r_alt))
     flags = max(r.flags for r in r_main)
 
@@ -374,9 +381,13 @@ def run_ours(args, ws, rank, local):
         "config": {"workload": desc, "path": "batched" if batched_default else "plain",
                    "launch_plain": {"threads": plain_cfg[0], "tile_px": plain_cfg[1], "ppb": plain_cfg[2]},
                    "launch_batched": {"threads": batch_cfg[0], "tile_px": batch_cfg[1], "ppb": batch_cfg[2]},
+                   "launch_source": "fixed (--launch)" if args.launch else "autotuned",
                    "solves_per_step": n_solves, "l2": "scrubbed (256 MB write) before every step",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "particle_renders_per_s": value * renders_per_step / n_solves,
+        "face_renders_per_s": value * sum(s["particles"] * s["iterations"] * w["meshes"][s["mesh"]][1]
+                                          for s in w["solves"]) / n_solves,
+        "raster_atomics_per_s": value * writes_per_step / n_solves,
         "plain": {"value": plain_v, "unit": "solves/s"},
         "batched": {"value": batch_v, "unit": "solves/s", "speedup_vs_plain": batch_v / plain_v},
         "plain_batched_bit_identical": bool(agree), "device_error_bits": int(flags),
@@ -469,6 +480,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--launch", default="", help="THREADS,TILE_PX,PPB for both paths instead of autotuning")
     ap.add_argument("--rates", default="5,20,100,1000,20000", help="c4: arrival rates (req/s)")
     ap.add_argument("--requests", type=int, default=48, help="c4: requests per rate")
     ap.add_argument("--slots", type=int, default=64, help="c4: server slots")

@@ -95,6 +95,27 @@ qpso_status qpso_frame_upload(qpso_context *ctx, const uint16_t *depth_mm, const
                               const qpso_camera *cam, uint32_t *frame_id);
 qpso_status qpso_frame_release(qpso_context *ctx, uint32_t frame_id);
 
+/* One cluster of a frame's label map, as the segmentation's SegResults
+ * record carries it (GraphCannySeg.h:594-618): the pixel count
+ * (num_points), the bounding rectangle (rect_aabb_, max exclusive) and the
+ * centroid of the back-projected pixels that have depth (centroid3D,
+ * compute3DCentroid GraphCannySeg.h:2569-2597: X = (u - cx) z / fx,
+ * Y = (v - cy) z / fy, Z = z, in mm).  The sums are exact integers here. */
+typedef struct {
+    int32_t label;
+    uint32_t num_points;
+    int32_t min_x, max_x, min_y, max_y;
+    uint32_t depth_points;     /* pixels of the cluster with depth > 0 */
+    float centroid_mm[3];      /* 0,0,0 when no pixel has depth */
+} qpso_cluster;
+
+/* The cluster records of every label >= 0 of a resident frame's label map
+ * (computed on the GPU), ordered by label; labels without pixels are
+ * skipped.  With out == NULL only *n_clusters is set.  The frame needs a
+ * label map; labels above 65535 are refused. */
+qpso_status qpso_frame_clusters(qpso_context *ctx, uint32_t frame_id, qpso_cluster *out,
+                                uint32_t capacity, uint32_t *n_clusters);
+
 /* Overwrite a resident frame's depth (and labels, if it has a label map)
  * in place, without allocating: the per-frame input of a serving loop.
  * Same role as qpso_frame_upload for a frame that is already resident. */
@@ -145,7 +166,7 @@ qpso_status qpso_get_launch_config(const qpso_context *ctx, qpso_launch_config *
 /* Autotuner (no counterpart in the reference, whose launch shape is the
  * fixed 6x512 / 1x1024 of main.cu:1639,1674).  Times a short run (at most
  * tune_iters iterations) of the given solves for every valid candidate
- * (threads 128/256/512, tile 4K..32K px, 1/2/4 particles per work item)
+ * (threads 128/256/512, tile 4K..48K px, 1/2/4 particles per work item)
  * on the plain path (batched = 0) or the batched path (batched = 1),
  * installs the fastest in the context and returns it.  Results do not
  * depend on the launch shape, only the speed does. */
@@ -202,13 +223,40 @@ qpso_status qpso_score_poses_noalloc(const float *d_mesh_soa, uint32_t num_faces
                                      const float *d_poses, uint32_t n, float *d_fit_out,
                                      uint32_t *d_flags_out, void *stream);
 
-/* Render one pose of a mesh into a window [x0,x0+w) x [y0,y0+h) of the
- * raster domain (int32 mm, 60000 where nothing was drawn) and return the
- * render AABB {minx,maxx,miny,maxy}.  GPU counterpart of RenderCPU
- * (main.h:2012-2043) for the best-pose render-out. */
+/* Render one pose of a mesh with the solver's rasteriser (renderFixedPointAABB,
+ * main.h:1306-1491) into a window [x0,x0+w) x [y0,y0+h) of the raster
+ * domain (int32 mm, 60000 where nothing was drawn) and return the render
+ * AABB {minx,maxx,miny,maxy}: the depth the fitness of that pose saw. */
 qpso_status qpso_render(qpso_context *ctx, uint32_t mesh_id, const qpso_camera *cam,
                         const float pose[7], int32_t x0, int32_t y0, int32_t w, int32_t h,
                         int32_t *depth_out, int32_t box_out[4]);
+
+/* The depth image the reference writes for the best pose
+ * (results/<rgb>-<N>-best.csv, main.cu:1758-1762): RenderCPU
+ * (main.h:2012-2043) on the GPU, i.e. its own rasteriser CPUfixedPointRender
+ * (main.h:1857-1991; iround vertex snapping, float depth, background 60000)
+ * after the solver's projection.  depth_out receives width*height floats,
+ * row-major.  Writes outside the image are dropped (the reference indexes
+ * y*640+x unclipped). */
+qpso_status qpso_render_depth_f32(qpso_context *ctx, uint32_t mesh_id, const qpso_camera *cam,
+                                  const float pose[7], float *depth_out);
+
+/* ---- input formats (host only: no context, no GPU) ----
+ * Wavefront OBJ text into the loadOBJ3 layout (main.h:620-679, which reads
+ * it through assimp): `v` vertices and `f` faces with 1-based or negative
+ * indices and optional /t/n parts; polygons become triangle fans from their
+ * first corner.  With soa_out == NULL only *num_faces is set; otherwise
+ * soa_out holds 9*capacity_faces floats.  QPSO_ERR_NOT_FOUND when the file
+ * cannot be read, QPSO_ERR_ARG when it is malformed or too large. */
+qpso_status qpso_obj_load(const char *path, float *soa_out, uint32_t capacity_faces,
+                          uint32_t *num_faces);
+
+/* A uint16 image: the ACCV binary depth format of loadDepth (main.cu:35-64:
+ * int32 rows, int32 cols, rows*cols uint16, row-major, host byte order) or a
+ * greyscale PNG of 16 or 8 bits (not interlaced), told apart by the PNG
+ * signature.  With out == NULL only the size is set. */
+qpso_status qpso_image_u16_load(const char *path, uint16_t *out, uint64_t capacity_px,
+                                uint32_t *width, uint32_t *height);
 
 /* ---- serving: continuous batching of solve requests ----
  * No counterpart in the reference (one solve per process).  A scheduler

@@ -156,6 +156,21 @@ def render(mesh: np.ndarray, num_faces: int, s7, cam: Camera, zbuf: np.ndarray |
     return zbuf, box, n
 
 
+def render_cpu(mesh: np.ndarray, num_faces: int, s7, cam: Camera) -> np.ndarray:
+    """The reference's host render of a pose (RenderCPU): float depth over
+    the image, background 60000."""
+    out = np.empty((cam.height, cam.width), np.float32)
+    s = np.ascontiguousarray(s7, np.float32)
+    m = np.ascontiguousarray(mesh, np.float32)
+    lib().qo_render_cpu(ptr(m, _f), C.c_uint32(num_faces), ptr(s, _f), C.byref(cam), ptr(out, _f))
+    return out
+
+
+def raster_face_cpu(v1, v2, v3, cam: Camera, depth: np.ndarray) -> None:
+    a, b, c = (np.ascontiguousarray(v, np.float32) for v in (v1, v2, v3))
+    lib().qo_raster_face_cpu(ptr(a, _f), ptr(b, _f), ptr(c, _f), C.byref(cam), ptr(depth, _f))
+
+
 def score(zbuf: np.ndarray, box: np.ndarray, obs: np.ndarray, cam: Camera, prm: Params) -> Score:
     sc = Score()
     o = np.ascontiguousarray(obs, np.uint16)

@@ -549,6 +549,108 @@ int64_t qo_render(const float *mesh, uint32_t F, const float *s, const qo_camera
 }
 
 /* ------------------------------------------------------------------ */
+/* RenderCPU, main.h:2012-2043: the reference's host render of the best pose
+ * (written to results/<rgb>-<N>-best.csv).  Its projection,
+ * projectModelPointsToPixelsCPU (main.h:1823-1855), is the same arithmetic
+ * as the kernels' (qo_project).  Its rasteriser CPUfixedPointRender
+ * (main.h:1857-1991) differs from the GPU one in two places, kept exactly:
+ * vertices snap with iround(v) = (int)(v + 0.5f) (main.h:1808-1811),
+ * truncating toward zero, and depth stays a float compared with `<` in a
+ * float buffer that starts at 60000 (main.h:156).  The inside test is the
+ * same no-op, so the face's whole bounding rectangle is written.
+ *
+ * iround of a value outside the int range, which is undefined in C, is
+ * taken as saturating (NaN -> 0).  DEVIATION: writes are clipped to the
+ * image; the reference indexes y*640+x unclipped into a 640x480 stack array
+ * (main.h:1962), aliasing columns into neighbouring rows and writing past
+ * the array for rows outside the image. */
+static inline int32_t iround_ref(float v)
+{
+    const float t = v + 0.5f;
+    if (t != t) return 0;
+    if (t >= 2147483648.0f) return INT32_MAX;
+    if (t <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)t; /* truncation toward zero */
+}
+
+void qo_raster_face_cpu(const float v1[3], const float v2[3], const float v3[3],
+                        const qo_camera *cam, float *depth)
+{
+    const int32_t Y1 = iround_ref(16.0f * v1[1]);
+    const int32_t Y2 = iround_ref(16.0f * v2[1]);
+    const int32_t Y3 = iround_ref(16.0f * v3[1]);
+    const int32_t X1 = iround_ref(16.0f * v1[0]);
+    const int32_t X2 = iround_ref(16.0f * v2[0]);
+    const int32_t X3 = iround_ref(16.0f * v3[0]);
+
+    const int32_t DX12 = w_sub(X1, X2), DX23 = w_sub(X2, X3), DX31 = w_sub(X3, X1);
+    const int32_t DY12 = w_sub(Y1, Y2), DY23 = w_sub(Y2, Y3), DY31 = w_sub(Y3, Y1);
+    const int32_t tri_area = w_sub(w_mul(DX12, DY31), w_mul(DX31, DY12));
+    if (tri_area <= 0) return;
+    const float rA = 1.0f / (float)tri_area; /* overA_ / float(triArea), overA_ == 1 */
+
+    const int32_t FDX23 = w_shl(DX23, 4), FDX31 = w_shl(DX31, 4);
+    const int32_t FDY23 = w_shl(DY23, 4), FDY31 = w_shl(DY31, 4);
+    const int32_t minx = asr(w_add(imin(imin(X1, X2), X3), 0xF), 4);
+    const int32_t maxx = asr(w_add(imax(imax(X1, X2), X3), 0xF), 4);
+    const int32_t miny = asr(w_add(imin(imin(Y1, Y2), Y3), 0xF), 4);
+    const int32_t maxy = asr(w_add(imax(imax(Y1, Y2), Y3), 0xF), 4);
+    if (w_sub(maxx, minx) <= 0 || w_sub(maxy, miny) <= 0) return;
+
+    int32_t C2 = w_sub(w_mul(DY23, X2), w_mul(DX23, Y2));
+    int32_t C3 = w_sub(w_mul(DY31, X3), w_mul(DX31, Y3));
+    C2 = w_add(C2, (DY23 < 0 || (DY23 == 0 && DX23 > 0)) ? 1 : 0);
+    C3 = w_add(C3, (DY31 < 0 || (DY31 == 0 && DX31 > 0)) ? 1 : 0);
+    const int32_t MINY = w_shl(miny, 4), MINX = w_shl(minx, 4);
+    const int32_t CY2 = w_sub(w_add(C2, w_mul(DX23, MINY)), w_mul(DY23, MINX));
+    const int32_t CY3 = w_sub(w_add(C3, w_mul(DX31, MINY)), w_mul(DY31, MINX));
+    const float z1 = v1[2];
+    const float z2 = (v2[2] - v1[2]) * rA;
+    const float z3 = (v3[2] - v1[2]) * rA;
+
+    const int64_t ext_x = (int64_t)(uint32_t)w_sub(maxx, minx);
+    const int64_t ext_y = (int64_t)(uint32_t)w_sub(maxy, miny);
+    int64_t xa = minx, xb = (int64_t)minx + ext_x;
+    int64_t ya = miny, yb = (int64_t)miny + ext_y;
+    if (xa < 0) xa = 0;
+    if (xb > cam->width) xb = cam->width;
+    if (ya < 0) ya = 0;
+    if (yb > cam->height) yb = cam->height;
+    for (int64_t y = ya; y < yb; ++y) {
+        const int32_t ry = (int32_t)(y - (int64_t)miny);
+        for (int64_t x = xa; x < xb; ++x) {
+            const int32_t rx = (int32_t)(x - (int64_t)minx);
+            const int32_t CX2 = w_sub(w_add(CY2, w_mul(ry, FDX23)), w_mul(rx, FDY23));
+            const int32_t CX3 = w_sub(w_add(CY3, w_mul(ry, FDX31)), w_mul(rx, FDY31));
+            const int32_t cx2 = asr(w_add(CX2, 0xF), 8);
+            const int32_t cx3 = asr(w_add(CX3, 0xF), 8);
+            float d = z1;
+            d = d + (float)cx2 * z2;
+            d = d + (float)cx3 * z3;
+            float *px = &depth[(size_t)y * (size_t)cam->width + (size_t)x];
+            if (d < *px) *px = d;
+        }
+    }
+}
+
+void qo_render_cpu(const float *mesh, uint32_t F, const float *s, const qo_camera *cam,
+                   float *depth)
+{
+    const size_t n = (size_t)cam->width * (size_t)cam->height;
+    for (size_t i = 0; i < n; ++i) depth[i] = (float)QO_DEPTH_BG;
+    for (uint32_t f = 0; f < F; ++f) {
+        float v[3][3], uvz[3][3];
+        for (int j = 0; j < 3; ++j) {
+            v[j][0] = mesh[f + (size_t)j * F];
+            v[j][1] = mesh[f + 3 * (size_t)F + (size_t)j * F];
+            v[j][2] = mesh[f + 6 * (size_t)F + (size_t)j * F];
+            qo_project(s, v[j], cam, uvz[j]);
+        }
+        qo_raster_face_cpu(uvz[0], uvz[1], uvz[2], cam, depth);
+    }
+}
+
+/* ------------------------------------------------------------------ */
 /* ComputeFitnessKernel, main.cu:550-764.
  *
  * Window = union of the render AABB and the cluster AABB (main.cu:596-622);

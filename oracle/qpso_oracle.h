@@ -116,6 +116,14 @@ int64_t qo_raster_face(const float v1[3], const float v2[3], const float v3[3],
 int64_t qo_render(const float *mesh, uint32_t num_faces, const float *s,
                   const qo_camera *cam, int32_t *zbuf, int32_t box[4]);
 
+/* The reference's host render of the best pose (RenderCPU): iround snapping,
+ * float depth, the image only (width*height floats, row-major, filled with
+ * the background 60000 first). */
+void qo_raster_face_cpu(const float v1[3], const float v2[3], const float v3[3],
+                        const qo_camera *cam, float *depth);
+void qo_render_cpu(const float *mesh, uint32_t num_faces, const float *s,
+                   const qo_camera *cam, float *depth);
+
 /* ---- fitness ---- */
 void qo_score_zbuf(const int32_t *zbuf, const int32_t box[4], const uint16_t *obs,
                    const qo_camera *cam, const qo_params *prm, qo_score *out);

@@ -126,6 +126,14 @@ void pin_cpu_raster_face(const float *v1, const float *v2, const float *v3, floa
     CPUfixedPointRender(buf, a, b, c);
 }
 
+/* projection of the host render (main.h:1823-1855) */
+void pin_project_cpu(const float *s, const float *v, float *o)
+{
+    float4 p = make_float4(v[0], v[1], v[2], 0.f), r;
+    projectModelPointsToPixelsCPU(s, p, r);
+    o[0] = r.x; o[1] = r.y; o[2] = r.z;
+}
+
 int pin_rows(void) { return rows_; }
 int pin_cols(void) { return cols_; }
 

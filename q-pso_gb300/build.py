@@ -1,9 +1,11 @@
 """Build the sm_103a shared library ``_build/libqpso_gb300.so`` in-tree.
 
-nvcc compiles the two translation units in parallel with -gencode
+nvcc compiles the translation units in parallel with -gencode
 arch=compute_103a,code=sm_103a only, --fmad=false (the arithmetic contract
 of the fused kernels: one IEEE rounding per operation, fma only where the
-source writes one) and -lineinfo for the profiler.
+source writes one) and -lineinfo for the profiler.  The command-line
+drop-in ``_build/qpso_main`` (cli/qpso_main.cpp) links the library through
+its C ABI only.
 """
 from __future__ import annotations
 
@@ -17,11 +19,13 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(BUILD, "libqpso_gb300.so")
+CLI_SRC = os.path.join(HERE, "cli", "qpso_main.cpp")
+CLI = os.path.join(BUILD, "qpso_main")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "--fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-I", INCLUDE, "-I", CSRC]
-UNITS = ["qpso_kernels.cu", "qpso_api.cu", "qpso_noalloc.cu"]
+UNITS = ["qpso_kernels.cu", "qpso_api.cu", "qpso_noalloc.cu", "ingest.cpp"]
 HEADERS = ["qpso_device.cuh", "qpso_internal.cuh", "meshlets.h"]
 
 
@@ -31,10 +35,10 @@ def _sources():
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
-    t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(s) <= t for s in _sources())
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
+    return all(os.path.getmtime(s) <= t for s in _sources() + [CLI_SRC])
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -43,7 +47,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
 
     def compile_unit(u):
-        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(u)[0] + ".o")
         cmd = [NVCC, *ARCH, *FLAGS, "-c", os.path.join(CSRC, u), "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
@@ -62,6 +66,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr)
     os.replace(tmp, LIB)
+    tmp = CLI + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", "-I", INCLUDE, CLI_SRC, "-o", tmp, "-L", BUILD, "-lqpso_gb300",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("cli build failed:\n%s" % r.stderr)
+    os.replace(tmp, CLI)
     return LIB
 
 

@@ -14,7 +14,10 @@ namespace qpso {
 // nv float4 positions (x, y, z, 0; metres), then nf uint32 faces packing the
 // three local vertex ids in bits 0-9, 10-19, 20-29, padded to 16 bytes.
 // Built once at mesh upload; face order does not affect any result (depth
-// writes are atomic minima, the render AABB is a min/max).
+// writes are atomic minima, the render AABB is a min/max).  After the last
+// payload the blob holds one object-space box per meshlet, two float4 (lo,
+// hi) at `box_off`, over the meshlet's vertices: the fused kernels project
+// its corners to skip meshlets that miss a tile band.
 constexpr int kMletFaces = 128;
 constexpr int kMletVerts = 128;
 constexpr int kMletBytes = kMletVerts * 16 + kMletFaces * 4;
@@ -31,7 +34,7 @@ inline size_t mlet_align16(size_t x) { return (x + 15) / 16 * 16; }
 // faces are grown breadth-first over shared vertices so that each meshlet
 // is a compact surface patch whose vertices are transformed once per pose.
 inline void build_meshlets(const float* soa, uint32_t F, std::vector<MeshletHdr>& hdr,
-                    std::vector<unsigned char>& blob) {
+                           std::vector<unsigned char>& blob, size_t* box_off) {
   struct Key {
     uint32_t x, y, z;
     bool operator==(const Key& o) const { return x == o.x && y == o.y && z == o.z; }
@@ -125,6 +128,18 @@ inline void build_meshlets(const float* soa, uint32_t F, std::vector<MeshletHdr>
     }
     hdr.push_back(h);
     ++mid;
+  }
+  *box_off = blob.size();
+  blob.resize(blob.size() + hdr.size() * 32, 0);
+  for (size_t i = 0; i < hdr.size(); ++i) {
+    const float* pv = reinterpret_cast<const float*>(blob.data() + hdr[i].off);
+    float b[8] = {pv[0], pv[1], pv[2], 0.f, pv[0], pv[1], pv[2], 0.f};
+    for (uint32_t v = 1; v < hdr[i].nv; ++v)
+      for (int c = 0; c < 3; ++c) {
+        b[c] = pv[4 * v + c] < b[c] ? pv[4 * v + c] : b[c];
+        b[4 + c] = pv[4 * v + c] > b[4 + c] ? pv[4 * v + c] : b[4 + c];
+      }
+    std::memcpy(blob.data() + *box_off + 32 * i, b, 32);
   }
 }
 

@@ -39,6 +39,7 @@ struct MeshObj {
   MeshletHdr* mlets = nullptr;       // device
   unsigned char* blob = nullptr;     // device
   uint32_t n_mlets = 0;
+  size_t box_off = 0;                // per-meshlet boxes, bytes into blob
 };
 
 struct FrameObj {
@@ -286,6 +287,7 @@ void fill_meta(qpso_context* ctx, const Layout& L, const std::vector<const qpso_
     I.F = m.F;
     I.mlets = m.mlets;
     I.mlet_blob = m.blob;
+    I.mlet_box = reinterpret_cast<const float4*>(m.blob + m.box_off);
     I.n_mlets = m.n_mlets;
     for (int k = 0; k < 3; ++k) {
       I.mesh_lo[k] = m.lo[k];
@@ -417,10 +419,12 @@ qpso_status qpso_mesh_upload(qpso_context* ctx, const float* soa, uint32_t F, ui
   cudaSetDevice(ctx->device);
   std::vector<MeshletHdr> hdr;
   std::vector<unsigned char> blob;
-  build_meshlets(soa, F, hdr, blob);
+  size_t box_off = 0;
+  build_meshlets(soa, F, hdr, blob, &box_off);
   MeshObj m;
   m.F = F;
   m.n_mlets = (uint32_t)hdr.size();
+  m.box_off = box_off;
   QPSO_CUDA(ctx, cudaMalloc(&m.d, 9 * (size_t)F * sizeof(float) + 32));
   cudaError_t e = cudaMalloc(&m.mlets, hdr.size() * sizeof(MeshletHdr));
   if (e == cudaSuccess) e = cudaMalloc(&m.blob, blob.size());
@@ -810,7 +814,7 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
   if (!ctx->timers[0]) QPSO_CUDA(ctx, cudaEventCreate(&ctx->timers[0]));
   if (!ctx->timers[1]) QPSO_CUDA(ctx, cudaEventCreate(&ctx->timers[1]));
   const int threads[] = {128, 256, 512};
-  const int tiles[] = {4096, 8192, 16384, 32768};
+  const int tiles[] = {4096, 8192, 16384, 32768, 49152};
   const int ppbs[] = {1, 2, 4};
   for (int th : threads)
     for (int tp : tiles)
@@ -932,6 +936,82 @@ qpso_status qpso_render(qpso_context* ctx, uint32_t mesh_id, const qpso_camera* 
   QPSO_CUDA(ctx, cudaMemcpyAsync(depth_out, d + out_off, (size_t)w * h * 4, cudaMemcpyDeviceToHost, s));
   QPSO_CUDA(ctx, cudaMemcpyAsync(box_out, d + box_off, 16, cudaMemcpyDeviceToHost, s));
   QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  return QPSO_OK;
+}
+
+qpso_status qpso_frame_clusters(qpso_context* ctx, uint32_t frame_id, qpso_cluster* out, uint32_t capacity,
+                                uint32_t* n_clusters) {
+  if (!ctx || !n_clusters) return fail(ctx, QPSO_ERR_ARG, "bad cluster arguments");
+  auto fi = ctx->frames.find(frame_id);
+  if (fi == ctx->frames.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown frame id");
+  const FrameObj& f = fi->second;
+  if (!f.labels) return fail(ctx, QPSO_ERR_ARG, "frame has no label map");
+  cudaSetDevice(ctx->device);
+  const int32_t W = f.cam.width, H = f.cam.height;
+  qpso_status st;
+  if ((st = ensure_ws(ctx, 256 + 65536 * sizeof(ClusterAcc))) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  char* d = static_cast<char*>(ctx->ws.p);
+  int32_t maxl = -1;
+  QPSO_CUDA(ctx, launch_label_max(f.labels, (uint32_t)W * (uint32_t)H, reinterpret_cast<int32_t*>(d),
+                                  ctx->stream));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(&maxl, d, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (maxl > 65535) return fail(ctx, QPSO_ERR_ARG, "label above 65535");
+  std::vector<ClusterAcc> acc((size_t)(maxl + 1));
+  if (maxl >= 0) {
+    ClusterAcc* da = reinterpret_cast<ClusterAcc*>(d + 256);
+    QPSO_CUDA(ctx, launch_cluster_stats(f.depth, f.labels, W, H, da, maxl + 1, ctx->stream));
+    QPSO_CUDA(ctx, cudaMemcpyAsync(acc.data(), da, acc.size() * sizeof(ClusterAcc), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  uint32_t n = 0;
+  for (int32_t l = 0; l <= maxl; ++l) {
+    const ClusterAcc& a = acc[(size_t)l];
+    if (a.n == 0) continue;
+    if (out && n < capacity) {
+      qpso_cluster& c = out[n];
+      c.label = l;
+      c.num_points = a.n;
+      c.min_x = a.minx;
+      c.max_x = a.maxx;
+      c.min_y = a.miny;
+      c.max_y = a.maxy;
+      c.depth_points = a.nz;
+      if (a.nz) {
+        const double sz = (double)a.sum_z;
+        c.centroid_mm[0] = (float)(((double)a.sum_xz - (double)f.cam.cx * sz) / ((double)f.cam.fx * a.nz));
+        c.centroid_mm[1] = (float)(((double)a.sum_yz - (double)f.cam.cy * sz) / ((double)f.cam.fy * a.nz));
+        c.centroid_mm[2] = (float)(sz / a.nz);
+      } else {
+        c.centroid_mm[0] = c.centroid_mm[1] = c.centroid_mm[2] = 0.f;
+      }
+    }
+    ++n;
+  }
+  *n_clusters = n;
+  if (out && n > capacity) return fail(ctx, QPSO_ERR_ARG, "more clusters than capacity");
+  return QPSO_OK;
+}
+
+qpso_status qpso_render_depth_f32(qpso_context* ctx, uint32_t mesh_id, const qpso_camera* cam,
+                                  const float pose[7], float* depth_out) {
+  if (!ctx || !cam || !pose || !depth_out || cam->width <= 0 || cam->height <= 0 ||
+      (int64_t)cam->width * cam->height > (1 << 26))
+    return fail(ctx, QPSO_ERR_ARG, "bad render arguments");
+  auto mi = ctx->meshes.find(mesh_id);
+  if (mi == ctx->meshes.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown mesh id");
+  cudaSetDevice(ctx->device);
+  const size_t bytes = (size_t)cam->width * cam->height * sizeof(float);
+  qpso_status st;
+  if ((st = ensure_ws(ctx, bytes)) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  float* d = static_cast<float*>(ctx->ws.p);
+  const Camera c{cam->fx, cam->fy, cam->cx, cam->cy, cam->width, cam->height};
+  QPSO_CUDA(ctx, launch_host_render(mi->second.d, mi->second.F, pose, c, d, ctx->stream));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(depth_out, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return QPSO_OK;
 }
 
@@ -1086,6 +1166,7 @@ void server_loop(qpso_server* s) {
         I.F = m->F;
         I.mlets = m->mlets;
         I.mlet_blob = m->blob;
+        I.mlet_box = reinterpret_cast<const float4*>(m->blob + m->box_off);
         I.n_mlets = m->n_mlets;
         for (int k = 0; k < 3; ++k) {
           I.mesh_lo[k] = m->lo[k];

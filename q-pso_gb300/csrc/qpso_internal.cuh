@@ -25,6 +25,7 @@ struct Instance {
   uint32_t F;
   const MeshletHdr* mlets;  // meshlets of the same faces (the fused kernels read these)
   const unsigned char* mlet_blob;
+  const float4* mlet_box;   // per meshlet: object-space lo, hi (2 float4)
   uint32_t n_mlets;
   float mesh_lo[3], mesh_hi[3];
   const uint16_t* obs;      // cluster-masked observed depth (mm), width*height
@@ -104,5 +105,18 @@ cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* 
                                 cudaStream_t st);
 cudaError_t launch_copy_flags(const uint32_t* src, uint32_t* dst, cudaStream_t st);
 size_t smem_ctl_bytes();
+// Per-label accumulators of a label map (cluster records).
+struct ClusterAcc {
+  unsigned long long sum_z, sum_xz, sum_yz;
+  uint32_t n, nz;
+  int32_t minx, maxx, miny, maxy;
+};
+cudaError_t launch_label_max(const int32_t* labels, uint32_t n, int32_t* out, cudaStream_t st);
+cudaError_t launch_cluster_stats(const uint16_t* depth, const int32_t* labels, int32_t W, int32_t H,
+                                 ClusterAcc* acc, int32_t nlab, cudaStream_t st);
+// Float depth image of one pose with the arithmetic of the reference's host
+// render (RenderCPU); out: width*height floats on the device.
+cudaError_t launch_host_render(const float* mesh, uint32_t F, const float pose[7], const Camera& cam,
+                               float* out, cudaStream_t st);
 
 }  // namespace qpso

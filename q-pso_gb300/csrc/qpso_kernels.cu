@@ -103,6 +103,7 @@ constexpr int kLaneRasterMax = 32;  // larger face rectangles are rasterised by 
 struct FusedSmem {
   int4* vcache;          // [warps][kMletVerts] snapped X, Y and depth bits, per warp
   int4* mbox;            // [ppb][kCullCap] meshlet rectangles (minx, maxx, miny, maxy)
+  uint32_t* live;        // [ppb * kCullCap] listed items of a culled pass (particle << 28 | meshlet)
   int32_t* tiles;        // [ppb][tile_px] depth tiles
 };
 
@@ -110,6 +111,7 @@ struct SmemCtl {
   float pose[kMaxPpb][8];
   int32_t bound[4];
   uint32_t claim;
+  uint32_t n_live;     // listed items of the current pass and meshlet chunk
   int last;
   int maxpass;
   Partial warp[kMaxThreads / 32];
@@ -389,6 +391,8 @@ __device__ __forceinline__ FusedSmem carve_smem(unsigned char* dyn, int ppb) {
   o += (size_t)(blockDim.x >> 5) * kMletVerts * 16;
   sm.mbox = reinterpret_cast<int4*>(dyn + o);
   o += (size_t)ppb * kCullCap * 16;
+  sm.live = reinterpret_cast<uint32_t*>(dyn + o);
+  o += (size_t)ppb * kCullCap * 4;
   sm.tiles = reinterpret_cast<int32_t*>(dyn + o);
   return sm;
 }
@@ -399,11 +403,42 @@ __device__ __forceinline__ bool rect_overlaps(const int4& b, const PartCtl& pc) 
          b.w > pc.y0;
 }
 
+__device__ __forceinline__ int32_t clamp_px(float f, int32_t lo, int32_t hi) {
+  return (int32_t)fminf(fmaxf(f, (float)lo), (float)hi);
+}
+
+// Conservative pixel rectangle (minx, maxx, miny, maxy; half-open) of an
+// object-space box under `pose`: its 8 corners projected, widened by the
+// particle bound's margin, clipped to the raster domain.  Every vertex
+// inside the box projects inside the corners' hull when all corners lie in
+// front of the 50 mm plane (depth is affine in the object coordinates);
+// false when one does not, or a corner does not project to a number.
+__device__ __forceinline__ bool box_rect(const float* pose, const Camera& cam, float4 lo, float4 hi,
+                                         int32_t dx0, int32_t dx1, int32_t dy0, int32_t dy1, int4& r) {
+  float ulo = 3.0e38f, uhi = -3.0e38f, vlo = 3.0e38f, vhi = -3.0e38f;
+  bool ok = true;
+#pragma unroll 1
+  for (int c = 0; c < 8; ++c) {
+    float u, v, zz;
+    project(pose, (c & 1) ? hi.x : lo.x, (c & 2) ? hi.y : lo.y, (c & 4) ? hi.z : lo.z, cam, u, v, zz);
+    ok = ok && zz >= 50.0f && u == u && v == v;
+    ulo = fminf(ulo, u);
+    uhi = fmaxf(uhi, u);
+    vlo = fminf(vlo, v);
+    vhi = fmaxf(vhi, v);
+  }
+  r = make_int4(clamp_px(floorf(ulo) - 1.0f, dx0, dx1), clamp_px(floorf(uhi) + 2.0f, dx0, dx1),
+                clamp_px(floorf(vlo) - 1.0f, dy0, dy1), clamp_px(floorf(vhi) + 2.0f, dy0, dy1));
+  return ok;
+}
+
 // Render + score particles 0..np-1 whose poses are in ctl.pose.  All
 // threads call this; fitness k is returned in fit_out[k] (shared memory).
-// When a particle's conservative bound needs several tile passes, pass 0
-// records every meshlet's screen rectangle per particle and later passes
-// load and transform only the meshlets that overlap a live band.
+// When a particle's conservative bound needs several tile passes, later
+// passes load and transform only the meshlets that overlap a live band:
+// pass 0 records every meshlet's screen rectangle per particle when the
+// mesh has at most kCullCap meshlets; larger meshes project each meshlet's
+// object-space box instead (checked in pass 0 against the real rectangle).
 __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& sm, int tile_px,
                                    SmemCtl& ctl, float* fit_out) {
   const int tid = threadIdx.x, T = blockDim.x;
@@ -497,149 +532,227 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
     __syncthreads();
     // 2c. every warp takes (particle, meshlet) items on its own: vertices
     //     into its private cache, then the faces into the particle's tile.
-    //     In passes after the first, meshlets whose rectangle misses the
-    //     particle's band are skipped.
-    const bool cull = pass > 0 && cull_ok;
+    //     Pass 0 takes every item.  A later pass first lists, with one
+    //     thread per item, the meshlets that overlap the particle's band
+    //     (their pass-0 rectangle, or for meshes above kCullCap meshlets the
+    //     projection of their object-space box, kCullCap meshlets at a
+    //     time), then the warps share out the listed items.
+    const bool cull = pass > 0;
+    const bool check_boxes = !cull_ok && maxpass > 1;
     int4* vc = vcache + wid * kMletVerts;
-    for (uint32_t item = wid; item < (uint32_t)np * nm; item += nw) {
-      const int k = (int)(item / nm);
-      const uint32_t m = item - (uint32_t)k * nm;
-      PartCtl& pc = ctl.part[k];
-      if (pass >= pc.npass || (cull && !rect_overlaps(mbox[k * kCullCap + m], pc))) continue;
-      const uint2 hw = __ldg(reinterpret_cast<const uint2*>(I.mlets + m));
-      MeshletHdr h;
-      h.off = hw.x;
-      h.nv = (uint16_t)(hw.y & 0xffffu);
-      h.nf = (uint16_t)(hw.y >> 16);
-      const int nv = h.nv, nf = h.nf;
-      const float4* gv = reinterpret_cast<const float4*>(I.mlet_blob + h.off);
-      const uint32_t* gf = reinterpret_cast<const uint32_t*>(I.mlet_blob + h.off + nv * 16);
-      const float* pose = ctl.pose[k];
-      for (int v = lane; v < nv; v += 32) {
-        const float4 qv = __ldg(gv + v);
-        float u, vv, z;
-        project(pose, qv.x, qv.y, qv.z, I.cam, u, vv, z);
-        vc[v] = make_int4(__float2int_rn(16.0f * u), __float2int_rn(16.0f * vv), __float_as_int(z), 0);
-      }
-      __syncwarp();
-      int32_t bminx = kAabbInitMin, bmaxx = kAabbInitMax, bminy = kAabbInitMin, bmaxy = kAabbInitMax;
-      int32_t* tile = tiles + (size_t)k * tile_px;
-      const int32_t x0 = pc.x0, y0 = pc.y0, cwp = pc.cwp, thp = pc.thp;
-      // faces: a lane rasterises its own face when the clipped rectangle has
-      // at most kLaneRasterMax pixels; larger rectangles are rasterised by the
-      // whole warp (set-up broadcast by shuffles, pixels strided over lanes)
-      for (int base = 0; base < nf; base += 32) {
-        const int f = base + lane;
-        FaceSetup fs;
-        int32_t xa = 0, xb = 0, ya = 0, yb = 0;
-        bool big = false;
-        if (f < nf) {
-          const uint32_t fi = __ldg(gf + f);
-          const int4 a = vc[fi & 1023u], bb = vc[(fi >> 10) & 1023u], c = vc[(fi >> 20) & 1023u];
-          setup_face_fixed(a.x, a.y, __int_as_float(a.z), bb.x, bb.y, __int_as_float(bb.z), c.x, c.y,
-                           __int_as_float(c.z), fs);
-          bminx = min(bminx, fs.minx);
-          bmaxx = max(bmaxx, fs.maxx);
-          bminy = min(bminy, fs.miny);
-          bmaxy = max(bmaxy, fs.maxy);
-          if (fs.live) {
-            if (pass == 0) {
-              const int32_t ca = max(fs.minx, dx0), cb = min(fs.maxx, dx1);
-              const int32_t ra = max(fs.miny, dy0), rb = min(fs.maxy, dy1);
-              if (ca < cb && ra < rb &&
-                  (ca < pc.bound[0] || cb > pc.bound[1] || ra < pc.bound[2] || rb > pc.bound[3]))
-                violation = true;
-            }
-            xa = max(fs.minx, x0);
-            xb = min(fs.maxx, x0 + cwp);
-            ya = max(fs.miny, y0);
-            yb = min(fs.maxy, y0 + thp);
-            if (xa < xb && ya < yb) {
-              const int32_t n = (xb - xa) * (yb - ya);
-              writes += (unsigned long long)n;
-              if (n > kLaneRasterMax) {
-                big = true;
+    for (uint32_t mc = 0; mc < (cull ? nm : 1u); mc += (uint32_t)kCullCap) {
+      uint32_t n_items = (uint32_t)np * nm;
+      if (cull) {
+        const uint32_t nmc = min((uint32_t)kCullCap, nm - mc);
+        const uint32_t nt = (uint32_t)np * nmc;
+        if (tid == 0) ctl.n_live = 0;
+        __syncthreads();
+        for (uint32_t b = (uint32_t)(tid & ~31); b < nt; b += (uint32_t)T) {  // whole warps
+          const uint32_t i = b + (uint32_t)lane;
+          bool ov = false;
+          uint32_t k = 0, m = 0;
+          if (i < nt) {
+            k = i / nmc;
+            m = mc + (i - k * nmc);
+            const PartCtl& pc = ctl.part[k];
+            if (pass < pc.npass) {
+              if (cull_ok) {
+                ov = rect_overlaps(mbox[k * kCullCap + m], pc);
               } else {
-                const int32_t rx0 = xa - fs.minx;
-                for (int32_t y = ya; y < yb; ++y) {
-                  const int32_t ry = y - fs.miny;
-                  int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
-                  int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
-                  int32_t* row = tile + (y - y0) * cwp - x0;
-                  for (int32_t x = xa; x < xb; ++x) {
-                    const int32_t cx2 = wadd(CX2, 0xF) >> 8;
-                    const int32_t cx3 = wadd(CX3, 0xF) >> 8;
-                    float depth = fs.z1;
-                    depth = depth + (float)cx2 * fs.z2;
-                    depth = depth + (float)cx3 * fs.z3;
-                    const int32_t d = __float2int_rn(depth);
-                    if (d < kDepthBg) atomicMin(row + x, d);
-                    CX2 = wsub(CX2, fs.fdy23);
-                    CX3 = wsub(CX3, fs.fdy31);
+                int4 r;
+                ov = !box_rect(ctl.pose[k], I.cam, __ldg(I.mlet_box + 2 * m), __ldg(I.mlet_box + 2 * m + 1),
+                               dx0, dx1, dy0, dy1, r) ||
+                     rect_overlaps(r, pc);
+              }
+            }
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, ov);
+          uint32_t at = 0;
+          if (lane == 0 && bal) at = atomicAdd(&ctl.n_live, (uint32_t)__popc(bal));
+          at = __shfl_sync(0xffffffffu, at, 0);
+          if (ov) sm.live[at + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = (k << 28) | m;
+        }
+        __syncthreads();
+        n_items = ctl.n_live;
+      }
+      for (uint32_t item = wid; item < n_items; item += nw) {
+        int k;
+        uint32_t m;
+        if (cull) {
+          const uint32_t e = sm.live[item];
+          k = (int)(e >> 28);
+          m = e & 0x0fffffffu;
+        } else {
+          k = (int)(item / nm);
+          m = item - (uint32_t)k * nm;
+        }
+        PartCtl& pc = ctl.part[k];
+        const uint2 hw = __ldg(reinterpret_cast<const uint2*>(I.mlets + m));
+        MeshletHdr h;
+        h.off = hw.x;
+        h.nv = (uint16_t)(hw.y & 0xffffu);
+        h.nf = (uint16_t)(hw.y >> 16);
+        const int nv = h.nv, nf = h.nf;
+        const float4* gv = reinterpret_cast<const float4*>(I.mlet_blob + h.off);
+        const uint32_t* gf = reinterpret_cast<const uint32_t*>(I.mlet_blob + h.off + nv * 16);
+        const float* pose = ctl.pose[k];
+        for (int v = lane; v < nv; v += 32) {
+          const float4 qv = __ldg(gv + v);
+          float u, vv, z;
+          project(pose, qv.x, qv.y, qv.z, I.cam, u, vv, z);
+          vc[v] = make_int4(__float2int_rn(16.0f * u), __float2int_rn(16.0f * vv), __float_as_int(z), 0);
+        }
+        __syncwarp();
+        // the meshlet's own rectangle starts empty; the render AABB it is
+        // merged into starts from the reference's 50000 / -1
+        int32_t bminx = INT32_MAX, bmaxx = INT32_MIN, bminy = INT32_MAX, bmaxy = INT32_MIN;
+        int32_t* tile = tiles + (size_t)k * tile_px;
+        const int32_t x0 = pc.x0, y0 = pc.y0, cwp = pc.cwp, thp = pc.thp;
+        // faces: a lane rasterises its own face when the clipped rectangle has
+        // at most kLaneRasterMax pixels; larger rectangles are rasterised by the
+        // whole warp (set-up broadcast by shuffles, pixels strided over lanes)
+        for (int base = 0; base < nf; base += 32) {
+          const int f = base + lane;
+          FaceSetup fs;
+          int32_t xa = 0, xb = 0, ya = 0, yb = 0;
+          bool big = false;
+          if (f < nf) {
+            const uint32_t fi = __ldg(gf + f);
+            const int4 a = vc[fi & 1023u], bb = vc[(fi >> 10) & 1023u], c = vc[(fi >> 20) & 1023u];
+            setup_face_fixed(a.x, a.y, __int_as_float(a.z), bb.x, bb.y, __int_as_float(bb.z), c.x, c.y,
+                             __int_as_float(c.z), fs);
+            bminx = min(bminx, fs.minx);
+            bmaxx = max(bmaxx, fs.maxx);
+            bminy = min(bminy, fs.miny);
+            bmaxy = max(bmaxy, fs.maxy);
+            if (fs.live) {
+              if (pass == 0) {
+                const int32_t ca = max(fs.minx, dx0), cb = min(fs.maxx, dx1);
+                const int32_t ra = max(fs.miny, dy0), rb = min(fs.maxy, dy1);
+                if (ca < cb && ra < rb &&
+                    (ca < pc.bound[0] || cb > pc.bound[1] || ra < pc.bound[2] || rb > pc.bound[3]))
+                  violation = true;
+              }
+              xa = max(fs.minx, x0);
+              xb = min(fs.maxx, x0 + cwp);
+              ya = max(fs.miny, y0);
+              yb = min(fs.maxy, y0 + thp);
+              if (xa < xb && ya < yb) {
+                const int32_t n = (xb - xa) * (yb - ya);
+                writes += (unsigned long long)n;
+                if (n > kLaneRasterMax) {
+                  big = true;
+                } else {
+                  const int32_t rx0 = xa - fs.minx;
+                  for (int32_t y = ya; y < yb; ++y) {
+                    const int32_t ry = y - fs.miny;
+                    int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
+                    int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
+                    int32_t* row = tile + (y - y0) * cwp - x0;
+                    for (int32_t x = xa; x < xb; ++x) {
+                      const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+                      const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+                      float depth = fs.z1;
+                      depth = depth + (float)cx2 * fs.z2;
+                      depth = depth + (float)cx3 * fs.z3;
+                      const int32_t d = __float2int_rn(depth);
+                      if (d < kDepthBg) atomicMin(row + x, d);
+                      CX2 = wsub(CX2, fs.fdy23);
+                      CX3 = wsub(CX3, fs.fdy31);
+                    }
                   }
                 }
               }
             }
           }
-        }
-        unsigned bigmask = __ballot_sync(0xffffffffu, big);
-        while (bigmask) {
-          const int src = __ffs(bigmask) - 1;
-          bigmask &= bigmask - 1;
-          const int32_t fminx = __shfl_sync(0xffffffffu, fs.minx, src);
-          const int32_t fminy = __shfl_sync(0xffffffffu, fs.miny, src);
-          const int32_t cy2 = __shfl_sync(0xffffffffu, fs.cy2, src);
-          const int32_t cy3 = __shfl_sync(0xffffffffu, fs.cy3, src);
-          const int32_t fdx23 = __shfl_sync(0xffffffffu, fs.fdx23, src);
-          const int32_t fdx31 = __shfl_sync(0xffffffffu, fs.fdx31, src);
-          const int32_t fdy23 = __shfl_sync(0xffffffffu, fs.fdy23, src);
-          const int32_t fdy31 = __shfl_sync(0xffffffffu, fs.fdy31, src);
-          const float z1 = __shfl_sync(0xffffffffu, fs.z1, src);
-          const float z2 = __shfl_sync(0xffffffffu, fs.z2, src);
-          const float z3 = __shfl_sync(0xffffffffu, fs.z3, src);
-          const int32_t bxa = __shfl_sync(0xffffffffu, xa, src);
-          const int32_t bxb = __shfl_sync(0xffffffffu, xb, src);
-          const int32_t bya = __shfl_sync(0xffffffffu, ya, src);
-          const int32_t byb = __shfl_sync(0xffffffffu, yb, src);
-          const int32_t w = bxb - bxa;
-          const int32_t n = w * (byb - bya);
-          const float rw = 1.0f / (float)w;
-          for (int32_t pix = lane; pix < n; pix += 32) {
-            const int32_t r = small_div(pix, rw);
-            const int32_t x = bxa + (pix - r * w), y = bya + r;
-            const int32_t ry = y - fminy, rx = x - fminx;
-            const int32_t CX2 = wsub(wadd(cy2, wmul(ry, fdx23)), wmul(rx, fdy23));
-            const int32_t CX3 = wsub(wadd(cy3, wmul(ry, fdx31)), wmul(rx, fdy31));
-            const int32_t cx2 = wadd(CX2, 0xF) >> 8;
-            const int32_t cx3 = wadd(CX3, 0xF) >> 8;
-            float depth = z1;
-            depth = depth + (float)cx2 * z2;
-            depth = depth + (float)cx3 * z3;
-            const int32_t d = __float2int_rn(depth);
-            if (d < kDepthBg) atomicMin(tile + (y - y0) * cwp + (x - x0), d);
+          unsigned bigmask = __ballot_sync(0xffffffffu, big);
+          while (bigmask) {
+            const int src = __ffs(bigmask) - 1;
+            bigmask &= bigmask - 1;
+            const int32_t fminx = __shfl_sync(0xffffffffu, fs.minx, src);
+            const int32_t fminy = __shfl_sync(0xffffffffu, fs.miny, src);
+            const int32_t cy2 = __shfl_sync(0xffffffffu, fs.cy2, src);
+            const int32_t cy3 = __shfl_sync(0xffffffffu, fs.cy3, src);
+            const int32_t fdx23 = __shfl_sync(0xffffffffu, fs.fdx23, src);
+            const int32_t fdx31 = __shfl_sync(0xffffffffu, fs.fdx31, src);
+            const int32_t fdy23 = __shfl_sync(0xffffffffu, fs.fdy23, src);
+            const int32_t fdy31 = __shfl_sync(0xffffffffu, fs.fdy31, src);
+            const float z1 = __shfl_sync(0xffffffffu, fs.z1, src);
+            const float z2 = __shfl_sync(0xffffffffu, fs.z2, src);
+            const float z3 = __shfl_sync(0xffffffffu, fs.z3, src);
+            const int32_t bxa = __shfl_sync(0xffffffffu, xa, src);
+            const int32_t bxb = __shfl_sync(0xffffffffu, xb, src);
+            const int32_t bya = __shfl_sync(0xffffffffu, ya, src);
+            const int32_t byb = __shfl_sync(0xffffffffu, yb, src);
+            const int32_t w = bxb - bxa;
+            const int32_t n = w * (byb - bya);
+            const float rw = 1.0f / (float)w;
+            for (int32_t pix = lane; pix < n; pix += 32) {
+              const int32_t r = small_div(pix, rw);
+              const int32_t x = bxa + (pix - r * w), y = bya + r;
+              const int32_t ry = y - fminy, rx = x - fminx;
+              const int32_t CX2 = wsub(wadd(cy2, wmul(ry, fdx23)), wmul(rx, fdy23));
+              const int32_t CX3 = wsub(wadd(cy3, wmul(ry, fdx31)), wmul(rx, fdy31));
+              const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+              const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+              float depth = z1;
+              depth = depth + (float)cx2 * z2;
+              depth = depth + (float)cx3 * z3;
+              const int32_t d = __float2int_rn(depth);
+              if (d < kDepthBg) atomicMin(tile + (y - y0) * cwp + (x - x0), d);
+            }
           }
         }
-      }
-      if (pass == 0) {
-        bminx = __reduce_min_sync(0xffffffffu, bminx);
-        bmaxx = __reduce_max_sync(0xffffffffu, bmaxx);
-        bminy = __reduce_min_sync(0xffffffffu, bminy);
-        bmaxy = __reduce_max_sync(0xffffffffu, bmaxy);
-        if (lane == 0) {
-          atomicMin(&pc.box[0], bminx);
-          atomicMax(&pc.box[1], bmaxx);
-          atomicMin(&pc.box[2], bminy);
-          atomicMax(&pc.box[3], bmaxy);
-          if (cull_ok) {
-            int4* mb = mbox + k * kCullCap + m;
-            mb->x = max(bminx, dx0);
-            mb->y = min(bmaxx, dx1);
-            mb->z = max(bminy, dy0);
-            mb->w = min(bmaxy, dy1);
+        if (pass == 0) {
+          bminx = __reduce_min_sync(0xffffffffu, bminx);
+          bmaxx = __reduce_max_sync(0xffffffffu, bmaxx);
+          bminy = __reduce_min_sync(0xffffffffu, bminy);
+          bmaxy = __reduce_max_sync(0xffffffffu, bmaxy);
+          if (lane == 0) {
+            atomicMin(&pc.box[0], bminx);
+            atomicMax(&pc.box[1], bmaxx);
+            atomicMin(&pc.box[2], bminy);
+            atomicMax(&pc.box[3], bmaxy);
+            if (cull_ok) {
+              int4* mb = mbox + k * kCullCap + m;
+              mb->x = max(bminx, dx0);
+              mb->y = min(bmaxx, dx1);
+              mb->z = max(bminy, dy0);
+              mb->w = min(bmaxy, dy1);
+            }
+          }
+          if (check_boxes) {
+            // the projected box must contain the meshlet's rectangle, or the
+            // later passes could skip pixels it writes
+            int32_t cx0 = INT32_MAX, cx1 = INT32_MIN, cy0 = INT32_MAX, cy1 = INT32_MIN;
+            bool ok = true;
+            if (lane < 8) {
+              const float4 blo = __ldg(I.mlet_box + 2 * m), bhi = __ldg(I.mlet_box + 2 * m + 1);
+              const float x = (lane & 1) ? bhi.x : blo.x;
+              const float y = (lane & 2) ? bhi.y : blo.y;
+              const float z = (lane & 4) ? bhi.z : blo.z;
+              float u, v, zz;
+              project(pose, x, y, z, I.cam, u, v, zz);
+              ok = zz >= 50.0f && u == u && v == v;
+              cx0 = clamp_px(floorf(u) - 1.0f, dx0, dx1);
+              cx1 = clamp_px(floorf(u) + 2.0f, dx0, dx1);
+              cy0 = clamp_px(floorf(v) - 1.0f, dy0, dy1);
+              cy1 = clamp_px(floorf(v) + 2.0f, dy0, dy1);
+            }
+            ok = __all_sync(0xffffffffu, ok);
+            cx0 = __reduce_min_sync(0xffffffffu, cx0);
+            cx1 = __reduce_max_sync(0xffffffffu, cx1);
+            cy0 = __reduce_min_sync(0xffffffffu, cy0);
+            cy1 = __reduce_max_sync(0xffffffffu, cy1);
+            const int32_t ax0 = max(bminx, dx0), ax1 = min(bmaxx, dx1);
+            const int32_t ay0 = max(bminy, dy0), ay1 = min(bmaxy, dy1);
+            if (ok && ax0 < ax1 && ay0 < ay1 && (ax0 < cx0 || ax1 > cx1 || ay0 < cy0 || ay1 > cy1))
+              violation = true;
           }
         }
+        __syncwarp();
       }
-      __syncwarp();
+      if (cull) __syncthreads();  // the list is rebuilt for the next chunk
     }
     __syncthreads();
     // 2e. scan every active particle's tile over its render AABB
@@ -801,7 +914,7 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
 // Shared memory of the fused kernels: one vertex cache per warp, ppb
 // meshlet-rectangle tables, ppb depth tiles.
 size_t fused_smem_bytes(int threads, int ppb, int tile_px) {
-  return (size_t)(threads / 32) * kMletVerts * 16 + (size_t)ppb * kCullCap * 16 +
+  return (size_t)(threads / 32) * kMletVerts * 16 + (size_t)ppb * kCullCap * 20 +
          (size_t)ppb * tile_px * 4;
 }
 
@@ -1323,6 +1436,161 @@ cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, f
   cudaError_t e = ensure_smem(score_poses_kernel, smem);
   if (e != cudaSuccess) return e;
   score_poses_kernel<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// The reference's host render of one pose (RenderCPU, main.h:2012-2043), the
+// depth image of results/<rgb>-<N>-best.csv, on the GPU: the kernels'
+// projection, then CPUfixedPointRender (main.h:1857-1991), which snaps with
+// iround(v) = (int)(v + 0.5f) and keeps depth as a float in a float buffer
+// (background 60000) written where `depth < previous`.  The minimum over
+// faces is order-free, so the buffer holds order-preserving integer keys of
+// the floats and takes atomicMin; -0 is stored as +0 and NaN is never
+// written (`NaN < x` is false).  Writes are clipped to the image.
+
+struct Pose8 {
+  float s[8];
+};
+
+__device__ __forceinline__ uint32_t depth_key(float d) {
+  const uint32_t b = __float_as_uint(d == 0.0f ? 0.0f : d);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__device__ __forceinline__ float depth_from_key(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__device__ __forceinline__ int32_t iround_ref(float v) { return __float2int_rz(v + 0.5f); }
+
+__global__ void host_render_fill_kernel(uint32_t* keys, uint32_t n) {
+  const uint32_t bg = depth_key((float)kDepthBg);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) keys[i] = bg;
+}
+
+// one warp per face: every lane sets the face up, the lanes stride over its
+// clipped rectangle
+__global__ void __launch_bounds__(256) host_render_kernel(const float* __restrict__ mesh, uint32_t F,
+                                                          Pose8 pose, Camera cam, uint32_t* keys) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (f >= F) return;  // warp-uniform
+  int32_t X[3], Y[3];
+  float Z[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    float u, v;
+    project(pose.s, __ldg(mesh + f + (size_t)j * F), __ldg(mesh + f + (size_t)(3 + j) * F),
+            __ldg(mesh + f + (size_t)(6 + j) * F), cam, u, v, Z[j]);
+    X[j] = iround_ref(16.0f * u);
+    Y[j] = iround_ref(16.0f * v);
+  }
+  FaceSetup fs;
+  setup_face_fixed(X[0], Y[0], Z[0], X[1], Y[1], Z[1], X[2], Y[2], Z[2], fs);
+  if (!fs.live) return;
+  // rectangle [minx, maxx) x [miny, maxy) (extents below 2^31: the wrapped
+  // differences are positive) clipped to the image
+  const int64_t xa = max((int64_t)fs.minx, (int64_t)0);
+  const int64_t xb = min((int64_t)fs.minx + (int64_t)(uint32_t)wsub(fs.maxx, fs.minx), (int64_t)cam.width);
+  const int64_t ya = max((int64_t)fs.miny, (int64_t)0);
+  const int64_t yb = min((int64_t)fs.miny + (int64_t)(uint32_t)wsub(fs.maxy, fs.miny), (int64_t)cam.height);
+  if (xa >= xb || ya >= yb) return;
+  const int32_t w = (int32_t)(xb - xa);
+  const int32_t n = w * (int32_t)(yb - ya);
+  for (int32_t pix = (int32_t)lane; pix < n; pix += 32) {
+    const int32_t r = pix / w;
+    const int32_t x = (int32_t)xa + (pix - r * w), y = (int32_t)ya + r;
+    const int32_t rx = wsub(x, fs.minx), ry = wsub(y, fs.miny);
+    const int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx, fs.fdy23));
+    const int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx, fs.fdy31));
+    const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+    const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+    float d = fs.z1;
+    d = d + (float)cx2 * fs.z2;
+    d = d + (float)cx3 * fs.z3;
+    if (d == d) atomicMin(keys + (size_t)y * (size_t)cam.width + (size_t)x, depth_key(d));
+  }
+}
+
+__global__ void host_render_decode_kernel(uint32_t* keys, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    keys[i] = __float_as_uint(depth_from_key(keys[i]));
+}
+
+cudaError_t launch_host_render(const float* mesh, uint32_t F, const float pose[7], const Camera& cam,
+                               float* out, cudaStream_t st) {
+  Pose8 p;
+  for (int k = 0; k < 7; ++k) p.s[k] = pose[k];
+  p.s[7] = 0.f;
+  const uint32_t n = (uint32_t)cam.width * (uint32_t)cam.height;
+  uint32_t* keys = reinterpret_cast<uint32_t*>(out);
+  host_render_fill_kernel<<<(n + 255) / 256, 256, 0, st>>>(keys, n);
+  host_render_kernel<<<(unsigned)(((uint64_t)F * 32 + 255) / 256), 256, 0, st>>>(mesh, F, p, cam, keys);
+  host_render_decode_kernel<<<(n + 255) / 256, 256, 0, st>>>(keys, n);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// Cluster records of a label map (the fields of the segmentation's
+// SegResults that the solve reads): per label the pixel count, bounding
+// rectangle and exact integer sums for the centroid of the pixels with
+// depth.  One thread per pixel, global atomics (once per frame).
+
+__global__ void label_max_kernel(const int32_t* __restrict__ labels, uint32_t n, int32_t* out) {
+  int32_t m = -1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    m = max(m, __ldg(labels + i));
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void cluster_init_kernel(ClusterAcc* acc, int32_t nlab) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nlab) return;
+  ClusterAcc a;
+  a.sum_z = a.sum_xz = a.sum_yz = 0ull;
+  a.n = a.nz = 0u;
+  a.minx = a.miny = INT32_MAX;
+  a.maxx = a.maxy = INT32_MIN;
+  acc[i] = a;
+}
+
+__global__ void cluster_stats_kernel(const uint16_t* __restrict__ depth, const int32_t* __restrict__ labels,
+                                     int32_t W, int32_t H, ClusterAcc* acc, int32_t nlab) {
+  const uint32_t n = (uint32_t)W * (uint32_t)H;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int32_t l = __ldg(labels + i);
+    if (l < 0 || l >= nlab) continue;
+    const int32_t x = (int32_t)(i % (uint32_t)W), y = (int32_t)(i / (uint32_t)W);
+    ClusterAcc& a = acc[l];
+    atomicAdd(&a.n, 1u);
+    atomicMin(&a.minx, x);
+    atomicMax(&a.maxx, x + 1);
+    atomicMin(&a.miny, y);
+    atomicMax(&a.maxy, y + 1);
+    const uint32_t z = __ldg(depth + i);
+    if (z) {
+      atomicAdd(&a.nz, 1u);
+      atomicAdd(&a.sum_z, (unsigned long long)z);
+      atomicAdd(&a.sum_xz, (unsigned long long)z * (unsigned long long)x);
+      atomicAdd(&a.sum_yz, (unsigned long long)z * (unsigned long long)y);
+    }
+  }
+}
+
+cudaError_t launch_label_max(const int32_t* labels, uint32_t n, int32_t* out, cudaStream_t st) {
+  const int32_t init = -1;
+  cudaError_t e = cudaMemcpyAsync(out, &init, 4, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  label_max_kernel<<<304, 256, 0, st>>>(labels, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cluster_stats(const uint16_t* depth, const int32_t* labels, int32_t W, int32_t H,
+                                 ClusterAcc* acc, int32_t nlab, cudaStream_t st) {
+  cluster_init_kernel<<<(nlab + 255) / 256, 256, 0, st>>>(acc, nlab);
+  cluster_stats_kernel<<<608, 256, 0, st>>>(depth, labels, W, H, acc, nlab);
   return cudaGetLastError();
 }
 

@@ -32,7 +32,8 @@ EXPORTS = [
     "qpso_get_stream", "qpso_set_profiling", "qpso_get_profile", "qpso_timer_record",
     "qpso_timer_elapsed", "qpso_scrub_l2", "qpso_score_poses_noalloc", "qpso_autotune",
     "qpso_server_start", "qpso_server_submit", "qpso_server_poll", "qpso_server_wait",
-    "qpso_server_stats_get", "qpso_server_stop",
+    "qpso_server_stats_get", "qpso_server_stop", "qpso_render_depth_f32", "qpso_frame_clusters",
+    "qpso_obj_load", "qpso_image_u16_load",
 ]
 
 
@@ -79,6 +80,12 @@ class ServerStats(C.Structure):
                 ("budget_bytes", C.c_uint64), ("epochs", C.c_uint64), ("launches", C.c_uint64)]
 
 
+class Cluster(C.Structure):
+    _fields_ = [("label", C.c_int32), ("num_points", C.c_uint32), ("min_x", C.c_int32),
+                ("max_x", C.c_int32), ("min_y", C.c_int32), ("max_y", C.c_int32),
+                ("depth_points", C.c_uint32), ("centroid_mm", C.c_float * 3)]
+
+
 class QpsoError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__("%s: %s" % (STATUS_NAMES[status] if 0 <= status < 8 else status, msg))
@@ -122,6 +129,11 @@ def load_library(path: str = LIB_PATH):
     L.qpso_score_poses.argtypes = [vp, C.POINTER(SolveDesc), C.c_void_p, C.c_uint32, C.c_void_p]
     L.qpso_render.argtypes = [vp, C.c_uint32, C.POINTER(Camera), C.c_void_p, C.c_int32,
                               C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
+    L.qpso_render_depth_f32.argtypes = [vp, C.c_uint32, C.POINTER(Camera), C.c_void_p, C.c_void_p]
+    L.qpso_frame_clusters.argtypes = [vp, C.c_uint32, C.POINTER(Cluster), C.c_uint32, C.POINTER(C.c_uint32)]
+    L.qpso_obj_load.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]
+    L.qpso_image_u16_load.argtypes = [C.c_char_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint32)]
     L.qpso_barrier_selftest.argtypes = [vp, C.c_uint64, C.POINTER(C.c_uint32)]
     L.qpso_frame_update.argtypes = [vp, C.c_uint32, C.c_void_p, C.c_void_p]
     L.qpso_host_alloc.argtypes = [C.c_uint64]
@@ -300,6 +312,24 @@ class Context:
                                        out.ctypes.data, box.ctypes.data))
         return out, box
 
+    def frame_clusters(self, fid: int) -> list:
+        """Cluster records of the frame's label map (SegResults fields)."""
+        n = C.c_uint32()
+        self._check(self.L.qpso_frame_clusters(self.h, fid, None, 0, C.byref(n)))
+        arr = (Cluster * max(1, n.value))()
+        self._check(self.L.qpso_frame_clusters(self.h, fid, arr, n.value, C.byref(n)))
+        return [{"label": c.label, "num_points": c.num_points,
+                 "aabb": (c.min_x, c.max_x, c.min_y, c.max_y), "depth_points": c.depth_points,
+                 "centroid_mm": list(c.centroid_mm)} for c in arr[:n.value]]
+
+    def render_depth_f32(self, mesh_id: int, cam: Camera, pose) -> np.ndarray:
+        """The reference's best-pose depth image (RenderCPU arithmetic)."""
+        out = np.empty((cam.height, cam.width), np.float32)
+        p = _f32(pose)
+        self._check(self.L.qpso_render_depth_f32(self.h, mesh_id, C.byref(cam), p.ctypes.data,
+                                                 out.ctypes.data))
+        return out
+
     def frame_update(self, fid: int, depth_mm: np.ndarray, labels: np.ndarray | None = None):
         self._check(self.L.qpso_frame_update(self.h, fid, depth_mm.ctypes.data,
                                              None if labels is None else labels.ctypes.data))
@@ -408,6 +438,31 @@ class PinnedArray:
             self.close()
         except Exception:
             pass
+
+
+def _status(st: int, what: str):
+    if st != OK:
+        raise QpsoError(st, what)
+
+
+def obj_load(path: str):
+    """OBJ text -> (loadOBJ3 SoA float32 array of 9*F, F).  Host only."""
+    L = load_library()
+    F = C.c_uint32()
+    _status(L.qpso_obj_load(path.encode(), None, 0, C.byref(F)), path)
+    soa = np.empty(9 * F.value, np.float32)
+    _status(L.qpso_obj_load(path.encode(), soa.ctypes.data, F.value, C.byref(F)), path)
+    return soa, F.value
+
+
+def image_u16_load(path: str) -> np.ndarray:
+    """ACCV binary depth or greyscale PNG -> uint16 (height, width).  Host only."""
+    L = load_library()
+    w, h = C.c_uint32(), C.c_uint32()
+    _status(L.qpso_image_u16_load(path.encode(), None, 0, C.byref(w), C.byref(h)), path)
+    out = np.empty((h.value, w.value), np.uint16)
+    _status(L.qpso_image_u16_load(path.encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h)), path)
+    return out
 
 
 def result_dict(r: Result) -> dict:

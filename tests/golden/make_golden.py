@@ -1,5 +1,10 @@
 """Generate the committed golden fixtures of tests/golden/.
 
+ref_pin_cpu_render.npz -- the reference's host render of a pose (RenderCPU:
+projectModelPointsToPixelsCPU + CPUfixedPointRender, main.h:1823-1991):
+the single triangles above that write at most 2000 pixels, and whole
+C1-mesh renders at four poses.
+
 ref_pin.npz -- outputs of the reference's own main.h helpers, compiled for
 the host CPU from the reference sources by oracle/build.py (ref_pin): the
 fixed-point rasteriser renderFixedPointAABB with its AABB reduction, the
@@ -138,6 +143,58 @@ def main():
     K = np.zeros(4, np.float64)
     pin.pin_intrinsics(K.ctypes.data_as(C.POINTER(C.c_double)))
 
+    # ---- the host render of the best pose (RenderCPU, main.h:1823-2043):
+    # its own rasteriser on the same triangles, then whole C1-mesh renders
+    # through its own projection (every face inside the image) ----
+    cpu_idx, cpu_val, cpu_off, cpu_sel = [], [], [0], []
+    for i, v in enumerate(tris):
+        buf = np.full(480 * 640, 60000.0, np.float32)
+        a, b, c = (np.ascontiguousarray(v[i]) for i in range(3))
+        pin.pin_cpu_raster_face(a.ctypes.data_as(f_p), b.ctypes.data_as(f_p), c.ctypes.data_as(f_p),
+                                buf.ctypes.data_as(f_p))
+        idx = np.nonzero(buf != 60000.0)[0]
+        if idx.size > 2000:  # keeps the fixture small
+            continue
+        cpu_sel.append(i)
+        cpu_idx.append(idx.astype(np.int32))
+        cpu_val.append(buf[idx])
+        cpu_off.append(cpu_off[-1] + idx.size)
+    import scene
+    w1 = scene.workload_c1()
+    soa1, F1 = w1["meshes"][0]
+    gt = np.asarray(w1["solves"][0]["gt_pose"], np.float32)
+    r_poses = [gt]
+    for _ in range(3):
+        p = gt.copy()
+        p[:3] += rng.uniform(-0.05, 0.05, 3).astype(np.float32)
+        q = rng.normal(size=4)
+        p[3:] = (q / np.linalg.norm(q) * np.sign(q[0])).astype(np.float32)
+        r_poses.append(p)
+    r_idx, r_val, r_off = [], [], [0]
+    for pose in r_poses:
+        buf = np.full(480 * 640, 60000.0, np.float32)
+        for f in range(F1):
+            uvz = []
+            for j in range(3):
+                vtx = np.array([soa1[f + j * F1], soa1[3 * F1 + f + j * F1], soa1[6 * F1 + f + j * F1]],
+                               np.float32)
+                o = np.zeros(3, np.float32)
+                pin.pin_project_cpu(pose.ctypes.data_as(f_p), vtx.ctypes.data_as(f_p), o.ctypes.data_as(f_p))
+                assert 2.0 < o[0] < 636.0 and 2.0 < o[1] < 476.0
+                uvz.append(o)
+            pin.pin_cpu_raster_face(uvz[0].ctypes.data_as(f_p), uvz[1].ctypes.data_as(f_p),
+                                    uvz[2].ctypes.data_as(f_p), buf.ctypes.data_as(f_p))
+        idx = np.nonzero(buf != 60000.0)[0]
+        r_idx.append(idx.astype(np.int32))
+        r_val.append(buf[idx])
+        r_off.append(r_off[-1] + idx.size)
+    np.savez_compressed(
+        os.path.join(HERE, "ref_pin_cpu_render.npz"), tri_sel=np.array(cpu_sel, np.int32),
+        tri_idx=np.concatenate(cpu_idx),
+        tri_val=np.concatenate(cpu_val), tri_off=np.array(cpu_off, np.int64), poses=np.stack(r_poses),
+        render_idx=np.concatenate(r_idx), render_val=np.concatenate(r_val),
+        render_off=np.array(r_off, np.int64))
+
     np.savez_compressed(
         os.path.join(HERE, "ref_pin.npz"), tris=tris, boxes=np.array(boxes, np.int32),
         raster_depth=raster_depth, raster_off=np.array(offs, np.int64), S=S, Q=Q, V=Vv, W=Wv,
@@ -145,7 +202,6 @@ def main():
         proj=proj, proj_pose=proj_pose, proj_pt=proj_pt, intrinsics=K)
 
     # ---- oracle C1 solve, frozen ----
-    import scene
     w = scene.workload_c1()
     soa, F = w["meshes"][0]
     depth, labels, _ = w["frames"][0]

@@ -1,6 +1,7 @@
 // Checks the meshlet partition (q-pso_gb300/csrc/meshlets.h) of a mesh read
 // from a binary file of 9*F floats (loadOBJ3 layout): every face exactly
-// once, caps respected, local ids inside the meshlet, positions preserved.
+// once, caps respected, local ids inside the meshlet, positions preserved,
+// each meshlet's box the exact bounds of its vertices.
 // Prints "faces meshlets unique_vertex_slots".
 #include <cstdio>
 #include <cstdlib>
@@ -20,7 +21,9 @@ int main(int argc, char** argv) {
   const uint32_t F = (uint32_t)(soa.size() / 9);
   std::vector<qpso::MeshletHdr> hdr;
   std::vector<unsigned char> blob;
-  qpso::build_meshlets(soa.data(), F, hdr, blob);
+  size_t box_off = 0;
+  qpso::build_meshlets(soa.data(), F, hdr, blob, &box_off);
+  if (box_off % 16 != 0 || blob.size() != box_off + 32 * hdr.size()) return 7;
   // multiset of faces as (x,y,z) x 3 -> compare counts by summing a hash
   uint64_t want = 0, got = 0, slots = 0, faces = 0;
   auto fh = [](const float* a, const float* b, const float* c) {
@@ -52,6 +55,16 @@ int main(int argc, char** argv) {
       const uint32_t a = pf[i] & 1023u, b = (pf[i] >> 10) & 1023u, c = (pf[i] >> 20) & 1023u;
       if (a >= h.nv || b >= h.nv || c >= h.nv) return 5;
       got += fh(pv + 4 * a, pv + 4 * b, pv + 4 * c);
+    }
+    const float* bx = reinterpret_cast<const float*>(blob.data() + box_off) + 8 * (&h - hdr.data());
+    for (int c = 0; c < 3; ++c) {
+      bool lo_hit = false, hi_hit = false;
+      for (int v = 0; v < h.nv; ++v) {
+        if (pv[4 * v + c] < bx[c] || pv[4 * v + c] > bx[4 + c]) return 8;
+        lo_hit |= pv[4 * v + c] == bx[c];
+        hi_hit |= pv[4 * v + c] == bx[4 + c];
+      }
+      if (!lo_hit || !hi_hit) return 8;
     }
     slots += h.nv;
     faces += h.nf;

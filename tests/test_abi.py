@@ -57,6 +57,8 @@ int main(void) {
          offsetof(qpso_solve_desc, t_hi), offsetof(qpso_solve_desc, w), offsetof(qpso_solve_desc, qinit),
          offsetof(qpso_solve_desc, seed), offsetof(qpso_solve_desc, stream));
   printf("%zu %zu\n", offsetof(qpso_result, raster_writes), offsetof(qpso_result, tile_passes));
+  printf("%zu %zu %zu\n", sizeof(qpso_cluster), offsetof(qpso_cluster, depth_points),
+         offsetof(qpso_cluster, centroid_mm));
   return 0;
 }
 ''')
@@ -70,6 +72,8 @@ int main(void) {
     assert got[1] == [D.num_points.offset, D.t_hi.offset, D.w.offset, D.qinit.offset,
                       D.seed.offset, D.stream.offset]
     assert got[2] == [qpso.Result.raster_writes.offset, qpso.Result.tile_passes.offset]
+    K = qpso.Cluster
+    assert got[3] == [C.sizeof(K), K.depth_points.offset, K.centroid_mm.offset]
 
 
 def test_host_only_entry_points(lib):

@@ -1,0 +1,95 @@
+"""The command-line drop-in end to end on the GPU: OBJ model, ACCV binary
+and PNG depth, a PNG label map in place of the segmentation, and the two
+result files the reference writes (main.cu:1752-1762):
+results/<rgb>-<N>-bestpose.csv equals the library's solve of the same
+cluster printed as the reference prints it, and results/<rgb>-<N>-best.csv
+equals the oracle's restatement of the reference's host render of that pose.
+The cluster records equal the label map's own pixel statistics."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import qpso
+import scene
+from oracle import pyoracle as po
+from tests.test_ingest import CLI, write_accv, write_obj, write_png_gray
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def files(tmp_path_factory):
+    d = tmp_path_factory.mktemp("cli")
+    w = scene.workload_c2(frames=1, particles=32, iterations=6)
+    depth, labels, _ = w["frames"][0]
+    s = w["solves"][3]
+    soa, F = w["meshes"][s["mesh"]]
+    obj = str(d / "model.obj")
+    write_obj(obj, soa, F)
+    write_accv(str(d / "depth.bin"), depth)
+    write_png_gray(str(d / "depth.png"), depth, 16, 6, (0, 1, 2, 3, 4))
+    write_png_gray(str(d / "labels.png"), (labels + 1).astype(np.uint16), 16, 9, (4,))
+    return d, w, s, obj
+
+
+def run_cli(d, obj, depth_name, k, extra=()):
+    cmd = [CLI, obj, "img_0042.png", str(d / depth_name), str(k), "--labels", str(d / "labels.png"),
+           "--camera", "525,525,319.5,239.5", "--particles", "32", "--iterations", "6", "--seed", "7",
+           "--results", str(d / "results"), *extra]
+    return subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+
+
+def test_cluster_records_match_label_map(gpu_ctx, files):
+    d, w, s, _ = files
+    depth, labels, _ = w["frames"][0]
+    cam = qpso.Camera(*scene.camera_tuple())
+    fid = gpu_ctx.frame_upload(depth, cam, labels=labels)
+    got = gpu_ctx.frame_clusters(fid)
+    want = [scene.cluster_info(depth, labels, k) for k in range(int(labels.max()) + 1)]
+    want = [x for x in want if x is not None]
+    assert [g["label"] for g in got] == [x["label"] for x in want]
+    for g, x in zip(got, want):
+        assert g["num_points"] == x["num_points"] and tuple(g["aabb"]) == tuple(x["aabb"])
+        np.testing.assert_allclose(g["centroid_mm"], x["centroid_mm"], rtol=1e-5, atol=1e-3)
+    gpu_ctx.frame_release(fid)
+
+
+@pytest.mark.parametrize("depth_name", ["depth.bin", "depth.png"])
+def test_cli_outputs_equal_library_and_oracle(gpu_ctx, files, depth_name):
+    d, w, s, obj = files
+    k = s["cluster"]["label"]
+    r = run_cli(d, obj, depth_name, k)
+    assert r.returncode == 0, r.stderr
+    assert "Solution Best Pose:" in r.stdout
+
+    # the same solve through the library
+    soa, F = qpso.obj_load(obj)
+    depth, labels, _ = w["frames"][0]
+    cam = qpso.Camera(*scene.camera_tuple())
+    mid = gpu_ctx.mesh_upload(soa, F)
+    fid = gpu_ctx.frame_upload(depth, cam, labels=labels)
+    c = [x for x in gpu_ctx.frame_clusters(fid) if x["label"] == k][0]
+    lo, hi = qpso.box_from_centroid(c["centroid_mm"])
+    x0, x1, y0, y1 = c["aabb"]
+    desc = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=k, cl_min_x=x0, cl_max_x=x1,
+                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"], t_lo=lo, t_hi=hi,
+                           num_particles=32, iterations=6, seed=7, stream=0)
+    res = gpu_ctx.solve(desc)
+    stem = d / "results" / ("img_0042.png-%d" % k)
+    want = "%f,%f,%f,%f,%f,%f,%f,%f" % (res.fit, *res.pose)
+    assert (str(stem) + "-bestpose.csv") and open(str(stem) + "-bestpose.csv").read() == want
+
+    img = po.render_cpu(soa, F, np.array(res.pose[:], np.float32), po.camera())
+    text = "".join(", ".join("%g" % float(v) for v in row) + "\n" for row in img)
+    assert open(str(stem) + "-best.csv").read() == text
+    assert (img < 60000).sum() > 100
+    gpu_ctx.frame_release(fid)
+    gpu_ctx.mesh_release(mid)
+
+
+def test_cli_unknown_cluster(files):
+    d, w, s, obj = files
+    r = run_cli(d, obj, "depth.bin", 999)
+    assert r.returncode == 1 and "not in the label map" in r.stderr

@@ -59,6 +59,32 @@ def test_render_tiles_bit_exact(gpu_ctx, c1_gpu):
         np.testing.assert_array_equal(tile, want)
 
 
+def test_best_pose_depth_image_bit_exact(gpu_ctx, c1_gpu):
+    """The best-pose depth image (RenderCPU arithmetic: iround snapping,
+    float depth) equals the oracle's restatement, pinned against the
+    reference's own host render, for in-view, partly off-image and
+    near-camera poses of the C1 mesh and of a 12-face box."""
+    w, mids, _ = c1_gpu
+    soa, F = w["meshes"][0]
+    s = w["solves"][0]
+    rng = np.random.default_rng(12)
+    cam_o, cam_g = po.camera(), gpu_camera()
+    poses = [s["gt_pose"]] + list(random_poses(rng, s, 6, 0.6))
+    edge = np.array(s["gt_pose"], np.float32).copy()
+    edge[0] += 0.2  # partly right of the image
+    near = np.array(s["gt_pose"], np.float32).copy()
+    near[:3] = [0.0, 0.0, 0.1]  # object filling most of the frame
+    poses += [edge, near]
+    box_soa, box_F = scene.make_mesh("box", 12, 80.0, seed=1)
+    box_id = gpu_ctx.mesh_upload(box_soa, box_F)
+    for mesh, nf, mid in [(soa, F, mids[0]), (box_soa, box_F, box_id)]:
+        for pose in poses:
+            want = po.render_cpu(mesh, nf, pose, cam_o)
+            got = gpu_ctx.render_depth_f32(mid, cam_g, pose)
+            np.testing.assert_array_equal(got, want)
+    assert (po.render_cpu(soa, F, near, cam_o) < 60000).mean() > 0.2
+
+
 def _oracle_scores(w, s, poses, **over):
     soa, F = w["meshes"][s["mesh"]]
     prm = oracle_params(s, **over)
@@ -147,6 +173,43 @@ def test_low_poly_meshes_large_faces(gpu_ctx, c1_gpu, kind, n, extent):
     rb = gpu_ctx.solve_batch([gpu_desc(s2, mid, fids[0])])[0]
     assert rb.fit == want["fit"]
     gpu_ctx.mesh_release(mid)
+
+
+def test_stress_mesh_full_frame_window(gpu_ctx):
+    """The stress configuration's sizes: the 327,680-face level-7 icosphere
+    (2,560+ meshlets, so passes after the first cull meshlets by their
+    projected object-space boxes) and a full 640x480 fitness window.  Fitness
+    of several poses (near the ground truth and spread over the box) and a
+    short solve's trace equal the oracle's, with one pass per render and with
+    many tile passes."""
+    w = scene.workload_c5(particles=8, iterations=3)
+    mids, fids = upload_workload(gpu_ctx, w)
+    s = w["solves"][0]
+    soa, F = w["meshes"][0]
+    d = gpu_desc(s, mids[0], fids[0])
+    rng = np.random.default_rng(8)
+    poses = np.concatenate([s["gt_pose"][None], random_poses(rng, s, 5, 0.5)])
+    scores, _ = _oracle_scores(w, s, poses)
+    want = np.array([sc.fit for sc in scores], np.float32)
+    assert scores[0].n_rendered > 0
+    trace = po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s), trace=True)
+    old = gpu_ctx.get_launch_config()
+    try:
+        for cfg in [(256, 49152, 1), (256, 2048, 1), (128, 4096, 2)]:
+            gpu_ctx.set_launch_config(plain=cfg, batch=cfg)
+            np.testing.assert_array_equal(gpu_ctx.score_poses(d, poses), want)
+            r, st = gpu_ctx.solve_traced(d)
+            assert r.flags == 0
+            np.testing.assert_array_equal(st["trace_gbest"], trace["trace_gbest"])
+            rb = gpu_ctx.solve_batch([d])[0]
+            assert rb.flags == 0 and rb.fit == r.fit and list(rb.pose) == list(r.pose)
+            if cfg[1] == 2048:
+                assert r.tile_passes > 4 * s["particles"] * s["iterations"]
+    finally:
+        gpu_ctx.set_launch_config(plain=old[0], batch=old[1])
+    # the reported best fitness is the fitness of the reported pose
+    again = gpu_ctx.score_poses(d, np.array(r.pose[:], np.float32)[None])
+    assert again[0] == r.fit
 
 
 def test_small_tiles_force_multipass(gpu_ctx, c1_gpu):

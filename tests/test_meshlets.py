@@ -1,6 +1,7 @@
 """The meshlet partition built at mesh upload keeps every face exactly once,
-respects its caps (256 faces, 256 unique vertices), and shares vertices (the
-fused kernels transform each meshlet vertex once per pose)."""
+respects its caps (128 faces, 128 unique vertices), shares vertices (the
+fused kernels transform each meshlet vertex once per pose) and stores each
+meshlet's exact object-space box."""
 import os
 import subprocess
 

@@ -83,6 +83,43 @@ def test_raster_fixture_covers_edge_cases(ref):
     assert (sizes > 100).sum() >= 20
 
 
+def test_host_render_raster_matches_reference(ref):
+    """CPUfixedPointRender (main.h:1857-1991), the rasteriser of the
+    reference's best-pose CSV, compiled from the reference: iround snapping
+    and float depth differ from the kernel rasteriser; every written pixel
+    and value is bit-exact."""
+    g = np.load(os.path.join(G, "ref_pin_cpu_render.npz"))
+    cam = po.camera()
+    tris, sel, idx, val, off = ref["tris"], g["tri_sel"], g["tri_idx"], g["tri_val"], g["tri_off"]
+    assert len(sel) >= 250
+    assert (val != np.round(val)).mean() > 0.5  # depth is kept as a float
+    for j, i in enumerate(sel):
+        buf = np.full((480, 640), 60000.0, np.float32)
+        po.raster_face_cpu(tris[i][0], tris[i][1], tris[i][2], cam, buf)
+        want = np.full(480 * 640, 60000.0, np.float32)
+        want[idx[off[j]:off[j + 1]]] = val[off[j]:off[j + 1]]
+        np.testing.assert_array_equal(buf.ravel(), want, err_msg="triangle %d" % i)
+
+
+def test_host_render_of_mesh_matches_reference():
+    """RenderCPU (main.h:2012-2043) of the C1 mesh at four poses through the
+    reference's own projection and rasteriser: bit-exact."""
+    import scene
+    g = np.load(os.path.join(G, "ref_pin_cpu_render.npz"))
+    w = scene.workload_c1()
+    soa, F = w["meshes"][0]
+    K = np.load(os.path.join(G, "ref_pin.npz"))["intrinsics"]  # the reference's compiled-in camera
+    cam = po.camera(fx=float(np.float32(K[0])), fy=float(np.float32(K[1])), cx=float(np.float32(K[2])),
+                    cy=float(np.float32(K[3])))
+    idx, val, off = g["render_idx"], g["render_val"], g["render_off"]
+    for j, pose in enumerate(g["poses"]):
+        got = po.render_cpu(soa, F, pose, cam)
+        want = np.full(480 * 640, 60000.0, np.float32)
+        want[idx[off[j]:off[j + 1]]] = val[off[j]:off[j + 1]]
+        assert off[j + 1] - off[j] > 500
+        np.testing.assert_array_equal(got.ravel(), want, err_msg="pose %d" % j)
+
+
 def _f(a):
     return np.ascontiguousarray(a, np.float32)
 
