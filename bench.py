@@ -104,6 +104,16 @@ class ClockSampler:
                                           "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # nvidia-smi's start-up competes with the launching thread for the
+        # host and the driver: begin timing once it is sampling
+        t0 = time.time()
+        while time.time() - t0 < 5.0 and self.proc.poll() is None:
+            self.f.flush()
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.05)
+        time.sleep(0.3)
 
     def stop(self):
         if not self.proc:
@@ -342,10 +352,14 @@ def run_ours(args, ws, rank, local):
     sampler = ClockSampler(local)
     d.barrier()
     sampler.start()
-    ms_main, prof = timed(main_fn, args.steps, prof=True)
+    ms_main, _ = timed(main_fn, args.steps)
     clocks = sampler.stop()
     ms_main = d.max(ms_main)
     d.barrier()
+    # the same steps again with events around every kernel launch, for the
+    # roofline's per-launch kernel time (the events themselves slow the
+    # step by a few per cent, so the headline is timed without them)
+    _, prof = timed(main_fn, args.steps, prof=True)
     ms_e2e, _ = timed(main_fn, args.steps, e2e=True)
     ms_e2e = d.max(ms_e2e)
     alt_steps = max(1, args.steps if not batched_default else min(args.steps, 2))
@@ -475,7 +489,7 @@ def run_serving(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])

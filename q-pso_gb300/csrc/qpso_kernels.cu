@@ -118,7 +118,6 @@ struct SmemCtl {
   float argv[kMaxThreads / 32];
   uint32_t argi[kMaxThreads / 32];
   PartCtl part[kMaxPpb];
-  float corner[kMaxPpb][8][3];
 };
 
 // Conservative pixel bound of every face's raster rectangle at pose s: the
@@ -451,42 +450,57 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
   int4* vcache = sm.vcache;
   int4* mbox = sm.mbox;
 
-  // 1. conservative bounds: one thread per (particle, mesh-AABB corner)
-  if (tid < np * 8) {
-    const int k = tid >> 3, c = tid & 7;
-    const float x = (c & 1) ? I.mesh_hi[0] : I.mesh_lo[0];
-    const float y = (c & 2) ? I.mesh_hi[1] : I.mesh_lo[1];
-    const float z = (c & 4) ? I.mesh_hi[2] : I.mesh_lo[2];
-    float u, v, zz;
-    project(ctl.pose[k], x, y, z, I.cam, u, v, zz);
-    ctl.corner[k][c][0] = u;
-    ctl.corner[k][c][1] = v;
-    ctl.corner[k][c][2] = (zz >= 50.0f && u == u && v == v) ? 1.f : 0.f;
+  // 1. conservative bound of every particle: the union of its meshlets'
+  //    projected object-space boxes (box_rect; a box with a corner closer
+  //    than 50 mm bounds nothing and stands for the whole domain), far
+  //    tighter than the projected box of the whole mesh.  Whole warps take
+  //    32 meshlets of one particle; one shared atomic per warp and side.
+  if (tid < np) {
+    PartCtl& pc = ctl.part[tid];
+    pc.bound[0] = dx1;
+    pc.bound[1] = dx0;
+    pc.bound[2] = dy1;
+    pc.bound[3] = dy0;
   }
   if (cull_ok)
     for (int i = tid; i < np * (int)nm; i += T)
       mbox[(i / nm) * kCullCap + (i % nm)] = make_int4(kAabbInitMin, kAabbInitMax, kAabbInitMin, kAabbInitMax);
   __syncthreads();
+  for (int k = 0; k < np; ++k) {
+    PartCtl& pc = ctl.part[k];
+    for (uint32_t b = (uint32_t)(tid & ~31); b < nm; b += (uint32_t)T) {  // whole warps
+      const uint32_t m = b + (uint32_t)lane;
+      int32_t rx0 = INT32_MAX, rx1 = INT32_MIN, ry0 = INT32_MAX, ry1 = INT32_MIN;
+      if (m < nm) {
+        int4 r;
+        if (!box_rect(ctl.pose[k], I.cam, __ldg(I.mlet_box + 2 * m), __ldg(I.mlet_box + 2 * m + 1), dx0, dx1,
+                      dy0, dy1, r))
+          r = make_int4(dx0, dx1, dy0, dy1);
+        if (r.x < r.y && r.z < r.w) {
+          rx0 = r.x;
+          rx1 = r.y;
+          ry0 = r.z;
+          ry1 = r.w;
+        }
+      }
+      rx0 = __reduce_min_sync(0xffffffffu, rx0);
+      rx1 = __reduce_max_sync(0xffffffffu, rx1);
+      ry0 = __reduce_min_sync(0xffffffffu, ry0);
+      ry1 = __reduce_max_sync(0xffffffffu, ry1);
+      if (lane == 0 && rx0 < rx1) {
+        atomicMin(&pc.bound[0], rx0);
+        atomicMax(&pc.bound[1], rx1);
+        atomicMin(&pc.bound[2], ry0);
+        atomicMax(&pc.bound[3], ry1);
+      }
+    }
+  }
+  __syncthreads();
   if (tid < np) {
     PartCtl& pc = ctl.part[tid];
-    float ulo = 3.0e38f, uhi = -3.0e38f, vlo = 3.0e38f, vhi = -3.0e38f;
-    bool ok = true;
-    for (int c = 0; c < 8; ++c) {
-      ok = ok && ctl.corner[tid][c][2] != 0.f;
-      ulo = fminf(ulo, ctl.corner[tid][c][0]);
-      uhi = fmaxf(uhi, ctl.corner[tid][c][0]);
-      vlo = fminf(vlo, ctl.corner[tid][c][1]);
-      vhi = fmaxf(vhi, ctl.corner[tid][c][1]);
-    }
-    if (!ok) {
-      pc.bound[0] = dx0; pc.bound[1] = dx1; pc.bound[2] = dy0; pc.bound[3] = dy1;
-    } else {
-      pc.bound[0] = (int32_t)fmaxf(floorf(ulo) - 1.0f, (float)dx0);
-      pc.bound[1] = (int32_t)fminf(floorf(uhi) + 2.0f, (float)dx1);
-      pc.bound[2] = (int32_t)fmaxf(floorf(vlo) - 1.0f, (float)dy0);
-      pc.bound[3] = (int32_t)fminf(floorf(vhi) + 2.0f, (float)dy1);
-      if (pc.bound[1] < pc.bound[0]) pc.bound[1] = pc.bound[0];
-      if (pc.bound[3] < pc.bound[2]) pc.bound[3] = pc.bound[2];
+    if (pc.bound[1] <= pc.bound[0] || pc.bound[3] <= pc.bound[2]) {  // nothing inside the domain
+      pc.bound[0] = pc.bound[1] = dx1;
+      pc.bound[2] = pc.bound[3] = dy1;
     }
     plan_tiles(pc, tile_px);
     pc.box[0] = kAabbInitMin;
