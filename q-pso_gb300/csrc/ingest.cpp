@@ -19,7 +19,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/qpso.h"
+#include "qpso.h"
 
 namespace {
 

@@ -112,6 +112,7 @@ struct SmemCtl {
   int32_t bound[4];
   uint32_t claim;
   uint32_t n_live;     // listed items of the current pass and meshlet chunk
+  uint32_t next_item;  // items claimed so far beyond each warp's first
   int last;
   int maxpass;
   Partial warp[kMaxThreads / 32];
@@ -453,8 +454,8 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
   // 1. conservative bound of every particle: the union of its meshlets'
   //    projected object-space boxes (box_rect; a box with a corner closer
   //    than 50 mm bounds nothing and stands for the whole domain), far
-  //    tighter than the projected box of the whole mesh.  Whole warps take
-  //    32 meshlets of one particle; one shared atomic per warp and side.
+  //    tighter than the projected box of the whole mesh.  Eight lanes
+  //    project one box's corners; one shared atomic per warp and side.
   if (tid < np) {
     PartCtl& pc = ctl.part[tid];
     pc.bound[0] = dx1;
@@ -468,14 +469,35 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
   __syncthreads();
   for (int k = 0; k < np; ++k) {
     PartCtl& pc = ctl.part[k];
-    for (uint32_t b = (uint32_t)(tid & ~31); b < nm; b += (uint32_t)T) {  // whole warps
-      const uint32_t m = b + (uint32_t)lane;
+    const uint32_t n8 = nm * 8u;
+    for (uint32_t b = (uint32_t)(tid & ~31); b < n8; b += (uint32_t)T) {  // whole warps
+      // lanes 8j..8j+7 project the corners of one meshlet's box
+      const uint32_t i = b + (uint32_t)lane, m = i >> 3, c = i & 7u;
+      float u = 0.f, v = 0.f;
+      bool ok = true;
+      if (m < nm) {
+        const float4 blo = __ldg(I.mlet_box + 2 * m), bhi = __ldg(I.mlet_box + 2 * m + 1);
+        float zz;
+        project(ctl.pose[k], (c & 1u) ? bhi.x : blo.x, (c & 2u) ? bhi.y : blo.y, (c & 4u) ? bhi.z : blo.z, I.cam,
+                u, v, zz);
+        ok = zz >= 50.0f && u == u && v == v;
+      }
+      float ulo = u, uhi = u, vlo = v, vhi = v;
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        ulo = fminf(ulo, __shfl_xor_sync(0xffffffffu, ulo, o));
+        uhi = fmaxf(uhi, __shfl_xor_sync(0xffffffffu, uhi, o));
+        vlo = fminf(vlo, __shfl_xor_sync(0xffffffffu, vlo, o));
+        vhi = fmaxf(vhi, __shfl_xor_sync(0xffffffffu, vhi, o));
+      }
+      ok = ((__ballot_sync(0xffffffffu, !ok) >> (lane & ~7)) & 0xffu) == 0u;
       int32_t rx0 = INT32_MAX, rx1 = INT32_MIN, ry0 = INT32_MAX, ry1 = INT32_MIN;
       if (m < nm) {
-        int4 r;
-        if (!box_rect(ctl.pose[k], I.cam, __ldg(I.mlet_box + 2 * m), __ldg(I.mlet_box + 2 * m + 1), dx0, dx1,
-                      dy0, dy1, r))
-          r = make_int4(dx0, dx1, dy0, dy1);
+        // the rectangle of box_rect(); a box that bounds nothing stands for
+        // the whole domain
+        const int4 r = ok ? make_int4(clamp_px(floorf(ulo) - 1.0f, dx0, dx1), clamp_px(floorf(uhi) + 2.0f, dx0, dx1),
+                                      clamp_px(floorf(vlo) - 1.0f, dy0, dy1), clamp_px(floorf(vhi) + 2.0f, dy0, dy1))
+                          : make_int4(dx0, dx1, dy0, dy1);
         if (r.x < r.y && r.z < r.w) {
           rx0 = r.x;
           rx1 = r.y;
@@ -523,6 +545,7 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
 
   for (int pass = 0; pass < maxpass; ++pass) {
     // 2a. band of every particle still active in this pass
+    if (tid == 0) ctl.next_item = (uint32_t)nw;
     if (tid < np) {
       PartCtl& pc = ctl.part[tid];
       pc.x0 = pc.y0 = pc.cwp = pc.thp = 0;
@@ -559,7 +582,10 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
       if (cull) {
         const uint32_t nmc = min((uint32_t)kCullCap, nm - mc);
         const uint32_t nt = (uint32_t)np * nmc;
-        if (tid == 0) ctl.n_live = 0;
+        if (tid == 0) {
+          ctl.n_live = 0;
+          ctl.next_item = (uint32_t)nw;
+        }
         __syncthreads();
         for (uint32_t b = (uint32_t)(tid & ~31); b < nt; b += (uint32_t)T) {  // whole warps
           const uint32_t i = b + (uint32_t)lane;
@@ -589,7 +615,11 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
         __syncthreads();
         n_items = ctl.n_live;
       }
-      for (uint32_t item = wid; item < n_items; item += nw) {
+      // a warp's first item is its index, later ones come from a shared
+      // counter: items differ in cost (back-facing meshlets raster nothing)
+      // and the barrier after the items waits for the slowest warp
+      for (uint32_t item = wid; item < n_items;
+           item = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(&ctl.next_item, 1u) : 0u, 0)) {
         int k;
         uint32_t m;
         if (cull) {
@@ -785,38 +815,52 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
         const int32_t* tile = tiles + (size_t)k * tile_px;
         const uint16_t* __restrict__ obs = I.obs;
         const bool vec_obs = (W & 3) == 0;
-        for (int32_t gi = tid; gi < ng; gi += T) {
-          const int32_t r = small_div(gi, rg);
-          const int32_t x = gx0 + ((gi - r * gpr) << 2);
-          const int32_t y = sy0 + r;
-          const int4 zz = *reinterpret_cast<const int4*>(tile + (y - y0) * cwp + (x - x0));
-          if (zz.x >= kDepthBg && zz.y >= kDepthBg && zz.z >= kDepthBg && zz.w >= kDepthBg) continue;
-          uint32_t kk[4] = {0u, 0u, 0u, 0u};
-          if (y >= 0 && y < H) {
-            const uint16_t* orow = obs + (size_t)y * (size_t)W;
-            if (vec_obs && x >= 0 && x + 3 < W) {
-              const uint2 qo = __ldg(reinterpret_cast<const uint2*>(orow + x));
-              kk[0] = qo.x & 0xffffu;
-              kk[1] = qo.x >> 16;
-              kk[2] = qo.y & 0xffffu;
-              kk[3] = qo.y >> 16;
-            } else {
+        // two groups of four pixels per iteration: both groups' loads are in
+        // flight before either is counted
+        for (int32_t g0 = tid; g0 < ng; g0 += 2 * T) {
+          int4 zz[2];
+          uint32_t kk[2][4];
 #pragma unroll
-              for (int e = 0; e < 4; ++e)
-                if (x + e >= 0 && x + e < W) kk[e] = __ldg(orow + x + e);
+          for (int j = 0; j < 2; ++j) {
+            const int32_t gi = g0 + j * T;
+            zz[j] = make_int4(kDepthBg, kDepthBg, kDepthBg, kDepthBg);
+            kk[j][0] = kk[j][1] = kk[j][2] = kk[j][3] = 0u;
+            if (gi < ng) {
+              const int32_t r = small_div(gi, rg);
+              const int32_t x = gx0 + ((gi - r * gpr) << 2);
+              const int32_t y = sy0 + r;
+              zz[j] = *reinterpret_cast<const int4*>(tile + (y - y0) * cwp + (x - x0));
+              const bool any = zz[j].x < kDepthBg || zz[j].y < kDepthBg || zz[j].z < kDepthBg || zz[j].w < kDepthBg;
+              if (any && y >= 0 && y < H) {
+                const uint16_t* orow = obs + (size_t)y * (size_t)W;
+                if (vec_obs && x >= 0 && x + 3 < W) {
+                  const uint2 qo = __ldg(reinterpret_cast<const uint2*>(orow + x));
+                  kk[j][0] = qo.x & 0xffffu;
+                  kk[j][1] = qo.x >> 16;
+                  kk[j][2] = qo.y & 0xffffu;
+                  kk[j][3] = qo.y >> 16;
+                } else {
+#pragma unroll
+                  for (int e = 0; e < 4; ++e)
+                    if (x + e >= 0 && x + e < W) kk[j][e] = __ldg(orow + x + e);
+                }
+              }
             }
           }
-          const int32_t zr[4] = {zz.x, zz.y, zz.z, zz.w};
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            if (zr[e] < kDepthBg) {
-              acc.nR += 1;
-              if (kk[e] == 0u) {
-                acc.nNo += 1;
-              } else {
-                const int64_t d64 = wsub(zr[e], (int32_t)kk[e]);
-                add128(acc.lo, acc.hi, (uint64_t)(d64 * d64));
-                acc.nSegR += 1;
+          for (int j = 0; j < 2; ++j) {
+            const int32_t zr[4] = {zz[j].x, zz[j].y, zz[j].z, zz[j].w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              if (zr[e] < kDepthBg) {
+                acc.nR += 1;
+                if (kk[j][e] == 0u) {
+                  acc.nNo += 1;
+                } else {
+                  const int64_t d64 = wsub(zr[e], (int32_t)kk[j][e]);
+                  add128(acc.lo, acc.hi, (uint64_t)(d64 * d64));
+                  acc.nSegR += 1;
+                }
               }
             }
           }
@@ -840,13 +884,31 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
         ctl.warp[wid].hi = acc.hi;
       }
       __syncthreads();
-      if (tid == 0) {
-        for (int i = 0; i < nw; ++i) {
-          pc.nR += ctl.warp[i].nR;
-          pc.nNo += ctl.warp[i].nNo;
-          pc.nSegR += ctl.warp[i].nSegR;
-          pc.hi += ctl.warp[i].hi;
-          add128(pc.lo, pc.hi, ctl.warp[i].lo);
+      if (wid == 0) {  // the warps' partial sums, reduced by warp 0
+        BlockSums t = {0u, 0u, 0u, 0, 0};
+        if (lane < nw) {
+          t.nR = ctl.warp[lane].nR;
+          t.nNo = ctl.warp[lane].nNo;
+          t.nSegR = ctl.warp[lane].nSegR;
+          t.lo = ctl.warp[lane].lo;
+          t.hi = ctl.warp[lane].hi;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          t.nR += __shfl_xor_sync(0xffffffffu, t.nR, o);
+          t.nNo += __shfl_xor_sync(0xffffffffu, t.nNo, o);
+          t.nSegR += __shfl_xor_sync(0xffffffffu, t.nSegR, o);
+          const uint64_t lo = __shfl_xor_sync(0xffffffffu, t.lo, o);
+          const uint64_t hi = __shfl_xor_sync(0xffffffffu, t.hi, o);
+          t.hi += hi;
+          add128(t.lo, t.hi, lo);
+        }
+        if (lane == 0) {
+          pc.nR += t.nR;
+          pc.nNo += t.nNo;
+          pc.nSegR += t.nSegR;
+          pc.hi += t.hi;
+          add128(pc.lo, pc.hi, t.lo);
         }
       }
       __syncthreads();
