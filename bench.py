@@ -180,10 +180,11 @@ def algorithmic_bytes(w) -> tuple[float, float]:
     return tot, n
 
 
-def traffic_per_launch(workload: str):
+def traffic_per_launch(workload: str, kernel: str = "step"):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/step_kernel_<workload>.md, line 'dram_bytes_per_launch:')."""
-    p = os.path.join(ROOT, "profiles", "step_kernel_%s.md" % workload)
+    summary (profiles/<kernel>_kernel_<workload>.md, line
+    'dram_bytes_per_launch:')."""
+    p = os.path.join(ROOT, "profiles", "%s_kernel_%s.md" % (kernel, workload))
     try:
         for line in open(p):
             if line.strip().startswith("dram_bytes_per_launch:"):
@@ -411,7 +412,7 @@ def run_ours(args, ws, rank, local):
         "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm if achieved else None,
                      "peak_source": peak_kind,
-                     "traffic": traffic_per_launch(args.workload),
+                     "traffic": traffic_per_launch(args.workload, "batch" if batched_default else "step"),
                      "bytes_per_launch": bytes_launch, "avg_launch_ms": kern_ms,
                      "model": "36F + 2A + 96 bytes per particle-render"},
         "clocks": clocks,
