@@ -268,7 +268,10 @@ qpso_status qpso_image_u16_load(const char *path, uint16_t *out, uint64_t capaci
  * request by one iteration at its own iteration number, up to
  * iters_per_epoch times; finished requests leave and queued ones join
  * between epochs.  Meshes and frames are the context's resident objects
- * and must stay uploaded while requests use them.  A request's result is
+ * and must stay uploaded while requests use them.  A request reads its
+ * frame's depth and labels when it is admitted (its masked copy is made
+ * then): a qpso_frame_update issued while it is still queued is what it
+ * sees, one issued after its admission is not.  A request's result is
  * bit-identical to qpso_solve of the same descriptor, whatever else runs. */
 typedef struct qpso_server qpso_server;
 typedef struct {

@@ -33,7 +33,11 @@ class Params(C.Structure):
                 ("cl_min_x", C.c_int32), ("cl_max_x", C.c_int32),
                 ("cl_min_y", C.c_int32), ("cl_max_y", C.c_int32),
                 ("num_points", C.c_uint32), ("num_particles", C.c_uint32),
-                ("iterations", C.c_uint32), ("seed", C.c_uint64), ("stream", C.c_uint32)]
+                ("iterations", C.c_uint32), ("seed", C.c_uint64), ("stream", C.c_uint32),
+                ("raster_mode", C.c_uint32)]
+
+
+RASTER_REF, RASTER_EDGE = 0, 1
 
 
 class Score(C.Structure):
@@ -70,6 +74,8 @@ def lib():
             getattr(L, fn).argtypes = [C.c_float]
         L.qo_raster_face.restype = C.c_int64
         L.qo_render.restype = C.c_int64
+        L.qo_raster_face_mode.restype = C.c_int64
+        L.qo_render_mode.restype = C.c_int64
         L.qo_fitness_from_counts.restype = C.c_float
         L.qo_fitness_from_counts.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64,
                                              C.c_uint64, C.c_uint32]
@@ -134,25 +140,26 @@ def project(s7, v3, cam: Camera):
     return o
 
 
-def raster_face(v1, v2, v3, cam: Camera, zbuf: np.ndarray, box=None):
+def raster_face(v1, v2, v3, cam: Camera, zbuf: np.ndarray, box=None, mode: int = RASTER_REF):
     a = np.ascontiguousarray(v1, np.float32)
     b = np.ascontiguousarray(v2, np.float32)
     c = np.ascontiguousarray(v3, np.float32)
     if box is None:
         box = np.array([50000, -1, 50000, -1], np.int32)
-    n = lib().qo_raster_face(ptr(a, _f), ptr(b, _f), ptr(c, _f), C.byref(cam),
-                             ptr(zbuf, _i32), ptr(box, _i32))
+    n = lib().qo_raster_face_mode(ptr(a, _f), ptr(b, _f), ptr(c, _f), C.byref(cam),
+                                  ptr(zbuf, _i32), ptr(box, _i32), C.c_uint32(mode))
     return n, box
 
 
-def render(mesh: np.ndarray, num_faces: int, s7, cam: Camera, zbuf: np.ndarray | None = None):
+def render(mesh: np.ndarray, num_faces: int, s7, cam: Camera, zbuf: np.ndarray | None = None,
+           mode: int = RASTER_REF):
     if zbuf is None:
         zbuf = zbuf_new(cam)
     s = np.ascontiguousarray(s7, np.float32)
     box = np.zeros(4, np.int32)
     m = np.ascontiguousarray(mesh, np.float32)
-    n = lib().qo_render(ptr(m, _f), C.c_uint32(num_faces), ptr(s, _f), C.byref(cam),
-                        ptr(zbuf, _i32), ptr(box, _i32))
+    n = lib().qo_render_mode(ptr(m, _f), C.c_uint32(num_faces), ptr(s, _f), C.byref(cam),
+                             ptr(zbuf, _i32), ptr(box, _i32), C.c_uint32(mode))
     return zbuf, box, n
 
 

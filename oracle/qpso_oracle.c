@@ -449,6 +449,18 @@ void qo_zbuf_reset(int32_t *zbuf, const qo_camera *cam)
 int64_t qo_raster_face(const float v1[3], const float v2[3], const float v3[3],
                        const qo_camera *cam, int32_t *zbuf, int32_t box[4])
 {
+    return qo_raster_face_mode(v1, v2, v3, cam, zbuf, box, QO_RASTER_REF);
+}
+
+/* EDGE mode (not what the reference runs): the reference computes the
+ * inside mask (CX1 > 0) & (CX2 > 0) & (CX3 > 0) from the biased edge
+ * functions (main.h:1440) but its guard tests the mask's sign bit
+ * (main.h:1473), which is never set.  EDGE applies the mask: only covered
+ * pixels, with the top-left fill convention of the +1 bias
+ * (main.h:1393-1401), are written and counted. */
+int64_t qo_raster_face_mode(const float v1[3], const float v2[3], const float v3[3],
+                            const qo_camera *cam, int32_t *zbuf, int32_t box[4], uint32_t mode)
+{
     const int32_t Y1 = f2i_rn(16.0f * v1[1]);
     const int32_t Y2 = f2i_rn(16.0f * v2[1]);
     const int32_t Y3 = f2i_rn(16.0f * v3[1]);
@@ -475,15 +487,18 @@ int64_t qo_raster_face(const float v1[3], const float v2[3], const float v3[3],
 
     const float rA = 1.0f / (float)tri_area; /* overA_ == 1 (main.h:155) */
 
-    const int32_t FDX23 = w_shl(DX23, 4), FDX31 = w_shl(DX31, 4);
-    const int32_t FDY23 = w_shl(DY23, 4), FDY31 = w_shl(DY31, 4);
+    const int32_t FDX12 = w_shl(DX12, 4), FDX23 = w_shl(DX23, 4), FDX31 = w_shl(DX31, 4);
+    const int32_t FDY12 = w_shl(DY12, 4), FDY23 = w_shl(DY23, 4), FDY31 = w_shl(DY31, 4);
 
+    int32_t C1 = w_sub(w_mul(DY12, X1), w_mul(DX12, Y1));
     int32_t C2 = w_sub(w_mul(DY23, X2), w_mul(DX23, Y2));
     int32_t C3 = w_sub(w_mul(DY31, X3), w_mul(DX31, Y3));
+    C1 = w_add(C1, (DY12 < 0 || (DY12 == 0 && DX12 > 0)) ? 1 : 0);
     C2 = w_add(C2, (DY23 < 0 || (DY23 == 0 && DX23 > 0)) ? 1 : 0);
     C3 = w_add(C3, (DY31 < 0 || (DY31 == 0 && DX31 > 0)) ? 1 : 0);
 
     const int32_t MINY = w_shl(miny, 4), MINX = w_shl(minx, 4);
+    const int32_t CY1 = w_sub(w_add(C1, w_mul(DX12, MINY)), w_mul(DY12, MINX));
     const int32_t CY2 = w_sub(w_add(C2, w_mul(DX23, MINY)), w_mul(DY23, MINX));
     const int32_t CY3 = w_sub(w_add(C3, w_mul(DX31, MINY)), w_mul(DY31, MINX));
 
@@ -513,6 +528,10 @@ int64_t qo_raster_face(const float v1[3], const float v2[3], const float v3[3],
             const int32_t rx = (int32_t)(x - (int64_t)minx);
             const int32_t CX2 = w_sub(w_add(CY2, w_mul(ry, FDX23)), w_mul(rx, FDY23));
             const int32_t CX3 = w_sub(w_add(CY3, w_mul(ry, FDX31)), w_mul(rx, FDY31));
+            if (mode == QO_RASTER_EDGE) {
+                const int32_t CX1 = w_sub(w_add(CY1, w_mul(ry, FDX12)), w_mul(rx, FDY12));
+                if (!(CX1 > 0 && CX2 > 0 && CX3 > 0)) continue;
+            }
             const int32_t cx2 = asr(w_add(CX2, 0xF), 8);
             const int32_t cx3 = asr(w_add(CX3, 0xF), 8);
             float depth = z1;
@@ -532,6 +551,12 @@ int64_t qo_raster_face(const float v1[3], const float v2[3], const float v3[3],
 int64_t qo_render(const float *mesh, uint32_t F, const float *s, const qo_camera *cam,
                   int32_t *zbuf, int32_t box[4])
 {
+    return qo_render_mode(mesh, F, s, cam, zbuf, box, QO_RASTER_REF);
+}
+
+int64_t qo_render_mode(const float *mesh, uint32_t F, const float *s, const qo_camera *cam,
+                       int32_t *zbuf, int32_t box[4], uint32_t mode)
+{
     box[0] = QO_AABB_INIT_MIN; box[1] = QO_AABB_INIT_MAX;
     box[2] = QO_AABB_INIT_MIN; box[3] = QO_AABB_INIT_MAX;
     int64_t writes = 0;
@@ -543,7 +568,7 @@ int64_t qo_render(const float *mesh, uint32_t F, const float *s, const qo_camera
             v[j][2] = mesh[f + 6 * (size_t)F + (size_t)j * F];
             qo_project(s, v[j], cam, uvz[j]);
         }
-        writes += qo_raster_face(uvz[0], uvz[1], uvz[2], cam, zbuf, box);
+        writes += qo_raster_face_mode(uvz[0], uvz[1], uvz[2], cam, zbuf, box, mode);
     }
     return writes;
 }
@@ -923,7 +948,7 @@ int qo_solve_mt(const float *mesh, uint32_t F, const uint16_t *obs, const qo_cam
             float s[7];
             for (int d = 0; d < 7; ++d) s[d] = pos[p + (size_t)d * P];
             int32_t box[4];
-            wsum += (uint64_t)qo_render(mesh, F, s, cam, zbuf, box);
+            wsum += (uint64_t)qo_render_mode(mesh, F, s, cam, zbuf, box, prm->raster_mode);
             qo_score sc;
             qo_score_zbuf(zbuf, box, obs, cam, prm, &sc);
             fit[p] = sc.fit;

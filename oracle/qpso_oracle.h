@@ -65,7 +65,15 @@ typedef struct {
     uint32_t iterations;
     uint64_t seed;
     uint32_t stream;              /* Philox stream id of this solve instance */
+    uint32_t raster_mode;         /* QO_RASTER_REF (0) or QO_RASTER_EDGE (1) */
 } qo_params;
+
+/* Raster modes.  REF: what the reference computes, every pixel of a front
+ * face's bounding rectangle (its inside mask is never applied).  EDGE: the
+ * inside test the reference's mask encodes (main.h:1440), pixels with all
+ * three biased edge functions > 0 (top-left fill convention). */
+#define QO_RASTER_REF 0
+#define QO_RASTER_EDGE 1
 
 typedef struct {
     uint32_t n_rendered;          /* sNrenderedPointsWarpBallot total */
@@ -115,6 +123,12 @@ int64_t qo_raster_face(const float v1[3], const float v2[3], const float v3[3],
 /* Render a whole mesh (loadOBJ3 SoA layout, 9*F floats) at pose s. */
 int64_t qo_render(const float *mesh, uint32_t num_faces, const float *s,
                   const qo_camera *cam, int32_t *zbuf, int32_t box[4]);
+/* The same with a raster mode; in EDGE mode the returned count is the
+ * number of covered pixels written. */
+int64_t qo_raster_face_mode(const float v1[3], const float v2[3], const float v3[3],
+                            const qo_camera *cam, int32_t *zbuf, int32_t box[4], uint32_t mode);
+int64_t qo_render_mode(const float *mesh, uint32_t num_faces, const float *s,
+                       const qo_camera *cam, int32_t *zbuf, int32_t box[4], uint32_t mode);
 
 /* The reference's host render of the best pose (RenderCPU): iround snapping,
  * float depth, the image only (width*height floats, row-major, filled with

@@ -19,6 +19,7 @@ def oracle_params(s, **over):
     prm.iterations = f["iterations"]
     prm.seed = f["seed"]
     prm.stream = f["stream"]
+    prm.raster_mode = f.get("raster_mode", 0)
     return prm
 
 
