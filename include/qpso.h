@@ -57,7 +57,20 @@ typedef struct {
     float qinit[4];            /* InitQPSO qinit (main.cu:128-132) */
     uint64_t seed;             /* Philox key (replaces the GSL mt19937 table) */
     uint32_t stream;           /* Philox stream id of this solve */
+    uint32_t raster_mode;      /* QPSO_RASTER_REF (default) or QPSO_RASTER_EDGE */
 } qpso_solve_desc;
+
+/* Raster modes of a solve.  REF: what the reference computes
+ * (renderFixedPointAABB, main.h:1306-1491): every pixel of a front face's
+ * bounding rectangle, because its inside mask (main.h:1440) is never
+ * applied (the guard of main.h:1473 tests a bit the mask never has).  EDGE:
+ * that mask applied, only pixels whose three biased edge functions are all
+ * > 0 (top-left fill convention, watertight across shared edges); no
+ * counterpart in what the reference runs.  The render AABB of the fitness
+ * window takes every face rectangle in both modes; raster_writes counts
+ * rectangle pixels in REF mode and covered pixels in EDGE mode. */
+#define QPSO_RASTER_REF 0
+#define QPSO_RASTER_EDGE 1
 
 typedef struct {
     float fit;                 /* d_solution_best_fit */

@@ -193,6 +193,8 @@ qpso_status check_desc(qpso_context* ctx, const qpso_solve_desc& d, const MeshOb
     return fail(ctx, QPSO_ERR_ARG, "frame has no label map");
   for (int k = 0; k < 3; ++k)
     if (!(d.t_lo[k] <= d.t_hi[k])) return fail(ctx, QPSO_ERR_ARG, "t_lo must be <= t_hi");
+  if (d.raster_mode != QPSO_RASTER_REF && d.raster_mode != QPSO_RASTER_EDGE)
+    return fail(ctx, QPSO_ERR_ARG, "raster_mode must be QPSO_RASTER_REF or QPSO_RASTER_EDGE");
   *m = &mi->second;
   *f = &fi->second;
   return QPSO_OK;
@@ -220,6 +222,7 @@ SolveParams to_params(const qpso_solve_desc& d) {
   p.iterations = d.iterations;
   p.seed = d.seed;
   p.stream = d.stream;
+  p.raster_mode = d.raster_mode;
   return p;
 }
 
@@ -664,7 +667,7 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
   if (prof && (st = ensure_events(ctx, 2 * (size_t)desc->iterations)) != QPSO_OK) return st;
   for (uint32_t it = 0; it < desc->iterations; ++it) {
     if (prof) QPSO_CUDA(ctx, cudaEventRecord(ctx->ev[2 * it], s));
-    QPSO_CUDA(ctx, launch_step(dinst, it, chunks, cfg, s));
+    QPSO_CUDA(ctx, launch_step(dinst, it, chunks, cfg, s, desc->raster_mode == QPSO_RASTER_EDGE));
     if (prof) QPSO_CUDA(ctx, cudaEventRecord(ctx->ev[2 * it + 1], s));
   }
   QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
@@ -708,8 +711,10 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   std::vector<uint32_t> order(n);
   std::vector<double> cost(n);
   uint32_t max_iters = 0, max_w = 0, max_h = 0;
+  bool edge = false;
   for (uint32_t i = 0; i < n; ++i) {
     order[i] = i;
+    edge = edge || ds[i]->raster_mode == QPSO_RASTER_EDGE;
     const double area = (double)(ds[i]->cl_max_x - ds[i]->cl_min_x) * (ds[i]->cl_max_y - ds[i]->cl_min_y);
     cost[i] = (double)ms[i]->F * 3.0 + area;
     max_iters = std::max(max_iters, ds[i]->iterations);
@@ -726,7 +731,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   if ((st = ensure_ws(ctx, L.total)) != QPSO_OK) return st;
   if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
   int per_sm = 0;
-  QPSO_CUDA(ctx, batch_max_grid(cfg, &per_sm));
+  QPSO_CUDA(ctx, batch_max_grid(cfg, edge, &per_sm));
   if (per_sm <= 0) return fail(ctx, QPSO_ERR_ARG, "batch launch config does not fit on an SM");
   const int grid = (int)std::min<size_t>(items.size(), (size_t)per_sm * ctx->num_sms);
   // wait before touching pinned staging that an earlier graph may read
@@ -741,7 +746,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   }
   std::vector<uint64_t> key = {(uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)h, L.total, L.meta_end,
                                n, items.size(), max_iters, (uint64_t)grid, (uint64_t)cfg.threads,
-                               (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h};
+                               (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h, (uint64_t)edge};
   if (!ctx->gexec || key != ctx->gkey) {
     if (ctx->gexec) {
       cudaGraphExecDestroy(ctx->gexec);
@@ -761,7 +766,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     cudaError_t e = cudaMemcpyAsync(d, h, L.meta_end, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
       e = launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), (int)n, (int)max_w, (int)max_h, s);
-    if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s);
+    if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s, edge);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h + L.hdr, d + L.hdr, n * sizeof(Header), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
@@ -805,7 +810,11 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
                           uint32_t tune_iters, qpso_launch_config* best, float* best_ms) {
   if (!ctx || !descs || n == 0 || tune_iters == 0) return fail(ctx, QPSO_ERR_ARG, "bad autotune arguments");
   std::vector<qpso_solve_desc> ds(descs, descs + n);
-  for (auto& d : ds) d.iterations = std::min(d.iterations, tune_iters);
+  bool edge = false;
+  for (auto& d : ds) {
+    d.iterations = std::min(d.iterations, tune_iters);
+    edge = edge || d.raster_mode == QPSO_RASTER_EDGE;
+  }
   const TileConfig saved = batched ? ctx->batch : ctx->plain;
   TileConfig win = saved;
   float win_ms = 3.0e38f;
@@ -824,7 +833,7 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
         const TileConfig tc{th, tp, pb};
         if (batched) {
           int per_sm = 0;
-          if (batch_max_grid(tc, &per_sm) != cudaSuccess || per_sm <= 0) continue;
+          if (batch_max_grid(tc, edge, &per_sm) != cudaSuccess || per_sm <= 0) continue;
           ctx->batch = tc;
         } else {
           ctx->plain = tc;
@@ -888,7 +897,8 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   const int grid = (int)std::min<uint32_t>(groups, (uint32_t)ctx->num_sms * 4);
   QPSO_CUDA(ctx, launch_score_mlets(reinterpret_cast<const Instance*>(d + L.inst),
                                     reinterpret_cast<const float*>(d + pose_off), n,
-                                    reinterpret_cast<float*>(d + fit_off), cfg, grid, s));
+                                    reinterpret_cast<float*>(d + fit_off), cfg, grid, s,
+                                    desc->raster_mode == QPSO_RASTER_EDGE));
   QPSO_CUDA(ctx, cudaMemcpyAsync(fit_out, d + fit_off, (size_t)n * sizeof(float),
                                  cudaMemcpyDeviceToHost, s));
   QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
@@ -1242,11 +1252,13 @@ void server_loop(qpso_server* s) {
     }
     // work items of this epoch: every chunk of every active request
     uint32_t n_items = 0, K = s->cfg.iters_per_epoch;
+    bool edge = false;
     {
       std::lock_guard<std::mutex> g(s->mu);
       for (int slot : active) {
         const ServerReq& r = s->reqs[s->slot_req[slot]];
         K = std::min(K, r.remaining);
+        edge = edge || r.desc.raster_mode == QPSO_RASTER_EDGE;
         const uint32_t chunks = s->h_slots[slot].chunks;
         for (uint32_t c = 0; c < chunks; ++c) s->h_items[n_items++] = WorkItem{(uint32_t)slot, c};
       }
@@ -1255,7 +1267,7 @@ void server_loop(qpso_server* s) {
       e = cudaMemcpyAsync(s->d_items, s->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
                           s->stream);
     for (uint32_t k = 0; k < K && e == cudaSuccess; ++k)
-      e = launch_multi_step(s->d_slots, s->d_items, n_items, s->tc, s->stream);
+      e = launch_multi_step(s->d_slots, s->d_items, n_items, s->tc, s->stream, edge);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s->h_hdr, s->d_hdr, S * sizeof(Header), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);

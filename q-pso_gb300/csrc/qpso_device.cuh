@@ -330,6 +330,7 @@ struct SolveParams {
   uint32_t iterations;
   uint64_t seed;
   uint32_t stream;
+  uint32_t raster_mode;  // kRasterRef or kRasterEdge
 };
 
 // InitQPSO, main.cu:72-198 (draw group 0).
@@ -465,6 +466,7 @@ struct FaceSetup {
   int32_t cy2, cy3;           // edge functions 2,3 at (minx, miny), 2^8 scale
   int32_t fdx23, fdx31;       // per-row steps
   int32_t fdy23, fdy31;       // per-column steps
+  int32_t cy1, fdx12, fdy12;  // edge function 1, set only for the EDGE raster mode
   float z1, z2, z3;           // z1 and the two depth gradients
   bool live;                  // front-facing with a non-empty rectangle
 };
@@ -473,7 +475,7 @@ struct FaceSetup {
 // (main.h:1333-1338) and the vertex depths in mm.
 __device__ __forceinline__ void setup_face_fixed(int32_t X1, int32_t Y1, float w1, int32_t X2, int32_t Y2,
                                                  float w2, int32_t X3, int32_t Y3, float w3,
-                                                 FaceSetup& f) {
+                                                 FaceSetup& f, bool edge = false) {
   f.minx = wadd(min(min(X1, X2), X3), 0xF) >> 4;
   f.maxx = wadd(max(max(X1, X2), X3), 0xF) >> 4;
   f.miny = wadd(min(min(Y1, Y2), Y3), 0xF) >> 4;
@@ -495,17 +497,32 @@ __device__ __forceinline__ void setup_face_fixed(int32_t X1, int32_t Y1, float w
   const int32_t MINY = wshl(f.miny, 4), MINX = wshl(f.minx, 4);
   f.cy2 = wsub(wadd(C2, wmul(DX23, MINY)), wmul(DY23, MINX));
   f.cy3 = wsub(wadd(C3, wmul(DX31, MINY)), wmul(DY31, MINX));
+  if (edge) {
+    f.fdx12 = wshl(DX12, 4);
+    f.fdy12 = wshl(DY12, 4);
+    int32_t C1 = wsub(wmul(DY12, X1), wmul(DX12, Y1));
+    C1 = wadd(C1, (DY12 < 0 || (DY12 == 0 && DX12 > 0)) ? 1 : 0);
+    f.cy1 = wsub(wadd(C1, wmul(DX12, MINY)), wmul(DY12, MINX));
+  }
   f.z1 = w1;
   f.z2 = (w2 - w1) * rA;
   f.z3 = (w3 - w1) * rA;
 }
 
 __device__ __forceinline__ void setup_face(float u1, float v1, float w1, float u2, float v2,
-                                           float w2, float u3, float v3, float w3, FaceSetup& f) {
+                                           float w2, float u3, float v3, float w3, FaceSetup& f,
+                                           bool edge = false) {
   setup_face_fixed(__float2int_rn(16.0f * u1), __float2int_rn(16.0f * v1), w1,
                    __float2int_rn(16.0f * u2), __float2int_rn(16.0f * v2), w2,
-                   __float2int_rn(16.0f * u3), __float2int_rn(16.0f * v3), w3, f);
+                   __float2int_rn(16.0f * u3), __float2int_rn(16.0f * v3), w3, f, edge);
 }
+
+// Raster modes.  REF (0): what the reference computes, every pixel of a
+// front face's bounding rectangle (its inside mask, main.h:1440, is never
+// applied because the guard of main.h:1473 tests a bit the mask never has).
+// EDGE (1): that mask applied, pixels whose three biased edge functions are
+// all > 0 (top-left fill convention).
+constexpr uint32_t kRasterRef = 0, kRasterEdge = 1;
 
 // Depth written at pixel (minx+rx, miny+ry) of a live face (main.h:1432-1448):
 // every pixel of the rectangle is written (the inside mask of main.h:1440

@@ -165,6 +165,7 @@ __device__ float render_score(const Instance& I, const float* s, int32_t* tile, 
   const int tid = threadIdx.x, T = blockDim.x;
   const int32_t W = I.cam.width, H = I.cam.height;
   const int32_t dx0 = -kGuard, dx1 = W + kGuard, dy0 = -kGuard, dy1 = H + kGuard;
+  const bool edge = I.prm.raster_mode == kRasterEdge;
   if (tid == 0) pose_bound(I, s, ctl.bound);
   __syncthreads();
   const int32_t bx0 = ctl.bound[0], bx1 = ctl.bound[1], by0 = ctl.bound[2], by1 = ctl.bound[3];
@@ -223,7 +224,7 @@ __device__ float render_score(const Instance& I, const float* s, int32_t* tile, 
         project(s, mx, my, mz, I.cam, u[j], v[j], z[j]);
       }
       FaceSetup fs;
-      setup_face(u[0], v[0], z[0], u[1], v[1], z[1], u[2], v[2], z[2], fs);
+      setup_face(u[0], v[0], z[0], u[1], v[1], z[1], u[2], v[2], z[2], fs, edge);
       if (pass == 0) {
         acc.rminx = min(acc.rminx, fs.minx);
         acc.rmaxx = max(acc.rmaxx, fs.maxx);
@@ -241,23 +242,28 @@ __device__ float render_score(const Instance& I, const float* s, int32_t* tile, 
       const int32_t xa = max(fs.minx, x0), xb = min(fs.maxx, x0 + cwp);
       const int32_t ya = max(fs.miny, y0), yb = min(fs.maxy, y0 + thp);
       if (xa >= xb || ya >= yb) continue;
-      acc.writes += (unsigned long long)(xb - xa) * (unsigned long long)(yb - ya);
+      if (!edge) acc.writes += (unsigned long long)(xb - xa) * (unsigned long long)(yb - ya);
       const int32_t rx0 = xa - fs.minx;
       for (int32_t y = ya; y < yb; ++y) {
         const int32_t ry = y - fs.miny;
         int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
         int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
+        int32_t CX1 = edge ? wsub(wadd(fs.cy1, wmul(ry, fs.fdx12)), wmul(rx0, fs.fdy12)) : 1;
         int32_t* row = tile + (y - y0) * cwp - x0;
         for (int32_t x = xa; x < xb; ++x) {
-          const int32_t cx2 = wadd(CX2, 0xF) >> 8;
-          const int32_t cx3 = wadd(CX3, 0xF) >> 8;
-          float depth = fs.z1;
-          depth = depth + (float)cx2 * fs.z2;
-          depth = depth + (float)cx3 * fs.z3;
-          const int32_t d = __float2int_rn(depth);
-          if (d < kDepthBg) atomicMin(row + x, d);
+          if (!edge || (CX1 > 0 && CX2 > 0 && CX3 > 0)) {
+            const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+            const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+            float depth = fs.z1;
+            depth = depth + (float)cx2 * fs.z2;
+            depth = depth + (float)cx3 * fs.z3;
+            const int32_t d = __float2int_rn(depth);
+            if (d < kDepthBg) atomicMin(row + x, d);
+            if (edge) acc.writes += 1ull;
+          }
           CX2 = wsub(CX2, fs.fdy23);
           CX3 = wsub(CX3, fs.fdy31);
+          if (edge) CX1 = wsub(CX1, fs.fdy12);
         }
       }
     }
@@ -439,8 +445,9 @@ __device__ __forceinline__ bool box_rect(const float* pose, const Camera& cam, f
 // pass 0 records every meshlet's screen rectangle per particle when the
 // mesh has at most kCullCap meshlets; larger meshes project each meshlet's
 // object-space box instead (checked in pass 0 against the real rectangle).
-__device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& sm, int tile_px,
-                                   SmemCtl& ctl, float* fit_out) {
+template <bool kEdge>
+__device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSmem& sm, int tile_px,
+                                        SmemCtl& ctl, float* fit_out) {
   const int tid = threadIdx.x, T = blockDim.x;
   const int lane = tid & 31, wid = tid >> 5, nw = T >> 5;
   const int32_t W = I.cam.width, H = I.cam.height;
@@ -664,7 +671,7 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
             const uint32_t fi = __ldg(gf + f);
             const int4 a = vc[fi & 1023u], bb = vc[(fi >> 10) & 1023u], c = vc[(fi >> 20) & 1023u];
             setup_face_fixed(a.x, a.y, __int_as_float(a.z), bb.x, bb.y, __int_as_float(bb.z), c.x, c.y,
-                             __int_as_float(c.z), fs);
+                             __int_as_float(c.z), fs, kEdge);
             bminx = min(bminx, fs.minx);
             bmaxx = max(bmaxx, fs.maxx);
             bminy = min(bminy, fs.miny);
@@ -683,7 +690,7 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
               yb = min(fs.maxy, y0 + thp);
               if (xa < xb && ya < yb) {
                 const int32_t n = (xb - xa) * (yb - ya);
-                writes += (unsigned long long)n;
+                if (!kEdge) writes += (unsigned long long)n;
                 if (n > kLaneRasterMax) {
                   big = true;
                 } else {
@@ -692,17 +699,22 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
                     const int32_t ry = y - fs.miny;
                     int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
                     int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
+                    int32_t CX1 = kEdge ? wsub(wadd(fs.cy1, wmul(ry, fs.fdx12)), wmul(rx0, fs.fdy12)) : 1;
                     int32_t* row = tile + (y - y0) * cwp - x0;
                     for (int32_t x = xa; x < xb; ++x) {
-                      const int32_t cx2 = wadd(CX2, 0xF) >> 8;
-                      const int32_t cx3 = wadd(CX3, 0xF) >> 8;
-                      float depth = fs.z1;
-                      depth = depth + (float)cx2 * fs.z2;
-                      depth = depth + (float)cx3 * fs.z3;
-                      const int32_t d = __float2int_rn(depth);
-                      if (d < kDepthBg) atomicMin(row + x, d);
+                      if (!kEdge || (CX1 > 0 && CX2 > 0 && CX3 > 0)) {
+                        const int32_t cx2 = wadd(CX2, 0xF) >> 8;
+                        const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+                        float depth = fs.z1;
+                        depth = depth + (float)cx2 * fs.z2;
+                        depth = depth + (float)cx3 * fs.z3;
+                        const int32_t d = __float2int_rn(depth);
+                        if (d < kDepthBg) atomicMin(row + x, d);
+                        if (kEdge) writes += 1ull;
+                      }
                       CX2 = wsub(CX2, fs.fdy23);
                       CX3 = wsub(CX3, fs.fdy31);
+                      if (kEdge) CX1 = wsub(CX1, fs.fdy12);
                     }
                   }
                 }
@@ -728,6 +740,12 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
             const int32_t bxb = __shfl_sync(0xffffffffu, xb, src);
             const int32_t bya = __shfl_sync(0xffffffffu, ya, src);
             const int32_t byb = __shfl_sync(0xffffffffu, yb, src);
+            int32_t cy1 = 0, fdx12 = 0, fdy12 = 0;
+            if (kEdge) {
+              cy1 = __shfl_sync(0xffffffffu, fs.cy1, src);
+              fdx12 = __shfl_sync(0xffffffffu, fs.fdx12, src);
+              fdy12 = __shfl_sync(0xffffffffu, fs.fdy12, src);
+            }
             const int32_t w = bxb - bxa;
             const int32_t n = w * (byb - bya);
             const float rw = 1.0f / (float)w;
@@ -737,6 +755,11 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
               const int32_t ry = y - fminy, rx = x - fminx;
               const int32_t CX2 = wsub(wadd(cy2, wmul(ry, fdx23)), wmul(rx, fdy23));
               const int32_t CX3 = wsub(wadd(cy3, wmul(ry, fdx31)), wmul(rx, fdy31));
+              if (kEdge) {
+                const int32_t CX1 = wsub(wadd(cy1, wmul(ry, fdx12)), wmul(rx, fdy12));
+                if (!(CX1 > 0 && CX2 > 0 && CX3 > 0)) continue;
+                writes += 1ull;
+              }
               const int32_t cx2 = wadd(CX2, 0xF) >> 8;
               const int32_t cx3 = wadd(CX3, 0xF) >> 8;
               float depth = z1;
@@ -939,7 +962,20 @@ __device__ void render_score_mlets(const Instance& I, int np, const FusedSmem& s
   __syncthreads();
 }
 
+// Render + score in the instance's raster mode (uniform per instance).
+// Kernels compiled with kAllowEdge = false hold only the REF raster, so the
+// default path's code and registers do not carry the EDGE variant.
+template <bool kAllowEdge>
+__device__ __forceinline__ void render_score_mlets(const Instance& I, int np, const FusedSmem& sm, int tile_px,
+                                                   SmemCtl& ctl, float* fit_out) {
+  if (kAllowEdge && I.prm.raster_mode == kRasterEdge)
+    render_score_mlets_mode<true>(I, np, sm, tile_px, ctl, fit_out);
+  else
+    render_score_mlets_mode<false>(I, np, sm, tile_px, ctl, fit_out);
+}
+
 // PSO step + render + score + personal best for one work item.
+template <bool kAllowEdge>
 __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, unsigned char* dyn,
                              int tile_px, SmemCtl& ctl) {
   const int tid = threadIdx.x;
@@ -973,7 +1009,7 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
     }
   }
   __syncthreads();
-  render_score_mlets(I, (int)np, carve_smem(dyn, (int)I.ppb), tile_px, ctl, ctl.argv);
+  render_score_mlets<kAllowEdge>(I, (int)np, carve_smem(dyn, (int)I.ppb), tile_px, ctl, ctl.argv);
   if (tid < (int)np) {
     const uint32_t p = p0 + tid;
     const float fv = ctl.argv[tid];
@@ -1061,12 +1097,13 @@ __device__ void instance_epilogue(const Instance& I, uint32_t iter, SmemCtl& ctl
 }
 
 // Plain form: one launch per iteration of one instance, one CTA per chunk.
+template <bool kAllowEdge>
 __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* __restrict__ inst,
                                                                 uint32_t iter, int tile_px) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
   const Instance& I = *inst;
-  process_item(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
+  process_item<kAllowEdge>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
   instance_epilogue(I, iter, ctl);
 }
 
@@ -1075,6 +1112,7 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* 
 // set of requests changes between launches).  CTA b runs work item b; the
 // CTA finishing an instance's last chunk updates its global best and
 // advances its iteration counter for the next launch.
+template <bool kAllowEdge>
 __global__ void __launch_bounds__(kMaxThreads) qpso_multi_step_kernel(Instance* __restrict__ slots,
                                                                       const WorkItem* __restrict__ items,
                                                                       int tile_px) {
@@ -1083,7 +1121,7 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_multi_step_kernel(Instance* 
   const WorkItem it = items[blockIdx.x];
   Instance& I = slots[it.inst];
   const uint32_t iter = __ldcg(&I.cur_iter);
-  process_item(I, it.chunk, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
+  process_item<kAllowEdge>(I, it.chunk, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
   instance_epilogue(I, iter, ctl);
   if (ctl.last && threadIdx.x == 0) I.cur_iter = iter + 1;
 }
@@ -1129,6 +1167,7 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t* err, unsigned long long ti
 // launch.  Step s runs the s-th iteration of all instances that have one;
 // CTAs claim work items (largest first) from a per-step counter, and the
 // last chunk of an instance updates its global best before the barrier.
+template <bool kAllowEdge>
 __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, int tile_px) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
@@ -1142,7 +1181,7 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, in
       const WorkItem it = A.items[k];
       const Instance& I = A.inst[it.inst];
       if (s >= I.prm.iterations) continue;
-      process_item(I, it.chunk, s, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
+      process_item<kAllowEdge>(I, it.chunk, s, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
       instance_epilogue(I, s, ctl);
     }
     if (s + 1 < A.max_iters && !grid_barrier(A.barrier, A.err, A.timeout_ns)) return;
@@ -1381,6 +1420,7 @@ __global__ void __launch_bounds__(kMaxThreads) score_poses_kernel(const Instance
 }
 
 // Score explicit poses with the meshlet path, ppb poses per CTA pass.
+template <bool kAllowEdge>
 __global__ void __launch_bounds__(kMaxThreads) score_poses_mlet_kernel(const Instance* __restrict__ inst,
                                                                        const float* __restrict__ poses,
                                                                        uint32_t n, int tile_px,
@@ -1396,7 +1436,7 @@ __global__ void __launch_bounds__(kMaxThreads) score_poses_mlet_kernel(const Ins
     const int np = (int)min(I.ppb, n - k0);
     if ((int)threadIdx.x < np * 7) ctl.pose[threadIdx.x / 7][threadIdx.x % 7] = poses[(size_t)k0 * 7 + threadIdx.x];
     __syncthreads();
-    render_score_mlets(I, np, sm, tile_px, ctl, ctl.argv);
+    render_score_mlets<kAllowEdge>(I, np, sm, tile_px, ctl, ctl.argv);
     if ((int)threadIdx.x < np) fit_out[k0 + threadIdx.x] = ctl.argv[threadIdx.x];
     __syncthreads();
   }
@@ -1474,24 +1514,27 @@ cudaError_t launch_mesh_aabb(const float* mesh, uint32_t F, float* out, cudaStre
 }
 
 cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, const TileConfig& cfg,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool edge) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
-  cudaError_t e = ensure_smem(qpso_step_kernel, smem);
+  auto* k = edge ? qpso_step_kernel<true> : qpso_step_kernel<false>;
+  cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  qpso_step_kernel<<<chunks, cfg.threads, smem, st>>>(inst, iter, cfg.tile_px);
+  k<<<chunks, cfg.threads, smem, st>>>(inst, iter, cfg.tile_px);
   return cudaGetLastError();
 }
 
-cudaError_t batch_max_grid(const TileConfig& cfg, int* blocks_per_sm) {
+cudaError_t batch_max_grid(const TileConfig& cfg, bool edge, int* blocks_per_sm) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
-  cudaError_t e = ensure_smem(qpso_batch_kernel, smem);
+  auto* k = edge ? qpso_batch_kernel<true> : qpso_batch_kernel<false>;
+  cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, qpso_batch_kernel, cfg.threads, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, cfg.threads, smem);
 }
 
-cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st) {
+cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, bool edge) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
-  cudaError_t e = ensure_smem(qpso_batch_kernel, smem);
+  auto* k = edge ? qpso_batch_kernel<true> : qpso_batch_kernel<false>;
+  cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3(grid);
@@ -1503,7 +1546,7 @@ cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg,
   attr[0].val.cooperative = 1;
   lc.attrs = attr;
   lc.numAttrs = 1;
-  return cudaLaunchKernelEx(&lc, qpso_batch_kernel, args, cfg.tile_px);
+  return cudaLaunchKernelEx(&lc, k, args, cfg.tile_px);
 }
 
 cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
@@ -1671,11 +1714,12 @@ cudaError_t launch_cluster_stats(const uint16_t* depth, const int32_t* labels, i
 }
 
 cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
-                               const TileConfig& cfg, int grid, cudaStream_t st) {
+                               const TileConfig& cfg, int grid, cudaStream_t st, bool edge) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
-  cudaError_t e = ensure_smem(score_poses_mlet_kernel, smem);
+  auto* k = edge ? score_poses_mlet_kernel<true> : score_poses_mlet_kernel<false>;
+  cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  score_poses_mlet_kernel<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out);
+  k<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out);
   return cudaGetLastError();
 }
 
@@ -1690,12 +1734,13 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
 }
 
 cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
-                              const TileConfig& cfg, cudaStream_t st) {
+                              const TileConfig& cfg, cudaStream_t st, bool edge) {
   if (n_items == 0) return cudaSuccess;
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
-  cudaError_t e = ensure_smem(qpso_multi_step_kernel, smem);
+  auto* k = edge ? qpso_multi_step_kernel<true> : qpso_multi_step_kernel<false>;
+  cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  qpso_multi_step_kernel<<<n_items, cfg.threads, smem, st>>>(slots, items, cfg.tile_px);
+  k<<<n_items, cfg.threads, smem, st>>>(slots, items, cfg.tile_px);
   return cudaGetLastError();
 }
 

@@ -81,6 +81,7 @@ extern "C" qpso_status qpso_score_poses_noalloc(const float* d_mesh_soa, uint32_
   if (desc->num_points == 0 || !(desc->cl_min_x < desc->cl_max_x && desc->cl_min_y < desc->cl_max_y))
     return QPSO_ERR_ARG;
   if (desc->cluster_label >= 0 && !d_labels) return QPSO_ERR_ARG;
+  if (desc->raster_mode != QPSO_RASTER_REF && desc->raster_mode != QPSO_RASTER_EDGE) return QPSO_ERR_ARG;
   const size_t w = (size_t)cam->width, h = (size_t)cam->height;
   // scratch layout: instance | prep job | header | masked depth | table
   const size_t o_inst = 0;
@@ -125,6 +126,7 @@ extern "C" qpso_status qpso_score_poses_noalloc(const float* d_mesh_soa, uint32_
   p.iterations = 1;
   p.seed = desc->seed;
   p.stream = desc->stream;
+  p.raster_mode = desc->raster_mode;
   I.gbest = reinterpret_cast<float*>(base + o_hdr + offsetof(Header, gbest));
   I.done = reinterpret_cast<uint32_t*>(base + o_hdr + offsetof(Header, done));
   I.err = reinterpret_cast<uint32_t*>(base + o_hdr + offsetof(Header, err));

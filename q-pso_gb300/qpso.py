@@ -49,7 +49,10 @@ class SolveDesc(C.Structure):
                 ("t_hi", C.c_float * 3), ("num_particles", C.c_uint32), ("iterations", C.c_uint32),
                 ("c1", C.c_float), ("c2", C.c_float), ("w", C.c_double), ("vdot", C.c_float),
                 ("ang_lo", C.c_float), ("ang_hi", C.c_float), ("qinit", C.c_float * 4),
-                ("seed", C.c_uint64), ("stream", C.c_uint32)]
+                ("seed", C.c_uint64), ("stream", C.c_uint32), ("raster_mode", C.c_uint32)]
+
+
+RASTER_REF, RASTER_EDGE = 0, 1
 
 
 class Result(C.Structure):

@@ -92,9 +92,66 @@ def _oracle_scores(w, s, poses, **over):
     cam = po.camera()
     out = []
     for pose in poses:
-        zb, box, _ = po.render(soa, F, pose, cam)
+        zb, box, _ = po.render(soa, F, pose, cam, mode=prm.raster_mode)
         out.append(po.score(zb, box, obs, cam, prm))
     return out, prm
+
+
+def test_edge_mode_fitness_trace_and_batch_bit_exact(gpu_ctx, c1_gpu):
+    """QPSO_RASTER_EDGE (the reference's inside mask applied): fitness of
+    given poses, a solve's per-iteration global best and final swarm, the
+    raster write count, and batched == plain with REF and EDGE solves mixed
+    in one launch, all equal to the oracle's EDGE mode."""
+    import qpso
+
+    w, mids, fids = c1_gpu
+    s = dict(w["solves"][0], particles=48, iterations=10, seed=11, stream=3)
+    soa, F = w["meshes"][0]
+    rng = np.random.default_rng(21)
+    poses = np.concatenate([s["gt_pose"][None], random_poses(rng, s, 15, 0.4)])
+    d_edge = gpu_desc(s, mids[0], fids[0], raster_mode=qpso.RASTER_EDGE)
+    d_ref = gpu_desc(s, mids[0], fids[0])
+    scores, _ = _oracle_scores(w, s, poses, raster_mode=po.RASTER_EDGE)
+    got = gpu_ctx.score_poses(d_edge, poses)
+    np.testing.assert_array_equal(got, np.array([sc.fit for sc in scores], np.float32))
+    assert not np.array_equal(got, gpu_ctx.score_poses(d_ref, poses))  # the modes do differ
+    want = po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s, raster_mode=po.RASTER_EDGE),
+                    trace=True)
+    r, st = gpu_ctx.solve_traced(d_edge)
+    assert r.flags == 0
+    np.testing.assert_array_equal(st["trace_gbest"], want["trace_gbest"])
+    np.testing.assert_array_equal(st["pos"], want["pos"])
+    np.testing.assert_array_equal(st["pbest_fit"], want["pbest_fit"])
+    assert r.raster_writes == want["raster_writes"]
+    rb = gpu_ctx.solve_batch([d_ref, d_edge, d_ref])
+    ra = gpu_ctx.solve(d_ref)
+    for x, y in [(rb[0], ra), (rb[1], r), (rb[2], ra)]:
+        assert x.fit == y.fit and list(x.pose) == list(y.pose) and x.raster_writes == y.raster_writes
+    old = gpu_ctx.get_launch_config()
+    try:  # several tile passes per render
+        gpu_ctx.set_launch_config(plain=(128, 1024, 2))
+        np.testing.assert_array_equal(gpu_ctx.score_poses(d_edge, poses), got)
+    finally:
+        gpu_ctx.set_launch_config(plain=old[0], batch=old[1])
+    with pytest.raises(qpso.QpsoError) as e:
+        gpu_ctx.solve(gpu_desc(s, mids[0], fids[0], raster_mode=7))
+    assert e.value.status == qpso.ERR_ARG
+
+
+def test_ref_mode_raster_writes_match_oracle(gpu_ctx, c1_gpu):
+    """The write count of a REF solve is the oracle's (rectangle pixels
+    inside the raster domain), at one and at many tile passes."""
+    w, mids, fids = c1_gpu
+    s = dict(w["solves"][0], particles=32, iterations=6, seed=2, stream=5)
+    soa, F = w["meshes"][0]
+    want = po.solve(soa, F, oracle_obs(w, s), po.camera(), oracle_params(s), trace=True)
+    old = gpu_ctx.get_launch_config()
+    try:
+        for cfg in [(256, 16384, 1), (128, 1024, 2)]:
+            gpu_ctx.set_launch_config(plain=cfg)
+            assert gpu_ctx.solve(gpu_desc(s, mids[0], fids[0])).raster_writes == want["raster_writes"]
+    finally:
+        gpu_ctx.set_launch_config(plain=old[0], batch=old[1])
 
 
 def test_fitness_bit_exact_and_fp64(gpu_ctx, c1_gpu):
