@@ -238,6 +238,24 @@ def cpu_baseline(w, budget_s: float = 12.0):
             "particle_renders_per_s": renders / dt}
 
 
+def accuracy_vs_ground_truth(ctx, w, descs, results):
+    """How close the solved poses are to the synthetic scenes' true poses:
+    median translation error (mm) and rotation error (degrees; symmetric
+    procedural shapes make this an upper bound), and the fraction of solves
+    whose best fitness is at most the true pose's own fitness (the swarm
+    found a pose the objective ranks at least as well as the truth)."""
+    t_err, r_err, le = [], [], 0
+    for s, d, r in zip(w["solves"], descs, results):
+        gt = np.asarray(s["gt_pose"], np.float32)
+        pose = np.asarray(r.pose[:], np.float64)
+        t_err.append(1000.0 * float(np.linalg.norm(pose[:3] - gt[:3])))
+        dq = abs(float(np.dot(pose[3:], gt[3:].astype(np.float64))))
+        r_err.append(2.0 * float(np.degrees(np.arccos(min(1.0, dq)))))
+        le += int(r.fit <= float(ctx.score_poses(d, gt[None])[0]))
+    return {"trans_mm_median": float(np.median(t_err)), "rot_deg_median": float(np.median(r_err)),
+            "fit_at_most_true_pose_fraction": le / len(results), "solves": len(results)}
+
+
 def run_reference(args, ws, rank):
     """Reference arm: the oracle port on the host cores (the reference's own
     program needs OpenCV 2.4, assimp, GSL and a missing header and cannot be
@@ -347,6 +365,7 @@ def run_ours(args, ws, rank, local):
     # correctness of what is timed: plain and batched agree bit for bit
     r_main, r_alt = main_fn(), alt_fn()
     writes_per_step = sum(r.raster_writes for r in r_main)
+    accuracy = accuracy_vs_ground_truth(ctx, w, descs, r_main)
     agree = all(a.fit == b.fit and list(a.pose) == list(b.pose) for a, b in zip(r_main, r_alt))
     flags = max(r.flags for r in r_main)
 
@@ -406,6 +425,7 @@ def run_ours(args, ws, rank, local):
         "plain": {"value": plain_v, "unit": "solves/s"},
         "batched": {"value": batch_v, "unit": "solves/s", "speedup_vs_plain": batch_v / plain_v},
         "plain_batched_bit_identical": bool(agree), "device_error_bits": int(flags),
+        "accuracy_vs_ground_truth": accuracy,
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(gpu_launches),

@@ -35,7 +35,7 @@ int usage(const char* argv0) {
   std::printf(
       "Usage: %s path/to/.obj color_image depth_image cluster_idx\n"
       "       [--labels FILE] [--particles N] [--iterations N] [--seed N] [--stream N]\n"
-      "       [--camera fx,fy,cx,cy] [--results DIR] [--device N]\n",
+      "       [--camera fx,fy,cx,cy] [--results DIR] [--device N] [--raster-mode ref|edge]\n",
       argv0);
   return 0;  // the reference returns 0 after its usage line too
 }
@@ -87,6 +87,7 @@ int main(int argc, char** argv) {
   std::string labels_path = depth_path + ".labels.png", results = "results";
   unsigned long long particles = 0, iterations = 0, seed = 0, stream = 0, device = 0;
   bool have_seed = false, have_stream = false;
+  int raster_mode = 0;
   // the reference's compiled-in ACCV intrinsics (main.h:30-33)
   qpso_camera cam = {572.41140f, 573.57043f, 325.26110f, 242.04899f, 0, 0};
   for (int i = 5; i < argc; ++i) {
@@ -102,6 +103,7 @@ int main(int argc, char** argv) {
     else if (a == "--stream") ok = have_stream = parse_u64(v, &stream);
     else if (a == "--device") ok = parse_u64(v, &device);
     else if (a == "--camera") ok = std::sscanf(v, "%f,%f,%f,%f", &cam.fx, &cam.fy, &cam.cx, &cam.cy) == 4;
+    else if (a == "--raster-mode") ok = (raster_mode = std::string(v) == "edge" ? 1 : std::string(v) == "ref" ? 0 : -1) >= 0;
     else return die("unknown option", a);
     if (!ok) return die("bad value", a + " " + v);
   }
@@ -178,6 +180,7 @@ int main(int argc, char** argv) {
   if (iterations) d.iterations = (uint32_t)iterations;
   if (have_seed) d.seed = seed;
   if (have_stream) d.stream = (uint32_t)stream;
+  d.raster_mode = raster_mode == 1 ? QPSO_RASTER_EDGE : QPSO_RASTER_REF;
   qpso_result r;
   if (qpso_solve(ctx, &d, &r) != QPSO_OK) return fail("solve");
   std::printf("Solution Best Pose: %f %f %f %f %f %f %f\nSolution Best Fit: %f\n", r.pose[0], r.pose[1],

@@ -89,6 +89,31 @@ def test_cli_outputs_equal_library_and_oracle(gpu_ctx, files, depth_name):
     gpu_ctx.mesh_release(mid)
 
 
+def test_cli_edge_raster_mode(gpu_ctx, files):
+    """--raster-mode edge solves with QPSO_RASTER_EDGE: the pose file equals
+    the library's EDGE solve of the same cluster."""
+    d, w, s, obj = files
+    k = s["cluster"]["label"]
+    r = run_cli(d, obj, "depth.bin", k, ("--raster-mode", "edge", "--results", str(d / "res_edge")))
+    assert r.returncode == 0, r.stderr
+    soa, F = qpso.obj_load(obj)
+    depth, labels, _ = w["frames"][0]
+    cam = qpso.Camera(*scene.camera_tuple())
+    mid = gpu_ctx.mesh_upload(soa, F)
+    fid = gpu_ctx.frame_upload(depth, cam, labels=labels)
+    c = [x for x in gpu_ctx.frame_clusters(fid) if x["label"] == k][0]
+    lo, hi = qpso.box_from_centroid(c["centroid_mm"])
+    x0, x1, y0, y1 = c["aabb"]
+    desc = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=k, cl_min_x=x0, cl_max_x=x1,
+                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"], t_lo=lo, t_hi=hi,
+                           num_particles=32, iterations=6, seed=7, stream=0, raster_mode=qpso.RASTER_EDGE)
+    res = gpu_ctx.solve(desc)
+    got = open(str(d / "res_edge" / ("img_0042.png-%d-bestpose.csv" % k))).read()
+    assert got == "%f,%f,%f,%f,%f,%f,%f,%f" % (res.fit, *res.pose)
+    gpu_ctx.frame_release(fid)
+    gpu_ctx.mesh_release(mid)
+
+
 def test_cli_unknown_cluster(files):
     d, w, s, obj = files
     r = run_cli(d, obj, "depth.bin", 999)
