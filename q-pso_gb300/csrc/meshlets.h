@@ -2,6 +2,7 @@
 // the fused kernels (plain C++, no CUDA).
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <unordered_map>
@@ -17,10 +18,20 @@ namespace qpso {
 // writes are atomic minima, the render AABB is a min/max).  After the last
 // payload the blob holds one object-space box per meshlet, two float4 (lo,
 // hi) at `box_off`, over the meshlet's vertices: the fused kernels project
-// its corners to skip meshlets that miss a tile band.
-constexpr int kMletFaces = 128;
-constexpr int kMletVerts = 128;
+// its corners to skip meshlets that miss a tile band.  After them come the
+// group boxes, the union of each run of kMletGroup meshlets' boxes, with
+// which a culled pass of a large mesh skips whole groups.
+constexpr int kMletFaces = 128;  // largest meshlet: faces
+constexpr int kMletVerts = 128;  // largest meshlet: unique vertices (vertex cache slots)
 constexpr int kMletBytes = kMletVerts * 16 + kMletFaces * 4;
+constexpr int kMletGroup = 16;   // meshlets per group box
+// Meshlet size by mesh size: meshes of up to kSmallMeshFaces faces are cut
+// into meshlets of 64 faces / 64 vertices (finer work items balance a
+// render over more warps, and a launch whose meshes are all small gets
+// 1 KB vertex caches per warp); larger meshes into 128 / 128, whose fewer
+// shared vertices and items cost less per face.
+constexpr uint32_t kSmallMeshFaces = 16384;
+inline int meshlet_cap(uint32_t num_faces) { return num_faces <= kSmallMeshFaces ? 64 : 128; }
 struct MeshletHdr {
   uint32_t off;
   uint16_t nv;
@@ -29,12 +40,12 @@ struct MeshletHdr {
 
 inline size_t mlet_align16(size_t x) { return (x + 15) / 16 * 16; }
 
-// Partition the faces into meshlets (kMletFaces faces, kMletVerts unique
-// vertices at most): vertices are deduplicated by exact bit pattern, then
+// Partition the faces into meshlets (`cap` faces and `cap` unique vertices
+// at most, cap <= kMletFaces): vertices are deduplicated by exact bit pattern, then
 // faces are grown breadth-first over shared vertices so that each meshlet
 // is a compact surface patch whose vertices are transformed once per pose.
 inline void build_meshlets(const float* soa, uint32_t F, std::vector<MeshletHdr>& hdr,
-                           std::vector<unsigned char>& blob, size_t* box_off) {
+                           std::vector<unsigned char>& blob, size_t* box_off, int cap = kMletFaces) {
   struct Key {
     uint32_t x, y, z;
     bool operator==(const Key& o) const { return x == o.x && y == o.y && z == o.z; }
@@ -88,12 +99,12 @@ inline void build_meshlets(const float* soa, uint32_t F, std::vector<MeshletHdr>
     std::vector<uint32_t> verts, faces;
     queue.clear();
     queue.push_back(seed);
-    for (size_t qi = 0; qi < queue.size() && faces.size() < (size_t)kMletFaces; ++qi) {
+    for (size_t qi = 0; qi < queue.size() && faces.size() < (size_t)cap; ++qi) {
       const uint32_t f = queue[qi];
       if (assigned[f]) continue;
       int fresh = 0;
       for (int j = 0; j < 3; ++j) fresh += stamp[fv[3 * (size_t)f + j]] != mid;
-      if (verts.size() + fresh > (size_t)kMletVerts) continue;
+      if (verts.size() + fresh > (size_t)cap) continue;
       assigned[f] = 1;
       faces.push_back(f);
       for (int j = 0; j < 3; ++j) {
@@ -130,7 +141,8 @@ inline void build_meshlets(const float* soa, uint32_t F, std::vector<MeshletHdr>
     ++mid;
   }
   *box_off = blob.size();
-  blob.resize(blob.size() + hdr.size() * 32, 0);
+  const size_t ng = (hdr.size() + kMletGroup - 1) / kMletGroup;
+  blob.resize(blob.size() + (hdr.size() + ng) * 32, 0);
   for (size_t i = 0; i < hdr.size(); ++i) {
     const float* pv = reinterpret_cast<const float*>(blob.data() + hdr[i].off);
     float b[8] = {pv[0], pv[1], pv[2], 0.f, pv[0], pv[1], pv[2], 0.f};
@@ -140,6 +152,21 @@ inline void build_meshlets(const float* soa, uint32_t F, std::vector<MeshletHdr>
         b[4 + c] = pv[4 * v + c] > b[4 + c] ? pv[4 * v + c] : b[4 + c];
       }
     std::memcpy(blob.data() + *box_off + 32 * i, b, 32);
+  }
+  // group boxes: the union of each run of kMletGroup consecutive meshlets'
+  // boxes (consecutive meshlets are neighbouring surface patches)
+  for (size_t g = 0; g < ng; ++g) {
+    float u[8];
+    std::memcpy(u, blob.data() + *box_off + 32 * (g * kMletGroup), 32);
+    for (size_t i = g * kMletGroup + 1; i < std::min(hdr.size(), (g + 1) * (size_t)kMletGroup); ++i) {
+      float b[8];
+      std::memcpy(b, blob.data() + *box_off + 32 * i, 32);
+      for (int c = 0; c < 3; ++c) {
+        u[c] = b[c] < u[c] ? b[c] : u[c];
+        u[4 + c] = b[4 + c] > u[4 + c] ? b[4 + c] : u[4 + c];
+      }
+    }
+    std::memcpy(blob.data() + *box_off + 32 * (hdr.size() + g), u, 32);
   }
 }
 

@@ -40,6 +40,7 @@ struct MeshObj {
   unsigned char* blob = nullptr;     // device
   uint32_t n_mlets = 0;
   size_t box_off = 0;                // per-meshlet boxes, bytes into blob
+  int mlet_cap = kMletVerts;         // meshlet size (faces, vertices) of this mesh
 };
 
 struct FrameObj {
@@ -164,10 +165,27 @@ double event_pairs_ms(qpso_context* ctx, size_t pairs) {
   return ms;
 }
 
-bool valid_cfg(const qpso_launch_config& c, int smem_optin) {
+// A launch shape is valid when its shared memory fits a CTA for meshlets of
+// vcap vertices (set_launch_config checks the smallest, 64; a launch checks
+// its meshes' own with fits_smem).
+bool valid_cfg(const qpso_launch_config& c, int smem_optin, int vcap = 64) {
   return c.threads >= 32 && c.threads <= 1024 && c.threads % 32 == 0 && c.tile_px >= 64 &&
          c.tile_px % 8 == 0 && c.ppb >= 1 && c.ppb <= 16 && c.threads >= 8 * c.ppb &&
-         fused_smem_bytes(c.threads, c.ppb, c.tile_px) <= (size_t)smem_optin;
+         fused_smem_bytes(c.threads, c.ppb, c.tile_px, vcap) <= (size_t)smem_optin;
+}
+
+int launch_vcap(const std::vector<const MeshObj*>& ms) {
+  int v = 64;
+  for (const MeshObj* m : ms) v = std::max(v, m->mlet_cap);
+  return v;
+}
+
+qpso_status fits_smem(qpso_context* ctx, const TileConfig& cfg, int vcap) {
+  if (fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap) > (size_t)ctx->smem_optin)
+    return fail(ctx, QPSO_ERR_ARG,
+                "launch config too large for meshes above 16384 faces (their 128-vertex meshlets need "
+                "larger vertex caches): choose fewer threads or a smaller tile");
+  return QPSO_OK;
 }
 
 qpso_status check_desc(qpso_context* ctx, const qpso_solve_desc& d, const MeshObj** m,
@@ -423,10 +441,12 @@ qpso_status qpso_mesh_upload(qpso_context* ctx, const float* soa, uint32_t F, ui
   std::vector<MeshletHdr> hdr;
   std::vector<unsigned char> blob;
   size_t box_off = 0;
-  build_meshlets(soa, F, hdr, blob, &box_off);
+  const int cap = meshlet_cap(F);
+  build_meshlets(soa, F, hdr, blob, &box_off, cap);
   MeshObj m;
   m.F = F;
   m.n_mlets = (uint32_t)hdr.size();
+  m.mlet_cap = cap;
   m.box_off = box_off;
   QPSO_CUDA(ctx, cudaMalloc(&m.d, 9 * (size_t)F * sizeof(float) + 32));
   cudaError_t e = cudaMalloc(&m.mlets, hdr.size() * sizeof(MeshletHdr));
@@ -650,6 +670,8 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
   qpso_status st = gather_descs(ctx, desc, 1, ds, ms, fs);
   if (st != QPSO_OK) return st;
   const TileConfig cfg = ctx->plain;
+  const int vcap = launch_vcap(ms);
+  if ((st = fits_smem(ctx, cfg, vcap)) != QPSO_OK) return st;
   const bool want_trace = trace != nullptr;
   Layout L = make_layout(ds, fs, 0, 0, want_trace);
   if ((st = ensure_ws(ctx, L.total)) != QPSO_OK) return st;
@@ -667,7 +689,7 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
   if (prof && (st = ensure_events(ctx, 2 * (size_t)desc->iterations)) != QPSO_OK) return st;
   for (uint32_t it = 0; it < desc->iterations; ++it) {
     if (prof) QPSO_CUDA(ctx, cudaEventRecord(ctx->ev[2 * it], s));
-    QPSO_CUDA(ctx, launch_step(dinst, it, chunks, cfg, s, desc->raster_mode == QPSO_RASTER_EDGE));
+    QPSO_CUDA(ctx, launch_step(dinst, it, chunks, cfg, s, desc->raster_mode == QPSO_RASTER_EDGE, vcap));
     if (prof) QPSO_CUDA(ctx, cudaEventRecord(ctx->ev[2 * it + 1], s));
   }
   QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
@@ -731,7 +753,9 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   if ((st = ensure_ws(ctx, L.total)) != QPSO_OK) return st;
   if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
   int per_sm = 0;
-  QPSO_CUDA(ctx, batch_max_grid(cfg, edge, &per_sm));
+  const int vcap = launch_vcap(ms);
+  if ((st = fits_smem(ctx, cfg, vcap)) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, batch_max_grid(cfg, edge, vcap, &per_sm));
   if (per_sm <= 0) return fail(ctx, QPSO_ERR_ARG, "batch launch config does not fit on an SM");
   const int grid = (int)std::min<size_t>(items.size(), (size_t)per_sm * ctx->num_sms);
   // wait before touching pinned staging that an earlier graph may read
@@ -746,7 +770,8 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   }
   std::vector<uint64_t> key = {(uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)h, L.total, L.meta_end,
                                n, items.size(), max_iters, (uint64_t)grid, (uint64_t)cfg.threads,
-                               (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h, (uint64_t)edge};
+                               (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h, (uint64_t)edge,
+                               (uint64_t)vcap};
   if (!ctx->gexec || key != ctx->gkey) {
     if (ctx->gexec) {
       cudaGraphExecDestroy(ctx->gexec);
@@ -766,7 +791,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     cudaError_t e = cudaMemcpyAsync(d, h, L.meta_end, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
       e = launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), (int)n, (int)max_w, (int)max_h, s);
-    if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s, edge);
+    if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s, edge, vcap);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h + L.hdr, d + L.hdr, n * sizeof(Header), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
@@ -811,9 +836,12 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
   if (!ctx || !descs || n == 0 || tune_iters == 0) return fail(ctx, QPSO_ERR_ARG, "bad autotune arguments");
   std::vector<qpso_solve_desc> ds(descs, descs + n);
   bool edge = false;
+  int vcap = 64;
   for (auto& d : ds) {
     d.iterations = std::min(d.iterations, tune_iters);
     edge = edge || d.raster_mode == QPSO_RASTER_EDGE;
+    auto mi = ctx->meshes.find(d.mesh_id);
+    if (mi != ctx->meshes.end()) vcap = std::max(vcap, mi->second.mlet_cap);
   }
   const TileConfig saved = batched ? ctx->batch : ctx->plain;
   TileConfig win = saved;
@@ -829,11 +857,11 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
     for (int tp : tiles)
       for (int pb : ppbs) {
         const qpso_launch_config c{th, tp, pb};
-        if (!valid_cfg(c, ctx->smem_optin)) continue;
+        if (!valid_cfg(c, ctx->smem_optin, vcap)) continue;
         const TileConfig tc{th, tp, pb};
         if (batched) {
           int per_sm = 0;
-          if (batch_max_grid(tc, edge, &per_sm) != cudaSuccess || per_sm <= 0) continue;
+          if (batch_max_grid(tc, edge, vcap, &per_sm) != cudaSuccess || per_sm <= 0) continue;
           ctx->batch = tc;
         } else {
           ctx->plain = tc;
@@ -884,6 +912,8 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
   QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const TileConfig cfg = ctx->plain;
+  const int vcap = launch_vcap(ms);
+  if ((st = fits_smem(ctx, cfg, vcap)) != QPSO_OK) return st;
   fill_meta(ctx, L, ds, ms, fs, {}, (uint32_t)cfg.ppb, false);
   char* d = static_cast<char*>(ctx->ws.p);
   char* h = static_cast<char*>(ctx->pin.p);
@@ -898,7 +928,7 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   QPSO_CUDA(ctx, launch_score_mlets(reinterpret_cast<const Instance*>(d + L.inst),
                                     reinterpret_cast<const float*>(d + pose_off), n,
                                     reinterpret_cast<float*>(d + fit_off), cfg, grid, s,
-                                    desc->raster_mode == QPSO_RASTER_EDGE));
+                                    desc->raster_mode == QPSO_RASTER_EDGE, vcap));
   QPSO_CUDA(ctx, cudaMemcpyAsync(fit_out, d + fit_off, (size_t)n * sizeof(float),
                                  cudaMemcpyDeviceToHost, s));
   QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
@@ -1063,6 +1093,7 @@ struct ServerReq {
   void* dmem = nullptr;
   size_t bytes = 0;
   uint32_t remaining = 0;
+  int vcap = 64;  // meshlet size of its mesh
 };
 
 size_t request_bytes(const qpso_solve_desc& d, const qpso_camera& c) {
@@ -1164,6 +1195,7 @@ void server_loop(qpso_server* s) {
         r.bytes = need;
         r.state = 1;
         r.remaining = r.desc.iterations;
+        r.vcap = m->mlet_cap;
         s->slot_req[slot] = rid;
         s->st.bytes_in_use += need;
         s->st.peak_bytes = std::max(s->st.peak_bytes, s->st.bytes_in_use);
@@ -1253,12 +1285,14 @@ void server_loop(qpso_server* s) {
     // work items of this epoch: every chunk of every active request
     uint32_t n_items = 0, K = s->cfg.iters_per_epoch;
     bool edge = false;
+    int vcap = 64;
     {
       std::lock_guard<std::mutex> g(s->mu);
       for (int slot : active) {
         const ServerReq& r = s->reqs[s->slot_req[slot]];
         K = std::min(K, r.remaining);
         edge = edge || r.desc.raster_mode == QPSO_RASTER_EDGE;
+        vcap = std::max(vcap, r.vcap);
         const uint32_t chunks = s->h_slots[slot].chunks;
         for (uint32_t c = 0; c < chunks; ++c) s->h_items[n_items++] = WorkItem{(uint32_t)slot, c};
       }
@@ -1267,7 +1301,7 @@ void server_loop(qpso_server* s) {
       e = cudaMemcpyAsync(s->d_items, s->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
                           s->stream);
     for (uint32_t k = 0; k < K && e == cudaSuccess; ++k)
-      e = launch_multi_step(s->d_slots, s->d_items, n_items, s->tc, s->stream, edge);
+      e = launch_multi_step(s->d_slots, s->d_items, n_items, s->tc, s->stream, edge, vcap);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s->h_hdr, s->d_hdr, S * sizeof(Header), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
@@ -1363,6 +1397,8 @@ qpso_status qpso_server_submit(qpso_server* s, const qpso_solve_desc* desc, uint
     st = check_desc(s->ctx, *desc, &m, &f);
   }
   if (st != QPSO_OK) return st;
+  if (fused_smem_bytes(s->tc.threads, s->tc.ppb, s->tc.tile_px, m->mlet_cap) > (size_t)s->ctx->smem_optin)
+    return fail(s->ctx, QPSO_ERR_ARG, "the server's launch config is too large for this mesh's meshlets");
   const uint32_t chunks = (desc->num_particles + s->tc.ppb - 1) / s->tc.ppb;
   if (request_bytes(*desc, f->cam) > s->st.budget_bytes || chunks * (uint64_t)s->cfg.max_slots > s->max_items)
     return QPSO_ERR_BUSY;

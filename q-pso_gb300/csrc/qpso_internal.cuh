@@ -87,23 +87,27 @@ cudaError_t launch_prep(const PrepDesc* jobs, int n, int max_w, int max_h, cudaS
 cudaError_t launch_mesh_aabb(const float* mesh, uint32_t F, float* out, cudaStream_t st);
 // `edge`: launch the kernel instance that also holds the EDGE raster (some
 // instance of the launch is in QPSO_RASTER_EDGE mode); the other instance
-// holds only the REF raster.
+// holds only the REF raster.  `vcap`: the largest meshlet (vertices) of the
+// launch's meshes, which sizes the per-warp vertex caches.
 cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, const TileConfig& cfg,
-                        cudaStream_t st, bool edge);
-cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, bool edge);
-cudaError_t batch_max_grid(const TileConfig& cfg, bool edge, int* blocks_per_sm);
+                        cudaStream_t st, bool edge, int vcap);
+cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, bool edge,
+                         int vcap);
+cudaError_t batch_max_grid(const TileConfig& cfg, bool edge, int vcap, int* blocks_per_sm);
 cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
                          const TileConfig& cfg, int grid, cudaStream_t st);
 cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
-                               const TileConfig& cfg, int grid, cudaStream_t st, bool edge);
-size_t fused_smem_bytes(int threads, int ppb, int tile_px);
+                               const TileConfig& cfg, int grid, cudaStream_t st, bool edge, int vcap);
+// Dynamic shared memory of the fused kernels; vcap: vertex cache slots per
+// warp, the largest meshlet of the launch's meshes (meshlet_cap()).
+size_t fused_smem_bytes(int threads, int ppb, int tile_px, int vcap);
 cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_t x0, int32_t y0,
                                  int32_t w, int32_t h, int32_t* out, int32_t* box, int threads,
                                  cudaStream_t st);
 cudaError_t launch_barrier_probe(uint32_t* bar, uint32_t* err, uint32_t grid, uint32_t expected,
                                  unsigned long long timeout_ns, cudaStream_t st);
 cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
-                              const TileConfig& cfg, cudaStream_t st, bool edge);
+                              const TileConfig& cfg, cudaStream_t st, bool edge, int vcap);
 cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* di, PrepDesc* dj,
                                 cudaStream_t st);
 cudaError_t launch_copy_flags(const uint32_t* src, uint32_t* dst, cudaStream_t st);

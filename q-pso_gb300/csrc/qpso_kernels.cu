@@ -97,11 +97,12 @@ struct PartCtl {
 };
 
 constexpr int kCullCap = 512;  // meshlets whose per-particle rectangles are kept
-constexpr int kLaneRasterMax = 32;  // larger face rectangles are rasterised by the whole warp
+constexpr int kLaneRasterMax = 64;  // larger face rectangles are rasterised by the whole warp
 
 // Dynamic shared memory of the fused kernels.
 struct FusedSmem {
-  int4* vcache;          // [warps][kMletVerts] snapped X, Y and depth bits, per warp
+  int4* vcache;          // [warps][vcap] snapped X, Y and depth bits, per warp
+  int vcap;              // vertex cache slots per warp: the launch's largest meshlet
   int4* mbox;            // [ppb][kCullCap] meshlet rectangles (minx, maxx, miny, maxy)
   uint32_t* live;        // [ppb * kCullCap] listed items of a culled pass (particle << 28 | meshlet)
   int32_t* tiles;        // [ppb][tile_px] depth tiles
@@ -112,6 +113,7 @@ struct SmemCtl {
   int32_t bound[4];
   uint32_t claim;
   uint32_t n_live;     // listed items of the current pass and meshlet chunk
+  uint8_t grp_live[kMaxPpb][kCullCap / kMletGroup];  // groups of a chunk that meet the band
   uint32_t next_item;  // items claimed so far beyond each warp's first
   int last;
   int maxpass;
@@ -390,11 +392,12 @@ __device__ __forceinline__ void plan_tiles(PartCtl& pc, int tile_px) {
   pc.npass = (pc.ncol * pc.nrow) > 0 ? pc.ncol * pc.nrow : 1;
 }
 
-__device__ __forceinline__ FusedSmem carve_smem(unsigned char* dyn, int ppb) {
+__device__ __forceinline__ FusedSmem carve_smem(unsigned char* dyn, int ppb, int vcap) {
   FusedSmem sm;
   size_t o = 0;
   sm.vcache = reinterpret_cast<int4*>(dyn + o);
-  o += (size_t)(blockDim.x >> 5) * kMletVerts * 16;
+  sm.vcap = vcap;
+  o += (size_t)(blockDim.x >> 5) * vcap * 16;
   sm.mbox = reinterpret_cast<int4*>(dyn + o);
   o += (size_t)ppb * kCullCap * 16;
   sm.live = reinterpret_cast<uint32_t*>(dyn + o);
@@ -474,16 +477,21 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
     for (int i = tid; i < np * (int)nm; i += T)
       mbox[(i / nm) * kCullCap + (i % nm)] = make_int4(kAabbInitMin, kAabbInitMax, kAabbInitMin, kAabbInitMax);
   __syncthreads();
+  // (group boxes would be cheaper for large meshes, but their looser
+  // bound costs more tile passes than the projections save)
+  const float4* grp_box = I.mlet_box + 2 * nm;
+  const uint32_t nbox = nm;
+  const float4* boxes = I.mlet_box;
   for (int k = 0; k < np; ++k) {
     PartCtl& pc = ctl.part[k];
-    const uint32_t n8 = nm * 8u;
+    const uint32_t n8 = nbox * 8u;
     for (uint32_t b = (uint32_t)(tid & ~31); b < n8; b += (uint32_t)T) {  // whole warps
-      // lanes 8j..8j+7 project the corners of one meshlet's box
+      // lanes 8j..8j+7 project the corners of one box
       const uint32_t i = b + (uint32_t)lane, m = i >> 3, c = i & 7u;
       float u = 0.f, v = 0.f;
       bool ok = true;
-      if (m < nm) {
-        const float4 blo = __ldg(I.mlet_box + 2 * m), bhi = __ldg(I.mlet_box + 2 * m + 1);
+      if (m < nbox) {
+        const float4 blo = __ldg(boxes + 2 * m), bhi = __ldg(boxes + 2 * m + 1);
         float zz;
         project(ctl.pose[k], (c & 1u) ? bhi.x : blo.x, (c & 2u) ? bhi.y : blo.y, (c & 4u) ? bhi.z : blo.z, I.cam,
                 u, v, zz);
@@ -499,7 +507,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
       }
       ok = ((__ballot_sync(0xffffffffu, !ok) >> (lane & ~7)) & 0xffu) == 0u;
       int32_t rx0 = INT32_MAX, rx1 = INT32_MIN, ry0 = INT32_MAX, ry1 = INT32_MIN;
-      if (m < nm) {
+      if (m < nbox) {
         // the rectangle of box_rect(); a box that bounds nothing stands for
         // the whole domain
         const int4 r = ok ? make_int4(clamp_px(floorf(ulo) - 1.0f, dx0, dx1), clamp_px(floorf(uhi) + 2.0f, dx0, dx1),
@@ -583,11 +591,29 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
     //     time), then the warps share out the listed items.
     const bool cull = pass > 0;
     const bool check_boxes = !cull_ok && maxpass > 1;
-    int4* vc = vcache + wid * kMletVerts;
+    int4* vc = vcache + wid * sm.vcap;
     for (uint32_t mc = 0; mc < (cull ? nm : 1u); mc += (uint32_t)kCullCap) {
       uint32_t n_items = (uint32_t)np * nm;
       if (cull) {
         const uint32_t nmc = min((uint32_t)kCullCap, nm - mc);
+        if (!cull_ok) {
+          // meshes above kCullCap meshlets: first the groups of this chunk
+          // (kCullCap / kMletGroup per particle) that meet the band, so that
+          // only their meshlets' boxes are projected
+          const uint32_t g0 = mc / kMletGroup, gn = (nmc + kMletGroup - 1) / kMletGroup;
+          for (uint32_t i = (uint32_t)tid; i < (uint32_t)np * gn; i += (uint32_t)T) {
+            const uint32_t k = i / gn, g = g0 + (i - k * gn);
+            const PartCtl& pc = ctl.part[k];
+            bool ov = false;
+            if (pass < pc.npass) {
+              int4 r;
+              ov = !box_rect(ctl.pose[k], I.cam, __ldg(grp_box + 2 * g), __ldg(grp_box + 2 * g + 1), dx0, dx1,
+                             dy0, dy1, r) ||
+                   rect_overlaps(r, pc);
+            }
+            ctl.grp_live[k][i - k * gn] = ov ? 1 : 0;
+          }
+        }
         const uint32_t nt = (uint32_t)np * nmc;
         if (tid == 0) {
           ctl.n_live = 0;
@@ -605,7 +631,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
             if (pass < pc.npass) {
               if (cull_ok) {
                 ov = rect_overlaps(mbox[k * kCullCap + m], pc);
-              } else {
+              } else if (ctl.grp_live[k][(m - mc) / kMletGroup]) {
                 int4 r;
                 ov = !box_rect(ctl.pose[k], I.cam, __ldg(I.mlet_box + 2 * m), __ldg(I.mlet_box + 2 * m + 1),
                                dx0, dx1, dy0, dy1, r) ||
@@ -977,7 +1003,7 @@ __device__ __forceinline__ void render_score_mlets(const Instance& I, int np, co
 // PSO step + render + score + personal best for one work item.
 template <bool kAllowEdge>
 __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, unsigned char* dyn,
-                             int tile_px, SmemCtl& ctl) {
+                             int tile_px, int vcap, SmemCtl& ctl) {
   const int tid = threadIdx.x;
   const uint32_t P = I.prm.num_particles;
   const uint32_t p0 = chunk * I.ppb;
@@ -1009,7 +1035,7 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
     }
   }
   __syncthreads();
-  render_score_mlets<kAllowEdge>(I, (int)np, carve_smem(dyn, (int)I.ppb), tile_px, ctl, ctl.argv);
+  render_score_mlets<kAllowEdge>(I, (int)np, carve_smem(dyn, (int)I.ppb, vcap), tile_px, ctl, ctl.argv);
   if (tid < (int)np) {
     const uint32_t p = p0 + tid;
     const float fv = ctl.argv[tid];
@@ -1025,8 +1051,8 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
 
 // Shared memory of the fused kernels: one vertex cache per warp, ppb
 // meshlet-rectangle tables, ppb depth tiles.
-size_t fused_smem_bytes(int threads, int ppb, int tile_px) {
-  return (size_t)(threads / 32) * kMletVerts * 16 + (size_t)ppb * kCullCap * 20 +
+size_t fused_smem_bytes(int threads, int ppb, int tile_px, int vcap) {
+  return (size_t)(threads / 32) * vcap * 16 + (size_t)ppb * kCullCap * 20 +
          (size_t)ppb * tile_px * 4;
 }
 
@@ -1099,11 +1125,11 @@ __device__ void instance_epilogue(const Instance& I, uint32_t iter, SmemCtl& ctl
 // Plain form: one launch per iteration of one instance, one CTA per chunk.
 template <bool kAllowEdge>
 __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* __restrict__ inst,
-                                                                uint32_t iter, int tile_px) {
+                                                                uint32_t iter, int tile_px, int vcap) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
   const Instance& I = *inst;
-  process_item<kAllowEdge>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
+  process_item<kAllowEdge>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
   instance_epilogue(I, iter, ctl);
 }
 
@@ -1115,13 +1141,13 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* 
 template <bool kAllowEdge>
 __global__ void __launch_bounds__(kMaxThreads) qpso_multi_step_kernel(Instance* __restrict__ slots,
                                                                       const WorkItem* __restrict__ items,
-                                                                      int tile_px) {
+                                                                      int tile_px, int vcap) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
   const WorkItem it = items[blockIdx.x];
   Instance& I = slots[it.inst];
   const uint32_t iter = __ldcg(&I.cur_iter);
-  process_item<kAllowEdge>(I, it.chunk, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
+  process_item<kAllowEdge>(I, it.chunk, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
   instance_epilogue(I, iter, ctl);
   if (ctl.last && threadIdx.x == 0) I.cur_iter = iter + 1;
 }
@@ -1168,7 +1194,7 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t* err, unsigned long long ti
 // CTAs claim work items (largest first) from a per-step counter, and the
 // last chunk of an instance updates its global best before the barrier.
 template <bool kAllowEdge>
-__global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, int tile_px) {
+__global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, int tile_px, int vcap) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
   for (uint32_t s = 0; s < A.max_iters; ++s) {
@@ -1181,7 +1207,7 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, in
       const WorkItem it = A.items[k];
       const Instance& I = A.inst[it.inst];
       if (s >= I.prm.iterations) continue;
-      process_item<kAllowEdge>(I, it.chunk, s, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, ctl);
+      process_item<kAllowEdge>(I, it.chunk, s, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
       instance_epilogue(I, s, ctl);
     }
     if (s + 1 < A.max_iters && !grid_barrier(A.barrier, A.err, A.timeout_ns)) return;
@@ -1424,12 +1450,12 @@ template <bool kAllowEdge>
 __global__ void __launch_bounds__(kMaxThreads) score_poses_mlet_kernel(const Instance* __restrict__ inst,
                                                                        const float* __restrict__ poses,
                                                                        uint32_t n, int tile_px,
-                                                                       float* __restrict__ fit_out) {
+                                                                       float* __restrict__ fit_out, int vcap) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
   const Instance& I = *inst;
   unsigned char* dyn = reinterpret_cast<unsigned char*>(dyn_smem);
-  const FusedSmem sm = carve_smem(dyn, (int)I.ppb);
+  const FusedSmem sm = carve_smem(dyn, (int)I.ppb, vcap);
   const uint32_t groups = (n + I.ppb - 1) / I.ppb;
   for (uint32_t gi = blockIdx.x; gi < groups; gi += gridDim.x) {
     const uint32_t k0 = gi * I.ppb;
@@ -1514,25 +1540,26 @@ cudaError_t launch_mesh_aabb(const float* mesh, uint32_t F, float* out, cudaStre
 }
 
 cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, const TileConfig& cfg,
-                        cudaStream_t st, bool edge) {
-  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
+                        cudaStream_t st, bool edge, int vcap) {
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
   auto* k = edge ? qpso_step_kernel<true> : qpso_step_kernel<false>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  k<<<chunks, cfg.threads, smem, st>>>(inst, iter, cfg.tile_px);
+  k<<<chunks, cfg.threads, smem, st>>>(inst, iter, cfg.tile_px, vcap);
   return cudaGetLastError();
 }
 
-cudaError_t batch_max_grid(const TileConfig& cfg, bool edge, int* blocks_per_sm) {
-  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
+cudaError_t batch_max_grid(const TileConfig& cfg, bool edge, int vcap, int* blocks_per_sm) {
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
   auto* k = edge ? qpso_batch_kernel<true> : qpso_batch_kernel<false>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, cfg.threads, smem);
 }
 
-cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, bool edge) {
-  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
+cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, bool edge,
+                         int vcap) {
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
   auto* k = edge ? qpso_batch_kernel<true> : qpso_batch_kernel<false>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
@@ -1546,7 +1573,7 @@ cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg,
   attr[0].val.cooperative = 1;
   lc.attrs = attr;
   lc.numAttrs = 1;
-  return cudaLaunchKernelEx(&lc, k, args, cfg.tile_px);
+  return cudaLaunchKernelEx(&lc, k, args, cfg.tile_px, vcap);
 }
 
 cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
@@ -1714,12 +1741,12 @@ cudaError_t launch_cluster_stats(const uint16_t* depth, const int32_t* labels, i
 }
 
 cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
-                               const TileConfig& cfg, int grid, cudaStream_t st, bool edge) {
-  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
+                               const TileConfig& cfg, int grid, cudaStream_t st, bool edge, int vcap) {
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
   auto* k = edge ? score_poses_mlet_kernel<true> : score_poses_mlet_kernel<false>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  k<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out);
+  k<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out, vcap);
   return cudaGetLastError();
 }
 
@@ -1734,13 +1761,13 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
 }
 
 cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
-                              const TileConfig& cfg, cudaStream_t st, bool edge) {
+                              const TileConfig& cfg, cudaStream_t st, bool edge, int vcap) {
   if (n_items == 0) return cudaSuccess;
-  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px);
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
   auto* k = edge ? qpso_multi_step_kernel<true> : qpso_multi_step_kernel<false>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  k<<<n_items, cfg.threads, smem, st>>>(slots, items, cfg.tile_px);
+  k<<<n_items, cfg.threads, smem, st>>>(slots, items, cfg.tile_px, vcap);
   return cudaGetLastError();
 }
 

@@ -1,8 +1,10 @@
 // Checks the meshlet partition (q-pso_gb300/csrc/meshlets.h) of a mesh read
 // from a binary file of 9*F floats (loadOBJ3 layout): every face exactly
 // once, caps respected, local ids inside the meshlet, positions preserved,
-// each meshlet's box the exact bounds of its vertices.
-// Prints "faces meshlets unique_vertex_slots".
+// each meshlet's box the exact bounds of its vertices, each group box the
+// union of its meshlets' boxes.
+// Prints "faces meshlets unique_vertex_slots cap".
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -22,8 +24,23 @@ int main(int argc, char** argv) {
   std::vector<qpso::MeshletHdr> hdr;
   std::vector<unsigned char> blob;
   size_t box_off = 0;
-  qpso::build_meshlets(soa.data(), F, hdr, blob, &box_off);
-  if (box_off % 16 != 0 || blob.size() != box_off + 32 * hdr.size()) return 7;
+  const int cap = qpso::meshlet_cap(F);
+  qpso::build_meshlets(soa.data(), F, hdr, blob, &box_off, cap);
+  const size_t ng = (hdr.size() + qpso::kMletGroup - 1) / qpso::kMletGroup;
+  if (box_off % 16 != 0 || blob.size() != box_off + 32 * (hdr.size() + ng)) return 7;
+  // every group box is the union of its meshlets' boxes
+  const float* boxes = reinterpret_cast<const float*>(blob.data() + box_off);
+  for (size_t g = 0; g < ng; ++g) {
+    float u[6] = {3e38f, 3e38f, 3e38f, -3e38f, -3e38f, -3e38f};
+    for (size_t i = g * qpso::kMletGroup; i < hdr.size() && i < (g + 1) * qpso::kMletGroup; ++i)
+      for (int c = 0; c < 3; ++c) {
+        u[c] = std::min(u[c], boxes[8 * i + c]);
+        u[3 + c] = std::max(u[3 + c], boxes[8 * i + 4 + c]);
+      }
+    const float* gb = boxes + 8 * (hdr.size() + g);
+    for (int c = 0; c < 3; ++c)
+      if (gb[c] != u[c] || gb[4 + c] != u[3 + c]) return 9;
+  }
   // multiset of faces as (x,y,z) x 3 -> compare counts by summing a hash
   uint64_t want = 0, got = 0, slots = 0, faces = 0;
   auto fh = [](const float* a, const float* b, const float* c) {
@@ -47,7 +64,7 @@ int main(int argc, char** argv) {
     want += fh(a, b, c);
   }
   for (const auto& h : hdr) {
-    if (h.nv == 0 || h.nf == 0 || h.nv > qpso::kMletVerts || h.nf > qpso::kMletFaces) return 3;
+    if (h.nv == 0 || h.nf == 0 || h.nv > cap || h.nf > cap) return 3;
     if (h.off % 16 != 0) return 4;
     const float* pv = reinterpret_cast<const float*>(blob.data() + h.off);
     const uint32_t* pf = reinterpret_cast<const uint32_t*>(blob.data() + h.off + h.nv * 16);
@@ -70,6 +87,6 @@ int main(int argc, char** argv) {
     faces += h.nf;
   }
   if (faces != F || got != want) return 6;
-  std::printf("%u %zu %llu\n", F, hdr.size(), (unsigned long long)slots);
+  std::printf("%u %zu %llu %d\n", F, hdr.size(), (unsigned long long)slots, cap);
   return 0;
 }

@@ -1,7 +1,8 @@
 """The meshlet partition built at mesh upload keeps every face exactly once,
-respects its caps (128 faces, 128 unique vertices), shares vertices (the
-fused kernels transform each meshlet vertex once per pose) and stores each
-meshlet's exact object-space box."""
+respects its caps (64 faces and vertices for meshes up to 16384 faces, 128
+above), shares vertices (the fused kernels transform each meshlet vertex once
+per pose) and stores each meshlet's exact object-space box and the group
+boxes."""
 import os
 import subprocess
 
@@ -29,9 +30,10 @@ def test_partition(checker, tmp_path, kind, n):
     soa.astype(np.float32).tofile(path)
     out = subprocess.run([checker, str(path)], capture_output=True, text=True)
     assert out.returncode == 0, out.returncode
-    faces, mlets, slots = map(int, out.stdout.split())
+    faces, mlets, slots, cap = map(int, out.stdout.split())
     assert faces == F
-    assert mlets >= (F + 127) // 128
+    assert cap == (64 if F <= 16384 else 128)
+    assert mlets >= (F + cap - 1) // cap
     # vertex sharing: well below 3 transforms per face on closed meshes
     if F >= 1000:
         assert slots / F < 0.8, slots / F
@@ -46,5 +48,5 @@ def test_partition_of_unshared_triangles(checker, tmp_path):
     soa.tofile(path)
     out = subprocess.run([checker, str(path)], capture_output=True, text=True)
     assert out.returncode == 0
-    faces, mlets, slots = map(int, out.stdout.split())
-    assert faces == F and slots == 3 * F and mlets >= (3 * F + 127) // 128
+    faces, mlets, slots, cap = map(int, out.stdout.split())
+    assert faces == F and slots == 3 * F and mlets >= (3 * F + cap - 1) // cap
