@@ -355,7 +355,7 @@ def run_ours(args, ws, rank, local):
     else:
         tune = descs[::max(1, len(descs) // 16)][:16]
         tune_iters = 4 if args.workload == "c5" else 30
-        plain_cfg, _ = ctx.autotune(tune[:4], batched=False, tune_iters=tune_iters)
+        plain_cfg, _ = ctx.autotune(tune[::max(1, len(tune) // 4)][:4], batched=False, tune_iters=tune_iters)
         batch_cfg, _ = ctx.autotune(tune, batched=True, tune_iters=tune_iters)
 
     main_fn, alt_fn = (step_batch, step_plain) if batched_default else (step_plain, step_batch)

@@ -171,6 +171,11 @@ void qpso_solve_desc_init(qpso_solve_desc *desc);
 void qpso_box_from_centroid(const float centroid_mm[3], float bound, float bound_z,
                             float t_lo[3], float t_hi[3]);
 
+/* Launch shapes of the plain and batched paths.  A shape is accepted when
+ * its shared memory fits a CTA with the vertex caches of meshes of up to
+ * 16384 faces; a launch over a larger mesh (128-vertex meshlets) that would
+ * not fit halves the tile, then the threads, until it does.  Results do not
+ * depend on the launch shape. */
 qpso_status qpso_set_launch_config(qpso_context *ctx, const qpso_launch_config *plain,
                                    const qpso_launch_config *batch);
 qpso_status qpso_get_launch_config(const qpso_context *ctx, qpso_launch_config *plain,

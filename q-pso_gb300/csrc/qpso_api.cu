@@ -180,11 +180,27 @@ int launch_vcap(const std::vector<const MeshObj*>& ms) {
   return v;
 }
 
-qpso_status fits_smem(qpso_context* ctx, const TileConfig& cfg, int vcap) {
-  if (fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap) > (size_t)ctx->smem_optin)
-    return fail(ctx, QPSO_ERR_ARG,
-                "launch config too large for meshes above 16384 faces (their 128-vertex meshlets need "
-                "larger vertex caches): choose fewer threads or a smaller tile");
+// The launch shape a launch uses: the installed one, or, when meshes above
+// 16384 faces (128-vertex meshlets, larger vertex caches) push its shared
+// memory past the CTA limit, the same shape with the tile halved (then the
+// threads halved) until it fits.  Results do not depend on the shape; the
+// particles per work item stay, so work items and chunks do too.
+bool shrink_cfg(TileConfig& cfg, int vcap, int smem_optin) {
+  while (fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap) > (size_t)smem_optin) {
+    if (cfg.tile_px >= 2 * 1024) {
+      cfg.tile_px = cfg.tile_px / 16 * 8;
+    } else if (cfg.threads / 2 >= std::max(32, 8 * cfg.ppb) && cfg.threads % 64 == 0) {
+      cfg.threads /= 2;
+    } else {
+      return false;
+    }
+  }
+  return true;
+}
+
+qpso_status fit_cfg(qpso_context* ctx, TileConfig& cfg, int vcap) {
+  if (!shrink_cfg(cfg, vcap, ctx->smem_optin))
+    return fail(ctx, QPSO_ERR_ARG, "launch config cannot fit the meshes' vertex caches");
   return QPSO_OK;
 }
 
@@ -669,9 +685,9 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
   std::vector<const FrameObj*> fs;
   qpso_status st = gather_descs(ctx, desc, 1, ds, ms, fs);
   if (st != QPSO_OK) return st;
-  const TileConfig cfg = ctx->plain;
+  TileConfig cfg = ctx->plain;
   const int vcap = launch_vcap(ms);
-  if ((st = fits_smem(ctx, cfg, vcap)) != QPSO_OK) return st;
+  if ((st = fit_cfg(ctx, cfg, vcap)) != QPSO_OK) return st;
   const bool want_trace = trace != nullptr;
   Layout L = make_layout(ds, fs, 0, 0, want_trace);
   if ((st = ensure_ws(ctx, L.total)) != QPSO_OK) return st;
@@ -728,7 +744,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   std::vector<const FrameObj*> fs;
   qpso_status st = gather_descs(ctx, descs, n, ds, ms, fs);
   if (st != QPSO_OK) return st;
-  const TileConfig cfg = ctx->batch;
+  TileConfig cfg = ctx->batch;
   // work items: every chunk of every instance, most expensive first
   std::vector<uint32_t> order(n);
   std::vector<double> cost(n);
@@ -754,7 +770,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
   int per_sm = 0;
   const int vcap = launch_vcap(ms);
-  if ((st = fits_smem(ctx, cfg, vcap)) != QPSO_OK) return st;
+  if ((st = fit_cfg(ctx, cfg, vcap)) != QPSO_OK) return st;
   QPSO_CUDA(ctx, batch_max_grid(cfg, edge, vcap, &per_sm));
   if (per_sm <= 0) return fail(ctx, QPSO_ERR_ARG, "batch launch config does not fit on an SM");
   const int grid = (int)std::min<size_t>(items.size(), (size_t)per_sm * ctx->num_sms);
@@ -911,9 +927,9 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   if ((st = ensure_ws(ctx, total)) != QPSO_OK) return st;
   if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
   QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  const TileConfig cfg = ctx->plain;
+  TileConfig cfg = ctx->plain;
   const int vcap = launch_vcap(ms);
-  if ((st = fits_smem(ctx, cfg, vcap)) != QPSO_OK) return st;
+  if ((st = fit_cfg(ctx, cfg, vcap)) != QPSO_OK) return st;
   fill_meta(ctx, L, ds, ms, fs, {}, (uint32_t)cfg.ppb, false);
   char* d = static_cast<char*>(ctx->ws.p);
   char* h = static_cast<char*>(ctx->pin.p);
@@ -1300,8 +1316,10 @@ void server_loop(qpso_server* s) {
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s->d_items, s->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
                           s->stream);
+    TileConfig tc = s->tc;  // fits every vcap (checked at submit)
+    shrink_cfg(tc, vcap, s->ctx->smem_optin);
     for (uint32_t k = 0; k < K && e == cudaSuccess; ++k)
-      e = launch_multi_step(s->d_slots, s->d_items, n_items, s->tc, s->stream, edge, vcap);
+      e = launch_multi_step(s->d_slots, s->d_items, n_items, tc, s->stream, edge, vcap);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s->h_hdr, s->d_hdr, S * sizeof(Header), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
@@ -1397,8 +1415,9 @@ qpso_status qpso_server_submit(qpso_server* s, const qpso_solve_desc* desc, uint
     st = check_desc(s->ctx, *desc, &m, &f);
   }
   if (st != QPSO_OK) return st;
-  if (fused_smem_bytes(s->tc.threads, s->tc.ppb, s->tc.tile_px, m->mlet_cap) > (size_t)s->ctx->smem_optin)
-    return fail(s->ctx, QPSO_ERR_ARG, "the server's launch config is too large for this mesh's meshlets");
+  TileConfig fit = s->tc;
+  if (!shrink_cfg(fit, m->mlet_cap, s->ctx->smem_optin))
+    return fail(s->ctx, QPSO_ERR_ARG, "the server's launch config cannot fit this mesh's vertex caches");
   const uint32_t chunks = (desc->num_particles + s->tc.ppb - 1) / s->tc.ppb;
   if (request_bytes(*desc, f->cam) > s->st.budget_bytes || chunks * (uint64_t)s->cfg.max_slots > s->max_items)
     return QPSO_ERR_BUSY;
