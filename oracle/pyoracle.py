@@ -23,7 +23,10 @@ _u16 = C.POINTER(C.c_uint16)
 
 class Camera(C.Structure):
     _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
-                ("width", C.c_int32), ("height", C.c_int32)]
+                ("width", C.c_int32), ("height", C.c_int32), ("proj", C.c_int32)]
+
+
+PROJ_FP32, PROJ_REF_ACCV = 0, 1
 
 
 class Params(C.Structure):
@@ -104,8 +107,14 @@ def ptr(a: np.ndarray, t):
     return a.ctypes.data_as(t)
 
 
-def camera(fx=525.0, fy=525.0, cx=319.5, cy=239.5, width=640, height=480) -> Camera:
-    return Camera(fx, fy, cx, cy, width, height)
+def camera(fx=525.0, fy=525.0, cx=319.5, cy=239.5, width=640, height=480, proj=PROJ_FP32) -> Camera:
+    return Camera(fx, fy, cx, cy, width, height, proj)
+
+
+def camera_ref_accv() -> Camera:
+    """The reference's compiled-in ACCV camera (main.h:30-33), projected in
+    double as its kernels do."""
+    return Camera(572.41140, 573.57043, 325.26110, 242.04899, 640, 480, PROJ_REF_ACCV)
 
 
 def default_params() -> Params:

@@ -398,8 +398,14 @@ void qo_project(const float *s, const float v[3], const qo_camera *cam, float o[
     p[1] = p[1] + s[TY];
     p[2] = p[2] + s[TZ];
     const float rz = 1.0f / p[2];
-    o[0] = fmaf(cam->fx, p[0] * rz, cam->cx);
-    o[1] = fmaf(cam->fy, p[1] * rz, cam->cy);
+    if (cam->proj == QO_PROJ_REF_ACCV) {
+        /* main.h:537-539 with FX, FY, CX, CY of main.h:30-33 */
+        o[0] = (float)(325.26110 + 572.41140 * (double)(p[0] * rz));
+        o[1] = (float)(242.04899 + 573.57043 * (double)(p[1] * rz));
+    } else {
+        o[0] = fmaf(cam->fx, p[0] * rz, cam->cx);
+        o[1] = fmaf(cam->fy, p[1] * rz, cam->cy);
+    }
     o[2] = 1000.0f * p[2];
 }
 

@@ -48,7 +48,16 @@ extern "C" {
 typedef struct {
     float fx, fy, cx, cy;
     int32_t width, height;
+    /* QO_PROJ_FP32: u = fmaf(fx, x/z, cx) with the fields above (the
+     * kernels' contract).  QO_PROJ_REF_ACCV: the reference's own
+     * expression with its compiled-in double ACCV intrinsics (main.h:30-33),
+     * u = (float)(CX + FX * (double)(x/z)), fx..cy ignored; used to check
+     * the reference's kernels rebuilt for the GPU. */
+    int32_t proj;
 } qo_camera;
+
+#define QO_PROJ_FP32 0
+#define QO_PROJ_REF_ACCV 1
 
 /* Per-solve constants: QPSOParams_t (main.h:182-204) plus the compile-time
  * macros of main.h:83-136 that this build makes runtime parameters. */

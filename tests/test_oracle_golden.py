@@ -182,6 +182,16 @@ def test_projection_matches_reference_double_path(ref):
         assert abs(o[1] - want[1]) <= 4 * np.spacing(np.float32(abs(want[1]))) + 1e-4
 
 
+def test_reference_camera_projection_bit_exact(ref):
+    """With the reference's own ACCV camera (projected in double, as its
+    kernels rebuilt for the GPU do) the oracle's projection equals the
+    reference's projectModelPointsToPixels bit for bit."""
+    cam = po.camera_ref_accv()
+    for i in range(len(ref["proj"])):
+        o = po.project(ref["proj_pose"][i], ref["proj_pt"][i], cam)
+        np.testing.assert_array_equal(np.asarray(o, np.float32), np.asarray(ref["proj"][i][:3], np.float32))
+
+
 def test_oracle_c1_solve_is_frozen():
     """The oracle's own C1 solve reproduces its committed trace bit for bit."""
     import scene
