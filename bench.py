@@ -238,6 +238,111 @@ def cpu_baseline(w, budget_s: float = 12.0):
             "particle_renders_per_s": renders / dt}
 
 
+# the ACCV intrinsics compiled into the reference's kernels (main.h:30-33)
+ACCV = (572.41140, 573.57043, 325.26110, 242.04899)
+REF_PARTICLES, REF_ITERATIONS = 1024, 20  # Nparticle_ and max_steps_, main.h:84, 97
+
+
+def reference_shape(w):
+    """The reference's own solve shape (1024 particles x 20 iterations, ACCV
+    camera) on the workload's first mesh and first solve's cluster, with a
+    translation box around (0, 0, 0.9 m) that keeps every particle's mesh
+    8 px inside the image at any rotation (the reference's raster does not
+    clip): a vertex lies within r of the translation, r the largest
+    object-space corner norm, so (b + r) / (z_lo - r) bounds x/z."""
+    soa, F = w["meshes"][0]
+    m = np.asarray(soa, np.float64).reshape(3, 3 * F)
+    r = float(np.linalg.norm(np.maximum(np.abs(m.min(axis=1)), np.abs(m.max(axis=1)))))
+    fx, fy, cx, cy = ACCV
+    zc = 0.9
+    zmin = zc - 0.1 - r
+    bx = 0.9 * (min(cx, 640 - cx) - 8) / fx * zmin - r
+    by = 0.9 * (min(cy, 480 - cy) - 8) / fy * zmin - r
+    if F > 64 * 512 or min(bx, by) < 0.02:
+        return None  # beyond the render's 64 block slots, or too large to stay in frame
+    s = w["solves"][0]
+    c = s["cluster"]
+    x0, x1, y0, y1 = c["aabb"]
+    return {"mesh": 0, "faces": F, "frame": s["frame"], "label": c["label"],
+            "t_lo": (-bx, -by, zc - 0.1), "t_hi": (bx, by, zc + 0.1), "num_points": c["num_points"],
+            "aabb": (x0, min(x1, 639), y0, min(y1, 479)), "seed": s["seed"], "stream": s["stream"],
+            "desc": "first mesh of the workload (%d faces), its first cluster, %d particles x %d "
+                    "iterations, ACCV camera, translation box +-(%.3f, %.3f) m around (0, 0, 0.9) m, "
+                    "+-0.1 m in z" % (F, REF_PARTICLES, REF_ITERATIONS, bx, by)}
+
+
+def reference_kernels_gb300(w):
+    """The reference's own CUDA kernels (main.h + main.cu:72-1195 built with
+    its Makefile's -use_fast_math -O3 for sm_103a) running its host loop
+    (main.cu:1601-1727) on this GPU for the reference-shaped solve, the
+    oracle's Philox draws in its uniform table."""
+    from oracle import refgpu
+
+    if not refgpu.available("fast"):
+        return {"unavailable": "reference kernels not built: the reference sources were absent "
+                               "where the repository was built"}
+    sh = reference_shape(w)
+    if sh is None:
+        return {"unavailable": "does not apply: the reference's render grid holds at most 32768 "
+                               "faces (64 block slots of 512 per particle, main.h:1290-1293)"}
+    soa, F = w["meshes"][sh["mesh"]]
+    dep, lab, _ = w["frames"][sh["frame"]]
+    obs = np.where(lab == sh["label"], dep, 0).astype(np.int32)
+    try:
+        with refgpu.RefKernels("fast") as rk:
+            rk.set_scene(soa, F, obs, sh["t_lo"], sh["t_hi"], sh["num_points"], sh["aabb"])
+            rk.set_rand_table(refgpu.uniform_table(sh["seed"], sh["stream"]))
+            rk.solve(2)  # warm-up
+            out = rk.solve(REF_ITERATIONS)
+    except Exception as e:  # a baseline, not the product: report, do not fail the arm
+        return {"unavailable": "reference kernels failed: %s" % e}
+    done, ms = out["done"], out["ms"]
+    res = {"build": "reference main.h + main.cu:72-1195, -use_fast_math -O3, sm_103a; host loop "
+                    "main.cu:1601-1727 (1024 render + 1024 fitness launches per iteration on 16 "
+                    "streams, thrust::min_element, best and particle updates)",
+           "config": sh["desc"], "render_grid": [max(6, -(-F // 512)), 512],
+           "iterations_done": done, "ms_per_iteration": ms / max(done, 1),
+           "particle_renders_per_s": REF_PARTICLES * done / (ms / 1000.0) if ms > 0 else None,
+           "best_fit": float(out["trace"][-1]) if done else None}
+    if done == REF_ITERATIONS:
+        res.update(value=1000.0 / ms, unit="solves/s", ms_per_solve=ms)
+    else:
+        res["stopped"] = out["error"]
+    return res
+
+
+def reference_shape_ours(ctx, w, repeats: int = 3):
+    """The reference-shaped solve through this library's plain path."""
+    import qpso
+
+    sh = reference_shape(w)
+    if sh is None:
+        return {"unavailable": "does not apply: mesh above the reference kernels' 32768 faces"}
+    soa, F = w["meshes"][sh["mesh"]]
+    dep, lab, _ = w["frames"][sh["frame"]]
+    mid = ctx.mesh_upload(soa, F)
+    fid = ctx.frame_upload(dep, qpso.Camera(*ACCV, 640, 480), labels=lab)
+    x0, x1, y0, y1 = sh["aabb"]
+    d = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=sh["label"], cl_min_x=x0, cl_max_x=x1,
+                        cl_min_y=y0, cl_max_y=y1, num_points=sh["num_points"], t_lo=sh["t_lo"],
+                        t_hi=sh["t_hi"], num_particles=REF_PARTICLES, iterations=REF_ITERATIONS,
+                        seed=sh["seed"], stream=sh["stream"])
+    r = ctx.solve(d)  # warm-up
+    tot = 0.0
+    for _ in range(repeats):
+        ctx.scrub_l2(L2_SCRUB_BYTES)
+        ctx.timer_record(0)
+        r = ctx.solve(d)
+        ctx.timer_record(1)
+        tot += ctx.timer_elapsed_ms(0, 1)
+    ctx.frame_release(fid)
+    ctx.mesh_release(mid)
+    ms = tot / repeats
+    return {"config": sh["desc"], "value": 1000.0 / ms, "unit": "solves/s", "ms_per_solve": ms,
+            "particle_renders_per_s": REF_PARTICLES * REF_ITERATIONS / (ms / 1000.0),
+            "best_fit": float(r.fit)}
+
+
 def accuracy_vs_ground_truth(ctx, w, descs, results):
     """How close the solved poses are to the synthetic scenes' true poses:
     median translation error (mm) and rotation error (degrees; symmetric
@@ -285,6 +390,8 @@ def run_reference(args, ws, rank):
                              "sample": sample},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    if not args.no_ref_kernels:
+        line["reference_kernels_gb300"] = reference_kernels_gb300(w)
     print(json.dumps(line))
 
 
@@ -437,6 +544,8 @@ def run_ours(args, ws, rank, local):
                      "model": "36F + 2A + 96 bytes per particle-render"},
         "clocks": clocks,
     }
+    if rank == 0 and ws == 1 and not args.no_ref_kernels:
+        line["reference_shape"] = reference_shape_ours(ctx, w)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w)
     if rank == 0:
@@ -515,6 +624,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-kernels", action="store_true",
+                    help="skip the reference-shaped solve (1024 particles x 20 iterations)")
     ap.add_argument("--launch", default="", help="THREADS,TILE_PX,PPB for both paths instead of autotuning")
     ap.add_argument("--rates", default="5,20,100,1000,20000", help="c4: arrival rates (req/s)")
     ap.add_argument("--requests", type=int, default=48, help="c4: requests per rate")

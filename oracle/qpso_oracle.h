@@ -6,15 +6,17 @@
  * baseline arm may load it.  The product path never calls it and has no CPU
  * fallback.
  *
- * Parity status: partially pinned.  The reference ships no tests, fixtures or
- * golden vectors.  The quaternion helpers, the vertex rotation and the
- * fixed-point rasteriser of the reference's main.h are compiled from the
- * reference sources by oracle/ref_pin (stub headers for OpenCV/assimp, one
- * emulated thread) and their outputs are committed as tests/golden fixtures;
- * this restatement is checked against them.  The fitness, best-update and
- * particle-update kernels live in main.cu, which cannot be compiled here
- * (OpenCV 2.4, GSL and a missing header), so those parts are restated from
- * the source and are unpinned beyond the helpers they call.
+ * Parity status: pinned.  The reference ships no tests, fixtures or golden
+ * vectors.  The quaternion helpers, the vertex rotation and the fixed-point
+ * rasteriser of the reference's main.h are compiled from the reference
+ * sources by oracle/ref_pin (stub headers for OpenCV/assimp, one emulated
+ * thread) and their outputs are committed as tests/golden fixtures; this
+ * restatement is checked against them.  The reference's whole program
+ * cannot be built (OpenCV 2.4, GSL and a missing header), but its kernels
+ * can: oracle/build.py compiles main.h and main.cu:72-1195 for the GPU, and
+ * tests/test_gpu_ref_kernels.py checks this restatement's raster, fitness,
+ * init, best update and particle update against them on identical inputs.
+ * Only GSL's random stream stays unpinned (Philox replaces it).
  *
  * Arithmetic contract shared with the CUDA kernels (both sides must agree
  * bit for bit):
