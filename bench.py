@@ -180,18 +180,31 @@ def algorithmic_bytes(w) -> tuple[float, float]:
     return tot, n
 
 
-def traffic_per_launch(workload: str, kernel: str = "step"):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/<kernel>_kernel_<workload>.md, line
-    'dram_bytes_per_launch:')."""
+def profile_figure(workload: str, kernel: str, key: str):
+    """A per-launch figure of the dominant kernel from the committed ncu
+    summary (profiles/<kernel>_kernel_<workload>.md, line '<key>: value')."""
     p = os.path.join(ROOT, "profiles", "%s_kernel_%s.md" % (kernel, workload))
     try:
         for line in open(p):
-            if line.strip().startswith("dram_bytes_per_launch:"):
+            if line.strip().startswith(key + ":"):
                 return float(line.split(":", 1)[1].split()[0])
     except OSError:
         pass
     return None
+
+
+def traffic_per_launch(workload: str, kernel: str = "step"):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)."""
+    return profile_figure(workload, kernel, "dram_bytes_per_launch")
+
+
+def sm_count(local: int) -> int:
+    try:
+        import torch
+
+        return int(torch.cuda.get_device_properties(local).multi_processor_count)
+    except Exception:
+        return 152  # GB300
 
 
 def _oracle_sample(w, budget_s: float, threads: int):
@@ -544,6 +557,19 @@ def run_ours(args, ws, rank, local):
                      "model": "36F + 2A + 96 bytes per particle-render"},
         "clocks": clocks,
     }
+    # the bound this kernel does meet: instruction issue.  Warp-instructions
+    # per launch (smsp__inst_executed.sum, mean over the launch list of a run
+    # of this workload) over the live launch time, against four schedulers
+    # per SM issuing one warp-instruction per cycle at the sampled SM clock
+    kind = "batch" if batched_default else "step"
+    inst = profile_figure(args.workload, kind, "inst_per_launch")
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    if inst and kern_ms > 0:
+        peak_issue = 4.0 * sm_count(local) * mhz * 1e6
+        line["issue_roofline"] = {"kernel": kname, "bound": "issue", "achieved": inst / (kern_ms / 1000.0),
+                                  "peak": peak_issue, "unit": "warp-inst/s",
+                                  "frac": inst / (kern_ms / 1000.0) / peak_issue, "inst_per_launch": inst,
+                                  "sm_mhz": mhz, "sms": sm_count(local)}
     if rank == 0 and ws == 1 and not args.no_ref_kernels:
         line["reference_shape"] = reference_shape_ours(ctx, w)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
