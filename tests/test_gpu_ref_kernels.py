@@ -220,3 +220,39 @@ def test_reference_solve_loop(rk, c1_scene):
     o = po.solve(soa, F, obs, po.camera_ref_accv(), _oracle_params(info, iterations=1), trace=True, threads=8)
     want = float(o["trace_gbest"][0][0])
     assert abs(float(tr[0]) - want) <= 1e-3 * abs(want), (float(tr[0]), want)
+
+
+@pytest.mark.skipif(not refgpu.available("fast"), reason="reference kernels not built")
+def test_library_solve_agrees_with_reference_kernels(c1_scene):
+    """The drop-in end to end: this library's qpso_solve and the reference's
+    own kernels (its -use_fast_math build and host loop) on the same mesh,
+    observed depth, cluster, translation box, camera (the ACCV intrinsics,
+    rounded to float for the library) and uniform draws, 1024 particles x
+    5 iterations.  The first iteration's best fitness agrees within 1e-3.
+    Later iterations are not compared: the swarm is chaotic, and the two
+    differ by float ulps from the first update on (CUDA's sinf/cosf/acosf
+    against this build's series, double against float intrinsics).  Both
+    best fitnesses can only fall."""
+    import qpso
+
+    soa, F, obs, info = c1_scene
+    w = scene.workload_c1()
+    depth, labels, _ = w["frames"][0]
+    with refgpu.RefKernels("fast") as rk:
+        rk.set_scene(soa, F, obs.astype(np.int32), T_LO, T_HI, info["num_points"], info["aabb"])
+        rk.set_rand_table(refgpu.uniform_table(SEED, STREAM))
+        ref = rk.solve(5)
+    assert ref["status"] == refgpu.OK and ref["done"] == 5
+    with qpso.Context(0) as ctx:
+        mid = ctx.mesh_upload(soa, F)
+        fid = ctx.frame_upload(depth, qpso.Camera(572.41140, 573.57043, 325.26110, 242.04899, 640, 480),
+                               labels=labels)
+        x0, x1, y0, y1 = info["aabb"]
+        d = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=0, cl_min_x=x0, cl_max_x=x1, cl_min_y=y0,
+                            cl_max_y=y1, num_points=info["num_points"], t_lo=T_LO, t_hi=T_HI, num_particles=N,
+                            iterations=5, seed=SEED, stream=STREAM)
+        r, st = ctx.solve_traced(d)
+    ours = st["trace_gbest"][:, 0]
+    assert r.flags == 0
+    assert abs(float(ours[0]) - float(ref["trace"][0])) <= 1e-3 * float(ref["trace"][0]), (ours[0], ref["trace"][0])
+    assert (np.diff(ours) <= 0).all() and (np.diff(ref["trace"]) <= 0).all()
