@@ -109,7 +109,7 @@ struct FusedSmem {
 };
 
 struct SmemCtl {
-  float pose[kMaxPpb][8];
+  float pose[kMaxPpb][8];  // d 0..6: the particle's pose; 7: its personal-best fitness
   int32_t bound[4];
   uint32_t claim;
   uint32_t n_live;     // listed items of the current pass and meshlet chunk
@@ -1016,8 +1016,12 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
 #pragma unroll
       for (int d = 0; d < 7; ++d) I.pbest[p + (size_t)d * P] = s[d];
       I.pbest_fit[p] = kBestInit;
+      ctl.pose[tid][7] = kBestInit;
     } else {
       float b[7], g[7];
+      // the personal-best fitness is read here, with the state, rather than
+      // after the render: one L2 round trip fewer at the end of the item
+      ctl.pose[tid][7] = __ldcg(I.pbest_fit + p);
 #pragma unroll
       for (int d = 0; d < 7; ++d) {
         s[d] = __ldcg(I.pos + p + (size_t)d * P);
@@ -1040,7 +1044,7 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
     const uint32_t p = p0 + tid;
     const float fv = ctl.argv[tid];
     I.fit[p] = fv;
-    if (fv < __ldcg(I.pbest_fit + p)) {
+    if (fv < ctl.pose[tid][7]) {
       I.pbest_fit[p] = fv;
 #pragma unroll
       for (int d = 0; d < 7; ++d) I.pbest[p + (size_t)d * P] = ctl.pose[tid][d];
@@ -1070,6 +1074,8 @@ __device__ void instance_epilogue(const Instance& I, uint32_t iter, SmemCtl& ctl
   if (!ctl.last) return;
   __threadfence();
   const uint32_t P = I.prm.num_particles;
+  // the global best is read while the fitness loads are in flight
+  const float gf = tid == 0 ? __ldcg(I.gbest) : 0.0f;
   float bv = __int_as_float(0x7f800000);
   uint32_t bi = 0xffffffffu;
   for (uint32_t p = tid; p < P; p += T) {
@@ -1105,7 +1111,6 @@ __device__ void instance_epilogue(const Instance& I, uint32_t iter, SmemCtl& ctl
         bi = oi;
       }
     }
-    const float gf = __ldcg(I.gbest);
     if (bi != 0xffffffffu && bv < gf) {
       I.gbest[0] = bv;
 #pragma unroll
