@@ -608,8 +608,9 @@ def run_serving(args, ws, rank, local):
     renders = {id(d): d.num_particles * d.iterations for d in pool}
     sampler = ClockSampler(local)
     sampler.start()
+    # the same requests at every rate, so that throughput compares across rates
+    picks = [pool[int(i)] for i in rng.integers(0, len(pool), per_rate)]
     for rate in rates:
-        picks = [pool[int(i)] for i in rng.integers(0, len(pool), per_rate)]
         gaps = rng.exponential(1.0 / rate, per_rate)
         with qpso.Server(ctx, max_slots=args.slots, iters_per_epoch=args.epoch_iters) as srv:
             ids = []

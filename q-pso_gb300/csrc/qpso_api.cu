@@ -1110,6 +1110,7 @@ struct ServerReq {
   size_t bytes = 0;
   uint32_t remaining = 0;
   int vcap = 64;  // meshlet size of its mesh
+  double cost = 0.0;  // render cost of one particle, for the order of work items
 };
 
 size_t request_bytes(const qpso_solve_desc& d, const qpso_camera& c) {
@@ -1212,6 +1213,8 @@ void server_loop(qpso_server* s) {
         r.state = 1;
         r.remaining = r.desc.iterations;
         r.vcap = m->mlet_cap;
+        r.cost = (double)m->F * 3.0 + (double)(r.desc.cl_max_x - r.desc.cl_min_x) *
+                                          (double)(r.desc.cl_max_y - r.desc.cl_min_y);
         s->slot_req[slot] = rid;
         s->st.bytes_in_use += need;
         s->st.peak_bytes = std::max(s->st.peak_bytes, s->st.bytes_in_use);
@@ -1298,13 +1301,18 @@ void server_loop(qpso_server* s) {
       if (e != cudaSuccess) server_fail_all(s, QPSO_ERR_CUDA, cudaGetErrorString(e));
       continue;
     }
-    // work items of this epoch: every chunk of every active request
+    // work items of this epoch: every chunk of every active request, the
+    // most expensive requests first so that no large render starts last
     uint32_t n_items = 0, K = s->cfg.iters_per_epoch;
     bool edge = false;
     int vcap = 64;
     {
       std::lock_guard<std::mutex> g(s->mu);
-      for (int slot : active) {
+      std::vector<int> order(active);
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return s->reqs[s->slot_req[a]].cost > s->reqs[s->slot_req[b]].cost;
+      });
+      for (int slot : order) {
         const ServerReq& r = s->reqs[s->slot_req[slot]];
         K = std::min(K, r.remaining);
         edge = edge || r.desc.raster_mode == QPSO_RASTER_EDGE;
