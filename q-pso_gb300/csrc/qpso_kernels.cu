@@ -36,6 +36,11 @@ namespace qpso {
 constexpr int kMaxPpb = 16;
 constexpr int kMaxThreads = 1024;
 
+// Bring a global line into L1 ahead of its use (no register is written).
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -464,8 +469,9 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
   // 1. conservative bound of every particle: the union of its meshlets'
   //    projected object-space boxes (box_rect; a box with a corner closer
   //    than 50 mm bounds nothing and stands for the whole domain), far
-  //    tighter than the projected box of the whole mesh.  Eight lanes
-  //    project one box's corners; one shared atomic per warp and side.
+  //    tighter than the projected box of the whole mesh.  Four lanes
+  //    project one box's corners, two each; one shared atomic per warp and
+  //    side.
   if (tid < np) {
     PartCtl& pc = ctl.part[tid];
     pc.bound[0] = dx1;
@@ -484,28 +490,33 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
   const float4* boxes = I.mlet_box;
   for (int k = 0; k < np; ++k) {
     PartCtl& pc = ctl.part[k];
-    const uint32_t n8 = nbox * 8u;
-    for (uint32_t b = (uint32_t)(tid & ~31); b < n8; b += (uint32_t)T) {  // whole warps
-      // lanes 8j..8j+7 project the corners of one box
-      const uint32_t i = b + (uint32_t)lane, m = i >> 3, c = i & 7u;
-      float u = 0.f, v = 0.f;
+    const uint32_t n4 = nbox * 4u;
+    for (uint32_t b = (uint32_t)(tid & ~31); b < n4; b += (uint32_t)T) {  // whole warps
+      // lanes 4j..4j+3 project the corners of one box: corner c (z low)
+      // and corner c + 4 (z high)
+      const uint32_t i = b + (uint32_t)lane, m = i >> 2, c = i & 3u;
+      float ulo = 0.f, uhi = 0.f, vlo = 0.f, vhi = 0.f;
       bool ok = true;
       if (m < nbox) {
         const float4 blo = __ldg(boxes + 2 * m), bhi = __ldg(boxes + 2 * m + 1);
-        float zz;
-        project(ctl.pose[k], (c & 1u) ? bhi.x : blo.x, (c & 2u) ? bhi.y : blo.y, (c & 4u) ? bhi.z : blo.z, I.cam,
-                u, v, zz);
-        ok = zz >= 50.0f && u == u && v == v;
+        const float x = (c & 1u) ? bhi.x : blo.x, y = (c & 2u) ? bhi.y : blo.y;
+        float u0, v0, z0, u1, v1, z1;
+        project(ctl.pose[k], x, y, blo.z, I.cam, u0, v0, z0);
+        project(ctl.pose[k], x, y, bhi.z, I.cam, u1, v1, z1);
+        ok = z0 >= 50.0f && u0 == u0 && v0 == v0 && z1 >= 50.0f && u1 == u1 && v1 == v1;
+        ulo = fminf(u0, u1);
+        uhi = fmaxf(u0, u1);
+        vlo = fminf(v0, v1);
+        vhi = fmaxf(v0, v1);
       }
-      float ulo = u, uhi = u, vlo = v, vhi = v;
 #pragma unroll
-      for (int o = 1; o < 8; o <<= 1) {
+      for (int o = 1; o < 4; o <<= 1) {
         ulo = fminf(ulo, __shfl_xor_sync(0xffffffffu, ulo, o));
         uhi = fmaxf(uhi, __shfl_xor_sync(0xffffffffu, uhi, o));
         vlo = fminf(vlo, __shfl_xor_sync(0xffffffffu, vlo, o));
         vhi = fmaxf(vhi, __shfl_xor_sync(0xffffffffu, vhi, o));
       }
-      ok = ((__ballot_sync(0xffffffffu, !ok) >> (lane & ~7)) & 0xffu) == 0u;
+      ok = ((__ballot_sync(0xffffffffu, !ok) >> (lane & ~3)) & 0xfu) == 0u;
       int32_t rx0 = INT32_MAX, rx1 = INT32_MIN, ry0 = INT32_MAX, ry1 = INT32_MIN;
       if (m < nbox) {
         // the rectangle of box_rect(); a box that bounds nothing stands for
@@ -1008,6 +1019,20 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
   const uint32_t P = I.prm.num_particles;
   const uint32_t p0 = chunk * I.ppb;
   const uint32_t np = min(I.ppb, P - p0);
+  // while the PSO update runs, the other warps bring the meshlet boxes and
+  // headers that the bound and the first items read into L1
+  // (meshes of up to kCullCap meshlets; every line lies inside the arrays)
+  if (tid >= 32 && I.n_mlets <= (uint32_t)kCullCap) {
+    const uint32_t nm = I.n_mlets;
+    const uint32_t box_lines = (nm + 3u) / 4u;   // 4 boxes (2 float4 each) per 128-byte line
+    const uint32_t hdr_lines = (nm + 15u) / 16u;  // 16 headers (8 bytes each) per line
+    for (uint32_t i = (uint32_t)tid - 32u; i < box_lines + hdr_lines; i += blockDim.x - 32u) {
+      if (i < box_lines)
+        prefetch_l1(reinterpret_cast<const char*>(I.mlet_box) + (size_t)i * 128u);
+      else
+        prefetch_l1(reinterpret_cast<const char*>(I.mlets) + (size_t)(i - box_lines) * 128u);
+    }
+  }
   if (tid < (int)np) {
     const uint32_t p = p0 + tid;
     float s[7], v[7];
