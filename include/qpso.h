@@ -318,9 +318,10 @@ qpso_status qpso_server_stats_get(qpso_server *srv, qpso_server_stats *out);
 /* Finish every queued and active request, then stop the scheduler. */
 qpso_status qpso_server_stop(qpso_server *srv);
 
-/* Checks the bounded device wait: a barrier that expects one more CTA
- * than arrives must expire after timeout_ns and report QPSO_ERR_TIMEOUT.
- * No counterpart in the reference (which has no device waits). */
+/* Checks the bounded device wait of the batched kernel: CTAs waiting for
+ * work from a queue whose next entry is never appended must give up after
+ * timeout_ns and report QPSO_ERR_TIMEOUT.  No counterpart in the reference
+ * (which has no device waits). */
 qpso_status qpso_barrier_selftest(qpso_context *ctx, uint64_t timeout_ns, uint32_t *err_bits);
 
 #ifdef __cplusplus

@@ -55,8 +55,9 @@ struct Buf {
 };
 
 // Offsets of one solve batch inside the device workspace and the pinned
-// staging buffer.  The metadata block (instances, headers, prep jobs, work
-// items) is contiguous so that one copy uploads it.
+// staging buffer.  The metadata block (instances, headers, prep jobs, the
+// work queue's first entries and its head/tail) is contiguous so that one
+// copy uploads it.
 struct Header {  // per instance, 64 bytes: result + counters read back once
   float gbest[8];
   uint32_t done;
@@ -67,7 +68,9 @@ struct Header {  // per instance, 64 bytes: result + counters read back once
 static_assert(sizeof(Header) == 64, "header layout");
 
 struct Layout {
-  size_t inst = 0, hdr = 0, prep = 0, items = 0, claim = 0, bar = 0, berr = 0, meta_end = 0;
+  // qinit / qctl: the batched kernel's first queue entries and head/tail
+  // (uploaded with the metadata); queue: its whole work queue (device only)
+  size_t inst = 0, hdr = 0, prep = 0, qinit = 0, qctl = 0, berr = 0, meta_end = 0, queue = 0;
   size_t total = 0;
   std::vector<size_t> obs, sat, pos, vel, pbest, pbf, fit, trace;
 };
@@ -261,8 +264,7 @@ SolveParams to_params(const qpso_solve_desc& d) {
 }
 
 Layout make_layout(const std::vector<const qpso_solve_desc*>& ds,
-                   const std::vector<const FrameObj*>& frames, uint32_t n_items, uint32_t max_iters,
-                   bool trace) {
+                   const std::vector<const FrameObj*>& frames, uint32_t q_entries, bool trace) {
   Layout L;
   const size_t n = ds.size();
   size_t o = 0;
@@ -272,15 +274,15 @@ Layout make_layout(const std::vector<const qpso_solve_desc*>& ds,
   o = align_up(o + n * sizeof(Header), 256);
   L.prep = o;
   o = align_up(o + n * sizeof(PrepDesc), 256);
-  L.items = o;
-  o = align_up(o + (size_t)n_items * sizeof(WorkItem), 256);
-  L.claim = o;
-  o = align_up(o + (size_t)max_iters * sizeof(uint32_t), 256);
-  L.bar = o;
-  o = align_up(o + 2 * sizeof(uint32_t), 256);
+  L.qinit = o;
+  o = align_up(o + (q_entries ? n : 0) * sizeof(QEntry), 256);
+  L.qctl = o;
+  o = align_up(o + sizeof(QCtl), 256);
   L.berr = o;
   o = align_up(o + sizeof(uint32_t), 256);
   L.meta_end = o;
+  L.queue = o;
+  o = align_up(o + (size_t)q_entries * sizeof(QEntry), 256);
   for (size_t i = 0; i < n; ++i) {
     const qpso_camera& c = frames[i]->cam;
     const size_t P = ds[i]->num_particles;
@@ -308,7 +310,7 @@ Layout make_layout(const std::vector<const qpso_solve_desc*>& ds,
 // Fill the pinned metadata block for a batch laid out by L.
 void fill_meta(qpso_context* ctx, const Layout& L, const std::vector<const qpso_solve_desc*>& ds,
                const std::vector<const MeshObj*>& meshes, const std::vector<const FrameObj*>& frames,
-               const std::vector<WorkItem>& items, uint32_t ppb, bool trace) {
+               uint32_t ppb, bool trace) {
   char* h = static_cast<char*>(ctx->pin.p);
   char* d = static_cast<char*>(ctx->ws.p);
   std::memset(h, 0, L.meta_end);
@@ -357,7 +359,6 @@ void fill_meta(qpso_context* ctx, const Layout& L, const std::vector<const qpso_
     p.obs = reinterpret_cast<uint16_t*>(d + L.obs[i]);
     p.sat = reinterpret_cast<int32_t*>(d + L.sat[i]);
   }
-  if (!items.empty()) std::memcpy(h + L.items, items.data(), items.size() * sizeof(WorkItem));
 }
 
 qpso_status gather_descs(qpso_context* ctx, const qpso_solve_desc* descs, uint32_t n,
@@ -689,10 +690,10 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
   const int vcap = launch_vcap(ms);
   if ((st = fit_cfg(ctx, cfg, vcap)) != QPSO_OK) return st;
   const bool want_trace = trace != nullptr;
-  Layout L = make_layout(ds, fs, 0, 0, want_trace);
+  Layout L = make_layout(ds, fs, 0, want_trace);
   if ((st = ensure_ws(ctx, L.total)) != QPSO_OK) return st;
   if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
-  fill_meta(ctx, L, ds, ms, fs, {}, (uint32_t)cfg.ppb, want_trace);
+  fill_meta(ctx, L, ds, ms, fs, (uint32_t)cfg.ppb, want_trace);
   char* d = static_cast<char*>(ctx->ws.p);
   char* h = static_cast<char*>(ctx->pin.p);
   cudaStream_t s = ctx->stream;
@@ -745,7 +746,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   qpso_status st = gather_descs(ctx, descs, n, ds, ms, fs);
   if (st != QPSO_OK) return st;
   TileConfig cfg = ctx->batch;
-  // work items: every chunk of every instance, most expensive first
+  // instances, most expensive first
   std::vector<uint32_t> order(n);
   std::vector<double> cost(n);
   uint32_t max_iters = 0, max_w = 0, max_h = 0;
@@ -760,12 +761,16 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     max_h = std::max(max_h, (uint32_t)fs[i]->cam.height);
   }
   std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
-  std::vector<WorkItem> items;
-  for (uint32_t i : order) {
-    const uint32_t chunks = (ds[i]->num_particles + cfg.ppb - 1) / cfg.ppb;
-    for (uint32_t c = 0; c < chunks; ++c) items.push_back(WorkItem{i, c});
+  // the work queue: one entry per (instance, iteration), iteration 0 of
+  // every instance first, most expensive first
+  size_t all_chunks = 0;
+  uint64_t q_entries = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    all_chunks += (ds[i]->num_particles + cfg.ppb - 1) / cfg.ppb;
+    q_entries += ds[i]->iterations;
   }
-  Layout L = make_layout(ds, fs, (uint32_t)items.size(), max_iters, false);
+  if (q_entries > 0xffffffffull) return fail(ctx, QPSO_ERR_ARG, "too many iterations in one batch");
+  Layout L = make_layout(ds, fs, (uint32_t)q_entries, false);
   if ((st = ensure_ws(ctx, L.total)) != QPSO_OK) return st;
   if ((st = ensure_pin(ctx, L.meta_end)) != QPSO_OK) return st;
   int per_sm = 0;
@@ -773,19 +778,24 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   if ((st = fit_cfg(ctx, cfg, vcap)) != QPSO_OK) return st;
   QPSO_CUDA(ctx, batch_max_grid(cfg, edge, vcap, &per_sm));
   if (per_sm <= 0) return fail(ctx, QPSO_ERR_ARG, "batch launch config does not fit on an SM");
-  const int grid = (int)std::min<size_t>(items.size(), (size_t)per_sm * ctx->num_sms);
+  const int grid = (int)std::min<size_t>(all_chunks, (size_t)per_sm * ctx->num_sms);
   // wait before touching pinned staging that an earlier graph may read
   QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  fill_meta(ctx, L, ds, ms, fs, items, (uint32_t)cfg.ppb, false);
+  fill_meta(ctx, L, ds, ms, fs, (uint32_t)cfg.ppb, false);
   char* d = static_cast<char*>(ctx->ws.p);
   char* h = static_cast<char*>(ctx->pin.p);
+  {
+    QEntry* qi = reinterpret_cast<QEntry*>(h + L.qinit);
+    for (uint32_t k = 0; k < n; ++k) qi[k] = QEntry{order[k], 0u, 0u, 1u};
+    *reinterpret_cast<QCtl*>(h + L.qctl) = QCtl{0u, n, (uint32_t)q_entries, 0u};  // iteration 0 queued
+  }
   cudaStream_t s = ctx->stream;
   if (!ctx->gev[0]) {
     QPSO_CUDA(ctx, cudaEventCreate(&ctx->gev[0]));
     QPSO_CUDA(ctx, cudaEventCreate(&ctx->gev[1]));
   }
   std::vector<uint64_t> key = {(uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)h, L.total, L.meta_end,
-                               n, items.size(), max_iters, (uint64_t)grid, (uint64_t)cfg.threads,
+                               n, q_entries, max_iters, (uint64_t)grid, (uint64_t)cfg.threads,
                                (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h, (uint64_t)edge,
                                (uint64_t)vcap};
   if (!ctx->gexec || key != ctx->gkey) {
@@ -795,16 +805,17 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     }
     BatchArgs A;
     A.inst = reinterpret_cast<Instance*>(d + L.inst);
-    A.items = reinterpret_cast<const WorkItem*>(d + L.items);
-    A.n_items = (uint32_t)items.size();
-    A.step_claim = reinterpret_cast<uint32_t*>(d + L.claim);
-    A.barrier = reinterpret_cast<uint32_t*>(d + L.bar);
+    A.queue = reinterpret_cast<QEntry*>(d + L.queue);
+    A.qctl = reinterpret_cast<QCtl*>(d + L.qctl);
     A.err = reinterpret_cast<uint32_t*>(d + L.berr);
-    A.max_iters = max_iters;
-    A.timeout_ns = 20ull * 1000 * 1000 * 1000;  // 20 s per barrier
+    A.timeout_ns = 20ull * 1000 * 1000 * 1000;  // 20 s per wait for work
     cudaGraph_t graph;
     QPSO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaMemcpyAsync(d, h, L.meta_end, cudaMemcpyHostToDevice, s);
+    // every replay starts from an empty queue holding iteration 0 of each instance
+    if (e == cudaSuccess) e = cudaMemsetAsync(d + L.queue, 0, (size_t)q_entries * sizeof(QEntry), s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d + L.queue, d + L.qinit, n * sizeof(QEntry), cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess)
       e = launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), (int)n, (int)max_w, (int)max_h, s);
     if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s, edge, vcap);
@@ -842,7 +853,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     bad = bad || (hh[i].err & kErrBound);
   }
   const uint32_t berr = *reinterpret_cast<const uint32_t*>(h + L.berr);
-  if (berr & kErrTimeout) return fail(ctx, QPSO_ERR_TIMEOUT, "batch barrier timed out");
+  if (berr & kErrTimeout) return fail(ctx, QPSO_ERR_TIMEOUT, "batch wait for work timed out");
   if (bad) return fail(ctx, QPSO_ERR_INTERNAL, "raster bound violated");
   return QPSO_OK;
 }
@@ -920,7 +931,7 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   std::vector<const FrameObj*> fs;
   qpso_status st = gather_descs(ctx, desc, 1, ds, ms, fs);
   if (st != QPSO_OK) return st;
-  Layout L = make_layout(ds, fs, 0, 0, false);
+  Layout L = make_layout(ds, fs, 0, false);
   const size_t pose_off = align_up(L.total, 256);
   const size_t fit_off = align_up(pose_off + (size_t)n * 7 * sizeof(float), 256);
   const size_t total = align_up(fit_off + (size_t)n * sizeof(float), 256);
@@ -930,7 +941,7 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   TileConfig cfg = ctx->plain;
   const int vcap = launch_vcap(ms);
   if ((st = fit_cfg(ctx, cfg, vcap)) != QPSO_OK) return st;
-  fill_meta(ctx, L, ds, ms, fs, {}, (uint32_t)cfg.ppb, false);
+  fill_meta(ctx, L, ds, ms, fs, (uint32_t)cfg.ppb, false);
   char* d = static_cast<char*>(ctx->ws.p);
   char* h = static_cast<char*>(ctx->pin.p);
   cudaStream_t s = ctx->stream;
@@ -1079,12 +1090,18 @@ qpso_status qpso_barrier_selftest(qpso_context* ctx, uint64_t timeout_ns, uint32
   if ((st = ensure_ws(ctx, 256)) != QPSO_OK) return st;
   if ((st = ensure_pin(ctx, 16)) != QPSO_OK) return st;
   QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  uint32_t* d = static_cast<uint32_t*>(ctx->ws.p);
+  char* d = static_cast<char*>(ctx->ws.p);
   cudaStream_t s = ctx->stream;
-  QPSO_CUDA(ctx, cudaMemsetAsync(d, 0, 16, s));
-  // two CTAs arrive, three are expected: both waits must expire
-  QPSO_CUDA(ctx, launch_barrier_probe(d, d + 2, 2, 3, timeout_ns, s));
-  QPSO_CUDA(ctx, cudaMemcpyAsync(ctx->pin.p, d + 2, 4, cudaMemcpyDeviceToHost, s));
+  // a queue of one entry that is never appended (ready stays 0): both CTAs'
+  // claims must wait out the limit
+  QCtl* qc = reinterpret_cast<QCtl*>(d);
+  QEntry* q = reinterpret_cast<QEntry*>(d + 64);
+  uint32_t* err = reinterpret_cast<uint32_t*>(d + 128);
+  QPSO_CUDA(ctx, cudaMemsetAsync(d, 0, 256, s));
+  const uint32_t total = 1u;
+  QPSO_CUDA(ctx, cudaMemcpyAsync(&qc->total, &total, sizeof(total), cudaMemcpyHostToDevice, s));
+  QPSO_CUDA(ctx, launch_queue_probe(qc, q, err, 2, timeout_ns, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(ctx->pin.p, err, 4, cudaMemcpyDeviceToHost, s));
   QPSO_CUDA(ctx, cudaStreamSynchronize(s));
   *err_bits = *static_cast<uint32_t*>(ctx->pin.p);
   return (*err_bits & kErrTimeout) ? QPSO_ERR_TIMEOUT : QPSO_OK;

@@ -71,15 +71,30 @@ struct PrepDesc {
   int32_t* sat;
 };
 
+// Entry of the batched kernel's work queue: iteration `iter` of instance
+// `inst`.  CTAs claim its chunks through `next` once `ready` is set; the CTA
+// that completes the iteration appends the instance's next iteration.
+struct QEntry {
+  uint32_t inst;
+  uint32_t iter;
+  uint32_t next;   // chunks claimed so far
+  uint32_t ready;  // set (after inst and iter) when the entry may be claimed
+};
+
+// Head and tail of the batched kernel's work queue.
+struct QCtl {
+  uint32_t head;   // first entry with unclaimed chunks
+  uint32_t tail;   // next free entry
+  uint32_t total;  // entries: the instances' iterations
+  uint32_t pad;
+};
+
 struct BatchArgs {
   Instance* inst;           // device array of instances
-  const WorkItem* items;    // every chunk of every instance, largest first
-  uint32_t n_items;
-  uint32_t* step_claim;     // [max_iters] work-claim counters (zeroed)
-  uint32_t* barrier;        // [2] arrival counter, generation (zeroed)
+  QEntry* queue;            // [total]: iteration 0 of every instance, most expensive first, then appended
+  QCtl* qctl;
   uint32_t* err;            // batch-level error bits (zeroed)
-  uint32_t max_iters;
-  unsigned long long timeout_ns;
+  unsigned long long timeout_ns;  // limit of one wait for work
 };
 
 // Host-side launch wrappers (defined in qpso_kernels.cu).
@@ -104,8 +119,8 @@ size_t fused_smem_bytes(int threads, int ppb, int tile_px, int vcap);
 cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_t x0, int32_t y0,
                                  int32_t w, int32_t h, int32_t* out, int32_t* box, int threads,
                                  cudaStream_t st);
-cudaError_t launch_barrier_probe(uint32_t* bar, uint32_t* err, uint32_t grid, uint32_t expected,
-                                 unsigned long long timeout_ns, cudaStream_t st);
+cudaError_t launch_queue_probe(QCtl* qctl, QEntry* queue, uint32_t* err, uint32_t grid,
+                               unsigned long long timeout_ns, cudaStream_t st);
 cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
                               const TileConfig& cfg, cudaStream_t st, bool edge, int vcap);
 cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* di, PrepDesc* dj,

@@ -1182,89 +1182,108 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_multi_step_kernel(Instance* 
   if (ctl.last && threadIdx.x == 0) I.cur_iter = iter + 1;
 }
 
-// Grid-wide barrier for the cooperative persistent launch.  Waits are
-// bounded by timeout_ns of wall time; on expiry the CTA records kErrTimeout
-// and every CTA leaves at its next barrier.
-__device__ bool grid_barrier(uint32_t* bar, uint32_t* err, unsigned long long timeout_ns) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ok = 1;
-    volatile uint32_t* gen = bar + 1;
-    const uint32_t my = *gen;
+// Batched form: every iteration of every instance in one cooperative
+// launch, scheduled as a dataflow queue with no grid-wide barrier.  The
+// queue starts with iteration 0 of every instance (most expensive first);
+// CTAs claim the chunks of the entry at its head, and the CTA that completes
+// an instance's iteration updates its global best and appends the
+// instance's next iteration.  Instances are independent, so an instance
+// waits only for its own previous iteration, and the items of other
+// instances fill the gap.
+
+// One attempt to claim a chunk: 0 = chunk `chunk` of iteration `iter` of
+// instance `inst`; 1 = every entry has been claimed; 3 = nothing ready now
+// (the head entry's iteration is not appended yet).
+__device__ int try_claim_queue_item(const BatchArgs& A, uint32_t& inst, uint32_t& iter, uint32_t& chunk) {
+  volatile uint32_t* vhead = &A.qctl->head;
+  const uint32_t total = A.qctl->total;
+  while (true) {
+    const uint32_t h = *vhead;
+    if (h >= total) return 1;
+    QEntry* e = A.queue + h;
+    if (!*(volatile uint32_t*)&e->ready) return 3;
     __threadfence();
-    const uint32_t arrived = atomicAdd(bar, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(bar, 0u);
+    const uint32_t in = *(volatile uint32_t*)&e->inst, it = *(volatile uint32_t*)&e->iter;
+    const uint32_t c = atomicAdd(&e->next, 1u);
+    if (c < A.inst[in].chunks) {
       __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      const unsigned long long t0 = global_ns();
-      while (*gen == my) {
-        if (*(volatile uint32_t*)err != 0u) {
-          ok = 0;
-          break;
-        }
-        if (global_ns() - t0 > timeout_ns) {
-          atomicOr(err, kErrTimeout);
-          ok = 0;
-          break;
-        }
-        __nanosleep(256);
-      }
+      inst = in;
+      iter = it;
+      chunk = c;
+      return 0;
     }
-    __threadfence();
+    atomicCAS(&A.qctl->head, h, h + 1u);  // every chunk of the head entry is claimed
   }
-  __syncthreads();
-  return ok != 0;
 }
 
-// Batched form: every iteration of every instance in one cooperative
-// launch.  Step s runs the s-th iteration of all instances that have one;
-// CTAs claim work items (largest first) from a per-step counter, and the
-// last chunk of an instance updates its global best before the barrier.
+// Claim with a bounded wait: 0 = claimed, 1 = every entry claimed, 2 =
+// error or wait limit.  A wait (every open iteration is in progress) ends
+// when another CTA appends or after timeout_ns, and it always ends: the
+// iterations in progress run in resident CTAs and append on completion.
+__device__ int claim_queue_item(const BatchArgs& A, uint32_t& inst, uint32_t& iter, uint32_t& chunk) {
+  unsigned long long t0 = 0ull;
+  while (true) {
+    const int r = try_claim_queue_item(A, inst, iter, chunk);
+    if (r != 3) return r;
+    if (*(volatile uint32_t*)A.err != 0u) return 2;
+    const unsigned long long now = global_ns();
+    if (t0 == 0ull) {
+      t0 = now;
+    } else if (now - t0 > A.timeout_ns) {
+      atomicOr(A.err, kErrTimeout);
+      return 2;
+    }
+    __nanosleep(256);
+  }
+}
+
+// Append iteration `iter` of instance `inst` (thread 0 of the CTA that
+// completed the instance's previous iteration).
+__device__ void append_queue_item(const BatchArgs& A, uint32_t inst, uint32_t iter) {
+  const uint32_t slot = atomicAdd(&A.qctl->tail, 1u);
+  if (slot >= A.qctl->total) {  // cannot happen: one entry per (instance, iteration)
+    atomicOr(A.err, kErrTimeout);
+    return;
+  }
+  QEntry* e = A.queue + slot;
+  e->inst = inst;
+  e->iter = iter;
+  __threadfence();
+  atomicExch(&e->ready, 1u);
+}
+
 template <bool kAllowEdge>
 __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, int tile_px, int vcap) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
-  for (uint32_t s = 0; s < A.max_iters; ++s) {
-    while (true) {
-      if (threadIdx.x == 0) ctl.claim = atomicAdd(A.step_claim + s, 1u);
-      __syncthreads();
-      const uint32_t k = ctl.claim;
-      __syncthreads();
-      if (k >= A.n_items) break;
-      const WorkItem it = A.items[k];
-      const Instance& I = A.inst[it.inst];
-      if (s >= I.prm.iterations) continue;
-      process_item<kAllowEdge>(I, it.chunk, s, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
-      instance_epilogue(I, s, ctl);
-    }
-    if (s + 1 < A.max_iters && !grid_barrier(A.barrier, A.err, A.timeout_ns)) return;
+  __shared__ uint32_t q[4];  // claim result, instance, iteration, chunk
+  while (true) {
+    if (threadIdx.x == 0) q[0] = (uint32_t)claim_queue_item(A, q[1], q[2], q[3]);
+    __syncthreads();
+    const uint32_t state = q[0], in = q[1], it = q[2], chunk = q[3];
+    __syncthreads();
+    if (state != 0u) return;
+    const Instance& I = A.inst[in];
+    process_item<kAllowEdge>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
+    instance_epilogue(I, it, ctl);
+    if (ctl.last && threadIdx.x == 0 && it + 1 < I.prm.iterations) append_queue_item(A, in, it + 1);
   }
 }
 
-// Wait-expiry check for the bounded barrier: `expected` CTAs are awaited
-// but only gridDim.x arrive, so every waiter runs out its limit and the
-// kernel returns with kErrTimeout set; nothing else is touched.
-__global__ void qpso_barrier_probe_kernel(uint32_t* bar, uint32_t* err, uint32_t expected,
-                                          unsigned long long timeout_ns) {
+// Wait-expiry check for the batched kernel's bounded wait for work: the
+// queue's only entry is never appended, so every CTA's claim waits out
+// timeout_ns and returns with kErrTimeout set; nothing else is touched.
+__global__ void qpso_queue_probe_kernel(QCtl* qctl, QEntry* queue, uint32_t* err,
+                                        unsigned long long timeout_ns) {
   if (threadIdx.x != 0) return;
-  volatile uint32_t* gen = bar + 1;
-  const uint32_t my = *gen;
-  const uint32_t arrived = atomicAdd(bar, 1u);
-  if (arrived == expected - 1) {
-    atomicAdd(bar + 1, 1u);
-    return;
-  }
-  const unsigned long long t0 = global_ns();
-  while (*gen == my) {
-    if (global_ns() - t0 > timeout_ns) {
-      atomicOr(err, kErrTimeout);
-      return;
-    }
-    __nanosleep(1000);
-  }
+  BatchArgs A;
+  A.inst = nullptr;  // read only for a ready entry
+  A.queue = queue;
+  A.qctl = qctl;
+  A.err = err;
+  A.timeout_ns = timeout_ns;
+  uint32_t inst, iter, chunk;
+  claim_queue_item(A, inst, iter, chunk);
 }
 
 // ------------------------------------------------------------------------
@@ -1812,9 +1831,9 @@ cudaError_t launch_copy_flags(const uint32_t* src, uint32_t* dst, cudaStream_t s
   return cudaGetLastError();
 }
 
-cudaError_t launch_barrier_probe(uint32_t* bar, uint32_t* err, uint32_t grid, uint32_t expected,
-                                 unsigned long long timeout_ns, cudaStream_t st) {
-  qpso_barrier_probe_kernel<<<grid, 32, 0, st>>>(bar, err, expected, timeout_ns);
+cudaError_t launch_queue_probe(QCtl* qctl, QEntry* queue, uint32_t* err, uint32_t grid,
+                               unsigned long long timeout_ns, cudaStream_t st) {
+  qpso_queue_probe_kernel<<<grid, 32, 0, st>>>(qctl, queue, err, timeout_ns);
   return cudaGetLastError();
 }
 
