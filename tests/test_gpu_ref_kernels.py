@@ -256,3 +256,47 @@ def test_library_solve_agrees_with_reference_kernels(c1_scene):
     assert r.flags == 0
     assert abs(float(ours[0]) - float(ref["trace"][0])) <= 1e-3 * float(ref["trace"][0]), (ours[0], ref["trace"][0])
     assert (np.diff(ours) <= 0).all() and (np.diff(ref["trace"]) <= 0).all()
+
+
+@pytest.mark.skipif(not refgpu.available("fast"), reason="reference kernels not built")
+def test_fast_math_build_render_close_to_oracle(c1_scene):
+    """The reference's kernels as its Makefile builds them (-use_fast_math,
+    multiply-add contraction): on the same 48 poses the depth buffers may
+    differ from the oracle's raster only in rare pixels (measured on the
+    GB300: none of 167,315), by at most 1 mm where both wrote (a contracted
+    depth can round the other way at a .5), the render boxes by at most 1 px
+    (a vertex snapped to the neighbouring 1/16 px), and the fitness stays
+    within 1e-3 of the FP64 recomputation."""
+    soa, F, obs, info = c1_scene
+    poses = _poses(soa, F, 48, 1)
+    with refgpu.RefKernels("fast") as rk:
+        rk.set_scene(soa, F, obs.astype(np.int32), T_LO, T_HI, info["num_points"], info["aabb"])
+        pos = np.zeros((7, N), np.float32)
+        pos[:, :len(poses)] = poses.T
+        rk.set_state(pos=pos)
+        depth, aabb, fit = rk.render_score(len(poses), want_depth=True)
+    cam = po.camera_ref_accv()
+    G = po.GUARD
+    zb = po.zbuf_new(cam)
+    prm = _oracle_params(info)
+    x0, x1, y0, y1 = info["aabb"]
+    diff = written = 0
+    for i, s in enumerate(poses):
+        zb.fill(po.DEPTH_BG)
+        zbuf, box, _ = po.render(soa, F, s, cam, zb)
+        want = zbuf[G:G + 480, G:G + 640]
+        d = depth[i] != want
+        diff += int(d.sum())
+        written += int((want < po.DEPTH_BG).sum())
+        both = d & (depth[i] < po.DEPTH_BG) & (want < po.DEPTH_BG)
+        if both.any():
+            assert np.abs(depth[i][both].astype(np.int64) - want[both]).max() <= 1
+        assert np.abs(aabb[i] - box).max() <= 1
+        win = (min(box[0], x0), max(box[1], x1), min(box[2], y0), max(box[3], y1))
+        if _rows_exact(win):
+            sc = po.score(zbuf, box, obs, cam, prm)
+            ref = po.fitness_fp64(sc, info["num_points"])
+            assert abs(float(fit[i]) - ref) <= 1e-3 * abs(ref), (i, float(fit[i]), ref)
+    assert written > 48 * 200
+    print("fast-math build: %d of %d rendered pixels differ" % (diff, written))
+    assert diff <= written // 1000, (diff, written)
