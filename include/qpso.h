@@ -36,7 +36,17 @@ typedef int32_t qpso_status;
 typedef struct {
     float fx, fy, cx, cy;
     int32_t width, height;
+    /* QPSO_PROJ_FP32 (0): u = cx + fx * (x/z) as one fp32 fused multiply-add
+     * with the fields above.  QPSO_PROJ_REF_ACCV (1): the reference's own
+     * projection, with the ACCV intrinsics compiled into its kernels and
+     * host renderer (main.h:30-33) evaluated in double, u = (float)(CX + FX *
+     * (double)(x/z)) (main.h:537-539, 1849-1851); fx..cy are ignored.  Its
+     * renders equal the reference's kernels' bit for bit. */
+    int32_t projection;
 } qpso_camera;
+
+#define QPSO_PROJ_FP32 0
+#define QPSO_PROJ_REF_ACCV 1
 
 /* One pose solve: QPSOParams_t (main.h:182-204) plus the compile-time
  * constants of main.h:83-136 as run-time fields.  Defaults from

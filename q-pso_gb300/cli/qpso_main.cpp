@@ -35,7 +35,8 @@ int usage(const char* argv0) {
   std::printf(
       "Usage: %s path/to/.obj color_image depth_image cluster_idx\n"
       "       [--labels FILE] [--particles N] [--iterations N] [--seed N] [--stream N]\n"
-      "       [--camera fx,fy,cx,cy] [--results DIR] [--device N] [--raster-mode ref|edge]\n",
+      "       [--camera fx,fy,cx,cy] [--results DIR] [--device N] [--raster-mode ref|edge]\n"
+      "Without --camera the reference's own projection is used (its ACCV intrinsics in double).\n",
       argv0);
   return 0;  // the reference returns 0 after its usage line too
 }
@@ -89,7 +90,9 @@ int main(int argc, char** argv) {
   bool have_seed = false, have_stream = false;
   int raster_mode = 0;
   // the reference's compiled-in ACCV intrinsics (main.h:30-33)
-  qpso_camera cam = {572.41140f, 573.57043f, 325.26110f, 242.04899f, 0, 0};
+  // default: the reference's own projection (its compiled-in ACCV
+  // intrinsics in double); --camera gives fp32 intrinsics instead
+  qpso_camera cam = {572.41140f, 573.57043f, 325.26110f, 242.04899f, 0, 0, QPSO_PROJ_REF_ACCV};
   for (int i = 5; i < argc; ++i) {
     const std::string a = argv[i];
     if (i + 1 >= argc) return die("missing value for", a);
@@ -102,7 +105,10 @@ int main(int argc, char** argv) {
     else if (a == "--seed") ok = have_seed = parse_u64(v, &seed);
     else if (a == "--stream") ok = have_stream = parse_u64(v, &stream);
     else if (a == "--device") ok = parse_u64(v, &device);
-    else if (a == "--camera") ok = std::sscanf(v, "%f,%f,%f,%f", &cam.fx, &cam.fy, &cam.cx, &cam.cy) == 4;
+    else if (a == "--camera") {
+      ok = std::sscanf(v, "%f,%f,%f,%f", &cam.fx, &cam.fy, &cam.cx, &cam.cy) == 4;
+      cam.projection = QPSO_PROJ_FP32;
+    }
     else if (a == "--raster-mode") ok = (raster_mode = std::string(v) == "edge" ? 1 : std::string(v) == "ref" ? 0 : -1) >= 0;
     else return die("unknown option", a);
     if (!ok) return die("bad value", a + " " + v);

@@ -207,6 +207,33 @@ qpso_status fit_cfg(qpso_context* ctx, TileConfig& cfg, int vcap) {
   return QPSO_OK;
 }
 
+// The fused-kernel variant a solve needs (the launch takes the largest):
+// 2 for a frame in the reference projection, 1 for the EDGE raster, else 0.
+int kernel_variant(const qpso_solve_desc& d, const qpso_camera& c) {
+  if (c.projection == QPSO_PROJ_REF_ACCV) return 2;
+  return d.raster_mode == QPSO_RASTER_EDGE ? 1 : 0;
+}
+
+bool projection_ok(const qpso_camera* cam) {
+  return cam->projection == QPSO_PROJ_FP32 || cam->projection == QPSO_PROJ_REF_ACCV;
+}
+
+// The intrinsics a camera projects with: its fields, or the reference's
+// ACCV values (main.h:30-33).
+void camera_intrinsics(const qpso_camera& c, double k[4]) {
+  if (c.projection == QPSO_PROJ_REF_ACCV) {
+    k[0] = 572.41140;
+    k[1] = 573.57043;
+    k[2] = 325.26110;
+    k[3] = 242.04899;
+  } else {
+    k[0] = c.fx;
+    k[1] = c.fy;
+    k[2] = c.cx;
+    k[3] = c.cy;
+  }
+}
+
 qpso_status check_desc(qpso_context* ctx, const qpso_solve_desc& d, const MeshObj** m,
                        const FrameObj** f) {
   auto mi = ctx->meshes.find(d.mesh_id);
@@ -334,7 +361,7 @@ void fill_meta(qpso_context* ctx, const Layout& L, const std::vector<const qpso_
     }
     I.obs = reinterpret_cast<const uint16_t*>(d + L.obs[i]);
     I.sat = reinterpret_cast<const int32_t*>(d + L.sat[i]);
-    I.cam = Camera{f.cam.fx, f.cam.fy, f.cam.cx, f.cam.cy, f.cam.width, f.cam.height};
+    I.cam = Camera{f.cam.fx, f.cam.fy, f.cam.cx, f.cam.cy, f.cam.width, f.cam.height, f.cam.projection};
     I.prm = to_params(s);
     I.pos = reinterpret_cast<float*>(d + L.pos[i]);
     I.vel = reinterpret_cast<float*>(d + L.vel[i]);
@@ -518,6 +545,7 @@ qpso_status qpso_frame_upload(qpso_context* ctx, const uint16_t* depth, const in
   if (!(std::isfinite(cam->fx) && std::isfinite(cam->fy) && std::isfinite(cam->cx) &&
         std::isfinite(cam->cy)))
     return fail(ctx, QPSO_ERR_ARG, "non-finite intrinsics");
+  if (!projection_ok(cam)) return fail(ctx, QPSO_ERR_ARG, "unknown projection");
   cudaSetDevice(ctx->device);
   FrameObj f;
   f.cam = *cam;
@@ -706,7 +734,7 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
   if (prof && (st = ensure_events(ctx, 2 * (size_t)desc->iterations)) != QPSO_OK) return st;
   for (uint32_t it = 0; it < desc->iterations; ++it) {
     if (prof) QPSO_CUDA(ctx, cudaEventRecord(ctx->ev[2 * it], s));
-    QPSO_CUDA(ctx, launch_step(dinst, it, chunks, cfg, s, desc->raster_mode == QPSO_RASTER_EDGE, vcap));
+    QPSO_CUDA(ctx, launch_step(dinst, it, chunks, cfg, s, kernel_variant(*desc, fs[0]->cam), vcap));
     if (prof) QPSO_CUDA(ctx, cudaEventRecord(ctx->ev[2 * it + 1], s));
   }
   QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
@@ -750,10 +778,10 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   std::vector<uint32_t> order(n);
   std::vector<double> cost(n);
   uint32_t max_iters = 0, max_w = 0, max_h = 0;
-  bool edge = false;
+  int var = 0;
   for (uint32_t i = 0; i < n; ++i) {
     order[i] = i;
-    edge = edge || ds[i]->raster_mode == QPSO_RASTER_EDGE;
+    var = std::max(var, kernel_variant(*ds[i], fs[i]->cam));
     const double area = (double)(ds[i]->cl_max_x - ds[i]->cl_min_x) * (ds[i]->cl_max_y - ds[i]->cl_min_y);
     cost[i] = (double)ms[i]->F * 3.0 + area;
     max_iters = std::max(max_iters, ds[i]->iterations);
@@ -776,7 +804,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   int per_sm = 0;
   const int vcap = launch_vcap(ms);
   if ((st = fit_cfg(ctx, cfg, vcap)) != QPSO_OK) return st;
-  QPSO_CUDA(ctx, batch_max_grid(cfg, edge, vcap, &per_sm));
+  QPSO_CUDA(ctx, batch_max_grid(cfg, var, vcap, &per_sm));
   if (per_sm <= 0) return fail(ctx, QPSO_ERR_ARG, "batch launch config does not fit on an SM");
   const int grid = (int)std::min<size_t>(all_chunks, (size_t)per_sm * ctx->num_sms);
   // wait before touching pinned staging that an earlier graph may read
@@ -796,7 +824,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
   }
   std::vector<uint64_t> key = {(uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)h, L.total, L.meta_end,
                                n, q_entries, max_iters, (uint64_t)grid, (uint64_t)cfg.threads,
-                               (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h, (uint64_t)edge,
+                               (uint64_t)cfg.tile_px, (uint64_t)cfg.ppb, max_w, max_h, (uint64_t)var,
                                (uint64_t)vcap};
   if (!ctx->gexec || key != ctx->gkey) {
     if (ctx->gexec) {
@@ -818,7 +846,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
       e = cudaMemcpyAsync(d + L.queue, d + L.qinit, n * sizeof(QEntry), cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess)
       e = launch_prep(reinterpret_cast<PrepDesc*>(d + L.prep), (int)n, (int)max_w, (int)max_h, s);
-    if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s, edge, vcap);
+    if (e == cudaSuccess) e = launch_batch(A, grid, cfg, s, var, vcap);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h + L.hdr, d + L.hdr, n * sizeof(Header), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
@@ -862,11 +890,12 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
                           uint32_t tune_iters, qpso_launch_config* best, float* best_ms) {
   if (!ctx || !descs || n == 0 || tune_iters == 0) return fail(ctx, QPSO_ERR_ARG, "bad autotune arguments");
   std::vector<qpso_solve_desc> ds(descs, descs + n);
-  bool edge = false;
+  int var = 0;
   int vcap = 64;
   for (auto& d : ds) {
     d.iterations = std::min(d.iterations, tune_iters);
-    edge = edge || d.raster_mode == QPSO_RASTER_EDGE;
+    auto fi = ctx->frames.find(d.frame_id);
+    if (fi != ctx->frames.end()) var = std::max(var, kernel_variant(d, fi->second.cam));
     auto mi = ctx->meshes.find(d.mesh_id);
     if (mi != ctx->meshes.end()) vcap = std::max(vcap, mi->second.mlet_cap);
   }
@@ -888,7 +917,7 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
         const TileConfig tc{th, tp, pb};
         if (batched) {
           int per_sm = 0;
-          if (batch_max_grid(tc, edge, vcap, &per_sm) != cudaSuccess || per_sm <= 0) continue;
+          if (batch_max_grid(tc, var, vcap, &per_sm) != cudaSuccess || per_sm <= 0) continue;
           ctx->batch = tc;
         } else {
           ctx->plain = tc;
@@ -955,7 +984,7 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   QPSO_CUDA(ctx, launch_score_mlets(reinterpret_cast<const Instance*>(d + L.inst),
                                     reinterpret_cast<const float*>(d + pose_off), n,
                                     reinterpret_cast<float*>(d + fit_off), cfg, grid, s,
-                                    desc->raster_mode == QPSO_RASTER_EDGE, vcap));
+                                    kernel_variant(*desc, fs[0]->cam), vcap));
   QPSO_CUDA(ctx, cudaMemcpyAsync(fit_out, d + fit_off, (size_t)n * sizeof(float),
                                  cudaMemcpyDeviceToHost, s));
   QPSO_CUDA(ctx, cudaMemcpyAsync(h + L.hdr, d + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
@@ -968,7 +997,7 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
 qpso_status qpso_render(qpso_context* ctx, uint32_t mesh_id, const qpso_camera* cam,
                         const float pose[7], int32_t x0, int32_t y0, int32_t w, int32_t h,
                         int32_t* depth_out, int32_t box_out[4]) {
-  if (!ctx || !cam || !pose || !depth_out || !box_out || w <= 0 || h <= 0 || w % 4 != 0)
+  if (!ctx || !cam || !pose || !depth_out || !box_out || w <= 0 || h <= 0 || w % 4 != 0 || !projection_ok(cam))
     return fail(ctx, QPSO_ERR_ARG, "bad render arguments (w must be a positive multiple of 4)");
   if ((size_t)w * h * 4 > (size_t)ctx->smem_optin)
     return fail(ctx, QPSO_ERR_ARG, "render window exceeds one CTA's shared memory");
@@ -992,7 +1021,7 @@ qpso_status qpso_render(qpso_context* ctx, uint32_t mesh_id, const qpso_camera* 
     I.mesh_lo[k] = m.lo[k];
     I.mesh_hi[k] = m.hi[k];
   }
-  I.cam = Camera{cam->fx, cam->fy, cam->cx, cam->cy, cam->width, cam->height};
+  I.cam = Camera{cam->fx, cam->fy, cam->cx, cam->cy, cam->width, cam->height, cam->projection};
   std::memcpy(hp + pose_off, pose, 7 * sizeof(float));
   cudaStream_t s = ctx->stream;
   QPSO_CUDA(ctx, cudaMemcpyAsync(d, hp, 1024, cudaMemcpyHostToDevice, s));
@@ -1048,8 +1077,10 @@ qpso_status qpso_frame_clusters(qpso_context* ctx, uint32_t frame_id, qpso_clust
       c.depth_points = a.nz;
       if (a.nz) {
         const double sz = (double)a.sum_z;
-        c.centroid_mm[0] = (float)(((double)a.sum_xz - (double)f.cam.cx * sz) / ((double)f.cam.fx * a.nz));
-        c.centroid_mm[1] = (float)(((double)a.sum_yz - (double)f.cam.cy * sz) / ((double)f.cam.fy * a.nz));
+        double k[4];
+        camera_intrinsics(f.cam, k);
+        c.centroid_mm[0] = (float)(((double)a.sum_xz - k[2] * sz) / (k[0] * a.nz));
+        c.centroid_mm[1] = (float)(((double)a.sum_yz - k[3] * sz) / (k[1] * a.nz));
         c.centroid_mm[2] = (float)(sz / a.nz);
       } else {
         c.centroid_mm[0] = c.centroid_mm[1] = c.centroid_mm[2] = 0.f;
@@ -1065,7 +1096,7 @@ qpso_status qpso_frame_clusters(qpso_context* ctx, uint32_t frame_id, qpso_clust
 qpso_status qpso_render_depth_f32(qpso_context* ctx, uint32_t mesh_id, const qpso_camera* cam,
                                   const float pose[7], float* depth_out) {
   if (!ctx || !cam || !pose || !depth_out || cam->width <= 0 || cam->height <= 0 ||
-      (int64_t)cam->width * cam->height > (1 << 26))
+      (int64_t)cam->width * cam->height > (1 << 26) || !projection_ok(cam))
     return fail(ctx, QPSO_ERR_ARG, "bad render arguments");
   auto mi = ctx->meshes.find(mesh_id);
   if (mi == ctx->meshes.end()) return fail(ctx, QPSO_ERR_NOT_FOUND, "unknown mesh id");
@@ -1075,7 +1106,7 @@ qpso_status qpso_render_depth_f32(qpso_context* ctx, uint32_t mesh_id, const qps
   if ((st = ensure_ws(ctx, bytes)) != QPSO_OK) return st;
   QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   float* d = static_cast<float*>(ctx->ws.p);
-  const Camera c{cam->fx, cam->fy, cam->cx, cam->cy, cam->width, cam->height};
+  const Camera c{cam->fx, cam->fy, cam->cx, cam->cy, cam->width, cam->height, cam->projection};
   QPSO_CUDA(ctx, launch_host_render(mi->second.d, mi->second.F, pose, c, d, ctx->stream));
   QPSO_CUDA(ctx, cudaMemcpyAsync(depth_out, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1128,6 +1159,7 @@ struct ServerReq {
   uint32_t remaining = 0;
   int vcap = 64;  // meshlet size of its mesh
   double cost = 0.0;  // render cost of one particle, for the order of work items
+  int var = 0;  // fused-kernel variant it needs (kernel_variant)
 };
 
 size_t request_bytes(const qpso_solve_desc& d, const qpso_camera& c) {
@@ -1232,6 +1264,7 @@ void server_loop(qpso_server* s) {
         r.vcap = m->mlet_cap;
         r.cost = (double)m->F * 3.0 + (double)(r.desc.cl_max_x - r.desc.cl_min_x) *
                                           (double)(r.desc.cl_max_y - r.desc.cl_min_y);
+        r.var = kernel_variant(r.desc, f->cam);
         s->slot_req[slot] = rid;
         s->st.bytes_in_use += need;
         s->st.peak_bytes = std::max(s->st.peak_bytes, s->st.bytes_in_use);
@@ -1268,7 +1301,7 @@ void server_loop(qpso_server* s) {
         I.pbest_fit = reinterpret_cast<float*>(d + o);
         o += align_up(P * 4, 256);
         I.fit = reinterpret_cast<float*>(d + o);
-        I.cam = Camera{c.fx, c.fy, c.cx, c.cy, c.width, c.height};
+        I.cam = Camera{c.fx, c.fy, c.cx, c.cy, c.width, c.height, c.projection};
         I.prm = to_params(r.desc);
         Header* dh = s->d_hdr + slot;
         I.gbest = dh->gbest;
@@ -1321,7 +1354,7 @@ void server_loop(qpso_server* s) {
     // work items of this epoch: every chunk of every active request, the
     // most expensive requests first so that no large render starts last
     uint32_t n_items = 0, K = s->cfg.iters_per_epoch;
-    bool edge = false;
+    int var = 0;
     int vcap = 64;
     {
       std::lock_guard<std::mutex> g(s->mu);
@@ -1332,7 +1365,7 @@ void server_loop(qpso_server* s) {
       for (int slot : order) {
         const ServerReq& r = s->reqs[s->slot_req[slot]];
         K = std::min(K, r.remaining);
-        edge = edge || r.desc.raster_mode == QPSO_RASTER_EDGE;
+        var = std::max(var, r.var);
         vcap = std::max(vcap, r.vcap);
         const uint32_t chunks = s->h_slots[slot].chunks;
         for (uint32_t c = 0; c < chunks; ++c) s->h_items[n_items++] = WorkItem{(uint32_t)slot, c};
@@ -1344,7 +1377,7 @@ void server_loop(qpso_server* s) {
     TileConfig tc = s->tc;  // fits every vcap (checked at submit)
     shrink_cfg(tc, vcap, s->ctx->smem_optin);
     for (uint32_t k = 0; k < K && e == cudaSuccess; ++k)
-      e = launch_multi_step(s->d_slots, s->d_items, n_items, tc, s->stream, edge, vcap);
+      e = launch_multi_step(s->d_slots, s->d_items, n_items, tc, s->stream, var, vcap);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s->h_hdr, s->d_hdr, S * sizeof(Header), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);

@@ -424,12 +424,22 @@ __device__ __forceinline__ void update_particle(const SolveParams& prm, uint32_t
 struct Camera {
   float fx, fy, cx, cy;
   int32_t width, height;
+  int32_t proj;  // kProjFp32 or kProjRefAccv
 };
+
+constexpr int32_t kProjFp32 = 0, kProjRefAccv = 1;
+
 
 // Pose with the rotation's products hoisted: t = 2 q.xyz x v and
 // k = q.xyz x t are evaluated term by term exactly as the reference does.
-__device__ __forceinline__ void project(const float* s, float vx, float vy, float vz,
-                                        const Camera& cam, float& u, float& v, float& z) {
+// kRefProj selects the projection at compile time: the fp32 fused
+// multiply-add with the camera's intrinsics, or the reference's own
+// expression with its compiled-in ACCV intrinsics (double macros,
+// main.h:30-33), u = (float)(CX + FX * (double)(x/z)), as its kernels and
+// host renderer evaluate it (main.h:537-539, 1849-1851).
+template <bool kRefProj>
+__device__ __forceinline__ void project_t(const float* s, float vx, float vy, float vz, const Camera& cam,
+                                          float& u, float& v, float& z) {
   float t0 = s[kQ2] * vz - s[kQ3] * vy;
   float t1 = -(s[kQ1] * vz - s[kQ3] * vx);
   float t2 = s[kQ1] * vy - s[kQ2] * vx;
@@ -446,9 +456,24 @@ __device__ __forceinline__ void project(const float* s, float vx, float vy, floa
   py = py + s[kTY];
   pz = pz + s[kTZ];
   const float rz = 1.0f / pz;
-  u = __fmaf_rn(cam.fx, px * rz, cam.cx);
-  v = __fmaf_rn(cam.fy, py * rz, cam.cy);
+  if (kRefProj) {
+    u = (float)(325.26110 + 572.41140 * (double)(px * rz));
+    v = (float)(242.04899 + 573.57043 * (double)(py * rz));
+  } else {
+    u = __fmaf_rn(cam.fx, px * rz, cam.cx);
+    v = __fmaf_rn(cam.fy, py * rz, cam.cy);
+  }
   z = 1000.0f * pz;
+}
+
+// The camera's own projection, chosen at run time (paths outside the fused
+// kernels' inner loops).
+__device__ __forceinline__ void project(const float* s, float vx, float vy, float vz, const Camera& cam,
+                                        float& u, float& v, float& z) {
+  if (cam.proj == kProjRefAccv)
+    project_t<true>(s, vx, vy, vz, cam, u, v, z);
+  else
+    project_t<false>(s, vx, vy, vz, cam, u, v, z);
 }
 
 // ------------------------------------------------------------------------

@@ -100,19 +100,20 @@ struct BatchArgs {
 // Host-side launch wrappers (defined in qpso_kernels.cu).
 cudaError_t launch_prep(const PrepDesc* jobs, int n, int max_w, int max_h, cudaStream_t st);
 cudaError_t launch_mesh_aabb(const float* mesh, uint32_t F, float* out, cudaStream_t st);
-// `edge`: launch the kernel instance that also holds the EDGE raster (some
-// instance of the launch is in QPSO_RASTER_EDGE mode); the other instance
-// holds only the REF raster.  `vcap`: the largest meshlet (vertices) of the
-// launch's meshes, which sizes the per-warp vertex caches.
+// `var`: the fused-kernel variant the launch needs, the largest over its
+// solves: 0 = REF raster and fp32 projection only, 1 = the EDGE raster too
+// (some solve is in QPSO_RASTER_EDGE mode), 2 = the reference projection too
+// (some frame uses QPSO_PROJ_REF_ACCV).  `vcap`: the largest meshlet
+// (vertices) of the launch's meshes, which sizes the per-warp vertex caches.
 cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, const TileConfig& cfg,
-                        cudaStream_t st, bool edge, int vcap);
-cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, bool edge,
+                        cudaStream_t st, int var, int vcap);
+cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, int var,
                          int vcap);
-cudaError_t batch_max_grid(const TileConfig& cfg, bool edge, int vcap, int* blocks_per_sm);
+cudaError_t batch_max_grid(const TileConfig& cfg, int var, int vcap, int* blocks_per_sm);
 cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
                          const TileConfig& cfg, int grid, cudaStream_t st);
 cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
-                               const TileConfig& cfg, int grid, cudaStream_t st, bool edge, int vcap);
+                               const TileConfig& cfg, int grid, cudaStream_t st, int var, int vcap);
 // Dynamic shared memory of the fused kernels; vcap: vertex cache slots per
 // warp, the largest meshlet of the launch's meshes (meshlet_cap()).
 size_t fused_smem_bytes(int threads, int ppb, int tile_px, int vcap);
@@ -122,7 +123,7 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
 cudaError_t launch_queue_probe(QCtl* qctl, QEntry* queue, uint32_t* err, uint32_t grid,
                                unsigned long long timeout_ns, cudaStream_t st);
 cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
-                              const TileConfig& cfg, cudaStream_t st, bool edge, int vcap);
+                              const TileConfig& cfg, cudaStream_t st, int var, int vcap);
 cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* di, PrepDesc* dj,
                                 cudaStream_t st);
 cudaError_t launch_copy_flags(const uint32_t* src, uint32_t* dst, cudaStream_t st);

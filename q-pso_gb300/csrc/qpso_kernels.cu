@@ -427,6 +427,7 @@ __device__ __forceinline__ int32_t clamp_px(float f, int32_t lo, int32_t hi) {
 // inside the box projects inside the corners' hull when all corners lie in
 // front of the 50 mm plane (depth is affine in the object coordinates);
 // false when one does not, or a corner does not project to a number.
+template <bool kRefProj>
 __device__ __forceinline__ bool box_rect(const float* pose, const Camera& cam, float4 lo, float4 hi,
                                          int32_t dx0, int32_t dx1, int32_t dy0, int32_t dy1, int4& r) {
   float ulo = 3.0e38f, uhi = -3.0e38f, vlo = 3.0e38f, vhi = -3.0e38f;
@@ -434,7 +435,7 @@ __device__ __forceinline__ bool box_rect(const float* pose, const Camera& cam, f
 #pragma unroll 1
   for (int c = 0; c < 8; ++c) {
     float u, v, zz;
-    project(pose, (c & 1) ? hi.x : lo.x, (c & 2) ? hi.y : lo.y, (c & 4) ? hi.z : lo.z, cam, u, v, zz);
+    project_t<kRefProj>(pose, (c & 1) ? hi.x : lo.x, (c & 2) ? hi.y : lo.y, (c & 4) ? hi.z : lo.z, cam, u, v, zz);
     ok = ok && zz >= 50.0f && u == u && v == v;
     ulo = fminf(ulo, u);
     uhi = fmaxf(uhi, u);
@@ -453,7 +454,7 @@ __device__ __forceinline__ bool box_rect(const float* pose, const Camera& cam, f
 // pass 0 records every meshlet's screen rectangle per particle when the
 // mesh has at most kCullCap meshlets; larger meshes project each meshlet's
 // object-space box instead (checked in pass 0 against the real rectangle).
-template <bool kEdge>
+template <bool kEdge, bool kRefProj>
 __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSmem& sm, int tile_px,
                                         SmemCtl& ctl, float* fit_out) {
   const int tid = threadIdx.x, T = blockDim.x;
@@ -501,8 +502,8 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
         const float4 blo = __ldg(boxes + 2 * m), bhi = __ldg(boxes + 2 * m + 1);
         const float x = (c & 1u) ? bhi.x : blo.x, y = (c & 2u) ? bhi.y : blo.y;
         float u0, v0, z0, u1, v1, z1;
-        project(ctl.pose[k], x, y, blo.z, I.cam, u0, v0, z0);
-        project(ctl.pose[k], x, y, bhi.z, I.cam, u1, v1, z1);
+        project_t<kRefProj>(ctl.pose[k], x, y, blo.z, I.cam, u0, v0, z0);
+        project_t<kRefProj>(ctl.pose[k], x, y, bhi.z, I.cam, u1, v1, z1);
         ok = z0 >= 50.0f && u0 == u0 && v0 == v0 && z1 >= 50.0f && u1 == u1 && v1 == v1;
         ulo = fminf(u0, u1);
         uhi = fmaxf(u0, u1);
@@ -618,7 +619,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
             bool ov = false;
             if (pass < pc.npass) {
               int4 r;
-              ov = !box_rect(ctl.pose[k], I.cam, __ldg(grp_box + 2 * g), __ldg(grp_box + 2 * g + 1), dx0, dx1,
+              ov = !box_rect<kRefProj>(ctl.pose[k], I.cam, __ldg(grp_box + 2 * g), __ldg(grp_box + 2 * g + 1), dx0, dx1,
                              dy0, dy1, r) ||
                    rect_overlaps(r, pc);
             }
@@ -644,7 +645,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
                 ov = rect_overlaps(mbox[k * kCullCap + m], pc);
               } else if (ctl.grp_live[k][(m - mc) / kMletGroup]) {
                 int4 r;
-                ov = !box_rect(ctl.pose[k], I.cam, __ldg(I.mlet_box + 2 * m), __ldg(I.mlet_box + 2 * m + 1),
+                ov = !box_rect<kRefProj>(ctl.pose[k], I.cam, __ldg(I.mlet_box + 2 * m), __ldg(I.mlet_box + 2 * m + 1),
                                dx0, dx1, dy0, dy1, r) ||
                      rect_overlaps(r, pc);
               }
@@ -687,7 +688,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
         for (int v = lane; v < nv; v += 32) {
           const float4 qv = __ldg(gv + v);
           float u, vv, z;
-          project(pose, qv.x, qv.y, qv.z, I.cam, u, vv, z);
+          project_t<kRefProj>(pose, qv.x, qv.y, qv.z, I.cam, u, vv, z);
           vc[v] = make_int4(__float2int_rn(16.0f * u), __float2int_rn(16.0f * vv), __float_as_int(z), 0);
         }
         __syncwarp();
@@ -836,7 +837,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
               const float y = (lane & 2) ? bhi.y : blo.y;
               const float z = (lane & 4) ? bhi.z : blo.z;
               float u, v, zz;
-              project(pose, x, y, z, I.cam, u, v, zz);
+              project_t<kRefProj>(pose, x, y, z, I.cam, u, v, zz);
               ok = zz >= 50.0f && u == u && v == v;
               cx0 = clamp_px(floorf(u) - 1.0f, dx0, dx1);
               cx1 = clamp_px(floorf(u) + 2.0f, dx0, dx1);
@@ -999,20 +1000,30 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
   __syncthreads();
 }
 
-// Render + score in the instance's raster mode (uniform per instance).
-// Kernels compiled with kAllowEdge = false hold only the REF raster, so the
-// default path's code and registers do not carry the EDGE variant.
-template <bool kAllowEdge>
+// Render + score in the instance's raster mode and camera projection
+// (uniform per instance).  The fused kernels are compiled in three
+// variants, so that the default path's code and registers carry neither
+// the EDGE raster nor the reference projection:
+//   kVar 0: REF raster, fp32 projection (the default);
+//   kVar 1: REF or EDGE raster, fp32 projection;
+//   kVar 2: either raster, either projection.
+template <int kVar>
 __device__ __forceinline__ void render_score_mlets(const Instance& I, int np, const FusedSmem& sm, int tile_px,
                                                    SmemCtl& ctl, float* fit_out) {
-  if (kAllowEdge && I.prm.raster_mode == kRasterEdge)
-    render_score_mlets_mode<true>(I, np, sm, tile_px, ctl, fit_out);
+  const bool edge = kVar >= 1 && I.prm.raster_mode == kRasterEdge;
+  const bool ref = kVar == 2 && I.cam.proj == kProjRefAccv;
+  if (kVar == 2 && edge && ref)
+    render_score_mlets_mode<true, true>(I, np, sm, tile_px, ctl, fit_out);
+  else if (kVar == 2 && ref)
+    render_score_mlets_mode<false, true>(I, np, sm, tile_px, ctl, fit_out);
+  else if (kVar >= 1 && edge)
+    render_score_mlets_mode<true, false>(I, np, sm, tile_px, ctl, fit_out);
   else
-    render_score_mlets_mode<false>(I, np, sm, tile_px, ctl, fit_out);
+    render_score_mlets_mode<false, false>(I, np, sm, tile_px, ctl, fit_out);
 }
 
 // PSO step + render + score + personal best for one work item.
-template <bool kAllowEdge>
+template <int kVar>
 __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, unsigned char* dyn,
                              int tile_px, int vcap, SmemCtl& ctl) {
   const int tid = threadIdx.x;
@@ -1064,7 +1075,7 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
     }
   }
   __syncthreads();
-  render_score_mlets<kAllowEdge>(I, (int)np, carve_smem(dyn, (int)I.ppb, vcap), tile_px, ctl, ctl.argv);
+  render_score_mlets<kVar>(I, (int)np, carve_smem(dyn, (int)I.ppb, vcap), tile_px, ctl, ctl.argv);
   if (tid < (int)np) {
     const uint32_t p = p0 + tid;
     const float fv = ctl.argv[tid];
@@ -1153,13 +1164,13 @@ __device__ void instance_epilogue(const Instance& I, uint32_t iter, SmemCtl& ctl
 }
 
 // Plain form: one launch per iteration of one instance, one CTA per chunk.
-template <bool kAllowEdge>
+template <int kVar>
 __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* __restrict__ inst,
                                                                 uint32_t iter, int tile_px, int vcap) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
   const Instance& I = *inst;
-  process_item<kAllowEdge>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
+  process_item<kVar>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
   instance_epilogue(I, iter, ctl);
 }
 
@@ -1168,7 +1179,7 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* 
 // set of requests changes between launches).  CTA b runs work item b; the
 // CTA finishing an instance's last chunk updates its global best and
 // advances its iteration counter for the next launch.
-template <bool kAllowEdge>
+template <int kVar>
 __global__ void __launch_bounds__(kMaxThreads) qpso_multi_step_kernel(Instance* __restrict__ slots,
                                                                       const WorkItem* __restrict__ items,
                                                                       int tile_px, int vcap) {
@@ -1177,7 +1188,7 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_multi_step_kernel(Instance* 
   const WorkItem it = items[blockIdx.x];
   Instance& I = slots[it.inst];
   const uint32_t iter = __ldcg(&I.cur_iter);
-  process_item<kAllowEdge>(I, it.chunk, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
+  process_item<kVar>(I, it.chunk, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
   instance_epilogue(I, iter, ctl);
   if (ctl.last && threadIdx.x == 0) I.cur_iter = iter + 1;
 }
@@ -1252,7 +1263,7 @@ __device__ void append_queue_item(const BatchArgs& A, uint32_t inst, uint32_t it
   atomicExch(&e->ready, 1u);
 }
 
-template <bool kAllowEdge>
+template <int kVar>
 __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, int tile_px, int vcap) {
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
@@ -1264,7 +1275,7 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, in
     __syncthreads();
     if (state != 0u) return;
     const Instance& I = A.inst[in];
-    process_item<kAllowEdge>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
+    process_item<kVar>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
     instance_epilogue(I, it, ctl);
     if (ctl.last && threadIdx.x == 0 && it + 1 < I.prm.iterations) append_queue_item(A, in, it + 1);
   }
@@ -1495,7 +1506,7 @@ __global__ void __launch_bounds__(kMaxThreads) score_poses_kernel(const Instance
 }
 
 // Score explicit poses with the meshlet path, ppb poses per CTA pass.
-template <bool kAllowEdge>
+template <int kVar>
 __global__ void __launch_bounds__(kMaxThreads) score_poses_mlet_kernel(const Instance* __restrict__ inst,
                                                                        const float* __restrict__ poses,
                                                                        uint32_t n, int tile_px,
@@ -1511,7 +1522,7 @@ __global__ void __launch_bounds__(kMaxThreads) score_poses_mlet_kernel(const Ins
     const int np = (int)min(I.ppb, n - k0);
     if ((int)threadIdx.x < np * 7) ctl.pose[threadIdx.x / 7][threadIdx.x % 7] = poses[(size_t)k0 * 7 + threadIdx.x];
     __syncthreads();
-    render_score_mlets<kAllowEdge>(I, np, sm, tile_px, ctl, ctl.argv);
+    render_score_mlets<kVar>(I, np, sm, tile_px, ctl, ctl.argv);
     if ((int)threadIdx.x < np) fit_out[k0 + threadIdx.x] = ctl.argv[threadIdx.x];
     __syncthreads();
   }
@@ -1589,27 +1600,27 @@ cudaError_t launch_mesh_aabb(const float* mesh, uint32_t F, float* out, cudaStre
 }
 
 cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, const TileConfig& cfg,
-                        cudaStream_t st, bool edge, int vcap) {
+                        cudaStream_t st, int var, int vcap) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
-  auto* k = edge ? qpso_step_kernel<true> : qpso_step_kernel<false>;
+  auto* k = var == 2 ? qpso_step_kernel<2> : var == 1 ? qpso_step_kernel<1> : qpso_step_kernel<0>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
   k<<<chunks, cfg.threads, smem, st>>>(inst, iter, cfg.tile_px, vcap);
   return cudaGetLastError();
 }
 
-cudaError_t batch_max_grid(const TileConfig& cfg, bool edge, int vcap, int* blocks_per_sm) {
+cudaError_t batch_max_grid(const TileConfig& cfg, int var, int vcap, int* blocks_per_sm) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
-  auto* k = edge ? qpso_batch_kernel<true> : qpso_batch_kernel<false>;
+  auto* k = var == 2 ? qpso_batch_kernel<2> : var == 1 ? qpso_batch_kernel<1> : qpso_batch_kernel<0>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, cfg.threads, smem);
 }
 
-cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, bool edge,
+cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, int var,
                          int vcap) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
-  auto* k = edge ? qpso_batch_kernel<true> : qpso_batch_kernel<false>;
+  auto* k = var == 2 ? qpso_batch_kernel<2> : var == 1 ? qpso_batch_kernel<1> : qpso_batch_kernel<0>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t lc = {};
@@ -1790,9 +1801,9 @@ cudaError_t launch_cluster_stats(const uint16_t* depth, const int32_t* labels, i
 }
 
 cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
-                               const TileConfig& cfg, int grid, cudaStream_t st, bool edge, int vcap) {
+                               const TileConfig& cfg, int grid, cudaStream_t st, int var, int vcap) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
-  auto* k = edge ? score_poses_mlet_kernel<true> : score_poses_mlet_kernel<false>;
+  auto* k = var == 2 ? score_poses_mlet_kernel<2> : var == 1 ? score_poses_mlet_kernel<1> : score_poses_mlet_kernel<0>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
   k<<<grid, cfg.threads, smem, st>>>(inst, poses, n, cfg.tile_px, fit_out, vcap);
@@ -1810,10 +1821,10 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
 }
 
 cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
-                              const TileConfig& cfg, cudaStream_t st, bool edge, int vcap) {
+                              const TileConfig& cfg, cudaStream_t st, int var, int vcap) {
   if (n_items == 0) return cudaSuccess;
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
-  auto* k = edge ? qpso_multi_step_kernel<true> : qpso_multi_step_kernel<false>;
+  auto* k = var == 2 ? qpso_multi_step_kernel<2> : var == 1 ? qpso_multi_step_kernel<1> : qpso_multi_step_kernel<0>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
   k<<<n_items, cfg.threads, smem, st>>>(slots, items, cfg.tile_px, vcap);

@@ -76,7 +76,8 @@ extern "C" qpso_status qpso_score_poses_noalloc(const float* d_mesh_soa, uint32_
   if (!d_mesh_soa || num_faces == 0 || !d_depth_mm || !cam || !desc || !d_poses || !d_fit_out ||
       n == 0)
     return QPSO_ERR_ARG;
-  if (cam->width <= 0 || cam->height <= 0 || cam->width > 8192 || cam->height > 8192)
+  if (cam->width <= 0 || cam->height <= 0 || cam->width > 8192 || cam->height > 8192 ||
+      (cam->projection != QPSO_PROJ_FP32 && cam->projection != QPSO_PROJ_REF_ACCV))
     return QPSO_ERR_ARG;
   if (desc->num_points == 0 || !(desc->cl_min_x < desc->cl_max_x && desc->cl_min_y < desc->cl_max_y))
     return QPSO_ERR_ARG;
@@ -104,7 +105,7 @@ extern "C" qpso_status qpso_score_poses_noalloc(const float* d_mesh_soa, uint32_
   I.F = num_faces;
   I.obs = reinterpret_cast<const uint16_t*>(base + o_obs);
   I.sat = reinterpret_cast<const int32_t*>(base + o_sat);
-  I.cam = Camera{cam->fx, cam->fy, cam->cx, cam->cy, cam->width, cam->height};
+  I.cam = Camera{cam->fx, cam->fy, cam->cx, cam->cy, cam->width, cam->height, cam->projection};
   SolveParams& p = I.prm;
   p.c1 = desc->c1;
   p.c2 = desc->c2;

@@ -39,7 +39,12 @@ EXPORTS = [
 
 class Camera(C.Structure):
     _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
-                ("width", C.c_int32), ("height", C.c_int32)]
+                ("width", C.c_int32), ("height", C.c_int32), ("projection", C.c_int32)]
+
+
+# qpso_camera.projection: fp32 with the given intrinsics, or the reference's
+# own double-precision projection with its compiled-in ACCV intrinsics
+PROJ_FP32, PROJ_REF_ACCV = 0, 1
 
 
 class SolveDesc(C.Structure):

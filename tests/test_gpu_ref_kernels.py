@@ -300,3 +300,53 @@ def test_fast_math_build_render_close_to_oracle(c1_scene):
     assert written > 48 * 200
     print("fast-math build: %d of %d rendered pixels differ" % (diff, written))
     assert diff <= written // 1000, (diff, written)
+
+
+@pytest.mark.skipif(not refgpu.available("fast"), reason="reference kernels not built")
+def test_library_reference_projection_equals_reference_kernels(c1_scene):
+    """This library with QPSO_PROJ_REF_ACCV (the reference's projection,
+    its ACCV intrinsics in double) against the reference's own kernels as
+    its Makefile builds them, on the same 48 poses: every rendered window
+    and render box is bit-identical, and the fitness of the library's
+    exact counts is within 1e-5 of the reference kernel's float sums
+    wherever the reference's float row index visits every window pixel
+    once (elsewhere it double-visits or skips a pixel, a documented
+    deviation of the reference)."""
+    import qpso
+
+    soa, F, obs, info = c1_scene
+    w = scene.workload_c1()
+    depth_frame, labels, _ = w["frames"][0]
+    poses = _poses(soa, F, 48, 1)
+    with refgpu.RefKernels("fast") as rk:
+        rk.set_scene(soa, F, obs.astype(np.int32), T_LO, T_HI, info["num_points"], info["aabb"])
+        pos = np.zeros((7, N), np.float32)
+        pos[:, :len(poses)] = poses.T
+        rk.set_state(pos=pos)
+        ref_depth, ref_aabb, ref_fit = rk.render_score(len(poses), want_depth=True)
+    cam = qpso.Camera(0, 0, 0, 0, 640, 480, qpso.PROJ_REF_ACCV)
+    with qpso.Context(0) as ctx:
+        mid = ctx.mesh_upload(soa, F)
+        fid = ctx.frame_upload(depth_frame, cam, labels=labels)
+        x0, x1, y0, y1 = info["aabb"]
+        d = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=0, cl_min_x=x0, cl_max_x=x1,
+                            cl_min_y=y0, cl_max_y=y1, num_points=info["num_points"], t_lo=T_LO, t_hi=T_HI)
+        fit = ctx.score_poses(d, poses)
+        for i, s in enumerate(poses):
+            bx0, bx1, by0, by1 = (int(v) for v in ref_aabb[i])
+            wx0 = bx0 & ~3
+            ww = (bx1 - wx0 + 3) // 4 * 4
+            hh = by1 - by0
+            assert ww * hh * 4 < 200 * 1024, (ww, hh)
+            got, box = ctx.render(mid, cam, s, wx0, by0, ww, hh)
+            assert tuple(box) == tuple(ref_aabb[i]), i
+            want = ref_depth[i][by0:by0 + hh, wx0:wx0 + ww]
+            np.testing.assert_array_equal(got, want, err_msg="pose %d" % i)
+    checked = 0
+    for i in range(len(poses)):
+        b = ref_aabb[i]
+        win = (min(b[0], x0), max(b[1], x1), min(b[2], y0), max(b[3], y1))
+        if _rows_exact(win):
+            assert abs(float(fit[i]) - float(ref_fit[i])) <= 1e-5 * abs(float(ref_fit[i])), i
+            checked += 1
+    assert checked >= 32
