@@ -34,9 +34,9 @@ def files(tmp_path_factory):
     return d, w, s, obj
 
 
-def run_cli(d, obj, depth_name, k, extra=()):
+def run_cli(d, obj, depth_name, k, extra=(), camera=("--camera", "525,525,319.5,239.5")):
     cmd = [CLI, obj, "img_0042.png", str(d / depth_name), str(k), "--labels", str(d / "labels.png"),
-           "--camera", "525,525,319.5,239.5", "--particles", "32", "--iterations", "6", "--seed", "7",
+           *camera, "--particles", "32", "--iterations", "6", "--seed", "7",
            "--results", str(d / "results"), *extra]
     return subprocess.run(cmd, capture_output=True, text=True, timeout=300)
 
@@ -110,6 +110,37 @@ def test_cli_edge_raster_mode(gpu_ctx, files):
     res = gpu_ctx.solve(desc)
     got = open(str(d / "res_edge" / ("img_0042.png-%d-bestpose.csv" % k))).read()
     assert got == "%f,%f,%f,%f,%f,%f,%f,%f" % (res.fit, *res.pose)
+    gpu_ctx.frame_release(fid)
+    gpu_ctx.mesh_release(mid)
+
+
+def test_cli_default_reference_projection(gpu_ctx, files):
+    """Without --camera the command line projects as the reference does (its
+    ACCV intrinsics in double): the pose file equals the library's solve
+    with QPSO_PROJ_REF_ACCV, and the best-pose depth image equals the
+    oracle's restatement of the reference's host render in that
+    projection."""
+    d, w, s, obj = files
+    k = s["cluster"]["label"]
+    r = run_cli(d, obj, "depth.bin", k, ("--results", str(d / "res_ref")), camera=())
+    assert r.returncode == 0, r.stderr
+    soa, F = qpso.obj_load(obj)
+    depth, labels, _ = w["frames"][0]
+    cam = qpso.Camera(0, 0, 0, 0, 640, 480, qpso.PROJ_REF_ACCV)
+    mid = gpu_ctx.mesh_upload(soa, F)
+    fid = gpu_ctx.frame_upload(depth, cam, labels=labels)
+    c = [x for x in gpu_ctx.frame_clusters(fid) if x["label"] == k][0]
+    lo, hi = qpso.box_from_centroid(c["centroid_mm"])
+    x0, x1, y0, y1 = c["aabb"]
+    desc = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=k, cl_min_x=x0, cl_max_x=x1,
+                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"], t_lo=lo, t_hi=hi,
+                           num_particles=32, iterations=6, seed=7, stream=0)
+    res = gpu_ctx.solve(desc)
+    stem = d / "res_ref" / ("img_0042.png-%d" % k)
+    assert open(str(stem) + "-bestpose.csv").read() == "%f,%f,%f,%f,%f,%f,%f,%f" % (res.fit, *res.pose)
+    img = po.render_cpu(soa, F, np.array(res.pose[:], np.float32), po.camera_ref_accv())
+    text = "".join(", ".join("%g" % float(v) for v in row) + "\n" for row in img)
+    assert open(str(stem) + "-best.csv").read() == text
     gpu_ctx.frame_release(fid)
     gpu_ctx.mesh_release(mid)
 
