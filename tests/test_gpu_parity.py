@@ -421,3 +421,7 @@ def test_argument_errors(gpu_ctx, c1_gpu):
     assert e.value.status == qpso.ERR_ARG
     with pytest.raises(qpso.QpsoError):
         gpu_ctx.mesh_upload(np.full(9, np.nan, np.float32), 1)
+    depth, labels, _ = w["frames"][0]
+    with pytest.raises(qpso.QpsoError) as e:  # unknown projection
+        gpu_ctx.frame_upload(depth, qpso.Camera(525, 525, 319.5, 239.5, 640, 480, 7), labels=labels)
+    assert e.value.status == qpso.ERR_ARG
