@@ -213,7 +213,10 @@ qpso_status qpso_solve_traced(qpso_context *ctx, const qpso_solve_desc *desc, qp
                               float *trace, float *pos, float *vel, float *pbest, float *pbest_fit);
 
 /* Batched solve: every iteration of all n solves in one persistent
- * cooperative launch (replayed from a CUDA graph when the shape repeats). */
+ * cooperative launch (replayed from a CUDA graph when the shape repeats),
+ * scheduled as a queue of (solve, iteration) entries: a solve's next
+ * iteration starts as soon as its own previous one completes.  Results are
+ * bit-identical to n calls of qpso_solve. */
 qpso_status qpso_solve_batch(qpso_context *ctx, const qpso_solve_desc *descs, uint32_t n,
                              qpso_result *results);
 
