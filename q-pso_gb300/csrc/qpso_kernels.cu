@@ -265,7 +265,7 @@ __device__ float render_score(const Instance& I, const float* s, int32_t* tile, 
             depth = depth + (float)cx2 * fs.z2;
             depth = depth + (float)cx3 * fs.z3;
             const int32_t d = __float2int_rn(depth);
-            if (d < kDepthBg) atomicMin(row + x, d);
+            atomicMin(row + x, d);  // a depth at or above the background leaves the tile as it is
             if (edge) acc.writes += 1ull;
           }
           CX2 = wsub(CX2, fs.fdy23);
@@ -747,7 +747,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
                         depth = depth + (float)cx2 * fs.z2;
                         depth = depth + (float)cx3 * fs.z3;
                         const int32_t d = __float2int_rn(depth);
-                        if (d < kDepthBg) atomicMin(row + x, d);
+                        atomicMin(row + x, d);  // a depth at or above the background leaves the tile as it is
                         if (kEdge) writes += 1ull;
                       }
                       CX2 = wsub(CX2, fs.fdy23);
@@ -804,7 +804,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
               depth = depth + (float)cx2 * z2;
               depth = depth + (float)cx3 * z3;
               const int32_t d = __float2int_rn(depth);
-              if (d < kDepthBg) atomicMin(tile + (y - y0) * cwp + (x - x0), d);
+              atomicMin(tile + (y - y0) * cwp + (x - x0), d);
             }
           }
         }
