@@ -113,11 +113,15 @@ def test_host_render_of_mesh_matches_reference():
                     cy=float(np.float32(K[3])))
     idx, val, off = g["render_idx"], g["render_val"], g["render_off"]
     for j, pose in enumerate(g["poses"]):
-        got = po.render_cpu(soa, F, pose, cam)
         want = np.full(480 * 640, 60000.0, np.float32)
         want[idx[off[j]:off[j + 1]]] = val[off[j]:off[j + 1]]
         assert off[j + 1] - off[j] > 500
+        # with the intrinsics rounded to float (an fp32 fma; equal here)
+        got = po.render_cpu(soa, F, pose, cam)
         np.testing.assert_array_equal(got.ravel(), want, err_msg="pose %d" % j)
+        # and with the reference's own double projection (equal by construction)
+        got = po.render_cpu(soa, F, pose, po.camera_ref_accv())
+        np.testing.assert_array_equal(got.ravel(), want, err_msg="pose %d, reference projection" % j)
 
 
 def _f(a):
