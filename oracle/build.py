@@ -1,6 +1,6 @@
 """Build recipe for the test-side checkers under oracle/.
 
-TEST INFRASTRUCTURE ONLY.  Two shared libraries:
+TEST INFRASTRUCTURE ONLY.  Host libraries:
 
 * ``oracle/_build/libqpso_oracle.so`` -- the scalar C restatement
   (qpso_oracle.c), built everywhere (here and on the GPU host).
@@ -8,6 +8,10 @@ TEST INFRASTRUCTURE ONLY.  Two shared libraries:
   compiled for the host CPU (ref_pin/ref_pin.cpp).  Built only where the
   reference sources are present; its outputs are frozen into
   tests/golden/ by tests/golden/make_golden.py.
+* ``oracle/_ref/libqpso_segpin.so`` -- the reference's segmentation core
+  (GraphCannySeg's disjoint-set forest, segment_graph, small-component
+  merge, collectSets) compiled for the host between the stand-ins of
+  ref_pin/seg_*.h.  Same conditions; frozen into tests/golden/ref_seg.npz.
 
 and the reference's own CUDA kernels rebuilt for the GB300:
 
@@ -127,6 +131,94 @@ def build_ref_cubins(force: bool = False) -> dict | None:
     return REF_CUBINS
 
 
+SEGPIN_SO = os.path.join(REF_OUT, "libqpso_segpin.so")
+
+
+def _code_braces(line: str) -> int:
+    code = line.split("//", 1)[0]
+    return code.count("{") - code.count("}")
+
+
+def _block(lines: list[str], start: int) -> tuple[int, int]:
+    """[start, end) of the brace-balanced block that opens on or after
+    line `start` (// comments ignored)."""
+    depth, opened = 0, False
+    for i in range(start, len(lines)):
+        d = _code_braces(lines[i])
+        opened = opened or "{" in lines[i].split("//", 1)[0]
+        depth += d
+        if opened and depth == 0:
+            return start, i + 1
+    raise ValueError("unbalanced block at line %d" % (start + 1))
+
+
+def _find(lines: list[str], text: str, after: int = 0) -> int:
+    return next(i for i in range(after, len(lines)) if text in lines[i])
+
+
+def _segmentation_pieces(src: str) -> str:
+    """The reference's disjoint-set forest and graph segmentation, read
+    from GraphCannySeg.h/.cpp where they lie, each piece under a #line of
+    its own: THRESHOLD, edge, uni_elt, universe (header); edge's
+    constructors and operator<, universe's methods, segment_graph and the
+    small-component merge loop (source)."""
+    h = open(os.path.join(src, "GraphCannySeg.h")).read().splitlines(keepends=True)
+    c = open(os.path.join(src, "GraphCannySeg.cpp")).read().splitlines(keepends=True)
+
+    def piece(lines, name, a, b):
+        return '#line %d "%s"\n%s' % (a + 1, name, "".join(lines[a:b]))
+
+    out = []
+    i = _find(h, "#define THRESHOLD(size, c)")
+    out.append(piece(h, "GraphCannySeg.h", i, i + 1))
+    out.append("namespace GraphCanny {\n")
+    out.append(piece(h, "GraphCannySeg.h", *_block(h, _find(h, "struct edge{"))))
+    end = _find(h, "} uni_elt;")
+    start = max(i for i in range(end) if h[i].strip() == "typedef struct {")
+    out.append(piece(h, "GraphCannySeg.h", start, end + 1))
+    out.append(piece(h, "GraphCannySeg.h", *_block(h, _find(h, "class universe {"))))
+    out.append("}\n#include \"seg_class.h\"\nnamespace GraphCanny {\n")
+    for sig in ("edge::edge()", "edge::edge(int a_, int b_, float w_)", "bool operator<(const edge &a, const edge &b)",
+                "universe::universe(int elements)", "universe::~universe()", "int universe::find(int x)",
+                "void universe::join(int x, int y)", "bool universe::printSet(", "void universe::collectSets("):
+        out.append(piece(c, "GraphCannySeg.cpp", *_block(c, _find(c, sig))))
+    seg = _find(c, "GraphCannySeg<T>::segment_graph(int num_vertices")
+    assert c[seg - 1].strip() == "template <class T>"
+    out.append(piece(c, "GraphCannySeg.cpp", seg - 1, _block(c, seg)[1]))
+    loop = _find(c, "for (int i = 0; i < num; i++) {", _find(c, "// post process small components"))
+    out.append("template <class T>\nvoid GraphCannySeg<T>::merge_small(universe *u, edge *edges, int num) {\n")
+    out.append(piece(c, "GraphCannySeg.cpp", *_block(c, loop)))
+    out.append("}\n}\n")
+    return "".join(out)
+
+
+def build_seg_pin(force: bool = False) -> str | None:
+    """oracle/_ref/libqpso_segpin.so: the reference's segmentation core
+    (union-find forest, segment_graph, small-component merge, collectSets)
+    compiled for the host between the stand-ins of ref_pin/seg_*.h."""
+    hdr = os.path.join(REFERENCE_SRC, "GraphCannySeg.h")
+    cpp = os.path.join(REFERENCE_SRC, "GraphCannySeg.cpp")
+    if not (os.path.exists(hdr) and os.path.exists(cpp)):
+        return None
+    mine = [os.path.join(HERE, "ref_pin", f) for f in ("seg_prelude.h", "seg_class.h", "seg_api.h")]
+    if not force and _newer(SEGPIN_SO, [hdr, cpp, os.path.abspath(__file__), *mine]):
+        return SEGPIN_SO
+    os.makedirs(REF_OUT, exist_ok=True)
+    gen = os.path.join(REF_OUT, "seg_pin_gen%d.cpp" % os.getpid())
+    with open(gen, "w") as fp:
+        fp.write('#include "seg_prelude.h"\n')
+        fp.write(_segmentation_pieces(REFERENCE_SRC))
+        fp.write('#include "seg_api.h"\n')
+    tmp = SEGPIN_SO + ".tmp%d" % os.getpid()
+    try:
+        subprocess.run(["g++", "-O1", "-std=c++14", "-fPIC", "-shared", "-ffp-contract=off", "-w",
+                        "-I", os.path.join(HERE, "ref_pin"), gen, "-o", tmp], check=True)
+        os.replace(tmp, SEGPIN_SO)
+    finally:
+        os.remove(gen)
+    return SEGPIN_SO
+
+
 def build_refgpu(force: bool = False) -> str:
     """This project's harness for the reference kernels (no reference code)."""
     src = [os.path.join(HERE, "ref_gpu", "ref_gpu.cu"), os.path.join(HERE, "ref_gpu", "ref_gpu.h")]
@@ -143,4 +235,5 @@ def build_refgpu(force: bool = False) -> str:
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref_pin(force="--force" in sys.argv))
+    print(build_seg_pin(force="--force" in sys.argv))
     print(build_ref_cubins(force="--force" in sys.argv))

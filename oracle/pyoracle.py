@@ -60,6 +60,7 @@ class Result(C.Structure):
 
 _lib = None
 _pin = None
+_segpin = None
 
 
 def lib():
@@ -87,6 +88,9 @@ def lib():
         L.qo_domain_h.restype = C.c_int32
         L.qo_solve.restype = C.c_int
         L.qo_solve_mt.restype = C.c_int
+        L.qo_segment_graph.restype = C.c_int32
+        L.qo_segment_graph.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_float, C.c_float,
+                                       C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 
@@ -101,6 +105,20 @@ def pin():
             return None
         _pin = C.CDLL(path)
     return _pin
+
+
+def segpin():
+    """The reference's segmentation core (union-find forest, segment_graph,
+    small-component merge, collectSets) compiled for the host (None where
+    the reference sources are absent)."""
+    global _segpin
+    if _segpin is None:
+        path = _build.build_seg_pin()
+        if path is None:
+            return None
+        _segpin = C.CDLL(path)
+        _segpin.sp_segment.restype = C.c_int
+    return _segpin
 
 
 def ptr(a: np.ndarray, t):
@@ -258,3 +276,75 @@ def cosf(x):
 
 def acosf(x):
     return lib().qo_acosf(x)
+
+
+EDGE_DTYPE = np.dtype([("w", np.float32), ("a", np.int32), ("b", np.int32)])
+
+
+def edges_array(a, b, w) -> np.ndarray:
+    e = np.empty(len(w), EDGE_DTYPE)
+    e["a"], e["b"], e["w"] = a, b, w
+    return e
+
+
+def segment_graph(n_vertices: int, edges: np.ndarray, k: float, min_size: float, merge: bool = True,
+                  presorted: bool = False):
+    """The oracle's segmentation core.  edges: EDGE_DTYPE array (a copy is
+    sorted).  Returns (lists, num_sets, sorted_edges): lists is the
+    collectSets listing, one int32 array per set in the order of its
+    smallest pixel, each [first pixel, its parent, the rest of the set]."""
+    e = np.ascontiguousarray(edges, EDGE_DTYPE).copy()
+    offsets = np.zeros(n_vertices + 1, np.int32)
+    points = np.zeros(2 * n_vertices, np.int32)
+    ns = C.c_int32(0)
+    n = lib().qo_segment_graph(n_vertices, len(e), e.ctypes.data, int(presorted), k, min_size, int(merge),
+                               offsets.ctypes.data, points.ctypes.data, C.byref(ns))
+    if n < 0:
+        raise ValueError("qo_segment_graph refused its arguments")
+    return [points[offsets[i]:offsets[i + 1]].copy() for i in range(n)], ns.value, e
+
+
+def segment_graph_reference(H: int, W: int, edges: np.ndarray, k: float, min_size: float, merge: bool = True):
+    """The same through the reference's own code (segpin); None where the
+    reference sources are absent."""
+    sp = segpin()
+    if sp is None:
+        return None
+    n_vertices, m = H * W, len(edges)
+    ea = np.ascontiguousarray(edges["a"], np.int32)
+    eb = np.ascontiguousarray(edges["b"], np.int32)
+    ew = np.ascontiguousarray(edges["w"], np.float32)
+    sa, sb, sw = np.zeros(max(m, 1), np.int32), np.zeros(max(m, 1), np.int32), np.zeros(max(m, 1), np.float32)
+    offsets = np.zeros(n_vertices + 1, np.int32)
+    points = np.zeros(2 * n_vertices, np.int32)
+    nl, ns = C.c_int(0), C.c_int(0)
+    rc = sp.sp_segment(C.c_int(n_vertices), C.c_int(m), C.c_void_p(ea.ctypes.data), C.c_void_p(eb.ctypes.data),
+                       C.c_void_p(ew.ctypes.data), C.c_float(k), C.c_float(min_size), C.c_int(int(merge)),
+                       C.c_int(H), C.c_int(W), C.c_void_p(sa.ctypes.data), C.c_void_p(sb.ctypes.data),
+                       C.c_void_p(sw.ctypes.data), C.c_void_p(offsets.ctypes.data), C.c_void_p(points.ctypes.data),
+                       C.byref(nl), C.byref(ns))
+    if rc != 0:
+        raise ValueError("sp_segment refused its arguments")
+    lists = [points[offsets[i]:offsets[i + 1]].copy() for i in range(nl.value)]
+    return lists, ns.value, edges_array(sa[:m], sb[:m], sw[:m])
+
+
+def grid_edges(H: int, W: int, weight) -> np.ndarray:
+    """The reference's pixel graph (GraphCannySeg.cpp segment_image): for
+    each pixel (x, y) in row-major order, the edges to (x+1, y), (x, y+1),
+    (x+1, y+1) and (x+1, y-1) that lie inside the image, in that order;
+    weight(a, b) gives each edge's weight from the two pixel indices."""
+    a, b = [], []
+    for y in range(H):
+        for x in range(W):
+            i = y * W + x
+            if x < W - 1:
+                a.append(i); b.append(i + 1)
+            if y < H - 1:
+                a.append(i); b.append(i + W)
+            if x < W - 1 and y < H - 1:
+                a.append(i); b.append(i + W + 1)
+            if x < W - 1 and y > 0:
+                a.append(i); b.append(i - W + 1)
+    a, b = np.array(a, np.int32), np.array(b, np.int32)
+    return edges_array(a, b, np.asarray(weight(a, b), np.float32))

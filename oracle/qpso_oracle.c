@@ -1008,3 +1008,160 @@ int qo_solve(const float *mesh, uint32_t F, const uint16_t *obs, const qo_camera
     return qo_solve_mt(mesh, F, obs, cam, prm, pos, vel, pbest, pbest_fit, res, trace_gbest,
                        trace_fit, 1);
 }
+
+/* ------------------------------------------------------------------------
+ * Segmentation core: disjoint-set forest (GraphCannySeg.cpp:231-272),
+ * segment_graph (GraphCannySeg.cpp:1301-1373), the small-component merge
+ * (GraphCannySeg.cpp:1243-1248) and the set listing that numbers the
+ * clusters (collectSets, GraphCannySeg.cpp:305-352).
+ * ------------------------------------------------------------------------ */
+
+typedef struct {
+    int32_t *parent, *rank, *size, *link;
+    int32_t count;
+} qo_forest;
+
+/* find: walk to the root, then point x (only x) at it -- the reference's
+ * one-step compression (GraphCannySeg.cpp:247-253).  Which node a set's
+ * first pixel points at decides the duplicated entry of its list. */
+static int32_t qo_forest_find(qo_forest *f, int32_t x)
+{
+    int32_t r = x;
+    while (f->parent[r] != r) r = f->parent[r];
+    f->parent[x] = r;
+    return r;
+}
+
+/* join of two roots (GraphCannySeg.cpp:255-272): splice the circular member
+ * lists, then union by rank with y winning ties (y's rank grows). */
+static void qo_forest_join(qo_forest *f, int32_t x, int32_t y)
+{
+    const int32_t t = f->link[y];
+    f->link[y] = f->link[x];
+    f->link[x] = t;
+    if (f->rank[x] > f->rank[y]) {
+        f->parent[y] = x;
+        f->size[x] += f->size[y];
+    } else {
+        f->parent[x] = y;
+        f->size[y] += f->size[x];
+        if (f->rank[x] == f->rank[y]) f->rank[y] += 1;
+    }
+    f->count -= 1;
+}
+
+static const qo_edge *qo_sort_base;
+
+/* ascending weight; equal weights by input position (a total order, so
+ * qsort's lack of stability does not matter) */
+static int qo_edge_order(const void *pa, const void *pb)
+{
+    const int32_t i = *(const int32_t *)pa, j = *(const int32_t *)pb;
+    const float wi = qo_sort_base[i].w, wj = qo_sort_base[j].w;
+    if (wi < wj) return -1;
+    if (wj < wi) return 1;
+    return (i > j) - (i < j);
+}
+
+int32_t qo_segment_graph(int32_t n_vertices, int32_t n_edges, qo_edge *edges, int32_t presorted,
+                         float k, float min_size, int32_t merge, int32_t *offsets, int32_t *points,
+                         int32_t *num_sets)
+{
+    if (n_vertices <= 0 || n_edges < 0) return -1;
+    for (int32_t e = 0; e < n_edges; ++e)
+        if (edges[e].a < 0 || edges[e].a >= n_vertices || edges[e].b < 0 || edges[e].b >= n_vertices ||
+            edges[e].w != edges[e].w)
+            return -1;
+
+    if (!presorted && n_edges > 1) {
+        /* DEVIATION: ties keep their input order; the reference's std::sort
+         * (GraphCannySeg.cpp:1303) leaves the order of equal weights to the
+         * C++ library's introsort. */
+        int32_t *ord = (int32_t *)malloc((size_t)n_edges * sizeof(int32_t));
+        qo_edge *tmp = (qo_edge *)malloc((size_t)n_edges * sizeof(qo_edge));
+        if (!ord || !tmp) {
+            free(ord);
+            free(tmp);
+            return -1;
+        }
+        for (int32_t e = 0; e < n_edges; ++e) ord[e] = e;
+        qo_sort_base = edges;
+        qsort(ord, (size_t)n_edges, sizeof(int32_t), qo_edge_order);
+        for (int32_t e = 0; e < n_edges; ++e) tmp[e] = edges[ord[e]];
+        memcpy(edges, tmp, (size_t)n_edges * sizeof(qo_edge));
+        free(ord);
+        free(tmp);
+    }
+
+    const size_t n = (size_t)n_vertices;
+    qo_forest f;
+    f.parent = (int32_t *)malloc(4 * n * sizeof(int32_t));
+    float *thr = (float *)malloc(n * sizeof(float));
+    uint8_t *listed = (uint8_t *)calloc(n, 1);
+    if (!f.parent || !thr || !listed) {
+        free(f.parent);
+        free(thr);
+        free(listed);
+        return -1;
+    }
+    f.rank = f.parent + n;
+    f.size = f.parent + 2 * n;
+    f.link = f.parent + 3 * n;
+    f.count = n_vertices;
+    for (int32_t v = 0; v < n_vertices; ++v) {
+        f.parent[v] = v;
+        f.rank[v] = 0;
+        f.size[v] = 1;
+        f.link[v] = v;
+        thr[v] = k / (float)1;  /* THRESHOLD(1, k) = k / |C| with |C| = 1 */
+    }
+
+    /* Kruskal-like pass: merge when the edge is no heavier than both
+     * components' thresholds, then the merged root's threshold becomes
+     * w + k / |C| (segment_graph). */
+    for (int32_t e = 0; e < n_edges; ++e) {
+        const float w = edges[e].w;
+        int32_t a = qo_forest_find(&f, edges[e].a);
+        const int32_t b = qo_forest_find(&f, edges[e].b);
+        if (a == b || !(w <= thr[a] && w <= thr[b])) continue;
+        qo_forest_join(&f, a, b);
+        a = qo_forest_find(&f, a);
+        thr[a] = w + k / (float)f.size[a];
+    }
+
+    /* small components: the same sorted edges once more; min_size is a
+     * float and the comparison is int < float, as in the reference */
+    if (merge) {
+        for (int32_t e = 0; e < n_edges; ++e) {
+            const int32_t a = qo_forest_find(&f, edges[e].a);
+            const int32_t b = qo_forest_find(&f, edges[e].b);
+            if (a != b && ((float)f.size[a] < min_size || (float)f.size[b] < min_size))
+                qo_forest_join(&f, a, b);
+        }
+    }
+    *num_sets = f.count;
+
+    /* collectSets: sets in the order of their smallest pixel; each list is
+     * that pixel, its parent pointer (not find(): whatever node the forest
+     * left it pointing at, possibly the pixel itself), then the circular
+     * list from the pixel onward -- which visits the parent again. */
+    int32_t lists = 0, np = 0;
+    offsets[0] = 0;
+    for (int32_t v = 0; v < n_vertices; ++v) {
+        if (listed[v]) continue;
+        points[np++] = v;
+        listed[v] = 1;
+        const int32_t p = f.parent[v];
+        points[np++] = p;
+        listed[p] = 1;
+        for (int32_t x = f.link[v]; x != v; x = f.link[x]) {
+            listed[x] = 1;
+            points[np++] = x;
+        }
+        offsets[++lists] = np;
+    }
+    free(f.parent);
+    free(thr);
+    free(listed);
+    return lists;
+}

@@ -183,6 +183,36 @@ int qo_solve_mt(const float *mesh, uint32_t num_faces, const uint16_t *obs,
 
 void qo_default_params(qo_params *prm);
 
+/* ---- segmentation core (the producer of the clusters) ----
+ * The disjoint-set forest, segment_graph and the small-component merge of
+ * the reference's graph segmentation (GraphCannySeg.cpp:231-272,
+ * 1301-1373, 1243-1248), and the listing of its sets that numbers the
+ * clusters (collectSets, GraphCannySeg.cpp:305-352).  Pinned against
+ * those functions compiled from the reference sources (oracle/ref_pin,
+ * build_seg_pin) and against fixtures frozen from them. */
+typedef struct {
+    float w;
+    int32_t a, b;
+} qo_edge;
+
+/* Sorts the edges by weight in place (ascending; ties keep their input
+ * order, where the reference's unstable std::sort leaves the order of equal
+ * weights to the C++ library: DEVIATION) unless presorted != 0, merges
+ * with threshold k / |C| (segment_graph), then, when merge != 0, joins the
+ * ends of every edge, in the same order, whose components differ and one of
+ * which is smaller than min_size.  Then lists the sets as collectSets does:
+ * one list per set in the order of the set's smallest pixel index, each
+ * [first pixel, its parent, the rest of the set's circular list], so a set
+ * of n pixels gives a list of n + 1 entries.
+ *
+ * offsets receives n_lists + 1 entries (capacity n_vertices + 1), points
+ * the lists' pixel indices (capacity 2 * n_vertices).  *num_sets receives
+ * the forest's set count.  Returns n_lists, or -1 on bad arguments
+ * (non-positive n_vertices, an edge end out of range, a NaN weight). */
+int32_t qo_segment_graph(int32_t n_vertices, int32_t n_edges, qo_edge *edges, int32_t presorted,
+                         float k, float min_size, int32_t merge, int32_t *offsets, int32_t *points,
+                         int32_t *num_sets);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,7 +16,15 @@ intrinsics.  Needs the reference sources (QPSO_REFERENCE_SRC, default
 oracle_c1.npz -- the oracle's own C1 solve (per-iteration global best and
 final state), frozen so that later changes to the oracle are caught.
 
-Usage:  python tests/golden/make_golden.py
+ref_seg.npz -- the reference's segmentation core (disjoint-set forest,
+segment_graph, small-component merge, collectSets; GraphCannySeg.cpp) run
+by oracle/build.py's build_seg_pin on the pixel graphs of
+tests/test_segmentation_core.py: per case the edges, and the collectSets
+lists with the set count.  The tie case stores the edges in the order the
+reference's std::sort left them (presorted).
+
+Usage:  python tests/golden/make_golden.py            (every fixture)
+        python tests/golden/make_golden.py --only seg (ref_seg.npz alone)
 """
 from __future__ import annotations
 
@@ -70,7 +78,57 @@ def raster_cases(rng, n):
     return np.stack(tris)
 
 
+def make_seg_golden():
+    import test_segmentation_core as T
+
+    cases = [T.CASES[i] for i in (0, 1, 2, 4, 7, 8)]
+    runs = []
+    for case in cases:
+        H, W, _, k, min_size, merge, _ = case
+        edges = T._case_edges(case)
+        res = po.segment_graph_reference(H, W, edges, k, min_size, merge)
+        if res is None:
+            raise SystemExit("reference sources not found; set QPSO_REFERENCE_SRC")
+        runs.append((H, W, k, min_size, merge, 0, edges, res))
+    H, W = 24, 32
+    tied = T.region_weights(H, W, 6, np.random.default_rng(11), tie_levels=16)
+    res = po.segment_graph_reference(H, W, tied, 0.05, 20.0, True)
+    runs.append((H, W, 0.05, 20.0, True, 1, res[2], res))
+
+    e_off, l_off, bounds, pts = [0], [0], [], []
+    ea, eb, ew = [], [], []
+    for H, W, k, min_size, merge, presorted, edges, (lists, ns, _) in runs:
+        ea.append(edges["a"]); eb.append(edges["b"]); ew.append(edges["w"])
+        e_off.append(e_off[-1] + len(edges))
+        base = sum(len(p) for p in pts)
+        b = [base]
+        for L in lists:
+            pts.append(L.astype(np.int32))
+            b.append(b[-1] + len(L))
+        l_off.append(l_off[-1] + len(b))
+        bounds.extend(b)
+    # list_bounds holds, per case, n_lists + 1 absolute offsets into points;
+    # case c's block is list_bounds[list_off[c] : list_off[c+1]]
+    np.savez_compressed(
+        os.path.join(HERE, "ref_seg.npz"),
+        case_hw=np.array([(r[0], r[1]) for r in runs], np.int32),
+        case_k_min=np.array([(r[2], r[3]) for r in runs], np.float32),
+        case_merge=np.array([r[4] for r in runs], np.int32),
+        presorted=np.array([r[5] for r in runs], np.int32),
+        num_sets=np.array([r[7][1] for r in runs], np.int32),
+        edge_a=np.concatenate(ea).astype(np.int32), edge_b=np.concatenate(eb).astype(np.int32),
+        edge_w=np.concatenate(ew).astype(np.float32), edge_off=np.array(e_off, np.int64),
+        list_off=np.array(l_off, np.int64), list_bounds=np.array(bounds, np.int64),
+        points=np.concatenate(pts))
+
+
 def main():
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    if sys.argv[1:] == ["--only", "seg"]:
+        make_seg_golden()
+        print("wrote ref_seg.npz")
+        return
+    make_seg_golden()
     pin = po.pin()
     if pin is None:
         raise SystemExit("reference sources not found; set QPSO_REFERENCE_SRC")
