@@ -118,12 +118,21 @@ qpso_status qpso_frame_upload(qpso_context *ctx, const uint16_t *depth_mm, const
                               const qpso_camera *cam, uint32_t *frame_id);
 qpso_status qpso_frame_release(qpso_context *ctx, uint32_t frame_id);
 
-/* One cluster of a frame's label map, as the segmentation's SegResults
- * record carries it (GraphCannySeg.h:594-618): the pixel count
- * (num_points), the bounding rectangle (rect_aabb_, max exclusive) and the
- * centroid of the back-projected pixels that have depth (centroid3D,
- * compute3DCentroid GraphCannySeg.h:2569-2597: X = (u - cx) z / fx,
- * Y = (v - cy) z / fy, Z = z, in mm).  The sums are exact integers here. */
+/* One cluster of a frame's label map, with the fields of the segmentation's
+ * SegResults record (GraphCannySeg.h:594-618) that the solve reads: the
+ * pixel count (num_points), the bounding rectangle (rect_aabb_, max
+ * exclusive) and the centroid of the back-projected pixels that have depth
+ * (centroid3D, compute3DCentroid GraphCannySeg.h:2569-2597:
+ * X = (u - cx) z / fx, Y = (v - cy) z / fy, Z = z, in mm).  The sums are
+ * exact integers here.
+ *
+ * The reference's records are built from collectSets lists
+ * (GraphCannySeg.cpp:305-352), which hold one pixel of the cluster twice
+ * (the first pixel's union-find parent).  So its SegResults.num_points, the
+ * fitness's num_point_SegmentedCluster, is this num_points + 1, and its
+ * centroid counts that one pixel twice (which pixel a label map does not
+ * say).  To reproduce the reference's fitness from a label map, fill
+ * qpso_solve_desc.num_points with num_points + 1, as qpso_main does. */
 typedef struct {
     int32_t label;
     uint32_t num_points;

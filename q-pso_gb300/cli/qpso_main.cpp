@@ -180,7 +180,10 @@ int main(int argc, char** argv) {
   d.cl_max_x = c->max_x;
   d.cl_min_y = c->min_y;
   d.cl_max_y = c->max_y;
-  d.num_points = c->num_points;
+  // the reference's cluster size is its collectSets list length, which
+  // repeats one pixel (GraphCannySeg.cpp:305-352): pixels + 1 reach the
+  // fitness as num_point_SegmentedCluster (main.cu:1322)
+  d.num_points = c->num_points + 1;
   qpso_box_from_centroid(c->centroid_mm, 0.3f, 0.3f, d.t_lo, d.t_hi);  // main.cu:1285-1323
   if (particles) d.num_particles = (uint32_t)particles;
   if (iterations) d.iterations = (uint32_t)iterations;

@@ -2,7 +2,9 @@
 and PNG depth, a PNG label map in place of the segmentation, and the two
 result files the reference writes (main.cu:1752-1762):
 results/<rgb>-<N>-bestpose.csv equals the library's solve of the same
-cluster printed as the reference prints it, and results/<rgb>-<N>-best.csv
+cluster printed as the reference prints it (with the reference's cluster
+size, pixels + 1: its collectSets lists repeat one pixel), and
+results/<rgb>-<N>-best.csv
 equals the oracle's restatement of the reference's host render of that pose.
 The cluster records equal the label map's own pixel statistics."""
 import os
@@ -74,7 +76,7 @@ def test_cli_outputs_equal_library_and_oracle(gpu_ctx, files, depth_name):
     lo, hi = qpso.box_from_centroid(c["centroid_mm"])
     x0, x1, y0, y1 = c["aabb"]
     desc = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=k, cl_min_x=x0, cl_max_x=x1,
-                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"], t_lo=lo, t_hi=hi,
+                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"] + 1, t_lo=lo, t_hi=hi,
                            num_particles=32, iterations=6, seed=7, stream=0)
     res = gpu_ctx.solve(desc)
     stem = d / "results" / ("img_0042.png-%d" % k)
@@ -105,7 +107,7 @@ def test_cli_edge_raster_mode(gpu_ctx, files):
     lo, hi = qpso.box_from_centroid(c["centroid_mm"])
     x0, x1, y0, y1 = c["aabb"]
     desc = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=k, cl_min_x=x0, cl_max_x=x1,
-                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"], t_lo=lo, t_hi=hi,
+                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"] + 1, t_lo=lo, t_hi=hi,
                            num_particles=32, iterations=6, seed=7, stream=0, raster_mode=qpso.RASTER_EDGE)
     res = gpu_ctx.solve(desc)
     got = open(str(d / "res_edge" / ("img_0042.png-%d-bestpose.csv" % k))).read()
@@ -133,7 +135,7 @@ def test_cli_default_reference_projection(gpu_ctx, files):
     lo, hi = qpso.box_from_centroid(c["centroid_mm"])
     x0, x1, y0, y1 = c["aabb"]
     desc = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=k, cl_min_x=x0, cl_max_x=x1,
-                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"], t_lo=lo, t_hi=hi,
+                           cl_min_y=y0, cl_max_y=y1, num_points=c["num_points"] + 1, t_lo=lo, t_hi=hi,
                            num_particles=32, iterations=6, seed=7, stream=0)
     res = gpu_ctx.solve(desc)
     stem = d / "res_ref" / ("img_0042.png-%d" % k)
