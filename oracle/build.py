@@ -134,21 +134,48 @@ def build_ref_cubins(force: bool = False) -> dict | None:
 SEGPIN_SO = os.path.join(REF_OUT, "libqpso_segpin.so")
 
 
-def _code_braces(line: str) -> int:
-    code = line.split("//", 1)[0]
-    return code.count("{") - code.count("}")
+def _code_only(lines: list[str]) -> list[str]:
+    """The lines with comments, string and character literals blanked out
+    (line structure kept), for counting braces."""
+    out, block = [], False
+    for line in lines:
+        res, i, n = [], 0, len(line)
+        while i < n:
+            if block:
+                j = line.find("*/", i)
+                if j < 0:
+                    i = n
+                else:
+                    block, i = False, j + 2
+                continue
+            ch = line[i]
+            if line.startswith("//", i):
+                break
+            if line.startswith("/*", i):
+                block, i = True, i + 2
+                continue
+            if ch in "\"'":
+                j = i + 1
+                while j < n and line[j] != ch:
+                    j += 2 if line[j] == "\\" else 1
+                i = j + 1
+                continue
+            res.append(ch)
+            i += 1
+        out.append("".join(res))
+    return out
 
 
 def _block(lines: list[str], start: int) -> tuple[int, int]:
     """[start, end) of the brace-balanced block that opens on or after
-    line `start` (// comments ignored)."""
+    line `start` (comments and literals ignored)."""
+    code = _code_only(lines[start:])
     depth, opened = 0, False
-    for i in range(start, len(lines)):
-        d = _code_braces(lines[i])
-        opened = opened or "{" in lines[i].split("//", 1)[0]
-        depth += d
+    for k, text in enumerate(code):
+        opened = opened or "{" in text
+        depth += text.count("{") - text.count("}")
         if opened and depth == 0:
-            return start, i + 1
+            return start, start + k + 1
     raise ValueError("unbalanced block at line %d" % (start + 1))
 
 
@@ -157,37 +184,93 @@ def _find(lines: list[str], text: str, after: int = 0) -> int:
 
 
 def _segmentation_pieces(src: str) -> str:
-    """The reference's disjoint-set forest and graph segmentation, read
-    from GraphCannySeg.h/.cpp where they lie, each piece under a #line of
-    its own: THRESHOLD, edge, uni_elt, universe (header); edge's
-    constructors and operator<, universe's methods, segment_graph and the
-    small-component merge loop (source)."""
+    """The reference's graph segmentation from its pixel planes to its
+    cluster lists, read from GraphCannySeg.h/.cpp where they lie, each piece
+    under a #line of its own.  Header: deg2rad, THRESHOLD, the pixel types,
+    square, the image template, mapminmax, the Gaussian smoothing (mask,
+    normalisation, separable convolution), edge, uni_elt, universe, and the
+    edge weight diff() inside a stand-in of the GraphCannySeg class (members
+    in ref_pin/seg_class.h).  Source: the image constructor and destructor,
+    edge's constructors and operator<, universe's methods, segment_graph,
+    and three fragments of segment_image: the depth normalisation, the
+    pixel-graph loop and the small-component merge loop."""
     h = open(os.path.join(src, "GraphCannySeg.h")).read().splitlines(keepends=True)
     c = open(os.path.join(src, "GraphCannySeg.cpp")).read().splitlines(keepends=True)
 
     def piece(lines, name, a, b):
         return '#line %d "%s"\n%s' % (a + 1, name, "".join(lines[a:b]))
 
+    def hdr(a, b):
+        return piece(h, "GraphCannySeg.h", a, b)
+
+    def cpp(a, b):
+        return piece(c, "GraphCannySeg.cpp", a, b)
+
+    def templated(lines, sig):
+        i = _find(lines, sig)
+        assert lines[i - 1].strip() == "template <class T>", sig
+        return i - 1, _block(lines, i)[1]
+
     out = []
+    i = _find(h, "#ifndef deg2rad")
+    out.append(hdr(i, i + 3))
     i = _find(h, "#define THRESHOLD(size, c)")
-    out.append(piece(h, "GraphCannySeg.h", i, i + 1))
+    out.append(hdr(i, i + 1))
     out.append("namespace GraphCanny {\n")
-    out.append(piece(h, "GraphCannySeg.h", *_block(h, _find(h, "struct edge{"))))
+    for sig in ("struct edge{", "struct rgb{", "struct hsv{", "struct CIELab{"):
+        out.append(hdr(*_block(h, _find(h, sig))))
+    i = _find(h, "inline T square(const T &x)")
+    out.append(hdr(i - 1, i + 1))
+    out.append(hdr(*templated(h, "class image {")))
+    for macro in ("#define imRef(im, x, y)", "#define imPtr(im, x, y)"):
+        i = _find(h, macro)
+        out.append(hdr(i, i + 1))
+    out.append(hdr(*templated(h, "inline T mapminmax(const T& x")))
+    out.append(hdr(*_block(h, _find(h, "static inline void convolve_even(image<float> *src"))))
+    i = _find(h, "#define WIDTH 4.0")
+    out.append(hdr(i, i + 1))
+    out.append(hdr(*_block(h, _find(h, "static inline void normalize(std::vector<float> &mask)"))))
+    i = _find(h, "#define MAKE_FILTER(name, fun)")
+    j = i
+    while h[j].rstrip().endswith("\\"):
+        j += 1
+    out.append(hdr(i, j + 1))
+    i = _find(h, "MAKE_FILTER(fgauss,")
+    out.append(hdr(i, i + 1))
+    out.append(hdr(*_block(h, _find(h, "static inline image<float> *smooth(image<float> *src, float sigma)"))))
     end = _find(h, "} uni_elt;")
     start = max(i for i in range(end) if h[i].strip() == "typedef struct {")
-    out.append(piece(h, "GraphCannySeg.h", start, end + 1))
-    out.append(piece(h, "GraphCannySeg.h", *_block(h, _find(h, "class universe {"))))
-    out.append("}\n#include \"seg_class.h\"\nnamespace GraphCanny {\n")
+    out.append(hdr(start, end + 1))
+    out.append(hdr(*_block(h, _find(h, "class universe {"))))
+    out.append("template <class T>\nclass GraphCannySeg {\npublic:\n#include \"seg_class.h\"\n")
+    out.append(hdr(*_block(h, _find(h, "inline float diff(image<float> *r, image<float> *g, image<float> *b,"))))
+    out.append("};\n")
+    out.append(cpp(*templated(c, "image<T>::image(const int width, const int height, const bool init)")))
+    out.append(cpp(*templated(c, "image<T>::~image()")))
     for sig in ("edge::edge()", "edge::edge(int a_, int b_, float w_)", "bool operator<(const edge &a, const edge &b)",
                 "universe::universe(int elements)", "universe::~universe()", "int universe::find(int x)",
                 "void universe::join(int x, int y)", "bool universe::printSet(", "void universe::collectSets("):
-        out.append(piece(c, "GraphCannySeg.cpp", *_block(c, _find(c, sig))))
-    seg = _find(c, "GraphCannySeg<T>::segment_graph(int num_vertices")
-    assert c[seg - 1].strip() == "template <class T>"
-    out.append(piece(c, "GraphCannySeg.cpp", seg - 1, _block(c, seg)[1]))
+        out.append(cpp(*_block(c, _find(c, sig))))
+    out.append(cpp(*templated(c, "GraphCannySeg<T>::segment_graph(int num_vertices")))
+    # segment_image fragments, each wrapped in a member of the stand-in
+    seg_img = _find(c, "GraphCannySeg<T>::segment_image()")
+    a = _find(c, "uint16_t max_depth_val =", seg_img)
+    b = _block(c, _find(c, "for(size_t idx=0;idx<depth_mm_norm->WxH();++idx)", a))[1]
+    out.append("template <class T>\nimage<float> *GraphCannySeg<T>::depth_norm() {\n")
+    out.append(cpp(a, b))
+    out.append("return depth_mm_norm;\n}\n")
+    a = _find(c, "int num = 0;", _find(c, "// 8-connectivity", seg_img))
+    b = _block(c, a + 1)[1]
+    out.append("template <class T>\nint GraphCannySeg<T>::build_edges(image<float> *smooth_h, image<float> *smooth_s,\n"
+               "    image<float> *smooth_v, image<float> *depth_mm_norm, edge *edges) {\n"
+               "std::vector<float> w_planes(4 * (size_t)mWidth * mHeight);\n"
+               "float *pW1 = w_planes.data(), *pW2 = pW1 + (size_t)mWidth * mHeight;\n"
+               "float *pW3 = pW2 + (size_t)mWidth * mHeight, *pW4 = pW3 + (size_t)mWidth * mHeight;\n")
+    out.append(cpp(a, b))
+    out.append("return num;\n}\n")
     loop = _find(c, "for (int i = 0; i < num; i++) {", _find(c, "// post process small components"))
     out.append("template <class T>\nvoid GraphCannySeg<T>::merge_small(universe *u, edge *edges, int num) {\n")
-    out.append(piece(c, "GraphCannySeg.cpp", *_block(c, loop)))
+    out.append(cpp(*_block(c, loop)))
     out.append("}\n}\n")
     return "".join(out)
 

@@ -88,6 +88,7 @@ def lib():
         L.qo_domain_h.restype = C.c_int32
         L.qo_solve.restype = C.c_int
         L.qo_solve_mt.restype = C.c_int
+        L.qo_edge_weight.restype = C.c_float
         L.qo_segment_graph.restype = C.c_int32
         L.qo_segment_graph.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_float, C.c_float,
                                        C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -348,3 +349,103 @@ def grid_edges(H: int, W: int, weight) -> np.ndarray:
                 a.append(i); b.append(i - W + 1)
     a, b = np.array(a, np.int32), np.array(b, np.int32)
     return edges_array(a, b, np.asarray(weight(a, b), np.float32))
+
+
+class SegParams(C.Structure):
+    _fields_ = [("sigma", C.c_float), ("k", C.c_float), ("min_size", C.c_float), ("kx", C.c_float),
+                ("ky", C.c_float), ("ks", C.c_float), ("kdv", C.c_float), ("kdc", C.c_float)]
+
+
+def seg_params(**kw) -> SegParams:
+    """The reference main's segmentation constants (main.h:58-65,
+    main.cu:1214-1217), with keyword overrides."""
+    sp = SegParams()
+    lib().qo_seg_default_params(C.byref(sp))
+    for k, v in kw.items():
+        setattr(sp, k, v)
+    return sp
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def smooth(plane: np.ndarray, sigma: float) -> np.ndarray:
+    src = _f32(plane)
+    H, W = src.shape
+    dst = np.empty_like(src)
+    if lib().qo_smooth(src.ctypes.data_as(C.c_void_p), W, H, C.c_float(sigma), dst.ctypes.data_as(C.c_void_p)):
+        raise ValueError("qo_smooth refused its arguments")
+    return dst
+
+
+def depth_norm(depth: np.ndarray) -> np.ndarray:
+    d = np.ascontiguousarray(depth, np.uint16)
+    H, W = d.shape
+    out = np.empty((H, W), np.float32)
+    lib().qo_depth_norm(d.ctypes.data_as(C.c_void_p), W, H, out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def graph_edges(sh, ss, sv, dnorm, sal, sp: SegParams) -> np.ndarray:
+    """The pixel graph's edges (EDGE_DTYPE) over smoothed planes."""
+    sh, ss, sv, dnorm, sal = (_f32(x) for x in (sh, ss, sv, dnorm, sal))
+    H, W = sh.shape
+    out = np.empty(4 * W * H, EDGE_DTYPE)
+    n = lib().qo_graph_edges(*(x.ctypes.data_as(C.c_void_p) for x in (sh, ss, sv, dnorm, sal)), W, H,
+                             C.byref(sp), out.ctypes.data_as(C.c_void_p))
+    return out[:n].copy()
+
+
+def segment_planes(h8, s8, v8, depth, sal, sp: SegParams):
+    """End to end from 8-bit HSV planes, depth (mm) and saliency to the
+    collectSets lists and the set count."""
+    h8, s8, v8 = (np.ascontiguousarray(x, np.uint8) for x in (h8, s8, v8))
+    d = np.ascontiguousarray(depth, np.uint16)
+    sal = _f32(sal)
+    H, W = h8.shape
+    offsets = np.zeros(W * H + 1, np.int32)
+    points = np.zeros(2 * W * H, np.int32)
+    ns = C.c_int32(0)
+    n = lib().qo_segment_planes(*(x.ctypes.data_as(C.c_void_p) for x in (h8, s8, v8, d, sal)), W, H,
+                                C.byref(sp), offsets.ctypes.data_as(C.c_void_p), points.ctypes.data_as(C.c_void_p),
+                                C.byref(ns))
+    if n < 0:
+        raise ValueError("qo_segment_planes refused its arguments")
+    return [points[offsets[i]:offsets[i + 1]].copy() for i in range(n)], ns.value
+
+
+def smooth_reference(plane: np.ndarray, sigma: float):
+    """The reference's smooth() (segpin); None without the reference."""
+    sp_ = segpin()
+    if sp_ is None:
+        return None
+    src = _f32(plane)
+    H, W = src.shape
+    dst = np.empty_like(src)
+    if sp_.sp_smooth(C.c_int(W), C.c_int(H), C.c_void_p(src.ctypes.data), C.c_float(sigma),
+                     C.c_void_p(dst.ctypes.data)):
+        raise ValueError("sp_smooth refused its arguments")
+    return dst
+
+
+def graph_reference(h8, s8, v8, depth, sal, sp: SegParams):
+    """The reference's segment_image graph (segpin): (edges, smoothed planes
+    [3, H, W], normalised depth); None without the reference."""
+    lib_ = segpin()
+    if lib_ is None:
+        return None
+    h8, s8, v8 = (np.ascontiguousarray(x, np.uint8) for x in (h8, s8, v8))
+    d = np.ascontiguousarray(depth, np.uint16)
+    sal = _f32(sal)
+    H, W = h8.shape
+    ea, eb = np.zeros(4 * W * H, np.int32), np.zeros(4 * W * H, np.int32)
+    ew = np.zeros(4 * W * H, np.float32)
+    sm = np.zeros((3, H, W), np.float32)
+    dn = np.zeros((H, W), np.float32)
+    m = lib_.sp_graph(C.c_int(W), C.c_int(H), *(C.c_void_p(x.ctypes.data) for x in (h8, s8, v8, d, sal)),
+                      C.c_float(sp.sigma), C.c_float(sp.kdv), C.c_float(sp.kdc), C.c_float(sp.kx),
+                      C.c_float(sp.ky), C.c_float(sp.ks), *(C.c_void_p(x.ctypes.data) for x in (ea, eb, ew, sm, dn)))
+    if m < 0:
+        raise ValueError("sp_graph refused its arguments")
+    return edges_array(ea[:m], eb[:m], ew[:m]), sm, dn

@@ -1165,3 +1165,185 @@ int32_t qo_segment_graph(int32_t n_vertices, int32_t n_edges, qo_edge *edges, in
     free(listed);
     return lists;
 }
+
+/* ------------------------------------------------------------------------
+ * Pixel graph: Gaussian smoothing (GraphCannySeg.h:423-489), depth
+ * normalisation (GraphCannySeg.cpp:1105-1127), edge weight (the HSV +
+ * depth + saliency branch of diff, GraphCannySeg.h:2051-2288), the edge
+ * loop (GraphCannySeg.cpp:1174-1210).  The reference's float/double mix is
+ * kept operation by operation; cos, exp and log2f are the C library's, as
+ * the reference calls them.
+ * ------------------------------------------------------------------------ */
+
+void qo_seg_default_params(qo_seg_params *sp)
+{
+    sp->sigma = 0.8f;
+    sp->k = (float)50 / 10000.f;
+    sp->min_size = 500.0f;
+    sp->kx = (float)2000 / 1000.f;
+    sp->ky = (float)30 / 1000.f;
+    sp->ks = (float)49 / 1000.f;
+    sp->kdv = 4.5f;
+    sp->kdc = 0.1f;
+}
+
+int32_t qo_gauss_mask(float sigma, float *mask, int32_t capacity)
+{
+    if (sigma < 0.01f) sigma = 0.01f;
+    /* sigma * WIDTH is a double product (WIDTH is 4.0) */
+    const int32_t len = (int32_t)ceil((double)sigma * 4.0) + 1;
+    if (len > capacity) return -1;
+    for (int32_t i = 0; i < len; ++i) {
+        const float q = (float)i / sigma;
+        const float q2 = q * q;
+        mask[i] = (float)exp(-0.5 * (double)q2);
+    }
+    float sum = 0.0f;
+    for (int32_t i = 1; i < len; ++i) sum += fabsf(mask[i]);
+    sum = 2.0f * sum + fabsf(mask[0]);
+    for (int32_t i = 0; i < len; ++i) mask[i] /= sum;
+    return len;
+}
+
+/* one pass along the rows of a w x h plane, written transposed (h x w) */
+static void qo_convolve_rows_t(const float *src, int32_t w, int32_t h, const float *mask,
+                               int32_t len, float *dst_t)
+{
+    for (int32_t y = 0; y < h; ++y) {
+        const float *row = src + (size_t)y * w;
+        for (int32_t x = 0; x < w; ++x) {
+            float sum = mask[0] * row[x];
+            for (int32_t i = 1; i < len; ++i) {
+                const int32_t xl = x - i > 0 ? x - i : 0;
+                const int32_t xr = x + i < w - 1 ? x + i : w - 1;
+                sum += mask[i] * (row[xl] + row[xr]);
+            }
+            dst_t[(size_t)x * h + y] = sum;
+        }
+    }
+}
+
+int32_t qo_smooth(const float *src, int32_t W, int32_t H, float sigma, float *dst)
+{
+    float mask[256];
+    const int32_t len = qo_gauss_mask(sigma, mask, 256);
+    if (len < 0 || W <= 0 || H <= 0) return -1;
+    float *tmp = (float *)malloc((size_t)W * H * sizeof(float));
+    if (!tmp) return -1;
+    qo_convolve_rows_t(src, W, H, mask, len, tmp);  /* tmp: H wide, W high */
+    qo_convolve_rows_t(tmp, H, W, mask, len, dst);  /* back to W x H */
+    free(tmp);
+    return 0;
+}
+
+void qo_depth_norm(const uint16_t *depth, int32_t W, int32_t H, float *out)
+{
+    const size_t n = (size_t)W * H;
+    /* std::max_element/min_element over [first, last pixel): the last
+     * pixel is not in the range; with one pixel the empty range yields it */
+    uint16_t mx = depth[0], mn = depth[0];
+    if (n > 1) {
+        for (size_t i = 1; i + 1 < n; ++i) {
+            if (depth[i] > mx) mx = depth[i];
+            if (depth[i] < mn) mn = depth[i];
+        }
+    }
+    const float fmn = (float)mn, fmx = (float)mx;
+    for (size_t i = 0; i < n; ++i) {
+        const float d = (float)depth[i];
+        /* mapminmax(d, min, max, 0, 1) = (1 - 0) * (d - min) / (max - min) + 0 */
+        out[i] = (1.0f - 0.0f) * (d - fmn) / (fmx - fmn) + 0.0f;
+    }
+}
+
+float qo_edge_weight(const float *sh, const float *ss, const float *sv, const float *dnorm,
+                     const float *sal, int32_t W, int32_t x1, int32_t y1, int32_t x2, int32_t y2,
+                     const qo_seg_params *sp)
+{
+    const size_t p = (size_t)y1 * W + x1, q = (size_t)y2 * W + x2;
+    const float c_map = 1.f / 255.f;
+    const float h1 = sh[q] * 2.0f, s1 = ss[q] * c_map, v1 = sv[q] * c_map;
+    const float h2 = sh[p] * 2.0f, s2 = ss[p] * c_map, v2 = sv[p] * c_map;
+    const float z_pivot = dnorm[p], z_current = dnorm[q];
+
+    const float delta_v = sp->kdv * fabsf(v1 - v2);
+    const float delta_h = fabsf(h1 - h2);
+    const float theta = delta_h < 180 ? delta_h : 360 - delta_h;
+    /* theta * M_PI / 180.0f is a double expression, so is everything the
+     * cosine touches; the product rounds to float once, at the assignment */
+    const double ang = (double)theta * 3.14159265358979323846 / 180.0;  /* M_PI */
+    const double chord = (double)(s1 * s1 + s2 * s2) - (double)(2.0f * s1 * s2) * cos(ang);
+    const float delta_c = (float)((double)sp->kdc * sqrt(chord));
+    float dist_hsv = sqrtf(delta_v * delta_v + delta_c * delta_c);
+    if (isnan(dist_hsv) || isinf(dist_hsv)) dist_hsv = 0.0f;
+    if (v1 < 0.03f) dist_hsv = 0.01f;
+    dist_hsv /= sqrtf(sp->kdv * sp->kdv + sp->kdc * sp->kdc);
+
+    const float ds = sal[p];
+    const float delta_depth = fabsf(z_pivot - z_current);
+    return (sp->kx * delta_depth * log2f(1.0f + dist_hsv) + sp->ks * ds) / (sp->kx + sp->ks);
+}
+
+int32_t qo_graph_edges(const float *sh, const float *ss, const float *sv, const float *dnorm,
+                       const float *sal, int32_t W, int32_t H, const qo_seg_params *sp, qo_edge *out)
+{
+    int32_t n = 0;
+    for (int32_t y = 0; y < H; ++y)
+        for (int32_t x = 0; x < W; ++x) {
+            const int32_t i = y * W + x;
+            if (x < W - 1) {
+                out[n].a = i;
+                out[n].b = i + 1;
+                out[n++].w = qo_edge_weight(sh, ss, sv, dnorm, sal, W, x, y, x + 1, y, sp);
+            }
+            if (y < H - 1) {
+                out[n].a = i;
+                out[n].b = i + W;
+                out[n++].w = qo_edge_weight(sh, ss, sv, dnorm, sal, W, x, y, x, y + 1, sp);
+            }
+            if (x < W - 1 && y < H - 1) {
+                out[n].a = i;
+                out[n].b = i + W + 1;
+                out[n++].w = qo_edge_weight(sh, ss, sv, dnorm, sal, W, x, y, x + 1, y + 1, sp);
+            }
+            if (x < W - 1 && y > 0) {
+                out[n].a = i;
+                out[n].b = i - W + 1;
+                out[n++].w = qo_edge_weight(sh, ss, sv, dnorm, sal, W, x, y, x + 1, y - 1, sp);
+            }
+        }
+    return n;
+}
+
+int32_t qo_segment_planes(const uint8_t *h8, const uint8_t *s8, const uint8_t *v8,
+                          const uint16_t *depth, const float *sal, int32_t W, int32_t H,
+                          const qo_seg_params *sp, int32_t *offsets, int32_t *points,
+                          int32_t *num_sets)
+{
+    if (W <= 0 || H <= 0) return -1;
+    const size_t n = (size_t)W * H;
+    float *buf = (float *)malloc(7 * n * sizeof(float));
+    qo_edge *edges = (qo_edge *)malloc(4 * n * sizeof(qo_edge));
+    if (!buf || !edges) {
+        free(buf);
+        free(edges);
+        return -1;
+    }
+    float *hf = buf, *sf = buf + n, *vf = buf + 2 * n;
+    float *sh = buf + 3 * n, *ss = buf + 4 * n, *sv = buf + 5 * n, *dn = buf + 6 * n;
+    for (size_t i = 0; i < n; ++i) {
+        hf[i] = (float)h8[i];
+        sf[i] = (float)s8[i];
+        vf[i] = (float)v8[i];
+    }
+    int32_t r = -1;
+    if (qo_smooth(hf, W, H, sp->sigma, sh) == 0 && qo_smooth(sf, W, H, sp->sigma, ss) == 0 &&
+        qo_smooth(vf, W, H, sp->sigma, sv) == 0) {
+        qo_depth_norm(depth, W, H, dn);
+        const int32_t m = qo_graph_edges(sh, ss, sv, dn, sal, W, H, sp, edges);
+        r = qo_segment_graph(W * H, m, edges, 0, sp->k, sp->min_size, 1, offsets, points, num_sets);
+    }
+    free(buf);
+    free(edges);
+    return r;
+}

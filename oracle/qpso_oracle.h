@@ -213,6 +213,54 @@ int32_t qo_segment_graph(int32_t n_vertices, int32_t n_edges, qo_edge *edges, in
                          float k, float min_size, int32_t merge, int32_t *offsets, int32_t *points,
                          int32_t *num_sets);
 
+/* The pixel graph of segment_image (GraphCannySeg.cpp:1053-1250) for an
+ * HSV image, its inpainted depth and its saliency, with the constants the
+ * reference's main passes (main.h:58-65, main.cu:1214-1217). */
+typedef struct {
+    float sigma;      /* 0.8, Gaussian smoothing of each HSV plane */
+    float k;          /* 50 / 10000, segment_graph threshold constant */
+    float min_size;   /* 500, small-component merge */
+    float kx, ky, ks; /* 2000, 30, 49 / 1000: weight mix (ky is unread) */
+    float kdv, kdc;   /* 4.5, 0.1: HSV distance weights */
+} qo_seg_params;
+
+void qo_seg_default_params(qo_seg_params *sp);
+
+/* smooth (GraphCannySeg.h:423-489): the mask exp(-(i/sigma)^2 / 2),
+ * i < ceil(4 sigma) + 1, normalised to unit sum over both sides; a pass
+ * along the rows then one along the columns, edges clamped. */
+int32_t qo_gauss_mask(float sigma, float *mask, int32_t capacity);
+int32_t qo_smooth(const float *src, int32_t W, int32_t H, float sigma, float *dst);
+
+/* the depth mapped to [0, 1] by the minimum and maximum of every pixel
+ * but the last (GraphCannySeg.cpp:1105-1127: the ranges end at the last
+ * pixel's address) */
+void qo_depth_norm(const uint16_t *depth, int32_t W, int32_t H, float *out);
+
+/* the weight of the edge from pivot (x1, y1) to neighbour (x2, y2): the
+ * HSV + depth + saliency branch of diff (GraphCannySeg.h:2051-2288) over
+ * smoothed planes (H in 0..180, S and V in 0..255), normalised depth and
+ * saliency */
+float qo_edge_weight(const float *sh, const float *ss, const float *sv, const float *dnorm,
+                     const float *sal, int32_t W, int32_t x1, int32_t y1, int32_t x2, int32_t y2,
+                     const qo_seg_params *sp);
+
+/* the edges in the reference's order: per pixel in row-major order, to
+ * (x+1, y), (x, y+1), (x+1, y+1), (x+1, y-1) where inside
+ * (GraphCannySeg.cpp:1174-1210); capacity 4 W H; returns the count */
+int32_t qo_graph_edges(const float *sh, const float *ss, const float *sv, const float *dnorm,
+                       const float *sal, int32_t W, int32_t H, const qo_seg_params *sp, qo_edge *out);
+
+/* End to end from 8-bit HSV planes, uint16 depth (mm) and saliency: the
+ * planes as floats, smoothed, the depth normalised, the graph, then
+ * qo_segment_graph with k and min_size (merge on).  Returns n_lists, or -1
+ * (bad sizes, or a NaN weight: a depth image whose pixels but the last are
+ * all equal). */
+int32_t qo_segment_planes(const uint8_t *h8, const uint8_t *s8, const uint8_t *v8,
+                          const uint16_t *depth, const float *sal, int32_t W, int32_t H,
+                          const qo_seg_params *sp, int32_t *offsets, int32_t *points,
+                          int32_t *num_sets);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,23 +1,30 @@
 /*
- * seg_prelude.h -- stand-ins for the names the reference's disjoint-set
- * forest and graph segmentation (GraphCannySeg.h:47-58, 534-563;
- * GraphCannySeg.cpp:15-30, 231-352, 1301-1373, 1243-1248) take from
- * OpenCV, so that those pieces compile on the host without it.
+ * seg_prelude.h -- stand-ins for the names the reference's graph
+ * segmentation (its Gaussian smoothing, edge weight, disjoint-set forest,
+ * segment_graph and set listing in GraphCannySeg.h/.cpp) takes from OpenCV,
+ * so that those pieces compile on the host without it.
  *
  * TEST INFRASTRUCTURE ONLY.  oracle/build.py (build_seg_pin) writes a
  * translation unit that includes this file, then the reference's pieces
- * read from its sources where they lie, then seg_class.h and seg_api.h;
- * the unit exists only while g++ runs.
+ * read from its sources where they lie (with seg_class.h inside the
+ * stand-in class), then seg_api.h; the unit exists only while g++ runs.
  */
 #pragma once
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
+#include <math.h>
+#include <sys/types.h>
+#include <typeinfo>
 #include <vector>
 
 typedef unsigned char uchar;
 
 namespace cv {
+/* cv::Mat: named only in signatures of image<T> members never called */
+struct Mat {};
 /* cv::Point3i: three ints with a (x, y, z) constructor (collectSets) */
 struct Point3i {
     int x, y, z;

@@ -23,6 +23,11 @@ tests/test_segmentation_core.py: per case the edges, and the collectSets
 lists with the set count.  The tie case stores the edges in the order the
 reference's std::sort left them (presorted).
 
+ref_seg_graph.npz -- the reference's pixel graph (Gaussian smoothing, depth
+normalisation, edge loop and edge weight of GraphCannySeg) run by the same
+library on the frames of tests/test_segmentation_graph.py: per frame the
+HSV planes, depth and saliency, and the edges with their weights.
+
 Usage:  python tests/golden/make_golden.py            (every fixture)
         python tests/golden/make_golden.py --only seg (ref_seg.npz alone)
 """
@@ -121,12 +126,32 @@ def make_seg_golden():
         list_off=np.array(l_off, np.int64), list_bounds=np.array(bounds, np.int64),
         points=np.concatenate(pts))
 
+    import test_segmentation_graph as G
+
+    sp = po.seg_params()
+    hw, pix_off, planes = [], [0], {k: [] for k in ("h8", "s8", "v8", "depth", "sal")}
+    e_off, ea, eb, ew = [0], [], [], []
+    for fr in G.FRAMES:
+        h8, s8, v8, d, sal = G.frame(*fr)
+        edges, _, _ = po.graph_reference(h8, s8, v8, d, sal, sp)
+        hw.append(h8.shape)
+        pix_off.append(pix_off[-1] + h8.size)
+        for k, v in zip(planes, (h8, s8, v8, d, sal)):
+            planes[k].append(v.ravel())
+        ea.append(edges["a"]); eb.append(edges["b"]); ew.append(edges["w"])
+        e_off.append(e_off[-1] + len(edges))
+    np.savez_compressed(
+        os.path.join(HERE, "ref_seg_graph.npz"), hw=np.array(hw, np.int32),
+        pix_off=np.array(pix_off, np.int64), **{k: np.concatenate(v) for k, v in planes.items()},
+        edge_off=np.array(e_off, np.int64), edge_a=np.concatenate(ea).astype(np.int32),
+        edge_b=np.concatenate(eb).astype(np.int32), edge_w=np.concatenate(ew).astype(np.float32))
+
 
 def main():
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     if sys.argv[1:] == ["--only", "seg"]:
         make_seg_golden()
-        print("wrote ref_seg.npz")
+        print("wrote ref_seg.npz, ref_seg_graph.npz")
         return
     make_seg_golden()
     pin = po.pin()

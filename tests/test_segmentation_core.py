@@ -18,7 +18,7 @@ from oracle import pyoracle as po
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden", "ref_seg.npz")
-REF_K = 67 / 10000.0  # kfloat, main.cu:1214 (k = 67, GraphCannySeg.cpp:1477)
+REF_K = float(np.float32(50) / np.float32(10000))  # kfloat = k / 10000, k = 50 (main.h:58, main.cu:1214)
 
 
 def region_weights(H, W, n_rect, rng, tie_levels=0):
