@@ -346,6 +346,71 @@ qpso_status qpso_server_stop(qpso_server *srv);
  * (which has no device waits). */
 qpso_status qpso_barrier_selftest(qpso_context *ctx, uint64_t timeout_ns, uint32_t *err_bits);
 
+/* ---- segmentation: the graph stage of GraphCannySeg ----
+ * The reference segments the colour-and-depth frame before the solve
+ * (GraphCannySeg<hsv>::run, GraphCannySeg.cpp:1438-1459).  Its graph stage
+ * (segment_image, GraphCannySeg.cpp:1053-1250) takes an HSV image, the
+ * inpainted depth and a saliency map, builds the pixel graph with edges
+ * to (x+1, y), (x, y+1), (x+1, y+1) and (x+1, y-1), weighs them (diff,
+ * GraphCannySeg.h:2051-2288), merges with segment_graph
+ * (GraphCannySeg.cpp:1301-1373) and the small-component pass
+ * (GraphCannySeg.cpp:1243-1248), and numbers the sets by their smallest
+ * pixel (collectSets, GraphCannySeg.cpp:305-352).  The stages before it
+ * (HSV conversion, inpainting, Canny saliency) and the cluster filter
+ * after it (PostSegmFilter) are OpenCV's or call it and are not here.
+ *
+ * Equal weights: the reference's std::sort leaves their order to the C++
+ * library; here they are ordered by edge index. */
+typedef struct {
+    float sigma;      /* 0.8: Gaussian smoothing of each HSV plane (main.h:65) */
+    float k;          /* 50 / 10000: merge threshold constant (main.h:58, main.cu:1214) */
+    float min_size;   /* 500: smaller components are merged (main.h:64) */
+    float kx, ky, ks; /* 2000, 30, 49 / 1000: weight mix (main.h:59-61); ky is not read */
+    float kdv, kdc;   /* 4.5, 0.1: HSV distance weights (main.h:62-63) */
+} qpso_seg_params;
+
+/* The reference main's values above. */
+void qpso_seg_params_init(qpso_seg_params *p);
+
+/* Edges of the width x height pixel graph, (W-1)(4H-3) + H-1 for
+ * W, H >= 1; 0 for an empty or oversized (above 2^26 pixels) image. */
+uint64_t qpso_segment_num_edges(uint32_t width, uint32_t height);
+
+/* Every edge's ends (pixel indices y*W+x) in the reference's edge order
+ * (GraphCannySeg.cpp:1174-1210): per pixel in row-major order, right,
+ * down, down-right, up-right where inside.  Host only. */
+qpso_status qpso_segment_edge_ends(uint32_t width, uint32_t height, int32_t *a, int32_t *b);
+
+/* The smoothing mask (make_fgauss + normalize, GraphCannySeg.h:462-476):
+ * writes ceil(4 sigma) + 1 taps and returns their count, or -1 above
+ * capacity or for a NaN sigma.  Host only. */
+int32_t qpso_segment_gauss_mask(float sigma, float *mask, int32_t capacity);
+
+/* The merge passes over given edge weights (one per edge, in the order of
+ * qpso_segment_edge_ends): sorted ascending with ties by edge index, then
+ * segment_graph with prm->k and the small-component merge with
+ * prm->min_size.  labels (width*height) receives each pixel's set, sets
+ * numbered by their smallest pixel; *n_clusters the set count.  NaN
+ * weights are refused.  Host only. */
+qpso_status qpso_segment_edges(uint32_t width, uint32_t height, const float *weights,
+                               const qpso_seg_params *prm, int32_t *labels, uint32_t *n_clusters);
+
+/* The whole graph stage.  h, s, v: 8-bit planes (H in 0..180, OpenCV's
+ * 8-bit HSV), depth_mm: the inpainted depth, saliency: one float per
+ * pixel, all width*height row-major on the host.  The GPU smooths the
+ * planes, normalises the depth by the range of every pixel but the last
+ * (the reference's ranges end at the last pixel's address), weighs every
+ * edge and radix-sorts them; the merge passes run on the host as in
+ * qpso_segment_edges.  edge_weights (optional, qpso_segment_num_edges
+ * floats) receives the weights in edge order.  The weight calls CUDA's cos
+ * and log2f where the reference calls the C library's: weights agree to an
+ * ulp or so.  QPSO_ERR_ARG for a NaN weight (all pixels but the last at one
+ * depth, or a NaN saliency) or sigma above 7.75. */
+qpso_status qpso_segment_planes(qpso_context *ctx, const uint8_t *h, const uint8_t *s, const uint8_t *v,
+                                const uint16_t *depth_mm, const float *saliency, uint32_t width,
+                                uint32_t height, const qpso_seg_params *prm, int32_t *labels,
+                                float *edge_weights, uint32_t *n_clusters);
+
 #ifdef __cplusplus
 }
 #endif

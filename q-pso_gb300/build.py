@@ -25,7 +25,10 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "--fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-I", INCLUDE, "-I", CSRC]
-UNITS = ["qpso_kernels.cu", "qpso_api.cu", "qpso_noalloc.cu", "ingest.cpp"]
+UNITS = ["qpso_kernels.cu", "qpso_api.cu", "qpso_noalloc.cu", "qpso_segment.cu", "ingest.cpp"]
+# qpso_segment.cu's host code computes float expressions that must round like
+# the reference's on every host (no fused multiply-add on Arm either)
+UNIT_FLAGS = {"qpso_segment.cu": ["-Xcompiler", "-ffp-contract=off"]}
 HEADERS = ["qpso_device.cuh", "qpso_internal.cuh", "meshlets.h"]
 
 
@@ -48,7 +51,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_unit(u):
         obj = os.path.join(BUILD, os.path.splitext(u)[0] + ".o")
-        cmd = [NVCC, *ARCH, *FLAGS, "-c", os.path.join(CSRC, u), "-o", obj]
+        cmd = [NVCC, *ARCH, *FLAGS, *UNIT_FLAGS.get(u, []), "-c", os.path.join(CSRC, u), "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1138,6 +1138,104 @@ qpso_status qpso_barrier_selftest(qpso_context* ctx, uint64_t timeout_ns, uint32
   return (*err_bits & kErrTimeout) ? QPSO_ERR_TIMEOUT : QPSO_OK;
 }
 
+// ---- segmentation: the graph stage of GraphCannySeg ----
+
+void qpso_seg_params_init(qpso_seg_params* p) {
+  if (!p) return;
+  p->sigma = 0.8f;
+  p->k = (float)50 / 10000.f;
+  p->min_size = 500.0f;
+  p->kx = (float)2000 / 1000.f;
+  p->ky = (float)30 / 1000.f;
+  p->ks = (float)49 / 1000.f;
+  p->kdv = 4.5f;
+  p->kdc = 0.1f;
+}
+
+uint64_t qpso_segment_num_edges(uint32_t width, uint32_t height) {
+  if (width == 0 || height == 0 || (uint64_t)width * height > (1u << 26)) return 0;
+  return seg_num_edges((int32_t)width, (int32_t)height);
+}
+
+qpso_status qpso_segment_edge_ends(uint32_t width, uint32_t height, int32_t* a, int32_t* b) {
+  if (!a || !b || width == 0 || height == 0 || (uint64_t)width * height > (1u << 26)) return QPSO_ERR_ARG;
+  seg_edge_ends((int32_t)width, (int32_t)height, a, b);
+  return QPSO_OK;
+}
+
+int32_t qpso_segment_gauss_mask(float sigma, float* mask, int32_t capacity) {
+  if (!mask || capacity <= 0 || std::isnan(sigma)) return -1;
+  return seg_gauss_mask(sigma, mask, capacity);
+}
+
+}  // extern "C"
+
+namespace {
+
+bool seg_params_ok(const qpso_seg_params* p) {
+  float m[32];
+  return p && std::isfinite(p->sigma) && std::isfinite(p->k) && std::isfinite(p->min_size) &&
+         std::isfinite(p->kx) && std::isfinite(p->ks) && std::isfinite(p->kdv) && std::isfinite(p->kdc) &&
+         seg_gauss_mask(p->sigma, m, 32) > 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+qpso_status qpso_segment_edges(uint32_t width, uint32_t height, const float* weights, const qpso_seg_params* prm,
+                               int32_t* labels, uint32_t* n_clusters) {
+  if (!weights || !labels || !n_clusters || !seg_params_ok(prm) || width == 0 || height == 0 ||
+      (uint64_t)width * height > (1u << 26))
+    return QPSO_ERR_ARG;
+  const int32_t W = (int32_t)width, H = (int32_t)height;
+  const uint64_t E = seg_num_edges(W, H);
+  for (uint64_t e = 0; e < E; ++e)
+    if (std::isnan(weights[e])) return QPSO_ERR_ARG;
+  std::vector<int32_t> ea(E), eb(E);
+  seg_edge_ends(W, H, ea.data(), eb.data());
+  // ascending weight, equal weights by edge index
+  std::vector<uint32_t> order(E);
+  for (uint64_t e = 0; e < E; ++e) order[e] = (uint32_t)e;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t i, uint32_t j) { return weights[i] < weights[j]; });
+  *n_clusters = seg_merge((uint32_t)(W * H), E, order.data(), ea.data(), eb.data(), weights, prm->k,
+                          prm->min_size, labels);
+  return QPSO_OK;
+}
+
+qpso_status qpso_segment_planes(qpso_context* ctx, const uint8_t* h, const uint8_t* s, const uint8_t* v,
+                                const uint16_t* depth_mm, const float* saliency, uint32_t width, uint32_t height,
+                                const qpso_seg_params* prm, int32_t* labels, float* edge_weights,
+                                uint32_t* n_clusters) {
+  if (!ctx || !h || !s || !v || !depth_mm || !saliency || !labels || !n_clusters || width == 0 || height == 0 ||
+      (uint64_t)width * height > (1u << 26))
+    return fail(ctx, QPSO_ERR_ARG, "bad segmentation arguments");
+  if (!seg_params_ok(prm)) return fail(ctx, QPSO_ERR_ARG, "bad segmentation parameters (sigma above 7.75?)");
+  const int32_t W = (int32_t)width, H = (int32_t)height;
+  const uint64_t E = seg_num_edges(W, H);
+  float mask[32];
+  const int len = seg_gauss_mask(prm->sigma, mask, 32);
+  cudaSetDevice(ctx->device);
+  qpso_status st;
+  if ((st = ensure_ws(ctx, seg_workspace_bytes(W, H))) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<uint32_t> order(E);
+  std::vector<int32_t> ea(E), eb(E);
+  std::vector<float> w(E);
+  uint32_t err = 0;
+  const uint8_t* hsv[3] = {h, s, v};
+  QPSO_CUDA(ctx, seg_graph_sorted(hsv, depth_mm, saliency, W, H, mask, len, prm->kdv, prm->kdc, prm->kx, prm->ks,
+                                  ctx->ws.p, ctx->num_sms, ctx->stream, order.data(), ea.data(), eb.data(),
+                                  w.data(), &err));
+  if (err & 5u) return fail(ctx, QPSO_ERR_INTERNAL, "segmentation graph: index out of range");
+  if (err & 2u)
+    return fail(ctx, QPSO_ERR_ARG, "segmentation graph: NaN edge weight (depth range zero, or NaN saliency)");
+  if (edge_weights) std::memcpy(edge_weights, w.data(), sizeof(float) * E);
+  *n_clusters = seg_merge((uint32_t)(W * H), E, order.data(), ea.data(), eb.data(), w.data(), prm->k,
+                          prm->min_size, labels);
+  return QPSO_OK;
+}
+
 }  // extern "C"
 
 // ===========================================================================

@@ -142,4 +142,24 @@ cudaError_t launch_cluster_stats(const uint16_t* depth, const int32_t* labels, i
 cudaError_t launch_host_render(const float* mesh, uint32_t F, const float pose[7], const Camera& cam,
                                float* out, cudaStream_t st);
 
+// Graph stage of the segmentation (qpso_segment.cu).  seg_num_edges: edges
+// of the W x H pixel graph; seg_gauss_mask: the smoothing mask (length, or
+// -1 above capacity); seg_edge_ends: every edge's ends in the reference's
+// order; seg_merge: the merge passes over edges in the given order and the
+// labels numbered by each set's smallest pixel (returns the set count);
+// seg_graph_sorted: upload, smoothing, depth range, edge weights and the
+// radix sort on the GPU, then the sorted order, the edges' ends and weights
+// (in edge order) and the kernels' error bits back on the host
+// (1 and 4: an index out of range, 2: a NaN weight).
+uint64_t seg_num_edges(int32_t W, int32_t H);
+int seg_gauss_mask(float sigma, float* mask, int capacity);
+void seg_edge_ends(int32_t W, int32_t H, int32_t* a, int32_t* b);
+uint32_t seg_merge(uint32_t n_pixels, uint64_t n_edges, const uint32_t* order, const int32_t* ea,
+                   const int32_t* eb, const float* w, float k, float min_size, int32_t* labels);
+size_t seg_workspace_bytes(int32_t W, int32_t H);
+cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
+                             int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
+                             float ks, void* ws, int sms, cudaStream_t st, uint32_t* order_host,
+                             int32_t* ea_host, int32_t* eb_host, float* w_host, uint32_t* err_host);
+
 }  // namespace qpso

@@ -1,0 +1,477 @@
+// qpso_segment.cu -- the graph stage of the reference's segmentation
+// (segment_image, GraphCannySeg.cpp:1053-1250) on the GPU, and its
+// sequential merge pass on the host.
+//
+// GPU, one stream, no waits between kernels:
+//   1. the three 8-bit HSV planes smoothed with the reference's Gaussian
+//      (smooth, GraphCannySeg.h:423-489): a pass along the rows, then one
+//      along the columns, edges clamped, the mask's taps added in order and
+//      every product rounded on its own (no contraction);
+//   2. the depth range over every pixel but the last (the reference's
+//      min/max ranges end at the last pixel's address,
+//      GraphCannySeg.cpp:1105-1115);
+//   3. every edge of the pixel graph, written at its index in the
+//      reference's edge order (GraphCannySeg.cpp:1174-1210) with the
+//      HSV + depth + saliency weight of diff (GraphCannySeg.h:2051-2288),
+//      as a 64-bit key: the weight's order bits above the edge index;
+//   4. a least-significant-digit radix sort of the keys.  It is stable and
+//      the keys are distinct, so equal weights end in edge-index order.
+// Host: segment_graph's merge pass over the sorted edges
+// (GraphCannySeg.cpp:1301-1373), the small-component merge
+// (GraphCannySeg.cpp:1243-1248) and the numbering of the sets in the order
+// of their smallest pixel (collectSets, GraphCannySeg.cpp:305-352).  That
+// pass is a sequential union-find over about 4 edges per pixel, so it runs
+// on the CPU beside the GPU.
+//
+// This unit is compiled with -ffp-contract=off for its host code too: the
+// mask and the thresholds are float expressions that must round like the
+// reference's.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "qpso_internal.cuh"
+
+namespace qpso {
+
+// Edges before pixel (x, y) in the reference's order.  A pixel with
+// x < W-1 has 1 + 2 [y < H-1] + [y > 0] edges (right, down, down-right,
+// up-right); the last pixel of a row has [y < H-1] (down).  Summing rows:
+// start(y) = (W-1) (y + 2 min(y, H-1) + max(y-1, 0)) + min(y, H-1).
+__host__ __device__ inline uint64_t seg_edge_base(int32_t x, int32_t y, int32_t W, int32_t H) {
+  const uint64_t ym = (uint64_t)(y < H - 1 ? y : H - 1);
+  const uint64_t start = (uint64_t)(W - 1) * ((uint64_t)y + 2 * ym + (uint64_t)(y > 0 ? y - 1 : 0)) + ym;
+  const uint64_t per = 1u + 2u * (y < H - 1) + (y > 0);
+  return start + (uint64_t)x * per;
+}
+
+uint64_t seg_num_edges(int32_t W, int32_t H) {
+  return W <= 0 || H <= 0 ? 0 : seg_edge_base(0, H, W, H);
+}
+
+namespace {
+
+constexpr int kMaskCap = 32;
+constexpr int kRsThreads = 256;  // one thread per digit value
+constexpr int kRsItems = 16;
+constexpr int kRsTile = kRsThreads * kRsItems;  // keys per radix-sort block
+
+struct SegConst {
+  float mask[kMaskCap];
+  int32_t len;
+  int32_t W, H;
+  float kdv, kdc, kx, ks;
+};
+
+// ---- 1. smoothing ------------------------------------------------------
+
+__global__ void seg_rows_kernel(const uint8_t* __restrict__ in, float* __restrict__ out, SegConst c) {
+  const size_t n = (size_t)c.W * c.H;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < 3 * n; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t plane = t / n, p = t - plane * n;
+    const int32_t y = (int32_t)(p / (size_t)c.W), x = (int32_t)(p - (size_t)y * c.W);
+    const uint8_t* row = in + plane * n + (size_t)y * c.W;
+    float sum = c.mask[0] * (float)row[x];
+    for (int i = 1; i < c.len; ++i) {
+      const int32_t xl = x - i > 0 ? x - i : 0;
+      const int32_t xr = x + i < c.W - 1 ? x + i : c.W - 1;
+      sum = sum + c.mask[i] * ((float)row[xl] + (float)row[xr]);
+    }
+    out[t] = sum;
+  }
+}
+
+__global__ void seg_cols_kernel(const float* __restrict__ in, float* __restrict__ out, SegConst c) {
+  const size_t n = (size_t)c.W * c.H;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < 3 * n; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t plane = t / n, p = t - plane * n;
+    const int32_t y = (int32_t)(p / (size_t)c.W), x = (int32_t)(p - (size_t)y * c.W);
+    const float* col = in + plane * n + x;
+    float sum = c.mask[0] * col[(size_t)y * c.W];
+    for (int i = 1; i < c.len; ++i) {
+      const int32_t yu = y - i > 0 ? y - i : 0;
+      const int32_t yd = y + i < c.H - 1 ? y + i : c.H - 1;
+      sum = sum + c.mask[i] * (col[(size_t)yu * c.W] + col[(size_t)yd * c.W]);
+    }
+    out[t] = sum;
+  }
+}
+
+// ---- 2. depth range ----------------------------------------------------
+
+// mm[0] / mm[1] hold the first pixel's depth on entry
+__global__ void seg_range_kernel(const uint16_t* __restrict__ d, size_t m, uint32_t* mm) {
+  uint32_t lo = 0xFFFFu, hi = 0u;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < m; t += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t v = d[t];
+    lo = v < lo ? v : lo;
+    hi = v > hi ? v : hi;
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(mm, lo);
+    atomicMax(mm + 1, hi);
+  }
+}
+
+// ---- 3. edges ------------------------------------------------------------
+
+// mapminmax(d, min, max, 0, 1) = (1 - 0) (d - min) / (max - min) + 0
+__device__ __forceinline__ float seg_norm_depth(uint16_t d, float mn, float mx) {
+  return (1.0f - 0.0f) * ((float)d - mn) / (mx - mn) + 0.0f;
+}
+
+// The HSV + depth + saliency branch of diff.  The reference's deg2rad is
+// M_PI / 180.0f without parentheses, so the angle and everything the cosine
+// touches are double; the chroma term rounds to float once.  cos and log2f
+// are CUDA's here and the C library's in the reference: the weights agree
+// to an ulp or so.
+__device__ float seg_weight(const float* __restrict__ sh, const float* __restrict__ ss,
+                            const float* __restrict__ sv, size_t p, size_t q, float z_pivot, float z_current,
+                            float sal_p, const SegConst& c) {
+  const float c_map = 1.f / 255.f;
+  const float h1 = sh[q] * 2.0f, s1 = ss[q] * c_map, v1 = sv[q] * c_map;
+  const float h2 = sh[p] * 2.0f, s2 = ss[p] * c_map, v2 = sv[p] * c_map;
+  const float delta_v = c.kdv * fabsf(v1 - v2);
+  const float delta_h = fabsf(h1 - h2);
+  const float theta = delta_h < 180.0f ? delta_h : 360.0f - delta_h;
+  const double ang = (double)theta * 3.14159265358979323846 / 180.0;
+  const double chord = (double)(s1 * s1 + s2 * s2) - (double)(2.0f * s1 * s2) * cos(ang);
+  const float delta_c = (float)((double)c.kdc * sqrt(chord));
+  float dist = sqrtf(delta_v * delta_v + delta_c * delta_c);
+  if (isnan(dist) || isinf(dist)) dist = 0.0f;
+  if (v1 < 0.03f) dist = 0.01f;
+  dist = dist / sqrtf(c.kdv * c.kdv + c.kdc * c.kdc);
+  const float dd = fabsf(z_pivot - z_current);
+  return (c.kx * dd * log2f(1.0f + dist) + c.ks * sal_p) / (c.kx + c.ks);
+}
+
+// order bits of a float (ascending as unsigned); -0 is taken as +0, which
+// the reference's operator< does not tell apart either
+__device__ __forceinline__ uint32_t seg_order_bits(float w) {
+  const uint32_t u = __float_as_uint(w == 0.0f ? 0.0f : w);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void seg_edges_kernel(const float* __restrict__ sm, const uint16_t* __restrict__ depth,
+                                 const float* __restrict__ sal, const uint32_t* __restrict__ mm, SegConst c,
+                                 uint64_t n_edges, uint64_t* __restrict__ keys, float* __restrict__ wout,
+                                 int32_t* __restrict__ ea, int32_t* __restrict__ eb, uint32_t* err) {
+  const size_t n = (size_t)c.W * c.H;
+  const float* sh = sm;
+  const float* ss = sm + n;
+  const float* sv = sm + 2 * n;
+  const float mn = (float)mm[0], mx = (float)mm[1];
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int32_t y = (int32_t)(t / (size_t)c.W), x = (int32_t)(t - (size_t)y * c.W);
+    uint64_t e = seg_edge_base(x, y, c.W, c.H);
+    const float zp = seg_norm_depth(depth[t], mn, mx);
+    const float sp = sal[t];
+    const int32_t nx[4] = {x + 1, x, x + 1, x + 1};
+    const int32_t ny[4] = {y, y + 1, y + 1, y - 1};
+    const bool has[4] = {x < c.W - 1, y < c.H - 1, x < c.W - 1 && y < c.H - 1, x < c.W - 1 && y > 0};
+    for (int k = 0; k < 4; ++k) {
+      if (!has[k]) continue;
+      const size_t q = (size_t)ny[k] * c.W + nx[k];
+      const float w = seg_weight(sh, ss, sv, t, q, zp, seg_norm_depth(depth[q], mn, mx), sp, c);
+      if (e >= n_edges) {
+        atomicOr(err, 1u);
+        break;
+      }
+      if (isnan(w)) atomicOr(err, 2u);
+      keys[e] = ((uint64_t)seg_order_bits(w) << 32) | e;
+      wout[e] = w;
+      ea[e] = (int32_t)t;
+      eb[e] = (int32_t)q;
+      ++e;
+    }
+  }
+}
+
+// ---- 4. radix sort -------------------------------------------------------
+
+__global__ void rs_hist_kernel(const uint64_t* __restrict__ keys, uint32_t n, int shift, uint32_t* hist,
+                               uint32_t nblk) {
+  __shared__ uint32_t h[kRsThreads];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * kRsTile;
+  for (int i = 0; i < kRsItems; ++i) {
+    const size_t j = base + (size_t)i * kRsThreads + threadIdx.x;
+    if (j < n) atomicAdd(&h[(uint32_t)(keys[j] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
+}
+
+// exclusive prefix sum of a[0, total) in place, one block of 1024 threads
+__global__ void rs_scan_kernel(uint32_t* a, uint32_t total) {
+  __shared__ uint32_t part[1024];
+  const uint32_t per = (total + 1023u) / 1024u;
+  const uint32_t lo = threadIdx.x * per;
+  const uint32_t hi = lo + per < total ? lo + per : total;
+  uint32_t s = 0;
+  for (uint32_t i = lo; i < hi; ++i) s += a[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024u; off <<= 1) {
+    const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  for (uint32_t i = lo; i < hi; ++i) {
+    const uint32_t v = a[i];
+    a[i] = run;
+    run += v;
+  }
+}
+
+// Stable scatter of one block's tile: keys go out in tile order within each
+// digit.  Each round takes 256 consecutive keys; a key's place is the
+// digit's running position + the same digit's count in earlier warps of the
+// round + its rank among equal digits of its own warp.
+__global__ void rs_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* __restrict__ out, uint32_t n,
+                                  int shift, const uint32_t* __restrict__ offs, uint32_t nblk, uint32_t* err) {
+  __shared__ uint32_t base[kRsThreads];
+  __shared__ uint32_t wcnt[kRsThreads / 32][kRsThreads];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  base[threadIdx.x] = offs[(size_t)threadIdx.x * nblk + blockIdx.x];
+  const size_t tile = (size_t)blockIdx.x * kRsTile;
+  for (int r = 0; r < kRsItems; ++r) {
+    for (int w = 0; w < kRsThreads / 32; ++w) wcnt[w][threadIdx.x] = 0u;
+    __syncthreads();
+    const size_t j = tile + (size_t)r * kRsThreads + threadIdx.x;
+    const bool valid = j < n;
+    const uint64_t key = valid ? in[j] : 0ull;
+    const uint32_t d = valid ? (uint32_t)(key >> shift) & 255u : 256u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    uint32_t total = 0;
+    for (int w = 0; w < kRsThreads / 32; ++w) {
+      const uint32_t cnt = wcnt[w][threadIdx.x];
+      wcnt[w][threadIdx.x] = total;
+      total += cnt;
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = base[d] + wcnt[warp][d] + rank;
+      if (pos < n)
+        out[pos] = key;
+      else
+        atomicOr(err, 4u);
+    }
+    __syncthreads();
+    base[threadIdx.x] += total;
+    __syncthreads();
+  }
+}
+
+int grid_for(size_t work, int threads, int sms) {
+  const size_t blocks = (work + threads - 1) / threads;
+  const size_t cap = (size_t)sms * 8;
+  return (int)(blocks < 1 ? 1 : blocks < cap ? blocks : cap);
+}
+
+int bit_length(uint64_t v) {
+  int b = 0;
+  while (v) {
+    ++b;
+    v >>= 1;
+  }
+  return b;
+}
+
+}  // namespace
+
+// ---- host: mask, edge list, merge pass -----------------------------------
+
+int seg_gauss_mask(float sigma, float* mask, int capacity) {
+  if (!(sigma >= 0.01f)) sigma = 0.01f;  // std::max(sigma, 0.01F); NaN is refused by the caller
+  const int len = (int)std::ceil((double)sigma * 4.0) + 1;
+  if (len > capacity) return -1;
+  for (int i = 0; i < len; ++i) {
+    const float q = (float)i / sigma;
+    const float q2 = q * q;
+    mask[i] = (float)std::exp(-0.5 * (double)q2);
+  }
+  float sum = 0.0f;
+  for (int i = 1; i < len; ++i) sum += std::fabs(mask[i]);
+  sum = 2.0f * sum + std::fabs(mask[0]);
+  for (int i = 0; i < len; ++i) mask[i] /= sum;
+  return len;
+}
+
+void seg_edge_ends(int32_t W, int32_t H, int32_t* a, int32_t* b) {
+  for (int32_t y = 0; y < H; ++y)
+    for (int32_t x = 0; x < W; ++x) {
+      uint64_t e = seg_edge_base(x, y, W, H);
+      const int32_t i = y * W + x;
+      if (x < W - 1) a[e] = i, b[e++] = i + 1;
+      if (y < H - 1) a[e] = i, b[e++] = i + W;
+      if (x < W - 1 && y < H - 1) a[e] = i, b[e++] = i + W + 1;
+      if (x < W - 1 && y > 0) a[e] = i, b[e++] = i - W + 1;
+    }
+}
+
+namespace {
+
+// union-find over the pixels; the threshold of a set lives at its root
+struct Forest {
+  std::vector<int32_t> parent, size;
+  explicit Forest(size_t n) : parent(n), size(n, 1) {
+    for (size_t i = 0; i < n; ++i) parent[i] = (int32_t)i;
+  }
+  int32_t find(int32_t x) {
+    while (parent[x] != x) {
+      parent[x] = parent[parent[x]];
+      x = parent[x];
+    }
+    return x;
+  }
+  int32_t join(int32_t a, int32_t b) {  // roots; returns the new root
+    if (size[a] < size[b]) std::swap(a, b);
+    parent[b] = a;
+    size[a] += size[b];
+    return a;
+  }
+};
+
+}  // namespace
+
+// The merge pass over edges given in sorted order (order[i] = edge index,
+// ea/eb/w indexed by edge), then the small-component merge in the same
+// order, then labels numbered by each set's smallest pixel.  The partition
+// does not depend on the forest's union rule: a threshold is only read at
+// the current root of its set.
+uint32_t seg_merge(uint32_t n_pixels, uint64_t n_edges, const uint32_t* order, const int32_t* ea,
+                   const int32_t* eb, const float* w, float k, float min_size, int32_t* labels) {
+  Forest f(n_pixels);
+  std::vector<float> thr(n_pixels, k / (float)1);  // THRESHOLD(1, k)
+  for (uint64_t i = 0; i < n_edges; ++i) {
+    const uint32_t e = order[i];
+    const float we = w[e];
+    const int32_t a = f.find(ea[e]), b = f.find(eb[e]);
+    if (a == b || !(we <= thr[a] && we <= thr[b])) continue;
+    const int32_t r = f.join(a, b);
+    thr[r] = we + k / (float)f.size[r];
+  }
+  for (uint64_t i = 0; i < n_edges; ++i) {
+    const uint32_t e = order[i];
+    const int32_t a = f.find(ea[e]), b = f.find(eb[e]);
+    if (a != b && ((float)f.size[a] < min_size || (float)f.size[b] < min_size)) f.join(a, b);
+  }
+  std::vector<int32_t> id(n_pixels, -1);
+  uint32_t next = 0;
+  for (uint32_t v = 0; v < n_pixels; ++v) {
+    const int32_t r = f.find((int32_t)v);
+    if (id[r] < 0) id[r] = (int32_t)next++;
+    labels[v] = id[r];
+  }
+  return next;
+}
+
+// ---- GPU graph + sort ------------------------------------------------------
+
+size_t seg_workspace_bytes(int32_t W, int32_t H) {
+  const size_t n = (size_t)W * H;
+  const uint64_t E = seg_num_edges(W, H);
+  const size_t nblk = (size_t)((E + kRsTile - 1) / kRsTile);
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  return al(3 * n) + al(2 * n) + al(4 * n) + 2 * al(12 * n) + 2 * al(8 * E) + 3 * al(4 * E) +
+         al(4 * 256 * (nblk ? nblk : 1)) + al(16);
+}
+
+cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
+                             int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
+                             float ks, void* ws, int sms, cudaStream_t st, uint32_t* order_host,
+                             int32_t* ea_host, int32_t* eb_host, float* w_host, uint32_t* err_host) {
+  const size_t n = (size_t)W * H;
+  const uint64_t E = seg_num_edges(W, H);
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char* p = static_cast<char*>(ws);
+  uint8_t* d_hsv = (uint8_t*)p;
+  p += al(3 * n);
+  uint16_t* d_depth = (uint16_t*)p;
+  p += al(2 * n);
+  float* d_sal = (float*)p;
+  p += al(4 * n);
+  float* d_tmp = (float*)p;
+  p += al(12 * n);
+  float* d_sm = (float*)p;
+  p += al(12 * n);
+  uint64_t* d_k0 = (uint64_t*)p;
+  p += al(8 * E);
+  uint64_t* d_k1 = (uint64_t*)p;
+  p += al(8 * E);
+  float* d_w = (float*)p;
+  p += al(4 * E);
+  int32_t* d_ea = (int32_t*)p;
+  p += al(4 * E);
+  int32_t* d_eb = (int32_t*)p;
+  p += al(4 * E);
+  const uint32_t nblk = (uint32_t)((E + kRsTile - 1) / kRsTile);
+  uint32_t* d_hist = (uint32_t*)p;
+  p += al(4 * 256 * (nblk ? nblk : 1));
+  uint32_t* d_misc = (uint32_t*)p;  // [0] depth min, [1] depth max, [2] error bits
+
+  cudaError_t e;
+  for (int c = 0; c < 3; ++c)
+    if ((e = cudaMemcpyAsync(d_hsv + c * n, hsv_host[c], n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(d_depth, depth_host, 2 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(d_sal, sal_host, 4 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  const uint32_t misc[4] = {depth_host[0], depth_host[0], 0u, 0u};
+  if ((e = cudaMemcpyAsync(d_misc, misc, sizeof(misc), cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+
+  SegConst c{};
+  for (int i = 0; i < len; ++i) c.mask[i] = mask[i];
+  c.len = len;
+  c.W = W;
+  c.H = H;
+  c.kdv = kdv;
+  c.kdc = kdc;
+  c.kx = kx;
+  c.ks = ks;
+  seg_rows_kernel<<<grid_for(3 * n, 256, sms), 256, 0, st>>>(d_hsv, d_tmp, c);
+  seg_cols_kernel<<<grid_for(3 * n, 256, sms), 256, 0, st>>>(d_tmp, d_sm, c);
+  if (n > 1) seg_range_kernel<<<grid_for(n - 1, 256, sms), 256, 0, st>>>(d_depth, n - 1, d_misc);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (E > 0) {
+    seg_edges_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_sm, d_depth, d_sal, d_misc, c, E, d_k0, d_w,
+                                                            d_ea, d_eb, d_misc + 2);
+    // key bits: the edge index in the low bit_length(E - 1) bits, the
+    // weight's order bits in the high 32
+    const int idx_bits = bit_length(E - 1);
+    uint64_t* src = d_k0;
+    uint64_t* dst = d_k1;
+    for (int shift = 0; shift < 64; shift += 8) {
+      if (shift < 32 && shift >= idx_bits) continue;  // all keys share these digits
+      rs_hist_kernel<<<nblk, kRsThreads, 0, st>>>(src, (uint32_t)E, shift, d_hist, nblk);
+      rs_scan_kernel<<<1, 1024, 0, st>>>(d_hist, 256u * nblk);
+      rs_scatter_kernel<<<nblk, kRsThreads, 0, st>>>(src, dst, (uint32_t)E, shift, d_hist, nblk, d_misc + 2);
+      std::swap(src, dst);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // the sorted order: the low 32 bits of each key; copy keys back whole
+    std::vector<uint64_t> keys(E);
+    if ((e = cudaMemcpyAsync(keys.data(), src, 8 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(ea_host, d_ea, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(eb_host, d_eb, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(w_host, d_w, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(err_host, d_misc + 2, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    for (uint64_t i = 0; i < E; ++i) order_host[i] = (uint32_t)(keys[i] & 0xFFFFFFFFull);
+  } else {
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    *err_host = 0;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace qpso

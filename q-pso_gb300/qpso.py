@@ -33,7 +33,8 @@ EXPORTS = [
     "qpso_timer_elapsed", "qpso_scrub_l2", "qpso_score_poses_noalloc", "qpso_autotune",
     "qpso_server_start", "qpso_server_submit", "qpso_server_poll", "qpso_server_wait",
     "qpso_server_stats_get", "qpso_server_stop", "qpso_render_depth_f32", "qpso_frame_clusters",
-    "qpso_obj_load", "qpso_image_u16_load",
+    "qpso_obj_load", "qpso_image_u16_load", "qpso_seg_params_init", "qpso_segment_num_edges",
+    "qpso_segment_edge_ends", "qpso_segment_gauss_mask", "qpso_segment_edges", "qpso_segment_planes",
 ]
 
 
@@ -92,6 +93,11 @@ class Cluster(C.Structure):
     _fields_ = [("label", C.c_int32), ("num_points", C.c_uint32), ("min_x", C.c_int32),
                 ("max_x", C.c_int32), ("min_y", C.c_int32), ("max_y", C.c_int32),
                 ("depth_points", C.c_uint32), ("centroid_mm", C.c_float * 3)]
+
+
+class SegParams(C.Structure):
+    _fields_ = [("sigma", C.c_float), ("k", C.c_float), ("min_size", C.c_float), ("kx", C.c_float),
+                ("ky", C.c_float), ("ks", C.c_float), ("kdv", C.c_float), ("kdc", C.c_float)]
 
 
 class QpsoError(RuntimeError):
@@ -168,10 +174,21 @@ def load_library(path: str = LIB_PATH):
     L.qpso_score_poses_noalloc.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                            C.POINTER(Camera), C.POINTER(SolveDesc), C.c_void_p,
                                            C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.qpso_seg_params_init.argtypes = [C.POINTER(SegParams)]
+    L.qpso_seg_params_init.restype = None
+    L.qpso_segment_num_edges.argtypes = [C.c_uint32, C.c_uint32]
+    L.qpso_segment_num_edges.restype = C.c_uint64
+    L.qpso_segment_edge_ends.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
+    L.qpso_segment_gauss_mask.argtypes = [C.c_float, C.c_void_p, C.c_int32]
+    L.qpso_segment_edges.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.POINTER(SegParams), C.c_void_p,
+                                     C.POINTER(C.c_uint32)]
+    L.qpso_segment_planes.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_uint32, C.c_uint32, C.POINTER(SegParams), C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_uint32)]
     for fn in EXPORTS:
         if fn not in ("qpso_version", "qpso_destroy", "qpso_last_error", "qpso_solve_desc_init",
                       "qpso_box_from_centroid", "qpso_host_alloc", "qpso_host_free",
-                      "qpso_get_stream"):
+                      "qpso_get_stream", "qpso_seg_params_init", "qpso_segment_num_edges"):
             getattr(L, fn).restype = C.c_int32
     _lib = L
     return L
@@ -330,6 +347,31 @@ class Context:
                  "aabb": (c.min_x, c.max_x, c.min_y, c.max_y), "depth_points": c.depth_points,
                  "centroid_mm": list(c.centroid_mm)} for c in arr[:n.value]]
 
+    def segment_planes(self, h8, s8, v8, depth_mm, saliency, params: "SegParams | None" = None,
+                       weights: bool = False):
+        """The segmentation's graph stage on the GPU (qpso_segment_planes):
+        HSV planes (uint8, H in 0..180), depth (uint16 mm) and saliency
+        (float32), all (height, width).  Returns (labels int32 (height,
+        width), n_clusters) and, with weights=True, the edge weights in
+        the reference's edge order."""
+        h8, s8, v8 = (np.ascontiguousarray(x, np.uint8) for x in (h8, s8, v8))
+        d = np.ascontiguousarray(depth_mm, np.uint16)
+        sal = _f32(saliency)
+        H, W = h8.shape
+        if not all(x.shape == (H, W) for x in (s8, v8, d, sal)):
+            raise ValueError("planes differ in shape")
+        prm = params if params is not None else seg_params()
+        labels = np.empty((H, W), np.int32)
+        w = np.empty(max(1, segment_num_edges(W, H)), np.float32) if weights else None
+        n = C.c_uint32()
+        self._check(self.L.qpso_segment_planes(self.h, h8.ctypes.data, s8.ctypes.data, v8.ctypes.data,
+                                               d.ctypes.data, sal.ctypes.data, W, H, C.byref(prm),
+                                               labels.ctypes.data, None if w is None else w.ctypes.data,
+                                               C.byref(n)))
+        if weights:
+            return labels, n.value, w[:segment_num_edges(W, H)]
+        return labels, n.value
+
     def render_depth_f32(self, mesh_id: int, cam: Camera, pose) -> np.ndarray:
         """The reference's best-pose depth image (RenderCPU arithmetic)."""
         out = np.empty((cam.height, cam.width), np.float32)
@@ -476,3 +518,48 @@ def image_u16_load(path: str) -> np.ndarray:
 def result_dict(r: Result) -> dict:
     return {"fit": r.fit, "pose": np.array(r.pose[:], np.float32), "flags": r.flags,
             "raster_writes": r.raster_writes, "tile_passes": r.tile_passes}
+
+
+def seg_params(**kw) -> SegParams:
+    """The reference main's segmentation constants, fields overridden by kw."""
+    p = SegParams()
+    load_library().qpso_seg_params_init(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def segment_num_edges(width: int, height: int) -> int:
+    return int(load_library().qpso_segment_num_edges(width, height))
+
+
+def segment_edge_ends(width: int, height: int):
+    """(a, b): every edge's ends in the reference's edge order.  Host only."""
+    n = segment_num_edges(width, height)
+    a, b = np.empty(max(1, n), np.int32), np.empty(max(1, n), np.int32)
+    _status(load_library().qpso_segment_edge_ends(width, height, a.ctypes.data, b.ctypes.data),
+            "qpso_segment_edge_ends")
+    return a[:n], b[:n]
+
+
+def segment_gauss_mask(sigma: float) -> np.ndarray:
+    m = np.empty(64, np.float32)
+    n = load_library().qpso_segment_gauss_mask(C.c_float(sigma), m.ctypes.data, 64)
+    if n < 0:
+        raise QpsoError(ERR_ARG, "qpso_segment_gauss_mask")
+    return m[:n].copy()
+
+
+def segment_edges(width: int, height: int, weights, params: "SegParams | None" = None):
+    """The merge passes over given edge weights.  Host only.  Returns
+    (labels int32 (height, width), n_clusters)."""
+    w = _f32(weights)
+    if w.size != segment_num_edges(width, height):
+        raise ValueError("one weight per edge")
+    prm = params if params is not None else seg_params()
+    labels = np.empty((height, width), np.int32)
+    n = C.c_uint32()
+    wbuf = w if w.size else np.zeros(1, np.float32)
+    _status(load_library().qpso_segment_edges(width, height, wbuf.ctypes.data, C.byref(prm), labels.ctypes.data,
+                                              C.byref(n)), "qpso_segment_edges")
+    return labels, n.value
