@@ -1050,7 +1050,7 @@ static void qo_forest_join(qo_forest *f, int32_t x, int32_t y)
     f->count -= 1;
 }
 
-static const qo_edge *qo_sort_base;
+static _Thread_local const qo_edge *qo_sort_base;  /* qsort passes no context */
 
 /* ascending weight; equal weights by input position (a total order, so
  * qsort's lack of stability does not matter) */
