@@ -12,7 +12,9 @@ workload through the batched persistent kernel is reported under
 written) before every timed step.
 
 Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                        [--workload c2|c1|c3|c5]
+                        [--workload c2|c1|c3|c4|c5|seg]
+
+--workload seg times the segmentation's graph stage instead (frames/s).
 """
 from __future__ import annotations
 
@@ -654,13 +656,121 @@ def run_serving(args, ws, rank, local):
     ctx.close()
 
 
+SEG_METRIC = "segmentation frames/sec (GraphCannySeg graph stage, 640x480)"
+
+
+def segmentation_frame(H: int = 480, W: int = 640, seed: int = 11):
+    """A synthetic frame for the segmentation's graph stage: 8-bit HSV planes
+    (a background plus a dozen rectangles of other colours), depth in mm (a
+    tilted plane with the rectangles 50-400 mm nearer, 0-2 mm noise, 3%
+    dropout) and a saliency map (forward differences of V)."""
+    rng = np.random.default_rng(seed)
+    h8 = np.full((H, W), 20, np.uint8)
+    s8 = np.full((H, W), 60, np.uint8)
+    v8 = np.full((H, W), 120, np.uint8)
+    d = (900 + np.arange(H)[:, None] * 2 + np.arange(W)[None, :] // 2).astype(np.int32)
+    for _ in range(12):
+        y0, x0 = int(rng.integers(0, H - 40)), int(rng.integers(0, W - 40))
+        y1, x1 = y0 + int(rng.integers(30, 160)), x0 + int(rng.integers(30, 200))
+        h8[y0:y1, x0:x1] = rng.integers(0, 181)
+        s8[y0:y1, x0:x1] = rng.integers(40, 256)
+        v8[y0:y1, x0:x1] = rng.integers(40, 256)
+        d[y0:y1, x0:x1] -= int(rng.integers(50, 400))
+    d = d + rng.integers(0, 3, (H, W))
+    d[rng.random((H, W)) < 0.03] = 0
+    vf = v8.astype(np.float32)
+    gx, gy = np.zeros_like(vf), np.zeros_like(vf)
+    gx[:, :-1] = np.abs(np.diff(vf, axis=1))
+    gy[:-1, :] = np.abs(np.diff(vf, axis=0))
+    return h8, s8, v8, d.astype(np.uint16), ((gx + gy) / 510.0).astype(np.float32)
+
+
+def _oracle_segment_rate(frame, budget_s: float):
+    """The oracle's segmentation (smoothing, graph, sort, merge) of the frame
+    on one host core, repeated for about budget_s: frames/s."""
+    from oracle import pyoracle as po
+
+    sp = po.seg_params()
+    n, t0 = 0, time.perf_counter()
+    while True:
+        po.segment_planes(*frame, sp)
+        n += 1
+        dt = time.perf_counter() - t0
+        if dt >= budget_s:
+            return n / dt, n
+
+
+def run_segment(args, ws, rank, local):
+    """The segmentation's graph stage (qpso_segment_planes): a step is one
+    640x480 frame from host planes to the host label map, so every step
+    includes the uploads, the GPU graph and sort, the copies back and the
+    host merge passes; it is timed on the host clock around the call.
+    Replicas under torchrun segment their own frames."""
+    import qpso
+    import build as pkg_build
+
+    d = Dist(ws)
+    frame = segmentation_frame(seed=11 + rank)
+    H, W = frame[0].shape
+    if args.impl == "reference":
+        if rank == 0:
+            for _ in range(args.warmup):
+                _oracle_segment_rate(frame, 0.5)
+            rates = [_oracle_segment_rate(frame, 3.0)[0] for _ in range(args.steps)]
+            v = statistics.median(rates)
+            base = {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",
+                    "sample": "the oracle's segmentation of the frame, repeated for 3 s per step"}
+            print(json.dumps({"impl": "reference", "metric": SEG_METRIC, "value": v, "unit": "frames/s",
+                              "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                              "config": {"workload": "seg: one 640x480 HSV + depth + saliency frame"},
+                              "cpu_baseline": base,
+                              "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                                      "d2h_bytes_per_step": 0}}))
+        d.close()
+        return
+    pkg_build.build()
+    ctx = qpso.Context(local)
+    prm = qpso.seg_params()
+    for _ in range(args.warmup):
+        labels, n_sets = ctx.segment_planes(*frame, prm)
+    sampler = ClockSampler(local)
+    d.barrier()
+    sampler.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        labels, n_sets = ctx.segment_planes(*frame, prm)
+    dt = d.max(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    if rank == 0:
+        value = ws * args.steps / dt
+        E = qpso.segment_num_edges(W, H)
+        line = {"metric": SEG_METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dt * 1000.0 / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "seg: one 640x480 HSV + depth + saliency frame per step, "
+                                       "qpso_segment_planes from host planes to host labels",
+                           "edges": int(E), "sets": int(n_sets), "l2": "inputs uploaded every step"},
+                "edges_per_s": value * E, "gpu_launches": args.steps * 25, "clocks": clocks,
+                "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": int(H * W * 9),
+                        "d2h_bytes_per_step": int(20 * E)}}
+        if not args.no_cpu_baseline:
+            v, n = _oracle_segment_rate(frame, 10.0)
+            line["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",
+                                    "sample": "%d oracle segmentations of the frame" % n}
+        print(json.dumps(line))
+    ctx.close()
+    d.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "seg"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ref-kernels", action="store_true",
                     help="skip the reference-shaped solve (1024 particles x 20 iterations)")
@@ -671,6 +781,9 @@ def main():
     ap.add_argument("--epoch-iters", type=int, default=4, help="c4: iterations per epoch")
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "seg":
+        run_segment(args, ws, rank, local)
+        return
     if args.workload == "c4" and args.impl != "reference":
         run_serving(args, ws, rank, local)
         return

@@ -31,3 +31,29 @@ def test_summaries_carry_the_figures_bench_reads(workload, kernel):
 def test_missing_figures_read_as_none():
     assert bench.profile_figure("c2", "step", "no_such_key") is None
     assert bench.profile_figure("c9", "step", "inst_per_launch") is None
+
+
+@pytest.mark.timeout(120)
+def test_segmentation_reference_arm_line():
+    """bench.py --workload seg --impl reference: the oracle's segmentation
+    timed on the host, one JSON line with the contract's keys."""
+    import json
+    import subprocess
+
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "seg", "--steps", "1",
+                        "--warmup", "0"], cwd=ROOT, capture_output=True, text=True, timeout=100)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    j = json.loads(lines[0])
+    assert j["impl"] == "reference" and j["unit"] == "frames/s" and j["value"] > 0
+    assert j["cpu_baseline"]["kind"] == "port" and j["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_segmentation_frame_has_clusters():
+    """The seg workload's frame splits into a dozen sets with the reference
+    main's constants (min_size 500), on the oracle."""
+    from oracle import pyoracle as po
+
+    lists, ns = po.segment_planes(*bench.segmentation_frame(), po.seg_params())
+    assert 5 <= ns <= 40 and all(len(L) - 1 >= 500 for L in lists)
