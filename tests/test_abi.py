@@ -59,6 +59,8 @@ int main(void) {
   printf("%zu %zu\n", offsetof(qpso_result, raster_writes), offsetof(qpso_result, tile_passes));
   printf("%zu %zu %zu\n", sizeof(qpso_cluster), offsetof(qpso_cluster, depth_points),
          offsetof(qpso_cluster, centroid_mm));
+  printf("%zu %zu %zu %zu\n", sizeof(qpso_seg_params), offsetof(qpso_seg_params, kx),
+         offsetof(qpso_seg_params, ks), offsetof(qpso_seg_params, kdc));
   return 0;
 }
 ''')
@@ -74,6 +76,8 @@ int main(void) {
     assert got[2] == [qpso.Result.raster_writes.offset, qpso.Result.tile_passes.offset]
     K = qpso.Cluster
     assert got[3] == [C.sizeof(K), K.depth_points.offset, K.centroid_mm.offset]
+    G = qpso.SegParams
+    assert got[4] == [C.sizeof(G), G.kx.offset, G.ks.offset, G.kdc.offset]
 
 
 def test_host_only_entry_points(lib):

@@ -84,3 +84,12 @@ def test_merge_passes_refuse_nan_and_bad_sizes():
         qpso.segment_edges(4, 3, np.zeros(len(w), np.float32), qpso.seg_params(sigma=8.0))
     labels, n = qpso.segment_edges(1, 1, np.zeros(0, np.float32))
     assert n == 1 and labels.tolist() == [[0]]
+
+
+def test_default_constants_equal_oracle():
+    """qpso_seg_params_init and the oracle's defaults: the reference main's
+    constants (main.h:58-65, main.cu:1214-1217), field for field."""
+    a, b = qpso.seg_params(), po.seg_params()
+    for f, _ in qpso.SegParams._fields_:
+        assert np.float32(getattr(a, f)) == np.float32(getattr(b, f)), f
+    assert np.float32(a.k) == np.float32(50) / np.float32(10000) and a.min_size == 500.0
