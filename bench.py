@@ -24,6 +24,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -95,7 +96,7 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "qpso_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
