@@ -44,7 +44,7 @@ def test_two_ranks_barrier_and_max_over_ranks(tmp_path):
 
 @pytest.mark.timeout(300)
 def test_reference_arm_under_torchrun_prints_on_rank0_only():
-    """The reference arm launched like the driver launches N>1 runs: rank 0
+    """The reference arm launched as an N>1 run is (torchrun, one rank per GPU): rank 0
     times the CPU implementation and prints one line; rank 1 exits 0."""
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--impl",
