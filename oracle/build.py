@@ -1,4 +1,4 @@
-"""Build recipe for the test-side checkers under oracle/.
+"""Build recipe for the test infrastructure under oracle/.
 
 TEST INFRASTRUCTURE ONLY.  Host libraries:
 

@@ -1,7 +1,7 @@
 /*
  * qpso_oracle.c -- scalar CPU restatement of the Q-PSO pose-solve hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker; see qpso_oracle.h for the parity
+ * TEST INFRASTRUCTURE ONLY (the oracle; see qpso_oracle.h for the parity
  * status and the arithmetic contract).  Build with -ffp-contract=off.
  *
  * Every function cites the reference file:line it restates.  Where the
@@ -54,7 +54,7 @@ float qo_uniform(uint64_t seed, uint32_t stream, uint32_t particle, uint32_t dra
 /* ------------------------------------------------------------------ */
 /* sin/cos/acos.  The reference calls CUDA's cosf/sinf/acosf under
  * -use_fast_math (main.h:287-294, 391-399; main.cu:946,970); those differ
- * between CUDA and libm, so both sides of this build use the same series
+ * between CUDA and libm, so both sides of this project use the same series
  * instead.  The double forms (Cody-Waite reduction by pi/2 in three 30-bit
  * parts, Taylor polynomials on [-pi/4, pi/4], truncation < 1e-19; acos via
  * asin's Taylor series on [0, 1/2] and acos(x) = 2 asin(sqrt((1-x)/2))
@@ -388,7 +388,7 @@ void qo_rotate(const float *s, const float v[3], float o[3])
 /* projectModelPointsToPixels(const float*, const float4&, float4&),
  * main.h:513-545: rotate, translate, u = cx + fx x/z, v = cy + fy y/z with
  * x/z = x * rcp_rn(z), z in mm.  DEVIATION: the reference's intrinsics are
- * double macros, so it evaluates cx + fx*(x/z) in double; this build takes
+ * double macros, so it evaluates cx + fx*(x/z) in double; this library takes
  * fp32 intrinsics at run time and evaluates it as one fp32 fma. */
 void qo_project(const float *s, const float v[3], const qo_camera *cam, float o[3])
 {

@@ -1,7 +1,7 @@
 /*
  * qpso_oracle.h -- scalar CPU restatement of the Q-PSO pose-solve hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path in
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle for the CUDA path in
  * q-pso_gb300/csrc: only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline arm may load it.  The product path never calls it and has no CPU
  * fallback.
@@ -17,6 +17,10 @@
  * tests/test_gpu_ref_kernels.py checks this restatement's raster, fitness,
  * init, best update and particle update against them on identical inputs.
  * Only GSL's random stream stays unpinned (Philox replaces it).
+ * The segmentation's graph stage (GraphCannySeg's smoothing, depth
+ * normalisation, edge weights, segment_graph, small-component merge and
+ * collectSets) is compiled from the reference sources by oracle/build.py
+ * (build_seg_pin) and pinned the same way (tests/golden/ref_seg*.npz).
  *
  * Arithmetic contract shared with the CUDA kernels (both sides must agree
  * bit for bit):
@@ -62,7 +66,7 @@ typedef struct {
 #define QO_PROJ_REF_ACCV 1
 
 /* Per-solve constants: QPSOParams_t (main.h:182-204) plus the compile-time
- * macros of main.h:83-136 that this build makes runtime parameters. */
+ * macros of main.h:83-136 that this project makes runtime parameters. */
 typedef struct {
     float c1, c2;                 /* c1_, c2_ (main.h:104-105) */
     double w;                     /* psoW_ 0.3 (main.h:106), applied in double */

@@ -4,7 +4,7 @@
  * oracle/_ref/ref_kernels_{ieee,fast}.cubin where the reference sources
  * are present).
  *
- * TEST INFRASTRUCTURE ONLY: a checker and a measured baseline, never the
+ * TEST INFRASTRUCTURE ONLY: a parity reference and a measured baseline, never the
  * product.  The harness is this project's code; it loads the kernels with
  * the CUDA driver API and drives them the way the reference's main() does
  * (main.cu:1389-1727): Nparticle_ = 1024 particles in [7][1024] state

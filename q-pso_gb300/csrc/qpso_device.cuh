@@ -316,7 +316,7 @@ __device__ __forceinline__ void kinematics(const float* from, float* s, const fl
 
 // ------------------------------------------------------------------------
 // Solve parameters (QPSOParams_t, main.h:182-204, plus the main.h macros
-// this build makes runtime parameters).
+// this library makes runtime parameters).
 struct SolveParams {
   float c1, c2;
   double w;

@@ -231,7 +231,7 @@ def test_library_solve_agrees_with_reference_kernels(c1_scene):
     5 iterations.  The first iteration's best fitness agrees within 1e-3.
     Later iterations are not compared: the swarm is chaotic, and the two
     differ by float ulps from the first update on (CUDA's sinf/cosf/acosf
-    against this build's series, double against float intrinsics).  Both
+    against this project's series, double against float intrinsics).  Both
     best fitnesses can only fall."""
     import qpso
 

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.fixture(scope="module")
-def checker(tmp_path_factory):
+def meshlet_check(tmp_path_factory):
     exe = tmp_path_factory.mktemp("mlet") / "meshlet_check"
     subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "q-pso_gb300", "csrc"),
                     os.path.join(ROOT, "tests", "meshlet_check.cpp"), "-o", str(exe)], check=True)
@@ -24,11 +24,11 @@ def checker(tmp_path_factory):
 
 @pytest.mark.parametrize("kind,n", [("icosphere", 1280), ("icosphere", 20480), ("box", 5000),
                                     ("cylinder", 5000), ("ellipsoid", 12000), ("ellipsoid", 30)])
-def test_partition(checker, tmp_path, kind, n):
+def test_partition(meshlet_check, tmp_path, kind, n):
     soa, F = scene.make_mesh(kind, n, 100.0, seed=3)
     path = tmp_path / "mesh.bin"
     soa.astype(np.float32).tofile(path)
-    out = subprocess.run([checker, str(path)], capture_output=True, text=True)
+    out = subprocess.run([meshlet_check, str(path)], capture_output=True, text=True)
     assert out.returncode == 0, out.returncode
     faces, mlets, slots, cap = map(int, out.stdout.split())
     assert faces == F
@@ -39,14 +39,14 @@ def test_partition(checker, tmp_path, kind, n):
         assert slots / F < 0.8, slots / F
 
 
-def test_partition_of_unshared_triangles(checker, tmp_path):
+def test_partition_of_unshared_triangles(meshlet_check, tmp_path):
     """A soup of disjoint triangles has no sharing; caps still hold."""
     rng = np.random.default_rng(0)
     F = 700
     soa = rng.normal(size=9 * F).astype(np.float32)
     path = tmp_path / "soup.bin"
     soa.tofile(path)
-    out = subprocess.run([checker, str(path)], capture_output=True, text=True)
+    out = subprocess.run([meshlet_check, str(path)], capture_output=True, text=True)
     assert out.returncode == 0
     faces, mlets, slots, cap = map(int, out.stdout.split())
     assert faces == F and slots == 3 * F and mlets >= (3 * F + cap - 1) // cap
