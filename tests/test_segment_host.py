@@ -93,3 +93,11 @@ def test_default_constants_equal_oracle():
     for f, _ in qpso.SegParams._fields_:
         assert np.float32(getattr(a, f)) == np.float32(getattr(b, f)), f
     assert np.float32(a.k) == np.float32(50) / np.float32(10000) and a.min_size == 500.0
+
+
+def test_empty_images_are_refused():
+    for w, h in [(0, 3), (3, 0), (0, 0)]:
+        with pytest.raises(qpso.QpsoError):
+            qpso.segment_edges(w, h, np.zeros(0, np.float32))
+        with pytest.raises(qpso.QpsoError):
+            qpso.segment_edge_ends(w, h)
