@@ -245,18 +245,23 @@ qpso_status qpso_score_poses(qpso_context *ctx, const qpso_solve_desc *desc, con
  * (loadOBJ3 layout, 9*num_faces floats), the depth frame (uint16 mm,
  * cam->width*cam->height) and, when desc->cluster_label >= 0, its int32
  * label map; n poses (n x 7 floats); fit_out (n floats); flags_out
- * (optional, one uint32 of device error bits).  From desc only the cluster
- * fields (label, AABB, num_points) are read; mesh_id and frame_id are
- * ignored.  Work is queued on `stream` (a cudaStream_t, NULL for the legacy
- * default stream) on the current device; results are ready when the stream
- * is synchronised.  Intermediate buffers live in one 4 MiB device array
- * fixed at load time (held by every GPU that loads the library until
- * exit): frames above about 690,000 pixels (640x480 and 960x720 fit) are
- * rejected with QPSO_ERR_ARG.  The first call on a device looks up that
- * array's device address (cudaGetSymbolAddress), so make it before any
- * stream capture.  All calls on a device share the array and leave their
- * contents in it; calls that overlap on the GPU race, so issue them on one
- * stream. */
+ * (optional, one uint32 of device error bits).  From desc the cluster
+ * fields (label, AABB, num_points) and raster_mode are read and checked as
+ * qpso_score_poses checks them, and the camera as qpso_frame_upload checks
+ * it; the PSO constants are copied but play no part in a score; mesh_id
+ * and frame_id are ignored.  Work is queued on `stream` (a cudaStream_t,
+ * NULL for the legacy default stream) on the current device; results are
+ * ready when the stream is synchronised.  Intermediate buffers live in one
+ * 4 MiB device array fixed at load time (held by every GPU that loads the
+ * library until exit): frames above about 690,000 pixels (640x480 and
+ * 960x720 fit) are rejected with QPSO_ERR_ARG.  Every call looks up that
+ * array's device address in the current context (cudaGetSymbolAddress), so
+ * the address stays right after cudaDeviceReset.  The first call on a
+ * device also sets the scoring kernel's shared-memory limit
+ * (cudaFuncSetAttribute, 64 KB for its 16384-pixel tile): make one warm-up
+ * call per device before any stream capture.  All calls on a device share
+ * the array and leave their contents in it; calls that overlap on the GPU
+ * race, so issue them on one stream. */
 qpso_status qpso_score_poses_noalloc(const float *d_mesh_soa, uint32_t num_faces,
                                      const uint16_t *d_depth_mm, const int32_t *d_labels,
                                      const qpso_camera *cam, const qpso_solve_desc *desc,

@@ -33,7 +33,20 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_SRC = os.environ.get("QPSO_REFERENCE_SRC", "/root/reference")
+# Directory holding the reference's sources (main.cu, main.h,
+# GraphCannySeg.{h,cpp}), given by the environment: QPSO_REFERENCE_SRC.  The
+# reference builds below are skipped when it is unset or lacks the files.
+REFERENCE_SRC = os.environ.get("QPSO_REFERENCE_SRC", "")
+
+
+def _ref_path(name: str) -> str:
+    """A reference source file, or a path that never exists when the
+    reference directory is not given."""
+    if not REFERENCE_SRC:
+        return os.path.join(HERE, "_no_reference_given", name)
+    return os.path.join(REFERENCE_SRC, name)
+
+
 CUDA_INC = "/usr/local/cuda/include"
 
 ORACLE_SO = os.path.join(BUILD, "libqpso_oracle.so")
@@ -61,9 +74,10 @@ def build_oracle(force: bool = False) -> str:
 
 
 def build_ref_pin(force: bool = False) -> str | None:
-    main_h = os.path.join(REFERENCE_SRC, "main.h")
+    main_h = _ref_path("main.h")
     if not os.path.exists(main_h):
-        return None
+        # without the sources, a library built earlier from them still serves
+        return REFPIN_SO if os.path.exists(REFPIN_SO) else None
     src = [os.path.join(HERE, "ref_pin", "ref_pin.cpp"), main_h]
     if not force and _newer(REFPIN_SO, src):
         return REFPIN_SO
@@ -99,8 +113,8 @@ def _kernel_first_line(main_cu: str) -> int:
 
 
 def build_ref_cubins(force: bool = False) -> dict | None:
-    main_cu = os.path.join(REFERENCE_SRC, "main.cu")
-    main_h = os.path.join(REFERENCE_SRC, "main.h")
+    main_cu = _ref_path("main.cu")
+    main_h = _ref_path("main.h")
     if not (os.path.exists(main_cu) and os.path.exists(main_h)):
         return None
     prelude = os.path.join(HERE, "ref_gpu", "prelude.cuh")
@@ -279,10 +293,10 @@ def build_seg_pin(force: bool = False) -> str | None:
     """oracle/_ref/libqpso_segpin.so: the reference's segmentation core
     (union-find forest, segment_graph, small-component merge, collectSets)
     compiled for the host between the stand-ins of ref_pin/seg_*.h."""
-    hdr = os.path.join(REFERENCE_SRC, "GraphCannySeg.h")
-    cpp = os.path.join(REFERENCE_SRC, "GraphCannySeg.cpp")
+    hdr = _ref_path("GraphCannySeg.h")
+    cpp = _ref_path("GraphCannySeg.cpp")
     if not (os.path.exists(hdr) and os.path.exists(cpp)):
-        return None
+        return SEGPIN_SO if os.path.exists(SEGPIN_SO) else None
     mine = [os.path.join(HERE, "ref_pin", f) for f in ("seg_prelude.h", "seg_class.h", "seg_api.h")]
     if not force and _newer(SEGPIN_SO, [hdr, cpp, os.path.abspath(__file__), *mine]):
         return SEGPIN_SO

@@ -29,7 +29,7 @@ UNITS = ["qpso_kernels.cu", "qpso_api.cu", "qpso_noalloc.cu", "qpso_segment.cu",
 # qpso_segment.cu's host code computes float expressions that must round like
 # the reference's on every host (no fused multiply-add on Arm either)
 UNIT_FLAGS = {"qpso_segment.cu": ["-Xcompiler", "-ffp-contract=off"]}
-HEADERS = ["qpso_device.cuh", "qpso_internal.cuh", "meshlets.h"]
+HEADERS = ["qpso_device.cuh", "qpso_internal.cuh", "qpso_checks.h", "meshlets.h"]
 
 
 def _sources():

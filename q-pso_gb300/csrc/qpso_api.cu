@@ -24,6 +24,7 @@
 
 #include "meshlets.h"
 #include "qpso.h"
+#include "qpso_checks.h"
 #include "qpso_internal.cuh"
 
 using namespace qpso;
@@ -244,21 +245,12 @@ qpso_status check_desc(qpso_context* ctx, const qpso_solve_desc& d, const MeshOb
     return fail(ctx, QPSO_ERR_ARG, "num_particles must be in [1, 2^20]");
   if (d.iterations == 0 || d.iterations > (1u << 20))
     return fail(ctx, QPSO_ERR_ARG, "iterations must be in [1, 2^20]");
-  if (d.num_points == 0) return fail(ctx, QPSO_ERR_ARG, "num_points must be > 0");
-  if (!(d.cl_min_x < d.cl_max_x && d.cl_min_y < d.cl_max_y))
-    return fail(ctx, QPSO_ERR_ARG, "cluster AABB must be non-empty (min < max)");
   const qpso_camera& c = fi->second.cam;
-  if (d.cl_min_x < -kGuard || d.cl_max_x > c.width + kGuard || d.cl_min_y < -kGuard ||
-      d.cl_max_y > c.height + kGuard)
-    return fail(ctx, QPSO_ERR_ARG, "cluster AABB outside the raster domain");
-  if (d.cluster_label < 0 && d.cluster_label != -1)
-    return fail(ctx, QPSO_ERR_ARG, "cluster_label must be >= 0 or -1");
+  if (const char* why = cluster_error(d, c.width, c.height)) return fail(ctx, QPSO_ERR_ARG, why);
   if (d.cluster_label >= 0 && fi->second.labels == nullptr)
     return fail(ctx, QPSO_ERR_ARG, "frame has no label map");
   for (int k = 0; k < 3; ++k)
     if (!(d.t_lo[k] <= d.t_hi[k])) return fail(ctx, QPSO_ERR_ARG, "t_lo must be <= t_hi");
-  if (d.raster_mode != QPSO_RASTER_REF && d.raster_mode != QPSO_RASTER_EDGE)
-    return fail(ctx, QPSO_ERR_ARG, "raster_mode must be QPSO_RASTER_REF or QPSO_RASTER_EDGE");
   *m = &mi->second;
   *f = &fi->second;
   return QPSO_OK;
@@ -540,12 +532,7 @@ qpso_status qpso_mesh_release(qpso_context* ctx, uint32_t id) {
 qpso_status qpso_frame_upload(qpso_context* ctx, const uint16_t* depth, const int32_t* labels,
                               const qpso_camera* cam, uint32_t* frame_id) {
   if (!ctx || !depth || !cam || !frame_id) return fail(ctx, QPSO_ERR_ARG, "null argument");
-  if (cam->width <= 0 || cam->height <= 0 || cam->width > 8192 || cam->height > 8192)
-    return fail(ctx, QPSO_ERR_ARG, "frame size must be in [1, 8192]");
-  if (!(std::isfinite(cam->fx) && std::isfinite(cam->fy) && std::isfinite(cam->cx) &&
-        std::isfinite(cam->cy)))
-    return fail(ctx, QPSO_ERR_ARG, "non-finite intrinsics");
-  if (!projection_ok(cam)) return fail(ctx, QPSO_ERR_ARG, "unknown projection");
+  if (const char* why = camera_error(*cam)) return fail(ctx, QPSO_ERR_ARG, why);
   cudaSetDevice(ctx->device);
   FrameObj f;
   f.cam = *cam;

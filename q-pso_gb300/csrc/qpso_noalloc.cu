@@ -25,9 +25,9 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 
 #include "qpso.h"
+#include "qpso_checks.h"
 #include "qpso_internal.cuh"
 
 using namespace qpso;
@@ -35,25 +35,20 @@ using namespace qpso;
 namespace {
 
 constexpr size_t kNoallocScratchBytes = 4u << 20;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
-// Device address of g_noalloc_scratch per device.  In host code the symbol
-// name is only a host-side stand-in; the address comes from
-// cudaGetSymbolAddress with the device current, once per device.
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
-cudaError_t scratch_address(int dev, unsigned char** out) {
-  std::lock_guard<std::mutex> g(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_addr[dev] = p;
-  }
-  *out = static_cast<unsigned char*>(g_addr[dev]);
+// Device address of g_noalloc_scratch in the current device's context.  In
+// host code the symbol name is only a host-side stand-in, so the address
+// comes from cudaGetSymbolAddress with the device current.  It is looked up
+// on every call (a host-side table lookup, no device work): a cached address
+// would outlive the module it points into after cudaDeviceReset or a switch
+// to another context on the same device.
+cudaError_t scratch_address(unsigned char** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  *out = static_cast<unsigned char*>(p);
   return cudaSuccess;
 }
 
@@ -76,13 +71,9 @@ extern "C" qpso_status qpso_score_poses_noalloc(const float* d_mesh_soa, uint32_
   if (!d_mesh_soa || num_faces == 0 || !d_depth_mm || !cam || !desc || !d_poses || !d_fit_out ||
       n == 0)
     return QPSO_ERR_ARG;
-  if (cam->width <= 0 || cam->height <= 0 || cam->width > 8192 || cam->height > 8192 ||
-      (cam->projection != QPSO_PROJ_FP32 && cam->projection != QPSO_PROJ_REF_ACCV))
-    return QPSO_ERR_ARG;
-  if (desc->num_points == 0 || !(desc->cl_min_x < desc->cl_max_x && desc->cl_min_y < desc->cl_max_y))
-    return QPSO_ERR_ARG;
+  // the same checks as qpso_frame_upload (camera) and qpso_score_poses (cluster fields)
+  if (camera_error(*cam) || cluster_error(*desc, cam->width, cam->height)) return QPSO_ERR_ARG;
   if (desc->cluster_label >= 0 && !d_labels) return QPSO_ERR_ARG;
-  if (desc->raster_mode != QPSO_RASTER_REF && desc->raster_mode != QPSO_RASTER_EDGE) return QPSO_ERR_ARG;
   const size_t w = (size_t)cam->width, h = (size_t)cam->height;
   // scratch layout: instance | prep job | header | masked depth | table
   const size_t o_inst = 0;
@@ -94,9 +85,9 @@ extern "C" qpso_status qpso_score_poses_noalloc(const float* d_mesh_soa, uint32_
   if (need > kNoallocScratchBytes) return QPSO_ERR_ARG;  // frame too large for the fixed scratch
 
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return QPSO_ERR_CUDA;
+  if (cudaGetDevice(&dev) != cudaSuccess) return QPSO_ERR_CUDA;
   unsigned char* base = nullptr;
-  if (scratch_address(dev, &base) != cudaSuccess) return QPSO_ERR_CUDA;
+  if (scratch_address(&base) != cudaSuccess) return QPSO_ERR_CUDA;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
 
   Instance I;

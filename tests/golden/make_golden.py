@@ -10,8 +10,8 @@ the host CPU from the reference sources by oracle/build.py (ref_pin): the
 fixed-point rasteriser renderFixedPointAABB with its AABB reduction, the
 quaternion products, normalisation, hemisphere cast, vertex rotation, the
 exponential-map step and the projection with the reference's compiled-in
-intrinsics.  Needs the reference sources (QPSO_REFERENCE_SRC, default
-/root/reference); run once, commit the .npz.
+intrinsics.  Needs the directory of the reference sources in the
+environment variable QPSO_REFERENCE_SRC; run once, commit the .npz.
 
 oracle_c1.npz -- the oracle's own C1 solve (per-iteration global best and
 final state), frozen so that later changes to the oracle are caught.
