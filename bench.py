@@ -359,11 +359,14 @@ def reference_kernels_gb300(w):
         res.update(value=1000.0 / ms, unit="solves/s", ms_per_solve=ms)
     else:
         res["stopped"] = out["error"]
-    if all(o["done"] == REF_ITERATIONS for _, o in runs):
-        tot = sum(o["ms"] for _, o in runs)
-        res["all_clusters"] = {"config": REF_SHAPE_ALL, "solves": len(runs), "ms": tot,
-                               "value": 1000.0 * len(runs) / tot, "unit": "solves/s",
-                               "best_fits": [float(o["trace"][-1]) for _, o in runs]}
+    per = [{"faces": sh["faces"], "iterations_done": o["done"], "ms": o["ms"],
+            "best_fit": float(o["trace"][-1]) if o["done"] else None,
+            "stopped": o["error"] or None} for sh, o in runs]
+    full = [(sh, o) for sh, o in runs if o["done"] == REF_ITERATIONS]
+    tot = sum(o["ms"] for _, o in full)
+    res["all_clusters"] = {"config": REF_SHAPE_ALL, "solves": len(runs), "completed": len(full),
+                           "ms": tot, "value": 1000.0 * len(full) / tot if tot > 0 else None,
+                           "unit": "solves/s", "per_cluster": per}
     return res
 
 
