@@ -416,6 +416,85 @@ qpso_status qpso_segment_planes(qpso_context *ctx, const uint8_t *h, const uint8
                                 uint32_t height, const qpso_seg_params *prm, int32_t *labels,
                                 float *edge_weights, uint32_t *n_clusters);
 
+/* ---- segmentation: the stages around the graph stage ----
+ * GraphCannySeg<hsv>::run (GraphCannySeg.cpp:1438-1459) from the colour
+ * image and the raw depth: dynamicDepthSmoothing (GraphCannySeg.cpp:426-634),
+ * inpaintDepth (GraphCannySeg.h:1164-1230), myCannyWithOri2
+ * (GraphCannySeg.cpp:638-1050), the HSV conversion of segment_image, the
+ * graph stage above, and PostSegmFilter (GraphCannySeg.h:1639-1873), which
+ * keeps the sets that can be objects and gives them the order the
+ * reference's cluster index N counts in (main.cu:1253-1269).  The
+ * reference runs the stages before and after the graph with OpenCV 2.4;
+ * here they are GPU kernels restating the published algorithms (colour
+ * conversion, separable Gaussian, Scharr, exact Euclidean distance
+ * transform, summed-area tables, Telea's fast-marching inpainting,
+ * bilinear resizing, PCA of the pixel coordinates), with exact integer or
+ * fixed-order float arithmetic; OpenCV's own rounding is not reproduced. */
+typedef struct {
+    float beta;               /* 2000: dynamicDepthSmoothing(2000.f) (GraphCannySeg.cpp:1441) */
+    float gamma;              /* 18000: its depth-change threshold (default argument) */
+    int32_t inpaint_radius;   /* 20: cv::inpaint radius in inpaintDepth (GraphCannySeg.h:1186) */
+    float canny_low, canny_high; /* Lcanny / 1000, Hcanny / 1000 = 0.05, 0.075 (main.h:75-76) */
+    int32_t dth, plus_d, point_3d; /* 30 mm, 7 px, 5 px: the depth test (main.h:70-72) */
+    float g_angle, l_angle;   /* 148 and 151 degrees in radians (main.h:73-74) */
+    float fx, fy, cx, cy;     /* k_vec, the ACCV intrinsics (main.h:51-56) */
+    float far_obj_z;          /* 1500 mm: farther centroids are dropped (main.h:77) */
+    float max_ecc, max_l1, max_l2; /* 0.978, 13800, 1950: PCA limits (main.h:66-68) */
+} qpso_seg_front_params;
+
+/* The reference main's values above. */
+void qpso_seg_front_params_init(qpso_seg_front_params *p);
+
+/* One set of a label map: the SegResults fields the solve reads
+ * (GraphCannySeg.h:594-618) and what PostSegmFilter tests. */
+typedef struct {
+    int32_t label;            /* the set's number in the label map */
+    uint32_t num_points;      /* SegResults.num_points = pixels + 1 (collectSets lists one pixel twice) */
+    uint32_t pixels;
+    int32_t min_x, max_x, min_y, max_y; /* rect_aabb_ (cv::boundingRect), max exclusive */
+    float centroid_mm[3];     /* centroid3D of the pixels with inpainted depth (compute3DCentroid) */
+    float nan_ratio;          /* pixels without depth / num_points (dropped at >= 0.3) */
+    float dark_ratio;         /* pixels in the first 3 of 32 value bins / num_points (dropped at >= 0.3) */
+    double eig[2];            /* PCA eigenvalues of the pixel coordinates (computePCA) */
+    double eccentricity;      /* sqrt(1 - eig[1] / eig[0]) */
+    int32_t far;              /* centroid farther than far_obj_z */
+    int32_t kept;             /* passes every filter */
+} qpso_seg_cluster;
+
+/* Optional host copies of the intermediate planes (each W x H; any may be
+ * NULL): the 8-bit HSV planes and grey image, the smoothed and the
+ * inpainted depth (mm), the saliency map and the Canny edge map (0 / 255)
+ * after the depth test. */
+typedef struct {
+    uint8_t *h, *s, *v, *gray;
+    uint16_t *smoothed, *inpainted;
+    float *saliency;
+    uint8_t *edges;
+} qpso_seg_frame_out;
+
+/* Segment one frame from its colour image (bgr: width x height x 3, B G R)
+ * and raw depth (uint16 mm).  labels (width x height) receives every
+ * pixel's set, numbered by smallest pixel, *n_sets the set count;
+ * clusters (capacity records; may be NULL) the kept sets in the
+ * reference's order (vecSegResults), *n_clusters their count.  The solve
+ * of cluster N reads the inpainted depth (planes->inpainted) masked to it
+ * (SegResults.clusterDepth). */
+qpso_status qpso_segment_rgbd(qpso_context *ctx, const uint8_t *bgr, const uint16_t *depth_mm,
+                              uint32_t width, uint32_t height, const qpso_seg_params *prm,
+                              const qpso_seg_front_params *fp, int32_t *labels, uint32_t *n_sets,
+                              qpso_seg_cluster *clusters, uint32_t capacity, uint32_t *n_clusters,
+                              const qpso_seg_frame_out *planes);
+
+/* PostSegmFilter over a given label map (labels 0..n_sets-1, -1 none),
+ * its inpainted depth and its HSV value plane, all on the host: per-set
+ * moments on the GPU, the filter on the host.  With keep_all != 0 every
+ * set's record is returned (kept says which pass), else only the kept
+ * ones, in label order. */
+qpso_status qpso_segment_clusters(qpso_context *ctx, const int32_t *labels, uint32_t n_sets,
+                                  const uint16_t *inpainted_mm, const uint8_t *v_plane, uint32_t width,
+                                  uint32_t height, const qpso_seg_front_params *fp, int keep_all,
+                                  qpso_seg_cluster *out, uint32_t capacity, uint32_t *n_out);
+
 #ifdef __cplusplus
 }
 #endif

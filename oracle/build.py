@@ -61,13 +61,14 @@ def _newer(target: str, sources: list[str]) -> bool:
 
 
 def build_oracle(force: bool = False) -> str:
-    src = [os.path.join(HERE, "qpso_oracle.c"), os.path.join(HERE, "qpso_oracle.h")]
+    src = [os.path.join(HERE, "qpso_oracle.c"), os.path.join(HERE, "qpso_seg_front.c"),
+           os.path.join(HERE, "qpso_oracle.h")]
     if not force and _newer(ORACLE_SO, src):
         return ORACLE_SO
     os.makedirs(BUILD, exist_ok=True)
     tmp = ORACLE_SO + ".tmp%d" % os.getpid()
     cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off",
-           "-fno-fast-math", "-fopenmp", src[0], "-o", tmp, "-lm"]
+           "-fno-fast-math", "-fopenmp", src[0], src[1], "-o", tmp, "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, ORACLE_SO)
     return ORACLE_SO

@@ -449,3 +449,163 @@ def graph_reference(h8, s8, v8, depth, sal, sp: SegParams):
     if m < 0:
         raise ValueError("sp_graph refused its arguments")
     return edges_array(ea[:m], eb[:m], ew[:m]), sm, dn
+
+
+# ---- the stages around the graph segmentation (qpso_seg_front.c) ----
+
+class SegFrontParams(C.Structure):
+    _fields_ = [("beta", C.c_float), ("gamma", C.c_float), ("inpaint_radius", C.c_int32),
+                ("canny_low", C.c_float), ("canny_high", C.c_float), ("dth", C.c_int32),
+                ("plus_d", C.c_int32), ("point_3d", C.c_int32), ("g_angle", C.c_float),
+                ("l_angle", C.c_float), ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float),
+                ("cy", C.c_float), ("far_obj_z", C.c_float), ("max_ecc", C.c_float),
+                ("max_l1", C.c_float), ("max_l2", C.c_float)]
+
+
+class SegCluster(C.Structure):
+    _fields_ = [("label", C.c_int32), ("num_points", C.c_uint32), ("pixels", C.c_uint32),
+                ("min_x", C.c_int32), ("max_x", C.c_int32), ("min_y", C.c_int32), ("max_y", C.c_int32),
+                ("centroid_mm", C.c_float * 3), ("nan_ratio", C.c_float), ("dark_ratio", C.c_float),
+                ("eig", C.c_double * 2), ("eccentricity", C.c_double), ("far", C.c_int32),
+                ("kept", C.c_int32)]
+
+
+def seg_front_params(**kw) -> SegFrontParams:
+    """The reference main's constants for the stages around the graph
+    segmentation (main.h:51-77, main.cu:1214-1221), with overrides."""
+    fp = SegFrontParams()
+    lib().qo_seg_front_default_params(C.byref(fp))
+    for k, v in kw.items():
+        setattr(fp, k, v)
+    return fp
+
+
+def _vp(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def bgr_to_hsv_gray(bgr: np.ndarray):
+    """(h, s, v, gray) 8-bit planes of an H x W x 3 BGR image."""
+    b = np.ascontiguousarray(bgr, np.uint8)
+    H, W = b.shape[:2]
+    out = [np.empty((H, W), np.uint8) for _ in range(4)]
+    lib().qo_bgr_to_hsv_gray(_vp(b), W * H, *(_vp(x) for x in out))
+    return tuple(out)
+
+
+def depth_smooth(depth: np.ndarray, fp: SegFrontParams | None = None, with_maps: bool = False):
+    fp = fp or seg_front_params()
+    d = np.ascontiguousarray(depth, np.uint16)
+    H, W = d.shape
+    out = np.empty((H, W), np.uint16)
+    cm = np.empty((H, W), np.uint8)
+    rm = np.empty((H, W), np.float32)
+    L = lib()
+    L.qo_depth_smooth.restype = C.c_int32
+    if L.qo_depth_smooth(_vp(d), W, H, C.c_float(fp.beta), C.c_float(fp.gamma), _vp(out), _vp(cm), _vp(rm)):
+        raise ValueError("qo_depth_smooth refused its arguments")
+    return (out, cm, rm) if with_maps else out
+
+
+def telea(img: np.ndarray, mask: np.ndarray, radius: int = 20) -> np.ndarray:
+    a = np.ascontiguousarray(img, np.uint8).copy()
+    m = np.ascontiguousarray(mask, np.uint8)
+    h, w = a.shape
+    if lib().qo_telea(_vp(a), _vp(m), w, h, radius) < 0:
+        raise ValueError("qo_telea refused its arguments")
+    return a
+
+
+def resize_bilinear_u8(src: np.ndarray, dw: int, dh: int) -> np.ndarray:
+    s = np.ascontiguousarray(src, np.uint8)
+    sh, sw = s.shape
+    out = np.empty((dh, dw), np.uint8)
+    lib().qo_resize_bilinear_u8(_vp(s), sw, sh, _vp(out), dw, dh)
+    return out
+
+
+def inpaint_depth(smoothed: np.ndarray, fp: SegFrontParams | None = None, with_small: bool = False):
+    fp = fp or seg_front_params()
+    sm = np.ascontiguousarray(smoothed, np.uint16)
+    H, W = sm.shape
+    out = np.empty((H, W), np.uint16)
+    small = np.zeros((H // 5 + 1) * (W // 5 + 1), np.uint8)
+    sw, sh = C.c_int32(0), C.c_int32(0)
+    if lib().qo_inpaint_depth(_vp(sm), W, H, fp.inpaint_radius, _vp(out), _vp(small), C.byref(sw), C.byref(sh)):
+        raise ValueError("qo_inpaint_depth refused its arguments")
+    if with_small:
+        return out, small[:sw.value * sh.value].reshape(sh.value, sw.value).copy()
+    return out
+
+
+def gauss_taps(ksize: int) -> np.ndarray:
+    t = np.zeros(31, np.int32)
+    n = lib().qo_gauss_taps(ksize, _vp(t))
+    return t[:n].copy()
+
+
+def blur_u8(src: np.ndarray, ksize: int) -> np.ndarray:
+    s = np.ascontiguousarray(src, np.uint8)
+    H, W = s.shape
+    out = np.empty_like(s)
+    lib().qo_blur_u8(_vp(s), W, H, ksize, _vp(out))
+    return out
+
+
+def orient_bin(x: int, y: int) -> int:
+    return lib().qo_orient_bin(C.c_int32(x), C.c_int32(y))
+
+
+def canny_saliency(gray: np.ndarray, inpainted: np.ndarray, fp: SegFrontParams | None = None,
+                   with_edges: bool = False):
+    fp = fp or seg_front_params()
+    g = np.ascontiguousarray(gray, np.uint8)
+    z = np.ascontiguousarray(inpainted, np.uint16)
+    H, W = g.shape
+    sal = np.empty((H, W), np.float32)
+    edges = np.empty((H, W), np.uint8)
+    if lib().qo_canny_saliency(_vp(g), _vp(z), W, H, C.byref(fp), _vp(sal), _vp(edges)):
+        raise ValueError("qo_canny_saliency refused its arguments")
+    return (sal, edges) if with_edges else sal
+
+
+def seg_clusters(labels: np.ndarray, n_sets: int, inpainted: np.ndarray, v8: np.ndarray,
+                 fp: SegFrontParams | None = None, keep_all: bool = False) -> list:
+    fp = fp or seg_front_params()
+    lab = np.ascontiguousarray(labels, np.int32)
+    z = np.ascontiguousarray(inpainted, np.uint16)
+    v = np.ascontiguousarray(v8, np.uint8)
+    H, W = lab.shape
+    out = (SegCluster * max(1, n_sets))()
+    n = lib().qo_seg_clusters(_vp(lab), n_sets, _vp(z), _vp(v), W, H, C.byref(fp), out, int(keep_all))
+    if n < 0:
+        raise ValueError("qo_seg_clusters refused its arguments")
+    return list(out[:n])
+
+
+def labels_from_lists(lists, H: int, W: int) -> np.ndarray:
+    """Label map (set k for the pixels of the k-th collectSets list, -1
+    elsewhere) of segment_graph / segment_planes output."""
+    lab = np.full(H * W, -1, np.int32)
+    for k, pts in enumerate(lists):
+        lab[pts] = k
+    return lab.reshape(H, W)
+
+
+def segment_rgbd(bgr: np.ndarray, depth: np.ndarray, sp: SegParams | None = None,
+                 fp: SegFrontParams | None = None) -> dict:
+    """GraphCannySeg<hsv>::run from a BGR image and a depth map (mm): the
+    colour conversions, depth smoothing, inpainting, Canny saliency, the
+    graph segmentation and the cluster filter, each stage's output kept."""
+    sp = sp or seg_params()
+    fp = fp or seg_front_params()
+    h8, s8, v8, gray = bgr_to_hsv_gray(bgr)
+    smoothed = depth_smooth(depth, fp)
+    inp = inpaint_depth(smoothed, fp)
+    sal = canny_saliency(gray, inp, fp)
+    lists, n_sets = segment_planes(h8, s8, v8, inp, sal, sp)
+    H, W = gray.shape
+    labels = labels_from_lists(lists, H, W)
+    clusters = seg_clusters(labels, len(lists), inp, v8, fp)
+    return {"h": h8, "s": s8, "v": v8, "gray": gray, "smoothed": smoothed, "inpainted": inp,
+            "saliency": sal, "labels": labels, "n_sets": len(lists), "clusters": clusters}

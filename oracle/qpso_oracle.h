@@ -265,6 +265,70 @@ int32_t qo_segment_planes(const uint8_t *h8, const uint8_t *s8, const uint8_t *v
                           const qo_seg_params *sp, int32_t *offsets, int32_t *points,
                           int32_t *num_sets);
 
+/* ---- the stages around the graph segmentation (qpso_seg_front.c) ----
+ * GraphCannySeg<hsv>::run (GraphCannySeg.cpp:1438-1459) before and after
+ * segment_image, restated from the published algorithms OpenCV implements;
+ * unpinned against OpenCV (absent here).  See qpso_seg_front.c. */
+typedef struct {
+    float beta, gamma;          /* dynamicDepthSmoothing(2000), gamma 18000 */
+    int32_t inpaint_radius;     /* 20: cv::inpaint radius (GraphCannySeg.h:1186) */
+    float canny_low, canny_high;/* Lcanny / 1000, Hcanny / 1000 (main.h:75-76, main.cu:1220-1221) */
+    int32_t dth, plus_d, point_3d; /* 30, 7, 5 (main.h:70-72) */
+    float g_angle, l_angle;     /* 148 and 151 degrees in radians (main.h:73-74) */
+    float fx, fy, cx, cy;       /* k_vec (main.h:51-56): the ACCV intrinsics */
+    float far_obj_z;            /* 1500 mm (main.h:77) */
+    float max_ecc, max_l1, max_l2; /* 0.978, 13800, 1950 (main.h:66-68) */
+} qo_seg_front_params;
+
+void qo_seg_front_default_params(qo_seg_front_params *fp);
+
+void qo_bgr_to_hsv_gray(const uint8_t *bgr, int32_t n, uint8_t *h, uint8_t *s, uint8_t *v,
+                        uint8_t *gray);
+float qo_smooth_alfa(void);
+/* out: smoothed depth; c_out (optional): the depth-change map (0/1);
+ * r_out (optional): the smoothing radius map R before rounding */
+int32_t qo_depth_smooth(const uint16_t *d, int32_t W, int32_t H, float beta, float gamma,
+                        uint16_t *out, uint8_t *c_out, float *r_out);
+void qo_resize_bilinear_u8(const uint8_t *src, int32_t sw, int32_t sh, uint8_t *dst, int32_t dw, int32_t dh);
+float qo_eikonal(int k1, float t1, int k2, float t2);
+/* inpaints img where mask != 0 in place; returns the pixels filled */
+int32_t qo_telea(uint8_t *img, const uint8_t *mask, int32_t w, int32_t h, int32_t radius);
+/* small_out (optional, capacity (W/5 + 1) (H/5 + 1)): the shrunk 8-bit map after inpainting */
+int32_t qo_inpaint_depth(const uint16_t *sm, int32_t W, int32_t H, int32_t radius, uint16_t *out,
+                         uint8_t *small_out, int32_t *small_w, int32_t *small_h);
+int32_t qo_gauss_taps(int32_t ksize, int32_t *taps);
+void qo_blur_u8(const uint8_t *src, int32_t W, int32_t H, int32_t ksize, uint8_t *dst);
+int32_t qo_orient_bin(int32_t x, int32_t y);
+float qo_angle3(const float p1[3], const float p0[3], const float p2[3]);
+/* sal: the saliency map; edges_out (optional): the 0/255 edge map after
+ * the depth test, before the 7x7 blur */
+int32_t qo_canny_saliency(const uint8_t *gray, const uint16_t *inp, int32_t W, int32_t H,
+                          const qo_seg_front_params *fp, float *sal, uint8_t *edges_out);
+
+/* One set of the label map with the fields of SegResults the solve reads
+ * and the quantities PostSegmFilter tests. */
+typedef struct {
+    int32_t label;
+    uint32_t num_points;        /* n + 1: the length of the reference's list */
+    uint32_t pixels;            /* n */
+    int32_t min_x, max_x, min_y, max_y; /* boundingRect, max exclusive */
+    float centroid_mm[3];
+    float nan_ratio, dark_ratio;
+    double eig[2];
+    double eccentricity;
+    int32_t far, kept;
+} qo_seg_cluster;
+
+void qo_seg_cluster_stats(int64_t n, int64_t sx, int64_t sy, int64_t sxx, int64_t syy, int64_t sxy,
+                          int64_t nz, int64_t sz, int64_t suz, int64_t svz, int64_t nzero, const int64_t vb[3],
+                          const qo_seg_front_params *fp, qo_seg_cluster *r);
+/* labels: 0..n_sets-1 (sets numbered by smallest pixel), -1 none; out:
+ * capacity n_sets; the kept records (every record with keep_all != 0) in
+ * label order; returns their count */
+int32_t qo_seg_clusters(const int32_t *labels, int32_t n_sets, const uint16_t *inp, const uint8_t *v8,
+                        int32_t W, int32_t H, const qo_seg_front_params *fp, qo_seg_cluster *out,
+                        int32_t keep_all);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1223,6 +1223,193 @@ qpso_status qpso_segment_planes(qpso_context* ctx, const uint8_t* h, const uint8
   return QPSO_OK;
 }
 
+void qpso_seg_front_params_init(qpso_seg_front_params* p) {
+  if (!p) return;
+  p->beta = 2000.0f;
+  p->gamma = 18000.0f;
+  p->inpaint_radius = 20;
+  p->canny_low = (float)50 / 1000.f;
+  p->canny_high = (float)75 / 1000.f;
+  p->dth = 30;
+  p->plus_d = 7;
+  p->point_3d = 5;
+  // ((float)angle) * deg2rad with deg2rad = M_PI / 180.0f (GraphCannySeg.h:39): double arithmetic
+  p->g_angle = (float)((double)148.0f * 3.14159265358979323846 / 180.0);
+  p->l_angle = (float)((double)151.0f * 3.14159265358979323846 / 180.0);
+  p->fx = 572.41140f;
+  p->fy = 573.57043f;
+  p->cx = 325.26110f;
+  p->cy = 242.04899f;
+  p->far_obj_z = 1500.0f;
+  p->max_ecc = 0.978f;
+  p->max_l1 = 13800.0f;
+  p->max_l2 = 1950.0f;
+}
+
+}  // extern "C"
+
+namespace {
+
+bool front_params_ok(const qpso_seg_front_params* f) {
+  return f && std::isfinite(f->beta) && std::isfinite(f->gamma) && f->inpaint_radius >= 1 &&
+         f->inpaint_radius <= 64 && std::isfinite(f->canny_low) && std::isfinite(f->canny_high) && f->dth >= 0 &&
+         f->plus_d >= 1 && f->point_3d >= 1 && f->plus_d <= 64 && f->point_3d <= 64 && std::isfinite(f->g_angle) &&
+         std::isfinite(f->l_angle) && std::isfinite(f->fx) && f->fx != 0.0f && std::isfinite(f->fy) &&
+         f->fy != 0.0f && std::isfinite(f->cx) && std::isfinite(f->cy) && std::isfinite(f->far_obj_z) &&
+         std::isfinite(f->max_ecc) && std::isfinite(f->max_l1) && std::isfinite(f->max_l2);
+}
+
+// capacity of the per-set moment table: after the small-component merge
+// every set holds at least min_size pixels, unless the frame is one set
+size_t max_sets(size_t n, float min_size) {
+  if (!(min_size >= 1.0f)) return n;
+  const size_t m = (size_t)((double)n / (double)min_size) + 1;
+  return m < n ? m : n;
+}
+
+// Per-set moments on the GPU and the cluster records on the host.  labels,
+// inpainted depth and value plane are device pointers; moments has room
+// for n_sets records.
+qpso_status cluster_records(qpso_context* ctx, const int32_t* d_labels, const uint16_t* d_inp, const uint8_t* d_v,
+                            int32_t W, int32_t H, uint32_t n_sets, SetMoments* d_mom,
+                            const qpso_seg_front_params* fp, int keep_all, qpso_seg_cluster* out,
+                            uint32_t capacity, uint32_t* n_out) {
+  std::vector<SetMoments> mom(n_sets);
+  QPSO_CUDA(ctx, launch_set_moments(d_labels, d_inp, d_v, W, H, (int32_t)n_sets, d_mom, ctx->num_sms, ctx->stream));
+  if (n_sets)
+    QPSO_CUDA(ctx, cudaMemcpyAsync(mom.data(), d_mom, n_sets * sizeof(SetMoments), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  uint32_t k = 0;
+  for (uint32_t i = 0; i < n_sets; ++i) {
+    if (mom[i].n == 0) continue;
+    qpso_seg_cluster r;
+    seg_cluster_record(mom[i], (int32_t)i, *fp, &r);
+    if (!keep_all && !r.kept) continue;
+    if (out && k < capacity) out[k] = r;
+    ++k;
+  }
+  *n_out = k;
+  return QPSO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+qpso_status qpso_segment_rgbd(qpso_context* ctx, const uint8_t* bgr, const uint16_t* depth_mm, uint32_t width,
+                              uint32_t height, const qpso_seg_params* prm, const qpso_seg_front_params* fp,
+                              int32_t* labels, uint32_t* n_sets, qpso_seg_cluster* clusters, uint32_t capacity,
+                              uint32_t* n_clusters, const qpso_seg_frame_out* planes) {
+  if (!ctx || !bgr || !depth_mm || !labels || !n_sets || !n_clusters || width < 3 || height < 3 ||
+      (uint64_t)width * height > (1u << 26))
+    return fail(ctx, QPSO_ERR_ARG, "bad segmentation arguments");
+  if (!seg_params_ok(prm)) return fail(ctx, QPSO_ERR_ARG, "bad segmentation parameters (sigma above 7.75?)");
+  if (!front_params_ok(fp)) return fail(ctx, QPSO_ERR_ARG, "bad front-stage segmentation parameters");
+  const int32_t W = (int32_t)width, H = (int32_t)height;
+  const size_t n = (size_t)W * H;
+  const uint64_t E = seg_num_edges(W, H);
+  float mask[32];
+  const int len = seg_gauss_mask(prm->sigma, mask, 32);
+  cudaSetDevice(ctx->device);
+  const size_t graph_bytes = align_up(seg_workspace_bytes(W, H), 256);
+  const size_t front_bytes = align_up(seg_front_workspace_bytes(W, H, fp->inpaint_radius), 256);
+  const size_t label_bytes = align_up(n * sizeof(int32_t), 256);
+  const size_t mom_bytes = align_up(max_sets(n, prm->min_size) * sizeof(SetMoments), 256);
+  qpso_status st;
+  if ((st = ensure_ws(ctx, graph_bytes + front_bytes + label_bytes + mom_bytes)) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  char* base = static_cast<char*>(ctx->ws.p);
+  char* front_ws = base + graph_bytes;
+  int32_t* d_labels = reinterpret_cast<int32_t*>(front_ws + front_bytes);
+  SetMoments* d_mom = reinterpret_cast<SetMoments*>(front_ws + front_bytes + label_bytes);
+  uint8_t* d_hsv = nullptr;
+  uint16_t* d_depth = nullptr;
+  float* d_sal = nullptr;
+  seg_ws_inputs(base, W, H, &d_hsv, &d_depth, &d_sal);
+  SegFrontArgs a{};
+  a.bgr_host = bgr;
+  a.depth_host = depth_mm;
+  a.W = W;
+  a.H = H;
+  a.beta = fp->beta;
+  a.gamma = fp->gamma;
+  a.radius = fp->inpaint_radius;
+  a.canny_low = fp->canny_low;
+  a.canny_high = fp->canny_high;
+  a.dth = fp->dth;
+  a.plus_d = fp->plus_d;
+  a.point_3d = fp->point_3d;
+  a.g_angle = fp->g_angle;
+  a.l_angle = fp->l_angle;
+  a.fx = fp->fx;
+  a.fy = fp->fy;
+  a.cx = fp->cx;
+  a.cy = fp->cy;
+  a.hsv_out = d_hsv;
+  a.inpainted_out = d_depth;
+  a.saliency_out = d_sal;
+  if (planes) {
+    a.gray_host = planes->gray;
+    a.smoothed_host = planes->smoothed;
+    a.edges_host = planes->edges;
+  }
+  QPSO_CUDA(ctx, seg_front_run(a, front_ws, ctx->num_sms, (size_t)ctx->smem_optin, ctx->stream));
+  if (planes) {
+    uint8_t* hp[3] = {planes->h, planes->s, planes->v};
+    for (int c = 0; c < 3; ++c)
+      if (hp[c]) QPSO_CUDA(ctx, cudaMemcpyAsync(hp[c], d_hsv + c * n, n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (planes->inpainted)
+      QPSO_CUDA(ctx, cudaMemcpyAsync(planes->inpainted, d_depth, 2 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (planes->saliency)
+      QPSO_CUDA(ctx, cudaMemcpyAsync(planes->saliency, d_sal, 4 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  std::vector<uint32_t> order(E);
+  std::vector<int32_t> ea(E), eb(E);
+  std::vector<float> w(E);
+  uint32_t err = 0;
+  QPSO_CUDA(ctx, seg_graph_sorted(nullptr, nullptr, nullptr, W, H, mask, len, prm->kdv, prm->kdc, prm->kx, prm->ks,
+                                  base, ctx->num_sms, ctx->stream, order.data(), ea.data(), eb.data(), w.data(),
+                                  &err));
+  if (err & 5u) return fail(ctx, QPSO_ERR_INTERNAL, "segmentation graph: index out of range");
+  if (err & 2u) return fail(ctx, QPSO_ERR_ARG, "segmentation graph: NaN edge weight (flat inpainted depth?)");
+  const uint32_t ns = seg_merge((uint32_t)n, E, order.data(), ea.data(), eb.data(), w.data(), prm->k,
+                                prm->min_size, labels);
+  *n_sets = ns;
+  if ((size_t)ns * sizeof(SetMoments) > mom_bytes)
+    return fail(ctx, QPSO_ERR_INTERNAL, "segmentation: more sets than the small-component merge allows");
+  QPSO_CUDA(ctx, cudaMemcpyAsync(d_labels, labels, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+  return cluster_records(ctx, d_labels, d_depth, d_hsv + 2 * n, W, H, ns, d_mom, fp, 0, clusters, capacity,
+                         n_clusters);
+}
+
+qpso_status qpso_segment_clusters(qpso_context* ctx, const int32_t* labels, uint32_t n_sets,
+                                  const uint16_t* inpainted_mm, const uint8_t* v_plane, uint32_t width,
+                                  uint32_t height, const qpso_seg_front_params* fp, int keep_all,
+                                  qpso_seg_cluster* out, uint32_t capacity, uint32_t* n_out) {
+  if (!ctx || !labels || !inpainted_mm || !v_plane || !n_out || width == 0 || height == 0 ||
+      (uint64_t)width * height > (1u << 26) || n_sets > width * height)
+    return fail(ctx, QPSO_ERR_ARG, "bad cluster-filter arguments");
+  if (!front_params_ok(fp)) return fail(ctx, QPSO_ERR_ARG, "bad front-stage segmentation parameters");
+  const int32_t W = (int32_t)width, H = (int32_t)height;
+  const size_t n = (size_t)W * H;
+  cudaSetDevice(ctx->device);
+  const size_t lb = align_up(4 * n, 256), zb = align_up(2 * n, 256), vb = align_up(n, 256);
+  qpso_status st;
+  if ((st = ensure_ws(ctx, lb + zb + vb + align_up((size_t)n_sets * sizeof(SetMoments), 256) + 256)) != QPSO_OK)
+    return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  char* base = static_cast<char*>(ctx->ws.p);
+  int32_t* d_lab = reinterpret_cast<int32_t*>(base);
+  uint16_t* d_z = reinterpret_cast<uint16_t*>(base + lb);
+  uint8_t* d_v = reinterpret_cast<uint8_t*>(base + lb + zb);
+  SetMoments* d_mom = reinterpret_cast<SetMoments*>(base + lb + zb + vb);
+  QPSO_CUDA(ctx, cudaMemcpyAsync(d_lab, labels, 4 * n, cudaMemcpyHostToDevice, ctx->stream));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(d_z, inpainted_mm, 2 * n, cudaMemcpyHostToDevice, ctx->stream));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(d_v, v_plane, n, cudaMemcpyHostToDevice, ctx->stream));
+  return cluster_records(ctx, d_lab, d_z, d_v, W, H, n_sets, d_mom, fp, keep_all, out, capacity, n_out);
+}
+
 }  // extern "C"
 
 // ===========================================================================

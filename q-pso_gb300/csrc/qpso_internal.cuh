@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "meshlets.h"
+#include "qpso.h"
 #include "qpso_device.cuh"
 
 namespace qpso {
@@ -161,5 +162,41 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
                              int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
                              float ks, void* ws, int sms, cudaStream_t st, uint32_t* order_host,
                              int32_t* ea_host, int32_t* eb_host, float* w_host, uint32_t* err_host);
+
+// The stages around the graph stage (qpso_seg_front.cu): colour
+// conversions, depth smoothing, inpainting and Canny saliency, from host
+// BGR and raw depth to device planes in the graph stage's input slots.
+struct SegFrontArgs {
+  const uint8_t* bgr_host;   // W x H x 3, B G R
+  const uint16_t* depth_host;
+  int32_t W, H;
+  float beta, gamma;
+  int32_t radius;            // inpainting radius (shrunk map, px)
+  float canny_low, canny_high;
+  int32_t dth, plus_d, point_3d;
+  float g_angle, l_angle;
+  float fx, fy, cx, cy;
+  uint8_t* hsv_out;          // device: H, S, V planes (3 W H)
+  uint16_t* inpainted_out;   // device: W H
+  float* saliency_out;       // device: W H
+  uint8_t* gray_host;        // optional host copies
+  uint16_t* smoothed_host;
+  uint8_t* edges_host;
+};
+int seg_gauss_taps(int ksize, int32_t* taps);
+size_t seg_front_workspace_bytes(int32_t W, int32_t H, int32_t radius);
+cudaError_t seg_front_run(const SegFrontArgs& a, void* ws, int sms, size_t smem_optin, cudaStream_t st);
+
+// Per-set moments of a label map for the cluster filter (PostSegmFilter).
+struct SetMoments {
+  unsigned long long n, sx, sy, sxx, syy, sxy, nz, sz, suz, svz, nzero, vb[3];
+  int32_t minx, maxx, miny, maxy;
+};
+cudaError_t launch_set_moments(const int32_t* labels, const uint16_t* inp, const uint8_t* v8, int32_t W, int32_t H,
+                               int32_t n_sets, SetMoments* acc, int sms, cudaStream_t st);
+// the graph stage's device input slots inside its workspace
+void seg_ws_inputs(void* ws, int32_t W, int32_t H, uint8_t** hsv, uint16_t** depth, float** sal);
+// PostSegmFilter's record of one set from its moments (host).
+void seg_cluster_record(const SetMoments& m, int32_t label, const qpso_seg_front_params& fp, qpso_seg_cluster* r);
 
 }  // namespace qpso

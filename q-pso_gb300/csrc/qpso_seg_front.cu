@@ -1,0 +1,1124 @@
+// qpso_seg_front.cu -- the stages of the reference's segmentation around its
+// graph stage (GraphCannySeg<hsv>::run, GraphCannySeg.cpp:1438-1459) on the
+// GPU: the colour conversions, the depth smoothing, the depth inpainting and
+// the Canny saliency before segment_image, and the per-set moments that
+// PostSegmFilter (GraphCannySeg.h:1639-1873) tests after it.
+//
+// Every stage is defined exactly (integers where the data are integers, a
+// fixed order of float operations elsewhere) so that the kernels equal the
+// oracle's restatement bit for bit; the definitions, and where they depart
+// from OpenCV's own rounding, are stated beside each kernel.  The reference
+// runs these stages with OpenCV 2.4 on the CPU.
+//
+// Data layout: one frame of W x H pixels, planes row-major.  All stages run
+// on one stream with no host round trip; their outputs land in the graph
+// stage's input slots (HSV planes, inpainted depth, saliency), so a frame
+// goes from the colour image and raw depth to the label map with two copies
+// in and one label map out.
+//
+// This unit is compiled with -ffp-contract=off for its host code too.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "qpso.h"
+#include "qpso_internal.cuh"
+
+namespace qpso {
+
+namespace {
+
+constexpr int kTaps = 16;
+
+struct FrontConst {
+  int32_t W, H;
+  float alfa, beta, gamma;
+  int32_t blur5[kTaps], blur7[kTaps];
+  float canny_low, canny_high;
+  int32_t dth, plus_d, point_3d;
+  float g_angle, l_angle;
+  float kinv[4];  // 1/fx, -cx/fx, 1/fy, -cy/fy
+};
+
+__device__ __forceinline__ int32_t refl101(int32_t i, int32_t n) {
+  if (n == 1) return 0;
+  while (i < 0 || i >= n) {
+    if (i < 0) i = -i;
+    if (i >= n) i = 2 * (n - 1) - i;
+  }
+  return i;
+}
+
+#define GRID_STRIDE(t, n) \
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (n); t += (size_t)gridDim.x * blockDim.x)
+
+// ---- colour conversions ----------------------------------------------------
+// cvtColor BGR2HSV (convertMat2Image, GraphCannySeg.h:708-721) and BGR2GRAY
+// (constructor, GraphCannySeg.cpp:404): V = max, S = 255 (V - min) / V,
+// H = the hue in degrees / 2, each the exact rational rounded half up; grey
+// with the 14-bit weights of 0.299 / 0.587 / 0.114.
+__global__ void front_colour_kernel(const uint8_t* __restrict__ bgr, size_t n, uint8_t* __restrict__ hsv,
+                                    uint8_t* __restrict__ gray) {
+  GRID_STRIDE(i, n) {
+    const int b = bgr[3 * i], g = bgr[3 * i + 1], r = bgr[3 * i + 2];
+    const int mx = max(r, max(g, b)), mn = min(r, min(g, b)), d = mx - mn;
+    int h = 0;
+    if (d != 0) {
+      int num, off;
+      if (mx == r) {
+        num = g - b;
+        off = 0;
+      } else if (mx == g) {
+        num = b - r;
+        off = 60;
+      } else {
+        num = r - g;
+        off = 120;
+      }
+      int hd = 30 * num + off * d;
+      if (hd < 0) hd += 180 * d;
+      h = (2 * hd + d) / (2 * d);
+    }
+    hsv[i] = (uint8_t)h;
+    hsv[n + i] = mx == 0 ? 0 : (uint8_t)((510 * d + mx) / (2 * mx));
+    hsv[2 * n + i] = (uint8_t)mx;
+    gray[i] = (uint8_t)((4899 * r + 9617 * g + 1868 * b + 8192) >> 14);
+  }
+}
+
+// ---- dynamicDepthSmoothing (GraphCannySeg.cpp:426-634) ----------------------
+// Depth-change map as a gather: pixel p is marked when it, or its left or
+// right neighbour, is an interior pivot whose |z(x+1) - z(x)| reaches
+// gamma Fdc(pivot), or when it, or the pixel above or below, is one whose
+// |z(y+1) - z(y)| does.  misc[0] |= 1 when any pixel is marked.
+__device__ __forceinline__ float fdc_of(uint16_t z, float alfa) { return (float)((int64_t)z * z) * alfa; }
+
+__device__ __forceinline__ bool cond_x(const uint16_t* d, int32_t x, int32_t y, const FrontConst& c) {
+  if (x < 1 || x >= c.W - 1 || y < 1 || y >= c.H - 1) return false;
+  const size_t p = (size_t)y * c.W + x;
+  const float tdc = c.gamma * fdc_of(d[p], c.alfa);
+  return (float)abs((int)d[p + 1] - (int)d[p]) >= tdc;
+}
+
+__device__ __forceinline__ bool cond_y(const uint16_t* d, int32_t x, int32_t y, const FrontConst& c) {
+  if (x < 1 || x >= c.W - 1 || y < 1 || y >= c.H - 1) return false;
+  const size_t p = (size_t)y * c.W + x;
+  const float tdc = c.gamma * fdc_of(d[p], c.alfa);
+  return (float)abs((int)d[p + c.W] - (int)d[p]) >= tdc;
+}
+
+__global__ void smooth_cmap_kernel(const uint16_t* __restrict__ d, uint8_t* __restrict__ cm, uint32_t* misc,
+                                   FrontConst c) {
+  const size_t n = (size_t)c.W * c.H;
+  bool any = false;
+  GRID_STRIDE(p, n) {
+    const int32_t y = (int32_t)(p / c.W), x = (int32_t)(p - (size_t)y * c.W);
+    const bool m = cond_x(d, x, y, c) || cond_x(d, x - 1, y, c) || cond_x(d, x + 1, y, c) ||
+                   cond_y(d, x, y, c) || cond_y(d, x, y - 1, c) || cond_y(d, x, y + 1, c);
+    cm[p] = m;
+    any |= m;
+  }
+  if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) atomicOr(misc, 1u);
+}
+
+// Horizontal distance to the nearest marked pixel of the row (kInf: none),
+// one thread per row, two sweeps.
+constexpr int32_t kInf = 0x3fffffff;
+
+__global__ void edt_rows_kernel(const uint8_t* __restrict__ cm, int32_t* __restrict__ g, FrontConst c) {
+  const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= c.H) return;
+  const uint8_t* row = cm + (size_t)r * c.W;
+  int32_t* gr = g + (size_t)r * c.W;
+  int32_t last = -kInf;
+  for (int32_t x = 0; x < c.W; ++x) {
+    if (row[x]) last = x;
+    gr[x] = last == -kInf ? kInf : x - last;
+  }
+  last = kInf;
+  for (int32_t x = c.W - 1; x >= 0; --x) {
+    if (row[x]) last = x;
+    if (last != kInf && last - x < gr[x]) gr[x] = last - x;
+  }
+}
+
+// R = min(B, T): T the exact Euclidean distance (outward search over rows
+// while dy^2 < the best squared distance), times sqrt(1/2) in float.
+__global__ void smooth_radius_kernel(const uint16_t* __restrict__ d, const int32_t* __restrict__ g,
+                                     const uint32_t* misc, float* __restrict__ R, FrontConst c) {
+  const size_t n = (size_t)c.W * c.H;
+  const bool any = misc[0] & 1u;
+  GRID_STRIDE(p, n) {
+    const int32_t r = (int32_t)(p / c.W), x = (int32_t)(p - (size_t)r * c.W);
+    float T;
+    if (!any) {
+      T = __int_as_float(0x7f800000);
+    } else {
+      int64_t best = g[p] == kInf ? INT64_MAX : (int64_t)g[p] * g[p];
+      for (int32_t dy = 1; (int64_t)dy * dy < best; ++dy) {
+        if (r - dy < 0 && r + dy >= c.H) break;
+        if (r - dy >= 0) {
+          const int32_t gg = g[(size_t)(r - dy) * c.W + x];
+          if (gg != kInf) {
+            const int64_t d2 = (int64_t)dy * dy + (int64_t)gg * gg;
+            if (d2 < best) best = d2;
+          }
+        }
+        if (r + dy < c.H) {
+          const int32_t gg = g[(size_t)(r + dy) * c.W + x];
+          if (gg != kInf) {
+            const int64_t d2 = (int64_t)dy * dy + (int64_t)gg * gg;
+            if (d2 < best) best = d2;
+          }
+        }
+      }
+      T = __fmul_rn(__fsqrt_rn((float)best), 0.70710677f);
+    }
+    const float B = __fmul_rn(c.beta, fdc_of(d[p], c.alfa));
+    R[p] = B < T ? B : T;
+  }
+}
+
+// Summed-area tables of ModDepth (float, the running row sum added to the
+// entry above, in that order) and of its zeros (int).  Rows: one thread per
+// row, sequential in x; columns: one thread per column, sequential in y.
+__global__ void integral_rows_kernel(const uint16_t* __restrict__ d, const uint8_t* __restrict__ cm,
+                                     float* __restrict__ rs, int32_t* __restrict__ rz, FrontConst c) {
+  const int32_t y = blockIdx.x * blockDim.x + threadIdx.x;
+  if (y >= c.H) return;
+  float s = 0.0f;
+  int32_t z = 0;
+  for (int32_t x = 0; x < c.W; ++x) {
+    const size_t p = (size_t)y * c.W + x;
+    const uint16_t v = cm[p] ? 0 : d[p];
+    s = __fadd_rn(s, (float)v);
+    z += v == 0;
+    rs[p] = s;
+    rz[p] = z;
+  }
+}
+
+__global__ void integral_cols_kernel(const float* __restrict__ rs, const int32_t* __restrict__ rz,
+                                     float* __restrict__ I, int32_t* __restrict__ N, FrontConst c) {
+  const int32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x > c.W) return;
+  const size_t s1 = (size_t)c.W + 1;
+  float acc = 0.0f;
+  int32_t za = 0;
+  I[x] = 0.0f;
+  N[x] = 0;
+  for (int32_t y = 0; y < c.H; ++y) {
+    if (x > 0) {
+      acc = __fadd_rn(acc, rs[(size_t)y * c.W + x - 1]);
+      za += rz[(size_t)y * c.W + x - 1];
+    }
+    I[(size_t)(y + 1) * s1 + x] = acc;
+    N[(size_t)(y + 1) * s1 + x] = za;
+  }
+}
+
+__global__ void smooth_out_kernel(const uint16_t* __restrict__ d, const float* __restrict__ R,
+                                  const float* __restrict__ I, const int32_t* __restrict__ N,
+                                  uint16_t* __restrict__ out, FrontConst c) {
+  const size_t n = (size_t)c.W * c.H;
+  const size_t s1 = (size_t)c.W + 1;
+  GRID_STRIDE(p, n) {
+    const int32_t r = (int32_t)(p / c.W), x = (int32_t)(p - (size_t)r * c.W);
+    uint16_t o = 0;
+    if (r >= 15 && r < c.H - 15 && x >= 15 && x < c.W - 15) {
+      const int radi = (int)__fadd_rn(R[p], 0.5f);
+      if (radi == 0) {
+        o = d[p];
+      } else {
+        const int32_t x0 = max(x - radi, 0), x1 = min(x + radi + 1, c.W);
+        const int32_t y0 = max(r - radi, 0), y1 = min(r + radi + 1, c.H);
+        const int32_t den = (x1 - x0) * (y1 - y0);
+        const int32_t nz = N[y1 * s1 + x1] + N[y0 * s1 + x0] - N[y1 * s1 + x0] - N[y0 * s1 + x1];
+        if (den == nz) {
+          o = d[p];
+        } else {
+          const float sum = __fsub_rn(__fsub_rn(__fadd_rn(I[y1 * s1 + x1], I[y0 * s1 + x0]), I[y1 * s1 + x0]),
+                                      I[y0 * s1 + x1]);
+          const float v = __fadd_rn(__fmul_rn(__frcp_rn((float)(den - nz)), sum), 0.5f);
+          o = v <= 0.0f ? 0 : v >= 65535.0f ? 65535 : (uint16_t)v;
+        }
+      }
+    }
+    out[p] = o;
+  }
+}
+
+// ---- inpaintDepth (GraphCannySeg.h:1164-1230) ------------------------------
+
+// misc[2] = min, misc[3] = max of the smoothed depth (initialised 0xFFFF / 0)
+__global__ void minmax_u16_kernel(const uint16_t* __restrict__ d, size_t n, uint32_t* misc) {
+  uint32_t lo = 0xFFFFu, hi = 0u;
+  GRID_STRIDE(t, n) {
+    const uint32_t v = d[t];
+    lo = v < lo ? v : lo;
+    hi = v > hi ? v : hi;
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(misc + 2, lo);
+    atomicMax(misc + 3, hi);
+  }
+}
+
+struct InpaintDims {
+  int32_t sw, sh;  // the shrunk map
+};
+
+__device__ __forceinline__ uint8_t to_gray8(uint16_t z, uint32_t mn, uint32_t mx) {
+  const double alpha = 255.0 / (double)(mx - mn);
+  const double beta = -(double)mn * 255.0 / (double)(mx - mn);
+  const float f = __fadd_rn(__fmul_rn((float)z, (float)alpha), (float)beta);
+  const float q = rintf(f);
+  return (uint8_t)(q < 0.0f ? 0.0f : q > 255.0f ? 255.0f : q);
+}
+
+// the shrunk 8-bit map: samples at (5x + 2, 5y + 2), and its zero mask
+__global__ void inpaint_shrink_kernel(const uint16_t* __restrict__ sm, const uint32_t* misc,
+                                      uint8_t* __restrict__ small, FrontConst c, InpaintDims s) {
+  const uint32_t mn = misc[2], mx = misc[3];
+  if (mx == mn) return;
+  GRID_STRIDE(t, (size_t)s.sw * s.sh) {
+    const int32_t y = (int32_t)(t / s.sw), x = (int32_t)(t - (size_t)y * s.sw);
+    const int32_t sy = min(5 * y + 2, c.H - 1), sx = min(5 * x + 2, c.W - 1);
+    small[t] = to_gray8(sm[(size_t)sy * c.W + sx], mn, mx);
+  }
+}
+
+// Telea's fast-marching inpainting of the shrunk map's zero pixels, in one
+// CTA: thread 0 runs the band's priority queue, the whole CTA computes each
+// inpainted value (its weighted sum over the disc of `radius`, in 32.32
+// fixed point so that the sum does not depend on the order of terms).  The
+// state (flags, arrival times T, the map, the queue and every pixel's
+// queue slot) lives in shared memory when it fits, else in global memory.
+enum : uint8_t { kKnown = 0, kBand = 1, kInside = 2 };
+
+struct TeleaMem {
+  uint8_t* flag;
+  uint8_t* img;
+  float* T;
+  float* ht;     // queue entries: arrival time
+  int32_t* hi;   // queue entries: pixel
+  int32_t* pos;  // queue slot of each pixel, -1 when absent
+  short2* off;   // disc offsets
+};
+
+__device__ __forceinline__ bool tless(float ta, int32_t ia, float tb, int32_t ib) {
+  return ta < tb || (ta == tb && ia < ib);
+}
+
+__device__ void tswap(TeleaMem& m, int32_t i, int32_t j) {
+  const float t = m.ht[i];
+  const int32_t k = m.hi[i];
+  m.ht[i] = m.ht[j];
+  m.hi[i] = m.hi[j];
+  m.ht[j] = t;
+  m.hi[j] = k;
+  m.pos[m.hi[i]] = i;
+  m.pos[m.hi[j]] = j;
+}
+
+__device__ void tup(TeleaMem& m, int32_t i) {
+  while (i > 0) {
+    const int32_t p = (i - 1) / 2;
+    if (!tless(m.ht[i], m.hi[i], m.ht[p], m.hi[p])) break;
+    tswap(m, i, p);
+    i = p;
+  }
+}
+
+__device__ void tdown(TeleaMem& m, int32_t i, int32_t n) {
+  for (;;) {
+    const int32_t l = 2 * i + 1, r = l + 1;
+    int32_t s = i;
+    if (l < n && tless(m.ht[l], m.hi[l], m.ht[s], m.hi[s])) s = l;
+    if (r < n && tless(m.ht[r], m.hi[r], m.ht[s], m.hi[s])) s = r;
+    if (s == i) break;
+    tswap(m, i, s);
+    i = s;
+  }
+}
+
+__device__ void tset(TeleaMem& m, int32_t idx, float t, int32_t& n) {
+  int32_t i = m.pos[idx];
+  if (i < 0) {
+    i = n++;
+    m.hi[i] = idx;
+    m.ht[i] = t;
+    m.pos[idx] = i;
+    tup(m, i);
+  } else {
+    const float ot = m.ht[i];
+    m.ht[i] = t;
+    if (tless(t, idx, ot, idx))
+      tup(m, i);
+    else
+      tdown(m, i, n);
+  }
+}
+
+__device__ __forceinline__ float eikonal(bool k1, float t1, bool k2, float t2) {
+  if (k1 && k2) {
+    const float dt = __fsub_rn(t1, t2);
+    if (fabsf(dt) >= 1.0f) return __fadd_rn(t1 < t2 ? t1 : t2, 1.0f);
+    return __fmul_rn(__fadd_rn(__fadd_rn(t1, t2), __fsqrt_rn(__fsub_rn(2.0f, __fmul_rn(dt, dt)))), 0.5f);
+  }
+  if (k1) return __fadd_rn(t1, 1.0f);
+  if (k2) return __fadd_rn(t2, 1.0f);
+  return 1e6f;
+}
+
+__device__ __forceinline__ float grad1(bool km, float am, bool kp, float ap, float a0) {
+  if (km && kp) return __fmul_rn(__fsub_rn(ap, am), 0.5f);
+  if (kp) return __fsub_rn(ap, a0);
+  if (km) return __fsub_rn(a0, am);
+  return 0.0f;
+}
+
+// Partial sums of one inpainted value over this thread's disc offsets.
+__device__ void telea_terms(const TeleaMem& m, int32_t w, int32_t h, int32_t x, int32_t y, float gtx, float gty,
+                            int n_off, bool unit_dir, long long& num, long long& den) {
+  const size_t p = (size_t)y * w + x;
+  const float tp = m.T[p];
+  for (int o = threadIdx.x; o < n_off; o += blockDim.x) {
+    const int32_t dx = m.off[o].x, dy = m.off[o].y;
+    const int32_t kx = x + dx, ky = y + dy;
+    if (kx < 0 || kx >= w || ky < 0 || ky >= h) continue;
+    const size_t k = (size_t)ky * w + kx;
+    if (m.flag[k] == kInside) continue;
+    const int32_t rx = -dx, ry = -dy;
+    const float len2 = (float)(rx * rx + ry * ry);
+    const float len = __fsqrt_rn(len2);
+    const float dir =
+        unit_dir ? 1.0f : __fdiv_rn(fabsf(__fadd_rn(__fmul_rn((float)rx, gtx), __fmul_rn((float)ry, gty))), len);
+    const float dst = __fdiv_rn(1.0f, len2);
+    const float lev = __fdiv_rn(1.0f, __fadd_rn(1.0f, fabsf(__fsub_rn(m.T[k], tp))));
+    const float wt = __fmul_rn(__fmul_rn(dir, dst), lev);
+    const bool ixm = kx > 0 && m.flag[k - 1] != kInside, ixp = kx + 1 < w && m.flag[k + 1] != kInside;
+    const bool iym = ky > 0 && m.flag[k - w] != kInside, iyp = ky + 1 < h && m.flag[k + w] != kInside;
+    const float a0 = (float)m.img[k];
+    const float gix = grad1(ixm, ixm ? (float)m.img[k - 1] : 0.0f, ixp, ixp ? (float)m.img[k + 1] : 0.0f, a0);
+    const float giy = grad1(iym, iym ? (float)m.img[k - w] : 0.0f, iyp, iyp ? (float)m.img[k + w] : 0.0f, a0);
+    const float val = __fadd_rn(a0, __fadd_rn(__fmul_rn(gix, (float)rx), __fmul_rn(giy, (float)ry)));
+    den += __double2ll_rn(__dmul_rn((double)wt, 4294967296.0));
+    num += __double2ll_rn(__dmul_rn((double)__fmul_rn(wt, val), 4294967296.0));
+  }
+}
+
+__device__ void block_sum2(long long& a, long long& b, long long* red) {
+  for (int s = 16; s > 0; s >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, s);
+    b += __shfl_down_sync(0xffffffffu, b, s);
+  }
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[2 * wid] = a;
+    red[2 * wid + 1] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long sa = 0, sb = 0;
+    for (int i = 0; i < nw; ++i) {
+      sa += red[2 * i];
+      sb += red[2 * i + 1];
+    }
+    red[64] = sa;
+    red[65] = sb;
+  }
+  __syncthreads();
+  a = red[64];
+  b = red[65];
+}
+
+__global__ void __launch_bounds__(512) telea_kernel(uint8_t* __restrict__ img_io, const uint32_t* misc,
+                                                     int32_t w, int32_t h, int32_t radius, int n_off,
+                                                     unsigned char* __restrict__ gmem, int use_smem) {
+  extern __shared__ __align__(16) unsigned char tsm[];
+  __shared__ long long red[66];
+  __shared__ int32_t s_q, s_done;
+  __shared__ float s_gtx, s_gty;
+  if (misc[3] == misc[2]) return;  // flat depth: nothing is filled
+  const size_t n = (size_t)w * h;
+  unsigned char* base = use_smem ? tsm : gmem;
+  // layout: offsets | T | ht | hi | pos | flag | img
+  TeleaMem m;
+  size_t o = 0;
+  m.off = reinterpret_cast<short2*>(base + o);
+  o += ((size_t)n_off * sizeof(short2) + 15) & ~(size_t)15;
+  m.T = reinterpret_cast<float*>(base + o);
+  o += (n * 4 + 15) & ~(size_t)15;
+  m.ht = reinterpret_cast<float*>(base + o);
+  o += (n * 4 + 15) & ~(size_t)15;
+  m.hi = reinterpret_cast<int32_t*>(base + o);
+  o += (n * 4 + 15) & ~(size_t)15;
+  m.pos = reinterpret_cast<int32_t*>(base + o);
+  o += (n * 4 + 15) & ~(size_t)15;
+  m.flag = base + o;
+  o += (n + 15) & ~(size_t)15;
+  m.img = base + o;
+  // disc offsets in raster order
+  if (threadIdx.x == 0) {
+    int k = 0;
+    for (int32_t dy = -radius; dy <= radius; ++dy)
+      for (int32_t dx = -radius; dx <= radius; ++dx)
+        if ((dx || dy) && dx * dx + dy * dy <= radius * radius) m.off[k++] = make_short2((short)dx, (short)dy);
+  }
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const uint8_t v = img_io[i];
+    m.img[i] = v;
+    m.flag[i] = v == 0 ? kInside : kKnown;
+    m.T[i] = v == 0 ? 1e6f : 0.0f;
+    m.pos[i] = -1;
+  }
+  __syncthreads();
+  int32_t hn = 0;  // queue length (thread 0)
+  int32_t cur = -1, nb = 4;  // popped pixel and its next neighbour (thread 0)
+  if (threadIdx.x == 0) {
+    for (int32_t y = 0; y < h; ++y)
+      for (int32_t x = 0; x < w; ++x) {
+        const size_t p = (size_t)y * w + x;
+        if (m.flag[p] == kInside) continue;
+        const bool adj = (y > 0 && m.flag[p - w] == kInside) || (x > 0 && m.flag[p - 1] == kInside) ||
+                         (y + 1 < h && m.flag[p + w] == kInside) || (x + 1 < w && m.flag[p + 1] == kInside);
+        if (adj) {
+          m.flag[p] = kBand;
+          tset(m, (int32_t)p, 0.0f, hn);
+        }
+      }
+  }
+  for (;;) {
+    if (threadIdx.x == 0) {
+      // advance to the next neighbour that needs an inpainted value
+      s_q = -1;
+      s_done = 0;
+      for (;;) {
+        if (nb >= 4) {
+          if (hn == 0) {
+            s_done = 1;
+            break;
+          }
+          cur = m.hi[0];
+          tswap(m, 0, hn - 1);
+          --hn;
+          m.pos[cur] = -1;
+          if (hn > 0) tdown(m, 0, hn);
+          m.flag[cur] = kKnown;
+          nb = 0;
+        }
+        const int32_t px = cur % w, py = cur / w;
+        const int32_t j = nb++;
+        const int32_t x = j == 1 ? px - 1 : j == 3 ? px + 1 : px;
+        const int32_t y = j == 0 ? py - 1 : j == 2 ? py + 1 : py;
+        if (x < 0 || x >= w || y < 0 || y >= h) continue;
+        const size_t q = (size_t)y * w + x;
+        if (m.flag[q] == kKnown) continue;
+        const bool ku = y > 0 && m.flag[q - w] == kKnown, kd = y + 1 < h && m.flag[q + w] == kKnown;
+        const bool kl = x > 0 && m.flag[q - 1] == kKnown, kr = x + 1 < w && m.flag[q + 1] == kKnown;
+        const float tu = ku ? m.T[q - w] : 0.0f, td = kd ? m.T[q + w] : 0.0f;
+        const float tl = kl ? m.T[q - 1] : 0.0f, tr = kr ? m.T[q + 1] : 0.0f;
+        float t = eikonal(ku, tu, kl, tl);
+        float t2 = eikonal(kd, td, kl, tl);
+        if (t2 < t) t = t2;
+        t2 = eikonal(ku, tu, kr, tr);
+        if (t2 < t) t = t2;
+        t2 = eikonal(kd, td, kr, tr);
+        if (t2 < t) t = t2;
+        m.T[q] = t;
+        if (m.flag[q] == kInside) {
+          // inpainted while still INSIDE (its own value is not used), then BAND;
+          // the arrival-time gradient at q, over its non-INSIDE neighbours
+          const bool kxm = x > 0 && m.flag[q - 1] != kInside, kxp = x + 1 < w && m.flag[q + 1] != kInside;
+          const bool kym = y > 0 && m.flag[q - w] != kInside, kyp = y + 1 < h && m.flag[q + w] != kInside;
+          s_gtx = grad1(kxm, kxm ? m.T[q - 1] : 0.0f, kxp, kxp ? m.T[q + 1] : 0.0f, t);
+          s_gty = grad1(kym, kym ? m.T[q - w] : 0.0f, kyp, kyp ? m.T[q + w] : 0.0f, t);
+          s_q = (int32_t)q;
+          tset(m, (int32_t)q, t, hn);
+          break;
+        }
+        tset(m, (int32_t)q, t, hn);
+      }
+    }
+    __syncthreads();
+    if (s_done) break;
+    const int32_t q = s_q;
+    const int32_t qx = q % w, qy = q / w;
+    uint8_t val = 0;
+    bool set = false;
+    for (int pass = 0; pass < 2 && !set; ++pass) {
+      long long num = 0, den = 0;
+      telea_terms(m, w, h, qx, qy, s_gtx, s_gty, n_off, pass == 1, num, den);
+      block_sum2(num, den, red);
+      if (den > 0) {
+        const double v = rint((double)num / (double)den);
+        val = (uint8_t)(v < 0.0 ? 0.0 : v > 255.0 ? 255.0 : v);
+        set = true;
+      }
+    }
+    if (threadIdx.x == 0) {
+      m.img[q] = val;
+      m.flag[q] = kBand;
+    }
+    __syncthreads();
+  }
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) img_io[i] = m.img[i];
+}
+
+// Grow the inpainted map back to full size where it is needed and fill the
+// depth: bilinear with half-pixel centres and 11-bit weights, then
+// gray * (uint16)((max - min) / 255) + min at pixels without depth.
+struct LinCoef {
+  int32_t s0, s1, a0;
+};
+
+__device__ __forceinline__ LinCoef lin_coef(int32_t dx, int32_t sw, int32_t dw) {
+  float f = (float)__dsub_rn(__dmul_rn((double)dx + 0.5, __ddiv_rn((double)sw, (double)dw)), 0.5);
+  int32_t s = (int32_t)floorf(f);
+  f = __fsub_rn(f, (float)s);
+  if (s < 0) {
+    f = 0.0f;
+    s = 0;
+  }
+  if (s >= sw - 1) {
+    f = 0.0f;
+    s = sw - 1;
+  }
+  LinCoef c;
+  c.s0 = s;
+  c.s1 = s + 1 < sw ? s + 1 : sw - 1;
+  c.a0 = (int32_t)rintf(__fmul_rn(__fsub_rn(1.0f, f), 2048.0f));
+  return c;
+}
+
+__global__ void inpaint_fill_kernel(const uint16_t* __restrict__ sm, const uint32_t* misc,
+                                    const uint8_t* __restrict__ small, uint16_t* __restrict__ out, FrontConst c,
+                                    InpaintDims s) {
+  const size_t n = (size_t)c.W * c.H;
+  const uint32_t mn = misc[2], mx = misc[3];
+  const uint16_t dgs = mx == mn ? 0 : (uint16_t)((double)(mx - mn) / 255.0);
+  GRID_STRIDE(p, n) {
+    const uint16_t z = sm[p];
+    if (z != 0 || mx == mn || s.sw < 1 || s.sh < 1) {
+      out[p] = z;
+      continue;
+    }
+    int gv = to_gray8(z, mn, mx);
+    if (gv == 0) {
+      const int32_t y = (int32_t)(p / c.W), x = (int32_t)(p - (size_t)y * c.W);
+      const LinCoef cx = lin_coef(x, s.sw, c.W), cy = lin_coef(y, s.sh, c.H);
+      const int64_t r0 = (int64_t)cx.a0 * small[(size_t)cy.s0 * s.sw + cx.s0] +
+                         (int64_t)(2048 - cx.a0) * small[(size_t)cy.s0 * s.sw + cx.s1];
+      const int64_t r1 = (int64_t)cx.a0 * small[(size_t)cy.s1 * s.sw + cx.s0] +
+                         (int64_t)(2048 - cx.a0) * small[(size_t)cy.s1 * s.sw + cx.s1];
+      const int64_t v = ((int64_t)cy.a0 * r0 + (int64_t)(2048 - cy.a0) * r1 + (1 << 21)) >> 22;
+      gv = (int)(v < 0 ? 0 : v > 255 ? 255 : v);
+    }
+    out[p] = (uint16_t)(gv * dgs + mn);
+  }
+}
+
+// ---- myCannyWithOri2 (GraphCannySeg.cpp:638-1050) ---------------------------
+
+// integer separable Gaussian (taps summing to 256), border reflect-101
+__global__ void blur_rows_kernel(const uint8_t* __restrict__ src, int32_t* __restrict__ tmp, FrontConst c,
+                                 int k7) {
+  const size_t n = (size_t)c.W * c.H;
+  const int32_t* taps = k7 ? c.blur7 : c.blur5;
+  const int ks = k7 ? 7 : 5, hc = ks / 2;
+  GRID_STRIDE(p, n) {
+    const int32_t y = (int32_t)(p / c.W), x = (int32_t)(p - (size_t)y * c.W);
+    const uint8_t* row = src + (size_t)y * c.W;
+    int32_t s = 0;
+    for (int i = 0; i < ks; ++i) s += taps[i] * row[refl101(x + i - hc, c.W)];
+    tmp[p] = s;
+  }
+}
+
+__global__ void blur_cols_kernel(const int32_t* __restrict__ tmp, uint8_t* __restrict__ dst, FrontConst c,
+                                 int k7) {
+  const size_t n = (size_t)c.W * c.H;
+  const int32_t* taps = k7 ? c.blur7 : c.blur5;
+  const int ks = k7 ? 7 : 5, hc = ks / 2;
+  GRID_STRIDE(p, n) {
+    const int32_t y = (int32_t)(p / c.W), x = (int32_t)(p - (size_t)y * c.W);
+    int64_t s = 0;
+    for (int i = 0; i < ks; ++i) s += (int64_t)taps[i] * tmp[(size_t)refl101(y + i - hc, c.H) * c.W + x];
+    dst[p] = (uint8_t)((s + 32768) >> 16);
+  }
+}
+
+__device__ __forceinline__ int orient_bin(int32_t x, int32_t y) {
+  if (y < 0 || (y == 0 && x < 0)) {
+    x = -x;
+    y = -y;
+  }
+  if (x == 0 && y == 0) return 0;
+  const int64_t a = x < 0 ? -(int64_t)x : x, b = y;
+  if ((a + b) * (a + b) < 2 * a * a) return 0;
+  if (b > a && (b - a) * (b - a) > 2 * a * a) return 90;
+  return x >= 0 ? 45 : 135;
+}
+
+// Scharr dx and -dy (reflect-101), magnitude and orientation bin
+__global__ void scharr_kernel(const uint8_t* __restrict__ bl, float* __restrict__ G, uint8_t* __restrict__ bin,
+                              FrontConst c) {
+  const size_t n = (size_t)c.W * c.H;
+  GRID_STRIDE(p, n) {
+    const int32_t y = (int32_t)(p / c.W), x = (int32_t)(p - (size_t)y * c.W);
+    const int32_t xm = refl101(x - 1, c.W), xp = refl101(x + 1, c.W);
+    const int32_t ym = refl101(y - 1, c.H), yp = refl101(y + 1, c.H);
+#define B_(yy, xx) ((int32_t)bl[(size_t)(yy) * c.W + (xx)])
+    const int32_t dx = 3 * (B_(ym, xp) - B_(ym, xm)) + 10 * (B_(y, xp) - B_(y, xm)) + 3 * (B_(yp, xp) - B_(yp, xm));
+    const int32_t dy = 3 * (B_(yp, xm) - B_(ym, xm)) + 10 * (B_(yp, x) - B_(ym, x)) + 3 * (B_(yp, xp) - B_(ym, xp));
+#undef B_
+    G[p] = __fsqrt_rn(__fadd_rn((float)(dx * dx), (float)(dy * dy)));
+    bin[p] = (uint8_t)orient_bin(dx, -dy);
+  }
+}
+
+// non-maximum suppression over the interior; misc[4] = max (float bits)
+__global__ void nms_kernel(const float* __restrict__ G, const uint8_t* __restrict__ bin, float* __restrict__ BW,
+                           uint32_t* misc, FrontConst c) {
+  const size_t n = (size_t)c.W * c.H;
+  float mx = 0.0f;
+  GRID_STRIDE(p, n) {
+    const int32_t i = (int32_t)(p / c.W), j = (int32_t)(p - (size_t)i * c.W);
+    float v = 0.0f;
+    if (i >= 1 && i < c.H - 1 && j >= 1 && j < c.W - 1) {
+      float a, b;
+      switch (bin[p]) {
+        case 0: a = G[p + 1]; b = G[p - 1]; break;
+        case 45: a = G[p + c.W - 1]; b = G[p - c.W + 1]; break;
+        case 90: a = G[p + c.W]; b = G[p - c.W]; break;
+        default: a = G[p + c.W + 1]; b = G[p - c.W - 1]; break;
+      }
+      const float g = G[p];
+      const float m3 = g >= a ? (g >= b ? g : b) : (a >= b ? a : b);
+      if (g == m3) v = g;
+    }
+    BW[p] = v;
+    mx = v > mx ? v : mx;
+  }
+  const uint32_t bits = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));  // non-negative floats
+  if ((threadIdx.x & 31) == 0) atomicMax(misc + 4, bits);
+}
+
+__device__ __forceinline__ void back_project(const float* kinv, int32_t u, int32_t v, uint16_t z, float* o) {
+  const float p0 = (float)(u * (int32_t)z), p1 = (float)(v * (int32_t)z), p2 = (float)z;
+  o[0] = (float)__dadd_rn(__dmul_rn((double)kinv[0], (double)p0), __dmul_rn((double)kinv[1], (double)p2));
+  o[1] = (float)__dadd_rn(__dmul_rn((double)kinv[2], (double)p1), __dmul_rn((double)kinv[3], (double)p2));
+  o[2] = p2;
+}
+
+__device__ float angle3(const float* p1, const float* p0, const float* p2) {
+  float a[3], b[3], cr[3];
+  for (int k = 0; k < 3; ++k) {
+    a[k] = __fsub_rn(p1[k], p0[k]);
+    b[k] = __fsub_rn(p2[k], p0[k]);
+  }
+  const float la = (float)__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn((double)a[0], a[0]), __dmul_rn((double)a[1], a[1])),
+                                               __dmul_rn((double)a[2], a[2])));
+  const float lb = (float)__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn((double)b[0], b[0]), __dmul_rn((double)b[1], b[1])),
+                                               __dmul_rn((double)b[2], b[2])));
+  const float dot = (float)__dadd_rn(__dadd_rn(__dmul_rn((double)a[0], b[0]), __dmul_rn((double)a[1], b[1])),
+                                     __dmul_rn((double)a[2], b[2]));
+  const float cs = __fdiv_rn(dot, __fmul_rn(la, lb));
+  cr[0] = __fsub_rn(__fmul_rn(a[1], b[2]), __fmul_rn(a[2], b[1]));
+  cr[1] = __fsub_rn(__fmul_rn(a[2], b[0]), __fmul_rn(a[0], b[2]));
+  cr[2] = __fsub_rn(__fmul_rn(a[0], b[1]), __fmul_rn(a[1], b[0]));
+  const float lc = (float)__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn((double)cr[0], cr[0]), __dmul_rn((double)cr[1], cr[1])),
+                                               __dmul_rn((double)cr[2], cr[2])));
+  const float sn = __fdiv_rn(lc, __fmul_rn(la, lb));
+  float th = (float)atan2((double)sn, (double)cs);
+  if (cr[0] < 0.0f) th = -th;
+  return th;
+}
+
+// one hysteresis pass (8 neighbours, outside the image = 0), the border
+// of max(plusD, point3D) + 1 pixels zeroed, and the depth test
+__global__ void hyst_depth_kernel(const float* __restrict__ BW, const uint8_t* __restrict__ bin,
+                                  const uint16_t* __restrict__ inp, const uint32_t* misc, uint8_t* __restrict__ mag,
+                                  FrontConst c) {
+  const size_t n = (size_t)c.W * c.H;
+  const float mx = __uint_as_float(misc[4]);
+  const float tl = (float)__dmul_rn((double)c.canny_low, (double)mx);
+  const float th = (float)__dmul_rn((double)c.canny_high, (double)mx);
+  const int32_t pd = c.plus_d, p3 = c.point_3d;
+  const int32_t sp = (pd > p3 ? pd : p3) + 1;
+  GRID_STRIDE(p, n) {
+    const int32_t i = (int32_t)(p / c.W), j = (int32_t)(p - (size_t)i * c.W);
+    uint8_t m = 0;
+    const float v = BW[p];
+    if (!(v < tl)) {
+      if (v > th) {
+        m = 255;
+      } else {
+        for (int dy = -1; dy <= 1 && !m; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            if (!dx && !dy) continue;
+            const int32_t y = i + dy, x = j + dx;
+            if (y < 0 || y >= c.H || x < 0 || x >= c.W) continue;
+            if (BW[(size_t)y * c.W + x] > th) {
+              m = 255;
+              break;
+            }
+          }
+      }
+    }
+    if (i < sp || i > c.H - sp || j < sp || j > c.W - sp) m = 0;
+    if (m) {
+      int32_t ex, ey;
+      switch (bin[p]) {
+        case 0: ex = 1; ey = 0; break;
+        case 45: ex = 1; ey = -1; break;
+        case 90: ex = 0; ey = -1; break;
+        default: ex = -1; ey = -1; break;
+      }
+#define Z_(xx, yy) inp[(size_t)(yy) * c.W + (xx)]
+      const int z0 = Z_(j, i);
+      const uint16_t dp2 = (uint16_t)abs(z0 - (int)Z_(j + ex * pd, i + ey * pd));
+      const uint16_t dm2 = (uint16_t)abs(z0 - (int)Z_(j - ex * pd, i - ey * pd));
+      if (dp2 < c.dth && dm2 < c.dth) {
+        float q0[3], q1[3], q2[3];
+        back_project(c.kinv, j, i, Z_(j, i), q0);
+        back_project(c.kinv, j + ex * p3, i + ey * p3, Z_(j + ex * p3, i + ey * p3), q1);
+        back_project(c.kinv, j - ex * p3, i - ey * p3, Z_(j - ex * p3, i - ey * p3), q2);
+        const float theta = angle3(q1, q0, q2);
+        if (theta > c.g_angle || theta < c.l_angle) m = 0;
+      }
+#undef Z_
+    }
+    mag[p] = m;
+  }
+}
+
+// misc[5] = min, misc[6] = max of an 8-bit map (initialised 255 / 0)
+__global__ void minmax_u8_kernel(const uint8_t* __restrict__ a, size_t n, uint32_t* misc) {
+  uint32_t lo = 255u, hi = 0u;
+  GRID_STRIDE(t, n) {
+    const uint32_t v = a[t];
+    lo = v < lo ? v : lo;
+    hi = v > hi ? v : hi;
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(misc + 5, lo);
+    atomicMax(misc + 6, hi);
+  }
+}
+
+__global__ void saliency_kernel(const uint8_t* __restrict__ mb, const uint32_t* misc, float* __restrict__ sal,
+                                size_t n) {
+  const uint32_t mn = misc[5], mx = misc[6];
+  const float a = mx == mn ? 0.0f : (float)__ddiv_rn(1.0, (double)(mx - mn));
+  const float b = mx == mn ? 0.0f : (float)__ddiv_rn(-(double)mn * 1.0, (double)(mx - mn));
+  GRID_STRIDE(t, n) sal[t] = mx == mn ? 0.0f : __fadd_rn(__fmul_rn((float)mb[t], a), b);
+}
+
+__global__ void front_misc_init_kernel(uint32_t* misc) {
+  misc[0] = 0;        // any marked pixel
+  misc[1] = 0;
+  misc[2] = 0xFFFFu;  // smoothed depth min
+  misc[3] = 0;        // and max
+  misc[4] = 0;        // max of the suppressed gradient (float bits)
+  misc[5] = 255u;     // blurred edge map min
+  misc[6] = 0;        // and max
+  misc[7] = 0;
+}
+
+int grid_of(size_t work, int threads, int sms) {
+  const size_t blocks = (work + threads - 1) / threads;
+  const size_t cap = (size_t)sms * 8;
+  return (int)(blocks < 1 ? 1 : blocks < cap ? blocks : cap);
+}
+
+size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+int disc_count(int32_t radius) {
+  int k = 0;
+  for (int32_t dy = -radius; dy <= radius; ++dy)
+    for (int32_t dx = -radius; dx <= radius; ++dx)
+      if ((dx || dy) && dx * dx + dy * dy <= radius * radius) ++k;
+  return k;
+}
+
+size_t telea_bytes(int32_t sw, int32_t sh, int n_off) {
+  const size_t n = (size_t)sw * sh;
+  auto a16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+  return a16((size_t)n_off * 4) + 4 * a16(n * 4) + a16(n) + a16(n);
+}
+
+}  // namespace
+
+// ---- host side ---------------------------------------------------------------
+
+int seg_gauss_taps(int ksize, int32_t* taps) {
+  if (ksize < 1 || (ksize & 1) == 0 || ksize > 31) return -1;
+  const double sigma = 0.3 * ((ksize - 1) * 0.5 - 1.0) + 0.8;
+  const int c = ksize / 2;
+  double g[31], sum = 0.0;
+  for (int i = 0; i < ksize; ++i) {
+    const double x = (double)(i - c);
+    g[i] = std::exp(-(x * x) / (2.0 * sigma * sigma));
+    sum += g[i];
+  }
+  int32_t tot = 0;
+  for (int i = 0; i < ksize; ++i) {
+    taps[i] = (int32_t)std::floor(g[i] / sum * 256.0 + 0.5);
+    tot += taps[i];
+  }
+  taps[c] += 256 - tot;
+  return ksize;
+}
+
+size_t seg_front_workspace_bytes(int32_t W, int32_t H, int32_t radius) {
+  const size_t n = (size_t)W * H, n1 = (size_t)(W + 1) * (H + 1);
+  const int32_t sw = (int32_t)std::rint(W * 0.2), sh = (int32_t)std::rint(H * 0.2);
+  return al256(3 * n) + al256(n) + al256(2 * n) + al256(n) + al256(4 * n) + al256(4 * n) + 2 * al256(4 * n) +
+         2 * al256(4 * n1) + al256(2 * n) + al256((size_t)(sw > 0 ? sw : 1) * (sh > 0 ? sh : 1)) +
+         al256(4 * n) + al256(4 * n) + al256(n) + al256(4 * n) + al256(n) + al256(n) + al256(64) +
+         al256(telea_bytes(sw > 0 ? sw : 1, sh > 0 ? sh : 1, disc_count(radius)));
+}
+
+cudaError_t seg_front_run(const SegFrontArgs& a, void* ws, int sms, size_t smem_optin, cudaStream_t st) {
+  const int32_t W = a.W, H = a.H;
+  const size_t n = (size_t)W * H, n1 = (size_t)(W + 1) * (H + 1);
+  char* p = static_cast<char*>(ws);
+  auto take = [&](size_t b) {
+    char* q = p;
+    p += al256(b);
+    return q;
+  };
+  uint8_t* d_bgr = (uint8_t*)take(3 * n);
+  uint8_t* d_gray = (uint8_t*)take(n);
+  uint16_t* d_raw = (uint16_t*)take(2 * n);
+  uint8_t* d_cm = (uint8_t*)take(n);
+  int32_t* d_g = (int32_t*)take(4 * n);
+  float* d_R = (float*)take(4 * n);
+  float* d_rs = (float*)take(4 * n);
+  int32_t* d_rz = (int32_t*)take(4 * n);
+  float* d_I = (float*)take(4 * n1);
+  int32_t* d_N = (int32_t*)take(4 * n1);
+  uint16_t* d_sm = (uint16_t*)take(2 * n);
+  const int32_t sw = (int32_t)std::rint(W * 0.2), sh = (int32_t)std::rint(H * 0.2);
+  uint8_t* d_small = (uint8_t*)take((size_t)(sw > 0 ? sw : 1) * (sh > 0 ? sh : 1));
+  int32_t* d_tmp = (int32_t*)take(4 * n);
+  float* d_G = (float*)take(4 * n);
+  uint8_t* d_bin = (uint8_t*)take(n);
+  float* d_BW = (float*)take(4 * n);
+  uint8_t* d_mag = (uint8_t*)take(n);
+  uint8_t* d_mb = (uint8_t*)take(n);
+  uint32_t* d_misc = (uint32_t*)take(64);
+  const int n_off = disc_count(a.radius);
+  unsigned char* d_telea = (unsigned char*)take(telea_bytes(sw > 0 ? sw : 1, sh > 0 ? sh : 1, n_off));
+
+  FrontConst c{};
+  c.W = W;
+  c.H = H;
+  c.alfa = 0.0028f / 1e6f;
+  c.beta = a.beta;
+  c.gamma = a.gamma;
+  seg_gauss_taps(5, c.blur5);
+  seg_gauss_taps(7, c.blur7);
+  c.canny_low = a.canny_low;
+  c.canny_high = a.canny_high;
+  c.dth = a.dth;
+  c.plus_d = a.plus_d;
+  c.point_3d = a.point_3d;
+  c.g_angle = a.g_angle;
+  c.l_angle = a.l_angle;
+  c.kinv[0] = 1.0f / a.fx;
+  c.kinv[1] = -a.cx / a.fx;
+  c.kinv[2] = 1.0f / a.fy;
+  c.kinv[3] = -a.cy / a.fy;
+
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(d_bgr, a.bgr_host, 3 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(d_raw, a.depth_host, 2 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  const int T = 256;
+  front_misc_init_kernel<<<1, 1, 0, st>>>(d_misc);
+  front_colour_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_bgr, n, a.hsv_out, d_gray);
+  // depth smoothing
+  smooth_cmap_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_raw, d_cm, d_misc, c);
+  edt_rows_kernel<<<(H + 127) / 128, 128, 0, st>>>(d_cm, d_g, c);
+  smooth_radius_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_raw, d_g, d_misc, d_R, c);
+  integral_rows_kernel<<<(H + 127) / 128, 128, 0, st>>>(d_raw, d_cm, d_rs, d_rz, c);
+  integral_cols_kernel<<<(W + 1 + 127) / 128, 128, 0, st>>>(d_rs, d_rz, d_I, d_N, c);
+  smooth_out_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_raw, d_R, d_I, d_N, d_sm, c);
+  // inpainting
+  minmax_u16_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_sm, n, d_misc);
+  InpaintDims dims{sw, sh};
+  if (sw >= 1 && sh >= 1) {
+    inpaint_shrink_kernel<<<grid_of((size_t)sw * sh, T, sms), T, 0, st>>>(d_sm, d_misc, d_small, c, dims);
+    const size_t tb = telea_bytes(sw, sh, n_off);
+    // the kernel's static shared memory (reduction slots) must fit beside it
+    const int use_smem = tb + 1024 <= smem_optin ? 1 : 0;
+    const size_t dyn = use_smem ? tb : 0;
+    if (use_smem && dyn > 48 * 1024) {
+      if ((e = cudaFuncSetAttribute(telea_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn)) !=
+          cudaSuccess)
+        return e;
+    }
+    telea_kernel<<<1, 512, dyn, st>>>(d_small, d_misc, sw, sh, a.radius, n_off, d_telea, use_smem);
+  }
+  inpaint_fill_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_sm, d_misc, d_small, a.inpainted_out, c, dims);
+  // Canny saliency
+  blur_rows_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_gray, d_tmp, c, 0);
+  blur_cols_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_tmp, d_mb, c, 0);
+  scharr_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_mb, d_G, d_bin, c);
+  nms_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_G, d_bin, d_BW, d_misc, c);
+  hyst_depth_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_BW, d_bin, a.inpainted_out, d_misc, d_mag, c);
+  blur_rows_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_mag, d_tmp, c, 1);
+  blur_cols_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_tmp, d_mb, c, 1);
+  minmax_u8_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_mb, n, d_misc);
+  saliency_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_mb, d_misc, a.saliency_out, n);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // optional copies of the intermediate planes
+  if (a.gray_host && (e = cudaMemcpyAsync(a.gray_host, d_gray, n, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  if (a.smoothed_host &&
+      (e = cudaMemcpyAsync(a.smoothed_host, d_sm, 2 * n, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  if (a.edges_host && (e = cudaMemcpyAsync(a.edges_host, d_mag, n, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  return cudaSuccess;
+}
+
+// ---- per-set moments for the cluster filter ----------------------------------
+
+// One warp takes 32 consecutive pixels.  When they all belong to one set
+// (the common case inside a segment), the warp reduces its sums with
+// shuffles and one lane adds them; otherwise every lane adds its own.
+__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+  return v;
+}
+
+__global__ void set_moments_kernel(const int32_t* __restrict__ labels, const uint16_t* __restrict__ inp,
+                                   const uint8_t* __restrict__ v8, int32_t W, int32_t H, int32_t n_sets,
+                                   SetMoments* __restrict__ acc) {
+  const size_t n = (size_t)W * H;
+  const int lane = threadIdx.x & 31;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t base = blockIdx.x * (size_t)blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+    const size_t p = base + lane;
+    const int32_t k = p < n ? labels[p] : -1;
+    const bool valid = k >= 0 && k < n_sets;
+    const int32_t y = valid ? (int32_t)(p / W) : 0, x = valid ? (int32_t)(p - (size_t)y * W) : 0;
+    const uint64_t z = valid ? inp[p] : 0;
+    const uint8_t v = valid ? v8[p] : 255;
+    unsigned long long f[15];
+    f[0] = valid;
+    f[1] = (unsigned long long)x;
+    f[2] = (unsigned long long)y;
+    f[3] = (unsigned long long)((int64_t)x * x);
+    f[4] = (unsigned long long)((int64_t)y * y);
+    f[5] = (unsigned long long)((int64_t)x * y);
+    f[6] = valid && z;
+    f[7] = z;
+    f[8] = (unsigned long long)x * z;
+    f[9] = (unsigned long long)y * z;
+    f[10] = valid && !z;
+    f[11] = v < 8;
+    f[12] = v >= 8 && v < 16;
+    f[13] = v >= 16 && v < 24;
+    const int32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+    const bool uniform = __all_sync(0xffffffffu, valid && k == k0);
+    if (uniform) {
+      for (int i = 0; i < 14; ++i) f[i] = warp_sum64(f[i]);
+      const int32_t mnx = __reduce_min_sync(0xffffffffu, x), mxx = __reduce_max_sync(0xffffffffu, x);
+      const int32_t mny = __reduce_min_sync(0xffffffffu, y), mxy = __reduce_max_sync(0xffffffffu, y);
+      if (lane == 0) {
+        SetMoments* a = acc + k0;
+        unsigned long long* dst[14] = {&a->n,  &a->sx, &a->sy,  &a->sxx,   &a->syy,   &a->sxy,   &a->nz,
+                                       &a->sz, &a->suz, &a->svz, &a->nzero, &a->vb[0], &a->vb[1], &a->vb[2]};
+        for (int i = 0; i < 14; ++i)
+          if (f[i]) atomicAdd(dst[i], f[i]);
+        atomicMin(&a->minx, mnx);
+        atomicMax(&a->maxx, mxx);
+        atomicMin(&a->miny, mny);
+        atomicMax(&a->maxy, mxy);
+      }
+    } else if (valid) {
+      SetMoments* a = acc + k;
+      unsigned long long* dst[14] = {&a->n,  &a->sx, &a->sy,  &a->sxx,   &a->syy,   &a->sxy,   &a->nz,
+                                     &a->sz, &a->suz, &a->svz, &a->nzero, &a->vb[0], &a->vb[1], &a->vb[2]};
+      for (int i = 0; i < 14; ++i)
+        if (f[i]) atomicAdd(dst[i], f[i]);
+      atomicMin(&a->minx, x);
+      atomicMax(&a->maxx, x);
+      atomicMin(&a->miny, y);
+      atomicMax(&a->maxy, y);
+    }
+  }
+}
+
+__global__ void set_moments_init_kernel(SetMoments* acc, int32_t n_sets) {
+  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_sets; k += gridDim.x * blockDim.x) {
+    SetMoments m{};
+    m.minx = m.miny = 0x7fffffff;
+    m.maxx = m.maxy = -1;
+    acc[k] = m;
+  }
+}
+
+cudaError_t launch_set_moments(const int32_t* labels, const uint16_t* inp, const uint8_t* v8, int32_t W, int32_t H,
+                               int32_t n_sets, SetMoments* acc, int sms, cudaStream_t st) {
+  if (n_sets <= 0) return cudaSuccess;
+  set_moments_init_kernel<<<(n_sets + 255) / 256, 256, 0, st>>>(acc, n_sets);
+  set_moments_kernel<<<grid_of((size_t)W * H, 256, sms), 256, 0, st>>>(labels, inp, v8, W, H, n_sets, acc);
+  return cudaGetLastError();
+}
+
+// The record of one set from its exact moments, with PostSegmFilter's
+// tests (GraphCannySeg.h:1700-1765): centroid norm > far_obj_z; PCA
+// eccentricity > max_ecc or eigenvalues above max_l1 / max_l2
+// (computePCA, GraphCannySeg.cpp:1376-1435: eigenvalues of the covariance
+// normalised by the point count); a share of pixels without depth >= 0.3;
+// a share in the three darkest of 32 value bins >= 0.3.  The shares divide
+// by the reference's list length n + 1.  Host code of this unit is built
+// without floating-point contraction, like the oracle's restatement.
+void seg_cluster_record(const SetMoments& m, int32_t label, const qpso_seg_front_params& fp, qpso_seg_cluster* r) {
+  std::memset(r, 0, sizeof(*r));
+  const int64_t n = (int64_t)m.n;
+  r->label = label;
+  r->num_points = (uint32_t)(n + 1);
+  r->pixels = (uint32_t)n;
+  r->min_x = m.minx;
+  r->max_x = m.maxx + 1;
+  r->min_y = m.miny;
+  r->max_y = m.maxy + 1;
+  const double cx = fp.cx, cy = fp.cy, fx = fp.fx, fy = fp.fy;
+  if (m.nz > 0) {
+    r->centroid_mm[0] = (float)(((double)m.suz - cx * (double)m.sz) / (fx * (double)m.nz));
+    r->centroid_mm[1] = (float)(((double)m.svz - cy * (double)m.sz) / (fy * (double)m.nz));
+    r->centroid_mm[2] = (float)((double)m.sz / (double)m.nz);
+  }
+  const float cxm = r->centroid_mm[0], cym = r->centroid_mm[1], czm = r->centroid_mm[2];
+  const float l2c = std::sqrt(czm * czm + cym * cym + cxm * cxm);
+  const double dn = (double)n;
+  const double mx = (double)m.sx / dn, my = (double)m.sy / dn;
+  const double vxx = ((double)m.sxx - (double)m.sx * mx) / dn;
+  const double vyy = ((double)m.syy - (double)m.sy * my) / dn;
+  const double vxy = ((double)m.sxy - (double)m.sx * my) / dn;
+  const double hm = 0.5 * (vxx + vyy);
+  const double hd = 0.5 * (vxx - vyy);
+  const double rt = std::sqrt(hd * hd + vxy * vxy);
+  r->eig[0] = hm + rt;
+  r->eig[1] = hm - rt;
+  r->eccentricity = r->eig[0] > 0.0 ? std::sqrt(1.0 - r->eig[1] / r->eig[0]) : 0.0;
+  const float area = (float)(n + 1);
+  r->nan_ratio = (float)m.nzero / area;
+  r->dark_ratio = ((float)m.vb[0] / area + (float)m.vb[1] / area) + (float)m.vb[2] / area;
+  r->far = l2c > fp.far_obj_z;
+  r->kept = !r->far && !(r->eccentricity > fp.max_ecc || r->eig[0] > fp.max_l1 || r->eig[1] > fp.max_l2) &&
+            !(r->nan_ratio >= 0.3f) && !(r->dark_ratio >= 0.3f);
+}
+
+}  // namespace qpso

@@ -273,6 +273,13 @@ __global__ void rs_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* __r
   }
 }
 
+__global__ void seg_misc_init_kernel(const uint16_t* __restrict__ d, uint32_t* misc) {
+  misc[0] = d[0];
+  misc[1] = d[0];
+  misc[2] = 0;
+  misc[3] = 0;
+}
+
 int grid_for(size_t work, int threads, int sms) {
   const size_t blocks = (work + threads - 1) / threads;
   const size_t cap = (size_t)sms * 8;
@@ -388,6 +395,17 @@ size_t seg_workspace_bytes(int32_t W, int32_t H) {
          al(4 * 256 * (nblk ? nblk : 1)) + al(16);
 }
 
+void seg_ws_inputs(void* ws, int32_t W, int32_t H, uint8_t** hsv, uint16_t** depth, float** sal) {
+  const size_t n = (size_t)W * H;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char* p = static_cast<char*>(ws);
+  *hsv = (uint8_t*)p;
+  p += al(3 * n);
+  *depth = (uint16_t*)p;
+  p += al(2 * n);
+  *sal = (float*)p;
+}
+
 cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
                              int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
                              float ks, void* ws, int sms, cudaStream_t st, uint32_t* order_host,
@@ -422,12 +440,17 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
   uint32_t* d_misc = (uint32_t*)p;  // [0] depth min, [1] depth max, [2] error bits
 
   cudaError_t e;
-  for (int c = 0; c < 3; ++c)
-    if ((e = cudaMemcpyAsync(d_hsv + c * n, hsv_host[c], n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(d_depth, depth_host, 2 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(d_sal, sal_host, 4 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
-  const uint32_t misc[4] = {depth_host[0], depth_host[0], 0u, 0u};
-  if ((e = cudaMemcpyAsync(d_misc, misc, sizeof(misc), cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  if (hsv_host) {
+    for (int c = 0; c < 3; ++c)
+      if ((e = cudaMemcpyAsync(d_hsv + c * n, hsv_host[c], n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(d_depth, depth_host, 2 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(d_sal, sal_host, 4 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    const uint32_t misc[4] = {depth_host[0], depth_host[0], 0u, 0u};
+    if ((e = cudaMemcpyAsync(d_misc, misc, sizeof(misc), cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  } else {
+    // the inputs are already in their slots (written by the stages before)
+    seg_misc_init_kernel<<<1, 1, 0, st>>>(d_depth, d_misc);
+  }
 
   SegConst c{};
   for (int i = 0; i < len; ++i) c.mask[i] = mask[i];

@@ -35,6 +35,7 @@ EXPORTS = [
     "qpso_server_stats_get", "qpso_server_stop", "qpso_render_depth_f32", "qpso_frame_clusters",
     "qpso_obj_load", "qpso_image_u16_load", "qpso_seg_params_init", "qpso_segment_num_edges",
     "qpso_segment_edge_ends", "qpso_segment_gauss_mask", "qpso_segment_edges", "qpso_segment_planes",
+    "qpso_seg_front_params_init", "qpso_segment_rgbd", "qpso_segment_clusters",
 ]
 
 
@@ -98,6 +99,29 @@ class Cluster(C.Structure):
 class SegParams(C.Structure):
     _fields_ = [("sigma", C.c_float), ("k", C.c_float), ("min_size", C.c_float), ("kx", C.c_float),
                 ("ky", C.c_float), ("ks", C.c_float), ("kdv", C.c_float), ("kdc", C.c_float)]
+
+
+class SegFrontParams(C.Structure):
+    _fields_ = [("beta", C.c_float), ("gamma", C.c_float), ("inpaint_radius", C.c_int32),
+                ("canny_low", C.c_float), ("canny_high", C.c_float), ("dth", C.c_int32),
+                ("plus_d", C.c_int32), ("point_3d", C.c_int32), ("g_angle", C.c_float),
+                ("l_angle", C.c_float), ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float),
+                ("cy", C.c_float), ("far_obj_z", C.c_float), ("max_ecc", C.c_float),
+                ("max_l1", C.c_float), ("max_l2", C.c_float)]
+
+
+class SegCluster(C.Structure):
+    _fields_ = [("label", C.c_int32), ("num_points", C.c_uint32), ("pixels", C.c_uint32),
+                ("min_x", C.c_int32), ("max_x", C.c_int32), ("min_y", C.c_int32), ("max_y", C.c_int32),
+                ("centroid_mm", C.c_float * 3), ("nan_ratio", C.c_float), ("dark_ratio", C.c_float),
+                ("eig", C.c_double * 2), ("eccentricity", C.c_double), ("far", C.c_int32),
+                ("kept", C.c_int32)]
+
+
+class SegFrameOut(C.Structure):
+    _fields_ = [("h", C.c_void_p), ("s", C.c_void_p), ("v", C.c_void_p), ("gray", C.c_void_p),
+                ("smoothed", C.c_void_p), ("inpainted", C.c_void_p), ("saliency", C.c_void_p),
+                ("edges", C.c_void_p)]
 
 
 class QpsoError(RuntimeError):
@@ -185,10 +209,17 @@ def load_library(path: str = LIB_PATH):
     L.qpso_segment_planes.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_uint32, C.c_uint32, C.POINTER(SegParams), C.c_void_p, C.c_void_p,
                                       C.POINTER(C.c_uint32)]
+    L.qpso_segment_rgbd.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(SegParams),
+                                    C.POINTER(SegFrontParams), C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p,
+                                    C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(SegFrameOut)]
+    L.qpso_segment_clusters.argtypes = [vp, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
+                                        C.c_uint32, C.POINTER(SegFrontParams), C.c_int, C.c_void_p, C.c_uint32,
+                                        C.POINTER(C.c_uint32)]
     for fn in EXPORTS:
         if fn not in ("qpso_version", "qpso_destroy", "qpso_last_error", "qpso_solve_desc_init",
                       "qpso_box_from_centroid", "qpso_host_alloc", "qpso_host_free",
-                      "qpso_get_stream", "qpso_seg_params_init", "qpso_segment_num_edges"):
+                      "qpso_get_stream", "qpso_seg_params_init", "qpso_segment_num_edges",
+                      "qpso_seg_front_params_init"):
             getattr(L, fn).restype = C.c_int32
     _lib = L
     return L
@@ -346,6 +377,53 @@ class Context:
         return [{"label": c.label, "num_points": c.num_points,
                  "aabb": (c.min_x, c.max_x, c.min_y, c.max_y), "depth_points": c.depth_points,
                  "centroid_mm": list(c.centroid_mm)} for c in arr[:n.value]]
+
+    def segment_rgbd(self, bgr, depth_mm, params: "SegParams | None" = None,
+                     front: "SegFrontParams | None" = None, planes: bool = False):
+        """GraphCannySeg<hsv>::run on the GPU (qpso_segment_rgbd) from a
+        BGR image (uint8 (height, width, 3)) and raw depth (uint16 mm).
+        Returns {"labels", "n_sets", "clusters"} (the kept sets in the
+        reference's order) and, with planes=True, the intermediate planes
+        h, s, v, gray, smoothed, inpainted, saliency, edges."""
+        b = np.ascontiguousarray(bgr, np.uint8)
+        d = np.ascontiguousarray(depth_mm, np.uint16)
+        H, W = d.shape
+        if b.shape != (H, W, 3):
+            raise ValueError("bgr must be (height, width, 3) like the depth")
+        prm = params if params is not None else seg_params()
+        fp = front if front is not None else seg_front_params()
+        labels = np.empty((H, W), np.int32)
+        ns, nc = C.c_uint32(), C.c_uint32()
+        out = {}
+        po = None
+        if planes:
+            out = {k: np.empty((H, W), t) for k, t in (("h", np.uint8), ("s", np.uint8), ("v", np.uint8),
+                                                        ("gray", np.uint8), ("smoothed", np.uint16),
+                                                        ("inpainted", np.uint16), ("saliency", np.float32),
+                                                        ("edges", np.uint8))}
+            po = SegFrameOut(*(out[k].ctypes.data for k, _ in SegFrameOut._fields_))
+        cap = W * H // 16 + 16
+        arr = (SegCluster * cap)()
+        self._check(self.L.qpso_segment_rgbd(self.h, b.ctypes.data, d.ctypes.data, W, H, C.byref(prm),
+                                             C.byref(fp), labels.ctypes.data, C.byref(ns), arr, cap,
+                                             C.byref(nc), C.byref(po) if po is not None else None))
+        out.update(labels=labels, n_sets=ns.value, clusters=list(arr[:min(nc.value, cap)]))
+        return out
+
+    def segment_clusters(self, labels, n_sets: int, inpainted_mm, v_plane,
+                         front: "SegFrontParams | None" = None, keep_all: bool = False) -> list:
+        """PostSegmFilter over a label map (qpso_segment_clusters)."""
+        lab = np.ascontiguousarray(labels, np.int32)
+        z = np.ascontiguousarray(inpainted_mm, np.uint16)
+        v = np.ascontiguousarray(v_plane, np.uint8)
+        H, W = lab.shape
+        fp = front if front is not None else seg_front_params()
+        arr = (SegCluster * max(1, n_sets))()
+        n = C.c_uint32()
+        self._check(self.L.qpso_segment_clusters(self.h, lab.ctypes.data, n_sets, z.ctypes.data, v.ctypes.data,
+                                                 W, H, C.byref(fp), int(keep_all), arr, max(1, n_sets),
+                                                 C.byref(n)))
+        return list(arr[:n.value])
 
     def segment_planes(self, h8, s8, v8, depth_mm, saliency, params: "SegParams | None" = None,
                        weights: bool = False):
@@ -524,6 +602,16 @@ def seg_params(**kw) -> SegParams:
     """The reference main's segmentation constants, fields overridden by kw."""
     p = SegParams()
     load_library().qpso_seg_params_init(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def seg_front_params(**kw) -> SegFrontParams:
+    """The reference main's constants for the stages around the graph stage
+    (main.h:51-77), fields overridden by kw."""
+    p = SegFrontParams()
+    load_library().qpso_seg_front_params_init(C.byref(p))
     for k, v in kw.items():
         setattr(p, k, v)
     return p

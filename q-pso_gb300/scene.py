@@ -467,6 +467,28 @@ def workload_c4(seed: int = 0, n_meshes: int = 16, n_frames: int = 32, per_frame
     return {"meshes": meshes, "frames": fr, "solves": solves}
 
 
+def segmentation_frame_c5(seed: int = 0, n_objects: int = 15):
+    """The stress configuration's segmentation input: one 640x480 RGB-D
+    frame with 15 non-overlapping objects (procedural meshes of 2k-3k faces,
+    40-120 mm) over the tilted plane, each object with its own base colour
+    and sigma=8 per-channel noise, depth noise and 5% dropout.  Returns
+    (depth uint16, ground-truth labels int32, bgr uint8)."""
+    rng = np.random.default_rng(11000 + seed)
+    kinds = ["icosphere", "box", "cylinder", "ellipsoid"]
+    meshes = [make_mesh(k, 2560 if k == "icosphere" else 2400, rng.uniform(40, 120), seed * 10 + i)
+              for i, k in enumerate(kinds)]
+    taken, objs = [], []
+    while len(objs) < n_objects:
+        soa, F = meshes[int(rng.integers(0, len(meshes)))]
+        try:
+            pose = place_pose(rng, soa, F, margin_px=3, taken=taken, tries=400)
+        except RuntimeError:
+            continue
+        objs.append((soa, F, pose))
+    depth, labels, rgb = compose_frame(objs, seed=12000 + seed, with_rgb=True)
+    return depth, labels, rgb
+
+
 def workload_c5(seed: int = 0, particles: int = 4096, iterations: int = 200, level: int = 7):
     """Stress: one noise-displaced level-7 icosphere (250 mm extent) and a
     full 640x480 fitness window (cluster AABB = the frame)."""
