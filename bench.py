@@ -576,20 +576,32 @@ def extra_c4(ctx, slots: int = 64, epoch_iters: int = 4, rates=(10.0, 30.0, 100.
 
 
 def extra_seg(ctx, steps: int = 5):
-    """The segmentation in the default run: frames/s of qpso_segment_planes
-    on a 640x480 frame, host planes to host labels (run_segment's step)."""
+    """The segmentation in the default run: frames/s of qpso_segment_rgbd
+    (GraphCannySeg<hsv>::run, colour image and raw depth on the host to the
+    label map and the kept clusters on the host) on the stress
+    configuration's 640x480 frame with 15 objects, and of the graph stage
+    alone (qpso_segment_planes) on its own synthetic planes."""
     import qpso
+    import scene
 
+    depth, _, bgr = scene.segmentation_frame_c5()
+    ctx.segment_rgbd(bgr, depth)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        out = ctx.segment_rgbd(bgr, depth)
+    dt = time.perf_counter() - t0
     frame = segmentation_frame(seed=11)
     prm = qpso.seg_params()
     ctx.segment_planes(*frame, prm)
-    t0 = time.perf_counter()
+    t1 = time.perf_counter()
     for _ in range(steps):
-        _, n_sets = ctx.segment_planes(*frame, prm)
-    dt = time.perf_counter() - t0
-    return {"workload": "one 640x480 HSV + depth + saliency frame per step, qpso_segment_planes "
-                        "from host planes to host labels", "value": steps / dt, "unit": "frames/s",
-            "ms_per_frame": dt * 1000.0 / steps, "sets": int(n_sets)}
+        ctx.segment_planes(*frame, prm)
+    dt_g = time.perf_counter() - t1
+    return {"workload": "the stress configuration's 640x480 RGB-D frame with 15 objects, qpso_segment_rgbd "
+                        "from host BGR and depth to host labels and kept clusters",
+            "value": steps / dt, "unit": "frames/s", "ms_per_frame": dt * 1000.0 / steps,
+            "sets": int(out["n_sets"]), "clusters_kept": len(out["clusters"]),
+            "graph_stage_only": {"value": steps / dt_g, "unit": "frames/s", "ms_per_frame": dt_g * 1000.0 / steps}}
 
 
 def run_ours(args, ws, rank, local):
@@ -883,7 +895,7 @@ def run_serving(args, ws, rank, local):
     ctx.close()
 
 
-SEG_METRIC = "segmentation frames/sec (GraphCannySeg graph stage, 640x480)"
+SEG_METRIC = "segmentation frames/sec (GraphCannySeg from RGB-D, 640x480)"
 
 
 def segmentation_frame(H: int = 480, W: int = 640, seed: int = 11):
@@ -913,14 +925,15 @@ def segmentation_frame(H: int = 480, W: int = 640, seed: int = 11):
 
 
 def _oracle_segment_rate(frame, budget_s: float):
-    """The oracle's segmentation (smoothing, graph, sort, merge) of the frame
-    on one host core, repeated for about budget_s: frames/s."""
+    """The oracle's segmentation (GraphCannySeg<hsv>::run restated: depth
+    smoothing, inpainting, Canny saliency, graph, merge, cluster filter) of
+    the frame on one host core, repeated for about budget_s: frames/s."""
     from oracle import pyoracle as po
 
-    sp = po.seg_params()
+    depth, bgr = frame
     n, t0 = 0, time.perf_counter()
     while True:
-        po.segment_planes(*frame, sp)
+        po.segment_rgbd(bgr, depth)
         n += 1
         dt = time.perf_counter() - t0
         if dt >= budget_s:
@@ -928,17 +941,22 @@ def _oracle_segment_rate(frame, budget_s: float):
 
 
 def run_segment(args, ws, rank, local):
-    """The segmentation's graph stage (qpso_segment_planes): a step is one
-    640x480 frame from host planes to the host label map, so every step
-    includes the uploads, the GPU graph and sort, the copies back and the
-    host merge passes; it is timed on the host clock around the call.
-    Replicas under torchrun segment their own frames."""
+    """The segmentation (qpso_segment_rgbd): a step is one 640x480 RGB-D
+    frame with 15 objects from host colour image and depth to the host
+    label map and kept clusters, so every step includes the uploads, the
+    GPU stages, the copies back and the host merge passes; it is timed on
+    the host clock around the call.  Replicas under torchrun segment their
+    own frames."""
     import qpso
     import build as pkg_build
+    import scene
 
     d = Dist(ws)
-    frame = segmentation_frame(seed=11 + rank)
-    H, W = frame[0].shape
+    depth, _, bgr = scene.segmentation_frame_c5(seed=rank)
+    frame = (depth, bgr)
+    H, W = depth.shape
+    desc = ("seg: one 640x480 RGB-D frame with 15 objects per step (the stress configuration's "
+            "segmentation), GraphCannySeg<hsv>::run from host BGR and depth to host labels and clusters")
     if args.impl == "reference":
         if rank == 0:
             for _ in range(args.warmup):
@@ -951,23 +969,21 @@ def run_segment(args, ws, rank, local):
                               "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
                               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                              "config": {"workload": "seg: one 640x480 HSV + depth + saliency frame"},
-                              "cpu_baseline": base,
+                              "config": {"workload": desc}, "cpu_baseline": base,
                               "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
                                       "d2h_bytes_per_step": 0}}))
         d.close()
         return
     pkg_build.build()
     ctx = qpso.Context(local)
-    prm = qpso.seg_params()
     for _ in range(args.warmup):
-        labels, n_sets = ctx.segment_planes(*frame, prm)
+        out = ctx.segment_rgbd(bgr, depth)
     sampler = ClockSampler(local)
     d.barrier()
     sampler.start()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        labels, n_sets = ctx.segment_planes(*frame, prm)
+        out = ctx.segment_rgbd(bgr, depth)
     dt = d.max(time.perf_counter() - t0)
     clocks = sampler.stop()
     if rank == 0:
@@ -976,12 +992,13 @@ def run_segment(args, ws, rank, local):
         line = {"metric": SEG_METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dt * 1000.0 / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": "seg: one 640x480 HSV + depth + saliency frame per step, "
-                                       "qpso_segment_planes from host planes to host labels",
-                           "edges": int(E), "sets": int(n_sets), "l2": "inputs uploaded every step"},
-                "edges_per_s": value * E, "gpu_launches": args.steps * 25, "clocks": clocks,
-                "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": int(H * W * 9),
-                        "d2h_bytes_per_step": int(20 * E)}}
+                "config": {"workload": desc, "edges": int(E), "sets": int(out["n_sets"]),
+                           "clusters_kept": len(out["clusters"]), "l2": "inputs uploaded every step"},
+                # per frame: 22 front-stage kernels, 26 graph-stage kernels (4 + 7 sort passes of 3
+                # for a 640x480 frame), 2 for the per-set moments
+                "edges_per_s": value * E, "clocks": clocks, "gpu_launches": args.steps * 50,
+                "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": int(H * W * 5),
+                        "d2h_bytes_per_step": int(20 * E + 4 * H * W)}}
         if not args.no_cpu_baseline:
             v, n = _oracle_segment_rate(frame, 10.0)
             line["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",

@@ -303,6 +303,15 @@ qpso_status qpso_obj_load(const char *path, float *soa_out, uint32_t capacity_fa
 qpso_status qpso_image_u16_load(const char *path, uint16_t *out, uint64_t capacity_px,
                                 uint32_t *width, uint32_t *height);
 
+/* A colour image as 8-bit B, G, R (the channel order cv::imread gives the
+ * reference, main.cu:1238): a PNG (grey, RGB, grey + alpha or RGBA, 8 or
+ * 16 bits, not interlaced; alpha dropped, 16-bit samples keep their high
+ * byte) or a binary PPM (P6, maxval 255), told apart by the PNG signature.
+ * out receives width*height*3 bytes (capacity_px pixels); with out == NULL
+ * only the size is set. */
+qpso_status qpso_image_bgr8_load(const char *path, uint8_t *out, uint64_t capacity_px, uint32_t *width,
+                                 uint32_t *height);
+
 /* ---- serving: continuous batching of solve requests ----
  * No counterpart in the reference (one solve per process).  A scheduler
  * thread admits submitted requests into free slots while the slot count and

@@ -3,10 +3,14 @@
 //
 //   qpso_main path/to/.obj color_image depth_image cluster_idx [options]
 //
-// loads the object model (OBJ text) and the depth image (the ACCV binary
-// format of loadDepth, main.cu:35-64, or a 16-bit greyscale PNG), takes the
-// cluster `cluster_idx` of the frame's label map, solves its pose on the GPU
-// and writes what the reference writes:
+// loads the object model (OBJ text), the colour image (PNG or binary PPM)
+// and the depth image (the ACCV binary format of loadDepth, main.cu:35-64,
+// or a 16-bit greyscale PNG), segments the frame on the GPU as the
+// reference's GraphCannySeg does (qpso_segment_rgbd: depth smoothing,
+// inpainting, Canny saliency, graph segmentation, PostSegmFilter), takes
+// the kept cluster `cluster_idx` in the reference's order
+// (vecSegResult[N], main.cu:1253-1269), solves its pose on the GPU against
+// the cluster's inpainted depth and writes what the reference writes:
 //
 //   results/<color_image>-<cluster_idx>-bestpose.csv  fit,tx,ty,tz,q0,q1,q2,q3
 //                                                     (main.cu:1752-1757)
@@ -14,11 +18,11 @@
 //                                                     image (RenderCPU,
 //                                                     main.h:2012-2043)
 //
-// The clusters come from a label map (--labels FILE: a uint16 image in
-// either format, 0 = no cluster, k+1 = cluster k; default
-// <depth_image>.labels.png) in place of the reference's GraphCannySeg run on
-// the colour image, which is only named here: its file name names the
-// outputs, as in the reference.  Uses only the C ABI of libqpso_gb300.
+// With a label map (--labels FILE: a uint16 image in either format, 0 = no
+// cluster, k+1 = cluster k; or a file <depth_image>.labels.png beside the
+// depth) the clusters come from it instead, the raw depth is solved
+// against, and the colour image only names the outputs.  Uses only the C
+// ABI of libqpso_gb300.
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
@@ -36,7 +40,8 @@ int usage(const char* argv0) {
       "Usage: %s path/to/.obj color_image depth_image cluster_idx\n"
       "       [--labels FILE] [--particles N] [--iterations N] [--seed N] [--stream N]\n"
       "       [--camera fx,fy,cx,cy] [--results DIR] [--device N] [--raster-mode ref|edge]\n"
-      "Without --camera the reference's own projection is used (its ACCV intrinsics in double).\n",
+      "Without --camera the reference's own projection is used (its ACCV intrinsics in double).\n"
+      "Without a label map the frame is segmented from the colour image and the depth.\n",
       argv0);
   return 0;  // the reference returns 0 after its usage line too
 }
@@ -87,7 +92,7 @@ int main(int argc, char** argv) {
 
   std::string labels_path = depth_path + ".labels.png", results = "results";
   unsigned long long particles = 0, iterations = 0, seed = 0, stream = 0, device = 0;
-  bool have_seed = false, have_stream = false;
+  bool have_seed = false, have_stream = false, labels_given = false;
   int raster_mode = 0;
   // the reference's compiled-in ACCV intrinsics (main.h:30-33)
   // default: the reference's own projection (its compiled-in ACCV
@@ -98,7 +103,7 @@ int main(int argc, char** argv) {
     if (i + 1 >= argc) return die("missing value for", a);
     const char* v = argv[++i];
     bool ok = true;
-    if (a == "--labels") labels_path = v;
+    if (a == "--labels") labels_path = v, labels_given = true;
     else if (a == "--results") results = v;
     else if (a == "--particles") ok = parse_u64(v, &particles) && particles > 0;
     else if (a == "--iterations") ok = parse_u64(v, &iterations) && iterations > 0;
@@ -129,23 +134,34 @@ int main(int argc, char** argv) {
   std::vector<uint16_t> depth((size_t)W * H);
   if ((st = qpso_image_u16_load(depth_path.c_str(), depth.data(), depth.size(), &W, &H)) != QPSO_OK)
     return die(depth_path.c_str(), status_name(st));
-  if (!file_exists(labels_path))
-    return die("no label map",
-               labels_path + " (clusters come from a label map: pass --labels FILE, a uint16 image with "
-                             "0 = no cluster and k+1 = cluster k)");
-  uint32_t lw = 0, lh = 0;
-  std::vector<uint16_t> lab16((size_t)W * H);
-  if ((st = qpso_image_u16_load(labels_path.c_str(), lab16.data(), lab16.size(), &lw, &lh)) != QPSO_OK)
-    return die(labels_path.c_str(), status_name(st));
-  if (lw != W || lh != H) return die(labels_path.c_str(), "size differs from the depth image");
-  std::vector<int32_t> labels(lab16.size());
-  for (size_t i = 0; i < lab16.size(); ++i) labels[i] = (int32_t)lab16[i] - 1;
+  const bool use_labels = labels_given || file_exists(labels_path);
+  std::vector<int32_t> labels((size_t)W * H);
   cam.width = (int32_t)W;
   cam.height = (int32_t)H;
-  std::printf("rgb_file: %s depth_file: %s labels: %s (%ux%u)\n", rgb_path.c_str(), depth_path.c_str(),
-              labels_path.c_str(), W, H);
+  if (use_labels) {
+    uint32_t lw = 0, lh = 0;
+    std::vector<uint16_t> lab16((size_t)W * H);
+    if ((st = qpso_image_u16_load(labels_path.c_str(), lab16.data(), lab16.size(), &lw, &lh)) != QPSO_OK)
+      return die(labels_path.c_str(), status_name(st));
+    if (lw != W || lh != H) return die(labels_path.c_str(), "size differs from the depth image");
+    for (size_t i = 0; i < lab16.size(); ++i) labels[i] = (int32_t)lab16[i] - 1;
+    std::printf("rgb_file: %s depth_file: %s labels: %s (%ux%u)\n", rgb_path.c_str(), depth_path.c_str(),
+                labels_path.c_str(), W, H);
+  }
+  std::vector<uint8_t> bgr;
+  if (!use_labels) {
+    // GraphCannySeg<hsv> runs on the colour image and the depth (main.cu:1238-1256)
+    uint32_t cw = 0, chh = 0;
+    if ((st = qpso_image_bgr8_load(rgb_path.c_str(), nullptr, 0, &cw, &chh)) != QPSO_OK)
+      return die(rgb_path.c_str(), status_name(st));
+    if (cw != W || chh != H) return die(rgb_path.c_str(), "size differs from the depth image");
+    bgr.resize(3 * (size_t)W * H);
+    if ((st = qpso_image_bgr8_load(rgb_path.c_str(), bgr.data(), (uint64_t)W * H, &cw, &chh)) != QPSO_OK)
+      return die(rgb_path.c_str(), status_name(st));
+    std::printf("rgb_file: %s depth_file: %s (%ux%u)\n", rgb_path.c_str(), depth_path.c_str(), W, H);
+  }
 
-  // ---- solve (GPU) ----
+  // ---- segmentation and solve (GPU) ----
   qpso_context* ctx = nullptr;
   if ((st = qpso_create((int)device, &ctx)) != QPSO_OK) return die("qpso_create", status_name(st));
   auto fail = [&](const char* what) {
@@ -153,38 +169,77 @@ int main(int argc, char** argv) {
     qpso_destroy(ctx);
     return die(what, msg);
   };
-  uint32_t mesh_id = 0, frame_id = 0, ncl = 0;
+  uint32_t mesh_id = 0, frame_id = 0;
   if (qpso_mesh_upload(ctx, soa.data(), F, &mesh_id) != QPSO_OK) return fail("mesh upload");
-  if (qpso_frame_upload(ctx, depth.data(), labels.data(), &cam, &frame_id) != QPSO_OK)
-    return fail("frame upload");
-  if (qpso_frame_clusters(ctx, frame_id, nullptr, 0, &ncl) != QPSO_OK) return fail("clusters");
-  std::vector<qpso_cluster> cl(ncl);
-  if (ncl && qpso_frame_clusters(ctx, frame_id, cl.data(), ncl, &ncl) != QPSO_OK) return fail("clusters");
-  const qpso_cluster* c = nullptr;
-  for (const auto& x : cl)
-    if (x.label == idx) c = &x;
-  if (!c) {
-    qpso_destroy(ctx);
-    return die("cluster_idx", std::to_string(idx) + " is not in the label map (" + std::to_string(ncl) +
-                                  " clusters)");
+  int32_t label = idx;
+  int32_t box[4];
+  uint32_t num_points = 0;
+  float centroid[3];
+  if (use_labels) {
+    uint32_t ncl = 0;
+    if (qpso_frame_upload(ctx, depth.data(), labels.data(), &cam, &frame_id) != QPSO_OK)
+      return fail("frame upload");
+    if (qpso_frame_clusters(ctx, frame_id, nullptr, 0, &ncl) != QPSO_OK) return fail("clusters");
+    std::vector<qpso_cluster> cl(ncl);
+    if (ncl && qpso_frame_clusters(ctx, frame_id, cl.data(), ncl, &ncl) != QPSO_OK) return fail("clusters");
+    const qpso_cluster* c = nullptr;
+    for (const auto& x : cl)
+      if (x.label == idx) c = &x;
+    if (!c) {
+      qpso_destroy(ctx);
+      return die("cluster_idx", std::to_string(idx) + " is not in the label map (" + std::to_string(ncl) +
+                                    " clusters)");
+    }
+    box[0] = c->min_x, box[1] = c->max_x, box[2] = c->min_y, box[3] = c->max_y;
+    // the reference's cluster size is its collectSets list length, which
+    // repeats one pixel (GraphCannySeg.cpp:305-352): pixels + 1 reach the
+    // fitness as num_point_SegmentedCluster (main.cu:1322)
+    num_points = c->num_points + 1;
+    std::memcpy(centroid, c->centroid_mm, sizeof(centroid));
+  } else {
+    qpso_seg_params prm;
+    qpso_seg_params_init(&prm);
+    qpso_seg_front_params fp;
+    qpso_seg_front_params_init(&fp);
+    std::vector<uint16_t> inpainted((size_t)W * H);
+    qpso_seg_frame_out planes;
+    std::memset(&planes, 0, sizeof(planes));
+    planes.inpainted = inpainted.data();
+    const uint32_t cap = W * H / 64 + 16;
+    std::vector<qpso_seg_cluster> cl(cap);
+    uint32_t n_sets = 0, n_cl = 0;
+    if (qpso_segment_rgbd(ctx, bgr.data(), depth.data(), W, H, &prm, &fp, labels.data(), &n_sets, cl.data(), cap,
+                          &n_cl, &planes) != QPSO_OK)
+      return fail("segmentation");
+    std::printf("disjoint sets %u\nclusters kept %u\n", n_sets, n_cl);
+    if ((uint32_t)idx >= n_cl || idx >= (int32_t)cap) {
+      qpso_destroy(ctx);
+      return die("cluster_idx", std::to_string(idx) + " is beyond the " + std::to_string(n_cl) +
+                                    " clusters the segmentation kept");
+    }
+    const qpso_seg_cluster& c = cl[idx];
+    label = c.label;
+    box[0] = c.min_x, box[1] = c.max_x, box[2] = c.min_y, box[3] = c.max_y;
+    num_points = c.num_points;  // already the list length (pixels + 1)
+    std::memcpy(centroid, c.centroid_mm, sizeof(centroid));
+    // the observed depth is the cluster-masked inpainted depth (SegResults.clusterDepth,
+    // GraphCannySeg.h:1808-1809; main.cu:1548-1557)
+    if (qpso_frame_upload(ctx, inpainted.data(), labels.data(), &cam, &frame_id) != QPSO_OK)
+      return fail("frame upload");
   }
-  std::printf("centroid IDX_cluster: %d [%g, %g, %g]\n------\n", idx, c->centroid_mm[0], c->centroid_mm[1],
-              c->centroid_mm[2]);
+  std::printf("centroid IDX_cluster: %d [%g, %g, %g]\n------\n", idx, centroid[0], centroid[1], centroid[2]);
 
   qpso_solve_desc d;
   qpso_solve_desc_init(&d);
   d.mesh_id = mesh_id;
   d.frame_id = frame_id;
-  d.cluster_label = idx;
-  d.cl_min_x = c->min_x;
-  d.cl_max_x = c->max_x;
-  d.cl_min_y = c->min_y;
-  d.cl_max_y = c->max_y;
-  // the reference's cluster size is its collectSets list length, which
-  // repeats one pixel (GraphCannySeg.cpp:305-352): pixels + 1 reach the
-  // fitness as num_point_SegmentedCluster (main.cu:1322)
-  d.num_points = c->num_points + 1;
-  qpso_box_from_centroid(c->centroid_mm, 0.3f, 0.3f, d.t_lo, d.t_hi);  // main.cu:1285-1323
+  d.cluster_label = label;
+  d.cl_min_x = box[0];
+  d.cl_max_x = box[1];
+  d.cl_min_y = box[2];
+  d.cl_max_y = box[3];
+  d.num_points = num_points;
+  qpso_box_from_centroid(centroid, 0.3f, 0.3f, d.t_lo, d.t_hi);  // main.cu:1285-1323
   if (particles) d.num_particles = (uint32_t)particles;
   if (iterations) d.iterations = (uint32_t)iterations;
   if (have_seed) d.seed = seed;

@@ -15,6 +15,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cctype>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -292,9 +293,11 @@ uint32_t crc32_png(const unsigned char* p, size_t n) {
 
 const unsigned char kPngSig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
 
-// Greyscale PNG (colour type 0, bit depth 8 or 16, not interlaced) to uint16.
-qpso_status decode_png_gray(const std::vector<unsigned char>& f, std::vector<uint16_t>& px, uint32_t* w,
-                            uint32_t* h) {
+// The unfiltered scanlines of a PNG (not interlaced; colour types 0 grey,
+// 2 RGB, 4 grey + alpha, 6 RGBA; bit depth 8 or 16): rows of W * channels *
+// depth / 8 bytes, big-endian samples.
+qpso_status png_scanlines(const std::vector<unsigned char>& f, uint32_t* w, uint32_t* h, int* depth_out,
+                          int* channels_out, std::vector<unsigned char>& pix) {
   if (f.size() < 8 || std::memcmp(f.data(), kPngSig, 8) != 0) return QPSO_ERR_ARG;
   size_t at = 8;
   uint32_t W = 0, H = 0;
@@ -324,13 +327,14 @@ qpso_status decode_png_gray(const std::vector<unsigned char>& f, std::vector<uin
     at += (size_t)len + 12;
   }
   if (!seen_end || W == 0 || H == 0 || W > 16384 || H > 16384) return QPSO_ERR_ARG;
-  if (ctype != 0 || (depth != 8 && depth != 16) || interlace != 0) return QPSO_ERR_ARG;
-  const size_t bpp = depth / 8, row = (size_t)W * bpp;
+  const int channels = ctype == 0 ? 1 : ctype == 2 ? 3 : ctype == 4 ? 2 : ctype == 6 ? 4 : 0;
+  if (channels == 0 || (depth != 8 && depth != 16) || interlace != 0) return QPSO_ERR_ARG;
+  const size_t bpp = (size_t)channels * depth / 8, row = (size_t)W * bpp;
   std::vector<unsigned char> raw;
   const size_t want = (row + 1) * H;
   if (!zlib_inflate(idat.data(), idat.size(), raw, want) || raw.size() != want) return QPSO_ERR_ARG;
   std::vector<unsigned char> prev(row, 0), cur(row);
-  px.resize((size_t)W * H);
+  pix.resize(row * H);
   for (uint32_t y = 0; y < H; ++y) {
     const unsigned char* s = &raw[(size_t)y * (row + 1)];
     const int filter = s[0];
@@ -352,12 +356,99 @@ qpso_status decode_png_gray(const std::vector<unsigned char>& f, std::vector<uin
       }
       cur[i] = (unsigned char)(s[i] + pred);
     }
-    for (uint32_t x = 0; x < W; ++x)
-      px[(size_t)y * W + x] = depth == 16 ? (uint16_t)((cur[2 * x] << 8) | cur[2 * x + 1]) : cur[x];
+    std::memcpy(&pix[(size_t)y * row], cur.data(), row);
     prev.swap(cur);
   }
   *w = W;
   *h = H;
+  *depth_out = depth;
+  *channels_out = channels;
+  return QPSO_OK;
+}
+
+// Greyscale PNG (colour type 0, bit depth 8 or 16, not interlaced) to uint16.
+qpso_status decode_png_gray(const std::vector<unsigned char>& f, std::vector<uint16_t>& px, uint32_t* w,
+                            uint32_t* h) {
+  std::vector<unsigned char> pix;
+  int depth = 0, channels = 0;
+  uint32_t W = 0, H = 0;
+  const qpso_status st = png_scanlines(f, &W, &H, &depth, &channels, pix);
+  if (st != QPSO_OK) return st;
+  if (channels != 1) return QPSO_ERR_ARG;
+  px.resize((size_t)W * H);
+  for (size_t i = 0; i < px.size(); ++i)
+    px[i] = depth == 16 ? (uint16_t)((pix[2 * i] << 8) | pix[2 * i + 1]) : pix[i];
+  *w = W;
+  *h = H;
+  return QPSO_OK;
+}
+
+// Colour PNG to 8-bit B, G, R (OpenCV's channel order, as cv::imread gives
+// the reference): RGB and RGBA drop alpha, grey is replicated, 16-bit
+// samples keep their high byte.
+qpso_status decode_png_bgr(const std::vector<unsigned char>& f, std::vector<unsigned char>& bgr, uint32_t* w,
+                           uint32_t* h) {
+  std::vector<unsigned char> pix;
+  int depth = 0, channels = 0;
+  uint32_t W = 0, H = 0;
+  const qpso_status st = png_scanlines(f, &W, &H, &depth, &channels, pix);
+  if (st != QPSO_OK) return st;
+  const size_t n = (size_t)W * H, step = (size_t)channels * (depth / 8), sb = depth / 8;
+  bgr.resize(3 * n);
+  for (size_t i = 0; i < n; ++i) {
+    const unsigned char* p = &pix[i * step];
+    unsigned char r, g, b;
+    if (channels >= 3) {
+      r = p[0];
+      g = p[sb];
+      b = p[2 * sb];
+    } else {
+      r = g = b = p[0];
+    }
+    bgr[3 * i] = b;
+    bgr[3 * i + 1] = g;
+    bgr[3 * i + 2] = r;
+  }
+  *w = W;
+  *h = H;
+  return QPSO_OK;
+}
+
+// Binary PPM (P6, maxval 255): RGB samples to B, G, R.
+qpso_status decode_ppm_bgr(const std::vector<unsigned char>& f, std::vector<unsigned char>& bgr, uint32_t* w,
+                           uint32_t* h) {
+  if (f.size() < 2 || f[0] != 'P' || f[1] != '6') return QPSO_ERR_ARG;
+  size_t at = 2;
+  long vals[3];
+  for (int k = 0; k < 3; ++k) {
+    for (;;) {  // whitespace and comments
+      while (at < f.size() && std::isspace(f[at])) ++at;
+      if (at < f.size() && f[at] == '#') {
+        while (at < f.size() && f[at] != '\n') ++at;
+        continue;
+      }
+      break;
+    }
+    long v = 0;
+    int digits = 0;
+    while (at < f.size() && f[at] >= '0' && f[at] <= '9' && digits < 9) v = v * 10 + (f[at++] - '0'), ++digits;
+    if (digits == 0) return QPSO_ERR_ARG;
+    vals[k] = v;
+  }
+  if (at >= f.size() || !std::isspace(f[at])) return QPSO_ERR_ARG;
+  ++at;
+  const long W = vals[0], H = vals[1];
+  if (W <= 0 || H <= 0 || W > 16384 || H > 16384 || vals[2] != 255) return QPSO_ERR_ARG;
+  const size_t n = (size_t)W * H;
+  if (f.size() - at < 3 * n) return QPSO_ERR_ARG;
+  bgr.resize(3 * n);
+  for (size_t i = 0; i < n; ++i) {
+    bgr[3 * i] = f[at + 3 * i + 2];
+    bgr[3 * i + 1] = f[at + 3 * i + 1];
+    bgr[3 * i + 2] = f[at + 3 * i];
+  }
+  *w = (uint32_t)W;
+  *h = (uint32_t)H;
   return QPSO_OK;
 }
 
@@ -415,6 +506,24 @@ qpso_status qpso_image_u16_load(const char* path, uint16_t* out, uint64_t capaci
   if (!out) return QPSO_OK;
   if (px.size() > capacity_px) return QPSO_ERR_ARG;
   std::memcpy(out, px.data(), px.size() * 2);
+  return QPSO_OK;
+}
+
+qpso_status qpso_image_bgr8_load(const char* path, uint8_t* out, uint64_t capacity_px, uint32_t* width,
+                                 uint32_t* height) {
+  if (!path || !width || !height) return QPSO_ERR_ARG;
+  std::vector<unsigned char> f;
+  if (!read_file(path, f)) return QPSO_ERR_NOT_FOUND;
+  std::vector<unsigned char> bgr;
+  uint32_t w = 0, h = 0;
+  const bool png = f.size() >= 8 && std::memcmp(f.data(), kPngSig, 8) == 0;
+  const qpso_status st = png ? decode_png_bgr(f, bgr, &w, &h) : decode_ppm_bgr(f, bgr, &w, &h);
+  if (st != QPSO_OK) return st;
+  *width = w;
+  *height = h;
+  if (!out) return QPSO_OK;
+  if ((uint64_t)w * h > capacity_px) return QPSO_ERR_ARG;
+  std::memcpy(out, bgr.data(), bgr.size());
   return QPSO_OK;
 }
 

@@ -35,7 +35,7 @@ EXPORTS = [
     "qpso_server_stats_get", "qpso_server_stop", "qpso_render_depth_f32", "qpso_frame_clusters",
     "qpso_obj_load", "qpso_image_u16_load", "qpso_seg_params_init", "qpso_segment_num_edges",
     "qpso_segment_edge_ends", "qpso_segment_gauss_mask", "qpso_segment_edges", "qpso_segment_planes",
-    "qpso_seg_front_params_init", "qpso_segment_rgbd", "qpso_segment_clusters",
+    "qpso_seg_front_params_init", "qpso_segment_rgbd", "qpso_segment_clusters", "qpso_image_bgr8_load",
 ]
 
 
@@ -590,6 +590,17 @@ def image_u16_load(path: str) -> np.ndarray:
     _status(L.qpso_image_u16_load(path.encode(), None, 0, C.byref(w), C.byref(h)), path)
     out = np.empty((h.value, w.value), np.uint16)
     _status(L.qpso_image_u16_load(path.encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h)), path)
+    return out
+
+
+def image_bgr8_load(path: str) -> np.ndarray:
+    """Colour PNG or binary PPM -> uint8 (height, width, 3), B G R.  Host only."""
+    L = load_library()
+    w, h = C.c_uint32(), C.c_uint32()
+    _status(L.qpso_image_bgr8_load(path.encode(), None, 0, C.byref(w), C.byref(h)), path)
+    out = np.empty((h.value, w.value, 3), np.uint8)
+    _status(L.qpso_image_bgr8_load(path.encode(), out.ctypes.data, h.value * w.value, C.byref(w), C.byref(h)),
+            path)
     return out
 
 

@@ -151,3 +151,77 @@ def test_cli_unknown_cluster(files):
     d, w, s, obj = files
     r = run_cli(d, obj, "depth.bin", 999)
     assert r.returncode == 1 and "not in the label map" in r.stderr
+
+
+# ---- from the colour image and the depth alone (no label map) ----
+
+@pytest.fixture(scope="module")
+def rgbd_files(tmp_path_factory, gpu_ctx):
+    from tests.test_ingest import write_png_color, write_ppm
+
+    d = tmp_path_factory.mktemp("cli_rgbd")
+    w = scene.workload_c2(frames=1, particles=32, iterations=6)
+    depth, gt, bgr = w["frames"][0]
+    write_png_color(str(d / "img_0007.png"), bgr[..., ::-1])  # RGB order in the file
+    write_ppm(str(d / "img_0007.ppm"), bgr[..., ::-1])
+    write_png_gray(str(d / "depth.png"), depth, 16, 6, (0, 1, 2, 3, 4))
+    # the kept cluster that covers solve 2's object, and that object's mesh
+    s = w["solves"][2]
+    seg = gpu_ctx.segment_rgbd(bgr, depth)
+    m = gt == s["cluster"]["label"]
+    ious = [((seg["labels"] == c.label) & m).sum() / ((seg["labels"] == c.label) | m).sum() for c in seg["clusters"]]
+    n = int(np.argmax(ious))
+    assert ious[n] > 0.5
+    soa, F = w["meshes"][s["mesh"]]
+    obj = str(d / "model.obj")
+    write_obj(obj, soa, F)
+    return d, bgr, depth, obj, n
+
+
+@pytest.mark.parametrize("colour", ["img_0007.png", "img_0007.ppm"])
+def test_cli_segments_the_frame_itself(gpu_ctx, rgbd_files, colour):
+    """qpso_main obj rgb depth N with no label map: the frame is segmented on
+    the GPU (qpso_segment_rgbd), cluster N of the kept clusters is solved
+    against its inpainted depth, and the pose file equals the library's
+    solve of that cluster and the oracle's solve of the same inputs."""
+    d, bgr, depth, obj, n = rgbd_files
+    res_dir = d / ("res_" + colour.split(".")[1])
+    cmd = [CLI, obj, str(d / colour), str(d / "depth.png"), str(n), "--particles", "32", "--iterations", "6",
+           "--seed", "7", "--results", str(res_dir)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "clusters kept" in r.stdout
+
+    seg = gpu_ctx.segment_rgbd(bgr, depth, planes=True)
+    c = seg["clusters"][n]
+    soa, F = qpso.obj_load(obj)
+    cam = qpso.Camera(0, 0, 0, 0, 640, 480, qpso.PROJ_REF_ACCV)
+    mid = gpu_ctx.mesh_upload(soa, F)
+    fid = gpu_ctx.frame_upload(seg["inpainted"], cam, labels=seg["labels"])
+    lo, hi = qpso.box_from_centroid(list(c.centroid_mm))
+    desc = qpso.solve_desc(mesh_id=mid, frame_id=fid, cluster_label=c.label, cl_min_x=c.min_x, cl_max_x=c.max_x,
+                           cl_min_y=c.min_y, cl_max_y=c.max_y, num_points=c.num_points, t_lo=lo, t_hi=hi,
+                           num_particles=32, iterations=6, seed=7, stream=0)
+    res = gpu_ctx.solve(desc)
+    stem = res_dir / ("%s-%d" % (colour, n))
+    assert open(str(stem) + "-bestpose.csv").read() == "%f,%f,%f,%f,%f,%f,%f,%f" % (res.fit, *res.pose)
+    # the oracle on the same masked inpainted depth
+    prm = po.default_params()
+    prm.t_lo[:] = lo
+    prm.t_hi[:] = hi
+    prm.cl_min_x, prm.cl_max_x, prm.cl_min_y, prm.cl_max_y = c.min_x, c.max_x, c.min_y, c.max_y
+    prm.num_points = c.num_points
+    prm.num_particles, prm.iterations, prm.seed, prm.stream = 32, 6, 7, 0
+    obs = np.where(seg["labels"] == c.label, seg["inpainted"], 0).astype(np.uint16)
+    want = po.solve(soa, F, obs, po.camera_ref_accv(), prm)
+    assert res.fit == want["fit"]
+    np.testing.assert_array_equal(np.array(res.pose[:], np.float32), want["pose"])
+    gpu_ctx.frame_release(fid)
+    gpu_ctx.mesh_release(mid)
+
+
+def test_cli_cluster_beyond_the_kept_ones(rgbd_files):
+    d, _, _, obj, _ = rgbd_files
+    r = subprocess.run([CLI, obj, str(d / "img_0007.png"), str(d / "depth.png"), "999", "--particles", "8",
+                        "--iterations", "1"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1 and "beyond" in r.stderr

@@ -83,6 +83,44 @@ def write_png_gray(path, img, bits=16, level=6, filters=(0,), corrupt_crc=False,
     return comp
 
 
+def write_png_color(path, img, filters=(0, 1, 2, 3, 4), level=6, bits=8):
+    """RGB (h, w, 3), RGBA (h, w, 4) or grey + alpha (h, w, 2) PNG."""
+    img = np.asarray(img)
+    h, w, ch = img.shape
+    ctype = {2: 4, 3: 2, 4: 6}[ch]
+    bpp = ch * bits // 8
+    raw = bytearray()
+    prev = bytes(w * bpp)
+    for y in range(h):
+        row = img[y].astype(">u2").tobytes() if bits == 16 else img[y].astype(np.uint8).tobytes()
+        ft = filters[y % len(filters)]
+        out = bytearray()
+        for i in range(len(row)):
+            a = row[i - bpp] if i >= bpp else 0
+            b = prev[i]
+            c = prev[i - bpp] if i >= bpp else 0
+            pred = [0, a, b, (a + b) >> 1, _paeth(a, b, c)][ft]
+            out.append((row[i] - pred) & 0xFF)
+        raw += bytes([ft]) + out
+        prev = row
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xFFFFFFFF)
+
+    ihdr = struct.pack(">IIBBBBB", w, h, bits, ctype, 0, 0, 0)
+    data = (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", ihdr) + chunk(b"IDAT", zlib.compress(bytes(raw), level)) +
+            chunk(b"IEND", b""))
+    with open(path, "wb") as fp:
+        fp.write(data)
+
+
+def write_ppm(path, rgb, comment=True):
+    h, w, _ = rgb.shape
+    head = b"P6\n" + (b"# made by the tests\n" if comment else b"") + b"%d %d\n255\n" % (w, h)
+    with open(path, "wb") as fp:
+        fp.write(head + np.ascontiguousarray(rgb, np.uint8).tobytes())
+
+
 def _block_types(comp):
     """BTYPE of the first deflate block of a zlib stream."""
     return (comp[2] >> 1) & 3
@@ -228,9 +266,50 @@ def test_cli_usage_and_input_errors(tmp_path):
     write_obj(obj, soa, F)
     dep = str(tmp_path / "d.bin")
     write_accv(dep, _depth(4))
-    r = subprocess.run([CLI, obj, "rgb.png", dep, "0"], capture_output=True, text=True)
-    assert r.returncode == 1 and "no label map" in r.stderr
+    # no label map: the frame is segmented from the colour image, which must exist
+    r = subprocess.run([CLI, obj, str(tmp_path / "rgb.png"), dep, "0"], capture_output=True, text=True)
+    assert r.returncode == 1 and "rgb.png" in r.stderr and "not found" in r.stderr
+    rgb = str(tmp_path / "small.ppm")
+    write_ppm(rgb, np.zeros((10, 12, 3), np.uint8))
+    r = subprocess.run([CLI, obj, rgb, dep, "0"], capture_output=True, text=True)
+    assert r.returncode == 1 and "size differs" in r.stderr
     r = subprocess.run([CLI, obj, "rgb.png", dep, "x"], capture_output=True, text=True)
     assert r.returncode == 1 and "cluster_idx" in r.stderr
     r = subprocess.run([CLI, obj, "rgb.png", dep, "0", "--particles"], capture_output=True, text=True)
     assert r.returncode == 1 and "missing value" in r.stderr
+
+
+# ---- colour images ----
+def test_colour_png_and_ppm_to_bgr(tmp_path):
+    rng = np.random.default_rng(4)
+    rgb = rng.integers(0, 256, (23, 31, 3)).astype(np.uint8)
+    bgr = rgb[..., ::-1]
+    p = str(tmp_path / "c.png")
+    write_png_color(p, rgb)
+    np.testing.assert_array_equal(qpso.image_bgr8_load(p), bgr)
+    alpha = rng.integers(0, 256, (23, 31, 1)).astype(np.uint8)
+    write_png_color(p, np.concatenate([rgb, alpha], 2), filters=(4, 3))
+    np.testing.assert_array_equal(qpso.image_bgr8_load(p), bgr)
+    write_png_color(p, rgb.astype(np.uint16) * 256 + 3, bits=16)
+    np.testing.assert_array_equal(qpso.image_bgr8_load(p), bgr)
+    grey = rgb[..., 0]
+    write_png_color(p, np.stack([grey, alpha[..., 0]], 2))
+    np.testing.assert_array_equal(qpso.image_bgr8_load(p), np.repeat(grey[..., None], 3, 2))
+    write_png_gray(p, grey, bits=8)
+    np.testing.assert_array_equal(qpso.image_bgr8_load(p), np.repeat(grey[..., None], 3, 2))
+    q = str(tmp_path / "c.ppm")
+    write_ppm(q, rgb)
+    np.testing.assert_array_equal(qpso.image_bgr8_load(q), bgr)
+    write_ppm(q, rgb, comment=False)
+    np.testing.assert_array_equal(qpso.image_bgr8_load(q), bgr)
+
+
+@pytest.mark.parametrize("data", [b"P6\n4 4\n65535\n" + bytes(96), b"P6\n4 4\n255\n" + bytes(10), b"P5\n1 1\n255\n\x00",
+                                  b"P6\n-1 4\n255\n"])
+def test_bad_colour_images_are_refused(tmp_path, data):
+    p = str(tmp_path / "bad.ppm")
+    with open(p, "wb") as fp:
+        fp.write(data)
+    with pytest.raises(qpso.QpsoError) as e:
+        qpso.image_bgr8_load(p)
+    assert e.value.status == qpso.ERR_ARG
