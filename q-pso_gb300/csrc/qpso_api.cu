@@ -101,6 +101,10 @@ struct qpso_context {
   qpso_profile prof{};
   cudaEvent_t timers[64] = {};
   Buf scrub;
+  // segmentation: pinned landing buffer of the sorted edges and the events
+  // that mark its chunks
+  Buf segpin;
+  cudaEvent_t seg_ev[8] = {};
   std::mutex mu;
 };
 
@@ -147,6 +151,25 @@ qpso_status ensure_pin(qpso_context* ctx, size_t bytes) {
   const size_t cap = align_up(bytes + bytes / 4, 1 << 16);
   QPSO_CUDA(ctx, cudaMallocHost(&ctx->pin.p, cap));
   ctx->pin.cap = cap;
+  return QPSO_OK;
+}
+
+constexpr int kSegChunks = 8;
+
+// pinned buffer and chunk events of the streamed segmentation merge
+qpso_status ensure_segpin(qpso_context* ctx, size_t bytes) {
+  for (int i = 0; i < kSegChunks; ++i)
+    if (!ctx->seg_ev[i]) QPSO_CUDA(ctx, cudaEventCreateWithFlags(&ctx->seg_ev[i], cudaEventDisableTiming));
+  if (bytes <= ctx->segpin.cap) return QPSO_OK;
+  if (ctx->segpin.p) {
+    QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFreeHost(ctx->segpin.p);
+    ctx->segpin.p = nullptr;
+    ctx->segpin.cap = 0;
+  }
+  const size_t cap = align_up(bytes, 1 << 16);
+  QPSO_CUDA(ctx, cudaMallocHost(&ctx->segpin.p, cap));
+  ctx->segpin.cap = cap;
   return QPSO_OK;
 }
 
@@ -463,6 +486,9 @@ void qpso_destroy(qpso_context* ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->ws.p) cudaFree(ctx->ws.p);
   if (ctx->pin.p) cudaFreeHost(ctx->pin.p);
+  if (ctx->segpin.p) cudaFreeHost(ctx->segpin.p);
+  for (cudaEvent_t e : ctx->seg_ev)
+    if (e) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -1206,6 +1232,18 @@ qpso_status qpso_segment_planes(qpso_context* ctx, const uint8_t* h, const uint8
   qpso_status st;
   if ((st = ensure_ws(ctx, seg_workspace_bytes(W, H))) != QPSO_OK) return st;
   QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (!edge_weights) {
+    if ((st = ensure_segpin(ctx, seg_merge_pinned_bytes(W, H))) != QPSO_OK) return st;
+    const uint8_t* hsv[3] = {h, s, v};
+    uint32_t err = 0;
+    QPSO_CUDA(ctx, seg_graph_merge(hsv, depth_mm, saliency, W, H, mask, len, prm->kdv, prm->kdc, prm->kx, prm->ks,
+                                   ctx->ws.p, ctx->num_sms, ctx->stream, ctx->segpin.p, ctx->seg_ev, kSegChunks,
+                                   prm->k, prm->min_size, labels, n_clusters, &err));
+    if (err & 5u) return fail(ctx, QPSO_ERR_INTERNAL, "segmentation graph: index out of range");
+    if (err & 2u)
+      return fail(ctx, QPSO_ERR_ARG, "segmentation graph: NaN edge weight (depth range zero, or NaN saliency)");
+    return QPSO_OK;
+  }
   std::vector<uint32_t> order(E);
   std::vector<int32_t> ea(E), eb(E);
   std::vector<float> w(E);
@@ -1364,17 +1402,13 @@ qpso_status qpso_segment_rgbd(qpso_context* ctx, const uint8_t* bgr, const uint1
     if (planes->saliency)
       QPSO_CUDA(ctx, cudaMemcpyAsync(planes->saliency, d_sal, 4 * n, cudaMemcpyDeviceToHost, ctx->stream));
   }
-  std::vector<uint32_t> order(E);
-  std::vector<int32_t> ea(E), eb(E);
-  std::vector<float> w(E);
-  uint32_t err = 0;
-  QPSO_CUDA(ctx, seg_graph_sorted(nullptr, nullptr, nullptr, W, H, mask, len, prm->kdv, prm->kdc, prm->kx, prm->ks,
-                                  base, ctx->num_sms, ctx->stream, order.data(), ea.data(), eb.data(), w.data(),
-                                  &err));
+  if ((st = ensure_segpin(ctx, seg_merge_pinned_bytes(W, H))) != QPSO_OK) return st;
+  uint32_t err = 0, ns = 0;
+  QPSO_CUDA(ctx, seg_graph_merge(nullptr, nullptr, nullptr, W, H, mask, len, prm->kdv, prm->kdc, prm->kx, prm->ks,
+                                 base, ctx->num_sms, ctx->stream, ctx->segpin.p, ctx->seg_ev, kSegChunks, prm->k,
+                                 prm->min_size, labels, &ns, &err));
   if (err & 5u) return fail(ctx, QPSO_ERR_INTERNAL, "segmentation graph: index out of range");
   if (err & 2u) return fail(ctx, QPSO_ERR_ARG, "segmentation graph: NaN edge weight (flat inpainted depth?)");
-  const uint32_t ns = seg_merge((uint32_t)n, E, order.data(), ea.data(), eb.data(), w.data(), prm->k,
-                                prm->min_size, labels);
   *n_sets = ns;
   if ((size_t)ns * sizeof(SetMoments) > mom_bytes)
     return fail(ctx, QPSO_ERR_INTERNAL, "segmentation: more sets than the small-component merge allows");

@@ -17,6 +17,7 @@
 // in and one label map out.
 //
 // This unit is compiled with -ffp-contract=off for its host code too.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -313,53 +314,15 @@ __device__ __forceinline__ bool tless(float ta, int32_t ia, float tb, int32_t ib
   return ta < tb || (ta == tb && ia < ib);
 }
 
-__device__ void tswap(TeleaMem& m, int32_t i, int32_t j) {
-  const float t = m.ht[i];
-  const int32_t k = m.hi[i];
-  m.ht[i] = m.ht[j];
-  m.hi[i] = m.hi[j];
-  m.ht[j] = t;
-  m.hi[j] = k;
-  m.pos[m.hi[i]] = i;
-  m.pos[m.hi[j]] = j;
-}
-
-__device__ void tup(TeleaMem& m, int32_t i) {
-  while (i > 0) {
-    const int32_t p = (i - 1) / 2;
-    if (!tless(m.ht[i], m.hi[i], m.ht[p], m.hi[p])) break;
-    tswap(m, i, p);
-    i = p;
-  }
-}
-
-__device__ void tdown(TeleaMem& m, int32_t i, int32_t n) {
-  for (;;) {
-    const int32_t l = 2 * i + 1, r = l + 1;
-    int32_t s = i;
-    if (l < n && tless(m.ht[l], m.hi[l], m.ht[s], m.hi[s])) s = l;
-    if (r < n && tless(m.ht[r], m.hi[r], m.ht[s], m.hi[s])) s = r;
-    if (s == i) break;
-    tswap(m, i, s);
-    i = s;
-  }
-}
-
-__device__ void tset(TeleaMem& m, int32_t idx, float t, int32_t& n) {
-  int32_t i = m.pos[idx];
-  if (i < 0) {
-    i = n++;
-    m.hi[i] = idx;
-    m.ht[i] = t;
-    m.pos[idx] = i;
-    tup(m, i);
-  } else {
-    const float ot = m.ht[i];
-    m.ht[i] = t;
-    if (tless(t, idx, ot, idx))
-      tup(m, i);
-    else
-      tdown(m, i, n);
+// warp-wide minimum by (T, pixel index); lane 0 ends with it
+__device__ __forceinline__ void warp_argmin(float& t, int32_t& i) {
+  for (int s = 16; s > 0; s >>= 1) {
+    const float ot = __shfl_down_sync(0xffffffffu, t, s);
+    const int32_t oi = __shfl_down_sync(0xffffffffu, i, s);
+    if (tless(ot, oi, t, i)) {
+      t = ot;
+      i = oi;
+    }
   }
 }
 
@@ -406,8 +369,10 @@ __device__ void telea_terms(const TeleaMem& m, int32_t w, int32_t h, int32_t x, 
     const float gix = grad1(ixm, ixm ? (float)m.img[k - 1] : 0.0f, ixp, ixp ? (float)m.img[k + 1] : 0.0f, a0);
     const float giy = grad1(iym, iym ? (float)m.img[k - w] : 0.0f, iyp, iyp ? (float)m.img[k + w] : 0.0f, a0);
     const float val = __fadd_rn(a0, __fadd_rn(__fmul_rn(gix, (float)rx), __fmul_rn(giy, (float)ry)));
-    den += __double2ll_rn(__dmul_rn((double)wt, 4294967296.0));
-    num += __double2ll_rn(__dmul_rn((double)__fmul_rn(wt, val), 4294967296.0));
+    // x * 2^32 is exact in float as in double, so these equal
+    // llrint((double)x * 2^32) without the (slow) double pipe
+    den += __float2ll_rn(__fmul_rn(wt, 4294967296.0f));
+    num += __float2ll_rn(__fmul_rn(__fmul_rn(wt, val), 4294967296.0f));
   }
 }
 
@@ -441,7 +406,7 @@ __global__ void __launch_bounds__(512) telea_kernel(uint8_t* __restrict__ img_io
                                                      unsigned char* __restrict__ gmem, int use_smem) {
   extern __shared__ __align__(16) unsigned char tsm[];
   __shared__ long long red[66];
-  __shared__ int32_t s_q, s_done;
+  __shared__ int32_t s_q;
   __shared__ float s_gtx, s_gty;
   if (misc[3] == misc[2]) return;  // flat depth: nothing is filled
   const size_t n = (size_t)w * h;
@@ -477,94 +442,159 @@ __global__ void __launch_bounds__(512) telea_kernel(uint8_t* __restrict__ img_io
     m.pos[i] = -1;
   }
   __syncthreads();
+  // The initial band: known pixels with an unknown 4-neighbour, all at T = 0.
+  // Listed in pixel order they form a valid queue (equal times, increasing
+  // index), so each chunk of pixels is counted, then written at its offset.
+  __shared__ int32_t s_cnt[512 + 1];
   int32_t hn = 0;  // queue length (thread 0)
-  int32_t cur = -1, nb = 4;  // popped pixel and its next neighbour (thread 0)
-  if (threadIdx.x == 0) {
-    for (int32_t y = 0; y < h; ++y)
-      for (int32_t x = 0; x < w; ++x) {
-        const size_t p = (size_t)y * w + x;
-        if (m.flag[p] == kInside) continue;
-        const bool adj = (y > 0 && m.flag[p - w] == kInside) || (x > 0 && m.flag[p - 1] == kInside) ||
-                         (y + 1 < h && m.flag[p + w] == kInside) || (x + 1 < w && m.flag[p + 1] == kInside);
-        if (adj) {
-          m.flag[p] = kBand;
-          tset(m, (int32_t)p, 0.0f, hn);
-        }
-      }
-  }
-  for (;;) {
+  {
+    const int T = blockDim.x;
+    const size_t chunk = (n + T - 1) / T;
+    const size_t b0 = threadIdx.x * chunk, b1 = b0 + chunk < n ? b0 + chunk : n;
+    auto is_band = [&](size_t p) {
+      if (m.flag[p] == kInside) return false;
+      const int32_t y = (int32_t)(p / w), x = (int32_t)(p - (size_t)y * w);
+      return (y > 0 && m.flag[p - w] == kInside) || (x > 0 && m.flag[p - 1] == kInside) ||
+             (y + 1 < h && m.flag[p + w] == kInside) || (x + 1 < w && m.flag[p + 1] == kInside);
+    };
+    int32_t c = 0;
+    for (size_t p = b0; p < b1; ++p) c += is_band(p);
+    s_cnt[threadIdx.x + 1] = c;
+    __syncthreads();
     if (threadIdx.x == 0) {
-      // advance to the next neighbour that needs an inpainted value
-      s_q = -1;
-      s_done = 0;
-      for (;;) {
-        if (nb >= 4) {
-          if (hn == 0) {
-            s_done = 1;
+      s_cnt[0] = 0;
+      for (int i = 1; i <= T; ++i) s_cnt[i] += s_cnt[i - 1];
+    }
+    __syncthreads();
+    int32_t at = s_cnt[threadIdx.x];
+    for (size_t p = b0; p < b1; ++p)
+      if (is_band(p)) {
+        m.ht[at] = 0.0f;
+        m.hi[at] = (int32_t)p;
+        m.pos[p] = at;
+        ++at;
+      }
+    __syncthreads();
+    for (size_t p = b0; p < b1; ++p)
+      if (m.pos[p] >= 0) m.flag[p] = kBand;
+    hn = s_cnt[T];
+  }
+  // The band is an unordered list (ht/hi, s_B entries; pos: each pixel's
+  // slot).  Each step the whole CTA finds its first pixel by (T, pixel
+  // index) -- a total order, so the steps are those of any exact priority
+  // queue -- and thread 0 updates the list and the neighbours.
+  __shared__ float s_wt[32];
+  __shared__ int32_t s_wi[32];
+  __shared__ int32_t s_B;
+  if (threadIdx.x == 0) s_B = hn;
+  int32_t cur = -1, nb = 4;  // thread 0: the popped pixel and its next neighbour
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  for (;;) {
+    const int32_t B = s_B;
+    if (B == 0) break;
+    float bt = __int_as_float(0x7f800000);
+    int32_t bi = 0x7fffffff;
+    for (int32_t i = threadIdx.x; i < B; i += blockDim.x) {
+      const float t = m.ht[i];
+      const int32_t x = m.hi[i];
+      if (tless(t, x, bt, bi)) {
+        bt = t;
+        bi = x;
+      }
+    }
+    warp_argmin(bt, bi);
+    if (lane == 0) {
+      s_wt[wid] = bt;
+      s_wi[wid] = bi;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      bt = lane < nw ? s_wt[lane] : __int_as_float(0x7f800000);
+      bi = lane < nw ? s_wi[lane] : 0x7fffffff;
+      warp_argmin(bt, bi);
+      if (lane == 0) {
+        cur = bi;
+        const int32_t slot = m.pos[cur], last = B - 1;
+        if (slot != last) {
+          m.ht[slot] = m.ht[last];
+          m.hi[slot] = m.hi[last];
+          m.pos[m.hi[slot]] = slot;
+        }
+        m.pos[cur] = -1;
+        s_B = last;
+        m.flag[cur] = kKnown;
+        nb = 0;
+      }
+    }
+    // thread 0 walks the popped pixel's neighbours (up, left, down, right);
+    // each one that was INSIDE is inpainted by the whole CTA before the next
+    for (;;) {
+      if (threadIdx.x == 0) {
+        s_q = -1;
+        while (nb < 4) {
+          const int32_t px = cur % w, py = cur / w;
+          const int32_t j = nb++;
+          const int32_t x = j == 1 ? px - 1 : j == 3 ? px + 1 : px;
+          const int32_t y = j == 0 ? py - 1 : j == 2 ? py + 1 : py;
+          if (x < 0 || x >= w || y < 0 || y >= h) continue;
+          const size_t q = (size_t)y * w + x;
+          if (m.flag[q] == kKnown) continue;
+          const bool ku = y > 0 && m.flag[q - w] == kKnown, kd = y + 1 < h && m.flag[q + w] == kKnown;
+          const bool kl = x > 0 && m.flag[q - 1] == kKnown, kr = x + 1 < w && m.flag[q + 1] == kKnown;
+          const float tu = ku ? m.T[q - w] : 0.0f, td = kd ? m.T[q + w] : 0.0f;
+          const float tl = kl ? m.T[q - 1] : 0.0f, tr = kr ? m.T[q + 1] : 0.0f;
+          float t = eikonal(ku, tu, kl, tl);
+          float t2 = eikonal(kd, td, kl, tl);
+          if (t2 < t) t = t2;
+          t2 = eikonal(ku, tu, kr, tr);
+          if (t2 < t) t = t2;
+          t2 = eikonal(kd, td, kr, tr);
+          if (t2 < t) t = t2;
+          m.T[q] = t;
+          // into the band, or its time updated in place
+          if (m.pos[q] < 0) {
+            const int32_t slot = s_B++;
+            m.ht[slot] = t;
+            m.hi[slot] = (int32_t)q;
+            m.pos[q] = slot;
+          } else {
+            m.ht[m.pos[q]] = t;
+          }
+          if (m.flag[q] == kInside) {
+            // inpainted while still INSIDE (its own value is not used), then
+            // BAND; the arrival-time gradient at q over its non-INSIDE neighbours
+            const bool kxm = x > 0 && m.flag[q - 1] != kInside, kxp = x + 1 < w && m.flag[q + 1] != kInside;
+            const bool kym = y > 0 && m.flag[q - w] != kInside, kyp = y + 1 < h && m.flag[q + w] != kInside;
+            s_gtx = grad1(kxm, kxm ? m.T[q - 1] : 0.0f, kxp, kxp ? m.T[q + 1] : 0.0f, t);
+            s_gty = grad1(kym, kym ? m.T[q - w] : 0.0f, kyp, kyp ? m.T[q + w] : 0.0f, t);
+            s_q = (int32_t)q;
             break;
           }
-          cur = m.hi[0];
-          tswap(m, 0, hn - 1);
-          --hn;
-          m.pos[cur] = -1;
-          if (hn > 0) tdown(m, 0, hn);
-          m.flag[cur] = kKnown;
-          nb = 0;
         }
-        const int32_t px = cur % w, py = cur / w;
-        const int32_t j = nb++;
-        const int32_t x = j == 1 ? px - 1 : j == 3 ? px + 1 : px;
-        const int32_t y = j == 0 ? py - 1 : j == 2 ? py + 1 : py;
-        if (x < 0 || x >= w || y < 0 || y >= h) continue;
-        const size_t q = (size_t)y * w + x;
-        if (m.flag[q] == kKnown) continue;
-        const bool ku = y > 0 && m.flag[q - w] == kKnown, kd = y + 1 < h && m.flag[q + w] == kKnown;
-        const bool kl = x > 0 && m.flag[q - 1] == kKnown, kr = x + 1 < w && m.flag[q + 1] == kKnown;
-        const float tu = ku ? m.T[q - w] : 0.0f, td = kd ? m.T[q + w] : 0.0f;
-        const float tl = kl ? m.T[q - 1] : 0.0f, tr = kr ? m.T[q + 1] : 0.0f;
-        float t = eikonal(ku, tu, kl, tl);
-        float t2 = eikonal(kd, td, kl, tl);
-        if (t2 < t) t = t2;
-        t2 = eikonal(ku, tu, kr, tr);
-        if (t2 < t) t = t2;
-        t2 = eikonal(kd, td, kr, tr);
-        if (t2 < t) t = t2;
-        m.T[q] = t;
-        if (m.flag[q] == kInside) {
-          // inpainted while still INSIDE (its own value is not used), then BAND;
-          // the arrival-time gradient at q, over its non-INSIDE neighbours
-          const bool kxm = x > 0 && m.flag[q - 1] != kInside, kxp = x + 1 < w && m.flag[q + 1] != kInside;
-          const bool kym = y > 0 && m.flag[q - w] != kInside, kyp = y + 1 < h && m.flag[q + w] != kInside;
-          s_gtx = grad1(kxm, kxm ? m.T[q - 1] : 0.0f, kxp, kxp ? m.T[q + 1] : 0.0f, t);
-          s_gty = grad1(kym, kym ? m.T[q - w] : 0.0f, kyp, kyp ? m.T[q + w] : 0.0f, t);
-          s_q = (int32_t)q;
-          tset(m, (int32_t)q, t, hn);
-          break;
+      }
+      __syncthreads();
+      const int32_t q = s_q;
+      if (q < 0) break;
+      const int32_t qx = q % w, qy = q / w;
+      uint8_t val = 0;
+      bool set = false;
+      for (int pass = 0; pass < 2 && !set; ++pass) {
+        long long num = 0, den = 0;
+        telea_terms(m, w, h, qx, qy, s_gtx, s_gty, n_off, pass == 1, num, den);
+        block_sum2(num, den, red);
+        if (den > 0) {
+          const double v = rint((double)num / (double)den);
+          val = (uint8_t)(v < 0.0 ? 0.0 : v > 255.0 ? 255.0 : v);
+          set = true;
         }
-        tset(m, (int32_t)q, t, hn);
       }
-    }
-    __syncthreads();
-    if (s_done) break;
-    const int32_t q = s_q;
-    const int32_t qx = q % w, qy = q / w;
-    uint8_t val = 0;
-    bool set = false;
-    for (int pass = 0; pass < 2 && !set; ++pass) {
-      long long num = 0, den = 0;
-      telea_terms(m, w, h, qx, qy, s_gtx, s_gty, n_off, pass == 1, num, den);
-      block_sum2(num, den, red);
-      if (den > 0) {
-        const double v = rint((double)num / (double)den);
-        val = (uint8_t)(v < 0.0 ? 0.0 : v > 255.0 ? 255.0 : v);
-        set = true;
+      if (threadIdx.x == 0) {
+        m.img[q] = val;
+        m.flag[q] = kBand;
       }
+      __syncthreads();
     }
-    if (threadIdx.x == 0) {
-      m.img[q] = val;
-      m.flag[q] = kBand;
-    }
-    __syncthreads();
   }
   for (size_t i = threadIdx.x; i < n; i += blockDim.x) img_io[i] = m.img[i];
 }
@@ -1059,6 +1089,90 @@ __global__ void set_moments_kernel(const int32_t* __restrict__ labels, const uin
   }
 }
 
+// The same sums for frames with few sets: each block accumulates into a
+// shared-memory copy of the table (warp sums first, then shared atomics)
+// and adds its non-empty records to the global table once.
+__global__ void set_moments_smem_kernel(const int32_t* __restrict__ labels, const uint16_t* __restrict__ inp,
+                                        const uint8_t* __restrict__ v8, int32_t W, int32_t H, int32_t n_sets,
+                                        SetMoments* __restrict__ acc) {
+  extern __shared__ __align__(16) unsigned char msm[];
+  SetMoments* sm = reinterpret_cast<SetMoments*>(msm);
+  for (int32_t k = threadIdx.x; k < n_sets; k += blockDim.x) {
+    SetMoments z{};
+    z.minx = z.miny = 0x7fffffff;
+    z.maxx = z.maxy = -1;
+    sm[k] = z;
+  }
+  __syncthreads();
+  const size_t n = (size_t)W * H;
+  const int lane = threadIdx.x & 31;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t base = blockIdx.x * (size_t)blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+    const size_t p = base + lane;
+    const int32_t k = p < n ? labels[p] : -1;
+    const bool valid = k >= 0 && k < n_sets;
+    const int32_t y = valid ? (int32_t)(p / W) : 0, x = valid ? (int32_t)(p - (size_t)y * W) : 0;
+    const uint64_t z = valid ? inp[p] : 0;
+    const uint8_t v = valid ? v8[p] : 255;
+    unsigned long long f[14];
+    f[0] = valid;
+    f[1] = (unsigned long long)x;
+    f[2] = (unsigned long long)y;
+    f[3] = (unsigned long long)((int64_t)x * x);
+    f[4] = (unsigned long long)((int64_t)y * y);
+    f[5] = (unsigned long long)((int64_t)x * y);
+    f[6] = valid && z;
+    f[7] = z;
+    f[8] = (unsigned long long)x * z;
+    f[9] = (unsigned long long)y * z;
+    f[10] = valid && !z;
+    f[11] = v < 8;
+    f[12] = v >= 8 && v < 16;
+    f[13] = v >= 16 && v < 24;
+    const int32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+    const bool uniform = __all_sync(0xffffffffu, valid && k == k0);
+    int32_t mnx = x, mxx = x, mny = y, mxy = y;
+    int32_t kk = k;
+    bool act = valid;
+    if (uniform) {
+      for (int i = 0; i < 14; ++i) f[i] = warp_sum64(f[i]);
+      mnx = __reduce_min_sync(0xffffffffu, x);
+      mxx = __reduce_max_sync(0xffffffffu, x);
+      mny = __reduce_min_sync(0xffffffffu, y);
+      mxy = __reduce_max_sync(0xffffffffu, y);
+      kk = k0;
+      act = lane == 0;
+    }
+    if (act) {
+      SetMoments* a = sm + kk;
+      unsigned long long* dst[14] = {&a->n,  &a->sx, &a->sy,  &a->sxx,   &a->syy,   &a->sxy,   &a->nz,
+                                     &a->sz, &a->suz, &a->svz, &a->nzero, &a->vb[0], &a->vb[1], &a->vb[2]};
+      for (int i = 0; i < 14; ++i)
+        if (f[i]) atomicAdd(dst[i], f[i]);
+      atomicMin(&a->minx, mnx);
+      atomicMax(&a->maxx, mxx);
+      atomicMin(&a->miny, mny);
+      atomicMax(&a->maxy, mxy);
+    }
+  }
+  __syncthreads();
+  for (int32_t k = threadIdx.x; k < n_sets; k += blockDim.x) {
+    const SetMoments& m = sm[k];
+    if (m.n == 0) continue;
+    SetMoments* a = acc + k;
+    const unsigned long long src[14] = {m.n,  m.sx, m.sy,  m.sxx,   m.syy,   m.sxy,   m.nz,
+                                        m.sz, m.suz, m.svz, m.nzero, m.vb[0], m.vb[1], m.vb[2]};
+    unsigned long long* dst[14] = {&a->n,  &a->sx, &a->sy,  &a->sxx,   &a->syy,   &a->sxy,   &a->nz,
+                                   &a->sz, &a->suz, &a->svz, &a->nzero, &a->vb[0], &a->vb[1], &a->vb[2]};
+    for (int i = 0; i < 14; ++i)
+      if (src[i]) atomicAdd(dst[i], src[i]);
+    atomicMin(&a->minx, m.minx);
+    atomicMax(&a->maxx, m.maxx);
+    atomicMin(&a->miny, m.miny);
+    atomicMax(&a->maxy, m.maxy);
+  }
+}
+
 __global__ void set_moments_init_kernel(SetMoments* acc, int32_t n_sets) {
   for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_sets; k += gridDim.x * blockDim.x) {
     SetMoments m{};
@@ -1072,7 +1186,12 @@ cudaError_t launch_set_moments(const int32_t* labels, const uint16_t* inp, const
                                int32_t n_sets, SetMoments* acc, int sms, cudaStream_t st) {
   if (n_sets <= 0) return cudaSuccess;
   set_moments_init_kernel<<<(n_sets + 255) / 256, 256, 0, st>>>(acc, n_sets);
-  set_moments_kernel<<<grid_of((size_t)W * H, 256, sms), 256, 0, st>>>(labels, inp, v8, W, H, n_sets, acc);
+  if (n_sets <= 256) {
+    const int grid = std::min(grid_of((size_t)W * H, 256, sms), 2 * sms);
+    set_moments_smem_kernel<<<grid, 256, n_sets * sizeof(SetMoments), st>>>(labels, inp, v8, W, H, n_sets, acc);
+  } else {
+    set_moments_kernel<<<grid_of((size_t)W * H, 256, sms), 256, 0, st>>>(labels, inp, v8, W, H, n_sets, acc);
+  }
   return cudaGetLastError();
 }
 

@@ -406,10 +406,22 @@ void seg_ws_inputs(void* ws, int32_t W, int32_t H, uint8_t** hsv, uint16_t** dep
   *sal = (float*)p;
 }
 
-cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
+namespace {
+
+// Device buffers of the graph stage after the sort.
+struct SegGraphDev {
+  uint64_t* sorted;  // keys in ascending order (edge index in the low 32 bits)
+  uint64_t* spare;   // the sort's other key buffer (free after the sort)
+  float* w;          // weights in edge order
+  int32_t* ea;
+  int32_t* eb;
+  uint32_t* misc;    // [0] depth min, [1] depth max, [2] error bits
+};
+
+// Upload (or take the inputs already in their slots), smooth, weigh and sort.
+cudaError_t seg_graph_device(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
                              int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
-                             float ks, void* ws, int sms, cudaStream_t st, uint32_t* order_host,
-                             int32_t* ea_host, int32_t* eb_host, float* w_host, uint32_t* err_host) {
+                             float ks, void* ws, int sms, cudaStream_t st, SegGraphDev* out) {
   const size_t n = (size_t)W * H;
   const uint64_t E = seg_num_edges(W, H);
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
@@ -437,7 +449,7 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
   const uint32_t nblk = (uint32_t)((E + kRsTile - 1) / kRsTile);
   uint32_t* d_hist = (uint32_t*)p;
   p += al(4 * 256 * (nblk ? nblk : 1));
-  uint32_t* d_misc = (uint32_t*)p;  // [0] depth min, [1] depth max, [2] error bits
+  uint32_t* d_misc = (uint32_t*)p;
 
   cudaError_t e;
   if (hsv_host) {
@@ -465,14 +477,14 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
   seg_cols_kernel<<<grid_for(3 * n, 256, sms), 256, 0, st>>>(d_tmp, d_sm, c);
   if (n > 1) seg_range_kernel<<<grid_for(n - 1, 256, sms), 256, 0, st>>>(d_depth, n - 1, d_misc);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  uint64_t* src = d_k0;
+  uint64_t* dst = d_k1;
   if (E > 0) {
     seg_edges_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_sm, d_depth, d_sal, d_misc, c, E, d_k0, d_w,
                                                             d_ea, d_eb, d_misc + 2);
     // key bits: the edge index in the low bit_length(E - 1) bits, the
     // weight's order bits in the high 32
     const int idx_bits = bit_length(E - 1);
-    uint64_t* src = d_k0;
-    uint64_t* dst = d_k1;
     for (int shift = 0; shift < 64; shift += 8) {
       if (shift < 32 && shift >= idx_bits) continue;  // all keys share these digits
       rs_hist_kernel<<<nblk, kRsThreads, 0, st>>>(src, (uint32_t)E, shift, d_hist, nblk);
@@ -481,19 +493,130 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
       std::swap(src, dst);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  *out = SegGraphDev{src, dst, d_w, d_ea, d_eb, d_misc};
+  return cudaSuccess;
+}
+
+// The sorted edges packed for the host: (first end << 2 | direction) and the
+// weight, in sorted order.  Directions: 0 right, 1 down, 2 down-right,
+// 3 up-right (the second end is first + 1, W, W + 1, 1 - W).
+__global__ void seg_pack_kernel(const uint64_t* __restrict__ sorted, const int32_t* __restrict__ ea,
+                                const int32_t* __restrict__ eb, const float* __restrict__ w, uint32_t E,
+                                int32_t W, uint32_t* __restrict__ pk, float* __restrict__ pw) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < E; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t e = (uint32_t)(sorted[i] & 0xFFFFFFFFull);
+    const int32_t a = ea[e], d = eb[e] - a;
+    const uint32_t code = d == 1 ? 0u : d == W ? 1u : d == W + 1 ? 2u : 3u;
+    pk[i] = ((uint32_t)a << 2) | code;
+    pw[i] = w[e];
+  }
+}
+
+}  // namespace
+
+cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
+                             int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
+                             float ks, void* ws, int sms, cudaStream_t st, uint32_t* order_host,
+                             int32_t* ea_host, int32_t* eb_host, float* w_host, uint32_t* err_host) {
+  const uint64_t E = seg_num_edges(W, H);
+  SegGraphDev g;
+  cudaError_t e = seg_graph_device(hsv_host, depth_host, sal_host, W, H, mask, len, kdv, kdc, kx, ks, ws, sms, st, &g);
+  if (e != cudaSuccess) return e;
+  if (E > 0) {
     // the sorted order: the low 32 bits of each key; copy keys back whole
     std::vector<uint64_t> keys(E);
-    if ((e = cudaMemcpyAsync(keys.data(), src, 8 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(ea_host, d_ea, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(eb_host, d_eb, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(w_host, d_w, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(err_host, d_misc + 2, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(keys.data(), g.sorted, 8 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(ea_host, g.ea, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(eb_host, g.eb, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(w_host, g.w, 4 * E, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(err_host, g.misc + 2, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     for (uint64_t i = 0; i < E; ++i) order_host[i] = (uint32_t)(keys[i] & 0xFFFFFFFFull);
   } else {
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     *err_host = 0;
   }
+  return cudaSuccess;
+}
+
+size_t seg_merge_pinned_bytes(int32_t W, int32_t H) { return 8 * (size_t)seg_num_edges(W, H) + 64; }
+
+// The graph stage with the merge passes streamed: the GPU packs the sorted
+// edges (8 bytes each), they come back in n_chunks copies into pinned host
+// memory, and the host runs segment_graph's pass over each chunk as soon as
+// its copy has landed, reading the edges in order; then the small-component
+// pass and the labels.  Same partition and numbering as seg_merge over the
+// same sorted order.
+cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
+                            int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
+                            float ks, void* ws, int sms, cudaStream_t st, void* pinned, const cudaEvent_t* ev,
+                            int n_chunks, float k, float min_size, int32_t* labels, uint32_t* n_sets,
+                            uint32_t* err_host) {
+  const uint64_t E = seg_num_edges(W, H);
+  const uint32_t n = (uint32_t)((size_t)W * H);
+  SegGraphDev g;
+  cudaError_t e = seg_graph_device(hsv_host, depth_host, sal_host, W, H, mask, len, kdv, kdc, kx, ks, ws, sms, st, &g);
+  if (e != cudaSuccess) return e;
+  uint32_t* h_err = reinterpret_cast<uint32_t*>(pinned);
+  uint32_t* h_pk = reinterpret_cast<uint32_t*>(static_cast<char*>(pinned) + 64);
+  float* h_pw = reinterpret_cast<float*>(h_pk + E);
+  if (E > 0) {
+    uint32_t* d_pk = reinterpret_cast<uint32_t*>(g.spare);
+    float* d_pw = reinterpret_cast<float*>(d_pk + E);
+    seg_pack_kernel<<<grid_for(E, 256, sms), 256, 0, st>>>(g.sorted, g.ea, g.eb, g.w, (uint32_t)E, W, d_pk, d_pw);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(h_err, g.misc + 2, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    for (int c = 0; c < n_chunks; ++c) {
+      const uint64_t c0 = E * c / n_chunks, c1 = E * (c + 1) / n_chunks;
+      if (c1 > c0) {
+        if ((e = cudaMemcpyAsync(h_pk + c0, d_pk + c0, 4 * (c1 - c0), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+          return e;
+        if ((e = cudaMemcpyAsync(h_pw + c0, d_pw + c0, 4 * (c1 - c0), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+          return e;
+      }
+      if ((e = cudaEventRecord(ev[c], st)) != cudaSuccess) return e;
+    }
+    if ((e = cudaEventSynchronize(ev[0])) != cudaSuccess) return e;
+    *err_host = *h_err;
+    if (*err_host) {  // let the caller report it; finish the copies first
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+      return cudaSuccess;
+    }
+  } else {
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    *err_host = 0;
+  }
+  const int32_t dstep[4] = {1, W, W + 1, 1 - W};
+  Forest f(n);
+  std::vector<float> thr(n, k / (float)1);  // THRESHOLD(1, k)
+  for (int c = 0; c < (E > 0 ? n_chunks : 0); ++c) {
+    const uint64_t c0 = E * c / n_chunks, c1 = E * (c + 1) / n_chunks;
+    if ((e = cudaEventSynchronize(ev[c])) != cudaSuccess) return e;
+    for (uint64_t i = c0; i < c1; ++i) {
+      const uint32_t pk = h_pk[i];
+      const int32_t a0 = (int32_t)(pk >> 2), b0 = a0 + dstep[pk & 3u];
+      const float we = h_pw[i];
+      const int32_t a = f.find(a0), b = f.find(b0);
+      if (a == b || !(we <= thr[a] && we <= thr[b])) continue;
+      const int32_t r = f.join(a, b);
+      thr[r] = we + k / (float)f.size[r];
+    }
+  }
+  for (uint64_t i = 0; i < E; ++i) {
+    const uint32_t pk = h_pk[i];
+    const int32_t a0 = (int32_t)(pk >> 2), b0 = a0 + dstep[pk & 3u];
+    const int32_t a = f.find(a0), b = f.find(b0);
+    if (a != b && ((float)f.size[a] < min_size || (float)f.size[b] < min_size)) f.join(a, b);
+  }
+  std::vector<int32_t> id(n, -1);
+  uint32_t next = 0;
+  for (uint32_t v = 0; v < n; ++v) {
+    const int32_t r = f.find((int32_t)v);
+    if (id[r] < 0) id[r] = (int32_t)next++;
+    labels[v] = id[r];
+  }
+  *n_sets = next;
   return cudaSuccess;
 }
 
