@@ -318,10 +318,10 @@ qpso_status qpso_image_bgr8_load(const char *path, uint8_t *out, uint64_t capaci
  * the HBM budget allow (their swarm state, masked depth and summed-area
  * table are allocated on admission from the server's own memory pool and
  * stay resident until the request completes), and runs epochs: each epoch
- * launches the multi-request iteration kernel, which advances every active
- * request by one iteration at its own iteration number, up to
- * iters_per_epoch times; finished requests leave and queued ones join
- * between epochs.  Meshes and frames are the context's resident objects
+ * is one persistent launch of the batched solve's dataflow queue in which
+ * every active request advances by up to iters_per_epoch iterations, each
+ * at its own pace (a request waits only for its own previous iteration);
+ * finished requests leave and queued ones join between epochs.  Meshes and frames are the context's resident objects
  * and must stay uploaded while requests use them.  A request reads its
  * frame's depth and labels when it is admitted (its masked copy is made
  * then): a qpso_frame_update issued while it is still queued is what it
@@ -331,13 +331,13 @@ typedef struct qpso_server qpso_server;
 typedef struct {
     uint32_t max_slots;        /* requests on the GPU at once (>= 1) */
     uint64_t hbm_budget_bytes; /* request memory cap; 0 = half of free HBM at start */
-    uint32_t iters_per_epoch;  /* iterations per scheduling epoch (>= 1) */
+    uint32_t iters_per_epoch;  /* iterations a request advances per scheduling epoch (>= 1) */
 } qpso_server_config;
 typedef struct {
     uint64_t submitted, admitted, completed, failed;
     uint32_t pending, active, peak_active;
     uint64_t bytes_in_use, peak_bytes, budget_bytes;
-    uint64_t epochs, launches;
+    uint64_t epochs, launches;  /* launches: one per epoch */
 } qpso_server_stats;
 qpso_status qpso_server_start(qpso_context *ctx, const qpso_server_config *cfg, qpso_server **out);
 /* Queue a request; QPSO_ERR_BUSY if it could never fit the budget. */

@@ -1493,13 +1493,19 @@ struct qpso_server {
   // device slots
   Instance* d_slots = nullptr;
   Header* d_hdr = nullptr;
-  WorkItem* d_items = nullptr;
   PrepDesc* d_prep = nullptr;
+  // an epoch's dataflow queue: at most iters_per_epoch entries per slot
+  QEntry* d_queue = nullptr;
+  QCtl* d_qctl = nullptr;
+  uint32_t* d_end = nullptr;     // per slot: the epoch's last iteration + 1
+  uint32_t* d_berr = nullptr;
   Instance* h_slots = nullptr;  // pinned staging
   Header* h_hdr = nullptr;
-  WorkItem* h_items = nullptr;
   PrepDesc* h_prep = nullptr;
-  uint32_t max_items = 0;
+  QEntry* h_qinit = nullptr;    // the epoch's first entries, one per active slot
+  QCtl* h_qctl = nullptr;
+  uint32_t* h_end = nullptr;
+  uint32_t* h_berr = nullptr;
   std::vector<int> free_slots;
   std::vector<uint64_t> slot_req;
   qpso_server_stats st{};
@@ -1657,11 +1663,16 @@ void server_loop(qpso_server* s) {
       if (e != cudaSuccess) server_fail_all(s, QPSO_ERR_CUDA, cudaGetErrorString(e));
       continue;
     }
-    // work items of this epoch: every chunk of every active request, the
+    // the epoch: every active request advances by up to iters_per_epoch
+    // iterations, each at its own pace, in one launch of the dataflow
+    // queue; the queue starts with the requests' current iterations, the
     // most expensive requests first so that no large render starts last
-    uint32_t n_items = 0, K = s->cfg.iters_per_epoch;
+    const uint32_t E = s->cfg.iters_per_epoch;
     int var = 0;
     int vcap = 64;
+    uint32_t n_init = 0, total = 0;
+    uint64_t all_chunks = 0;
+    std::vector<uint32_t> ran(S, 0);
     {
       std::lock_guard<std::mutex> g(s->mu);
       std::vector<int> order(active);
@@ -1670,23 +1681,52 @@ void server_loop(qpso_server* s) {
       });
       for (int slot : order) {
         const ServerReq& r = s->reqs[s->slot_req[slot]];
-        K = std::min(K, r.remaining);
         var = std::max(var, r.var);
         vcap = std::max(vcap, r.vcap);
-        const uint32_t chunks = s->h_slots[slot].chunks;
-        for (uint32_t c = 0; c < chunks; ++c) s->h_items[n_items++] = WorkItem{(uint32_t)slot, c};
+        const uint32_t start = r.desc.iterations - r.remaining;
+        const uint32_t end = start + std::min(E, r.remaining);
+        ran[slot] = end - start;
+        s->h_end[slot] = end;
+        s->h_qinit[n_init++] = QEntry{(uint32_t)slot, start, 0u, 1u};
+        total += end - start;
+        all_chunks += s->h_slots[slot].chunks;
       }
     }
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(s->d_items, s->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
-                          s->stream);
+    *s->h_qctl = QCtl{0u, n_init, total, 0u};
+    *s->h_berr = 0u;
     TileConfig tc = s->tc;  // fits every vcap (checked at submit)
     shrink_cfg(tc, vcap, s->ctx->smem_optin);
-    for (uint32_t k = 0; k < K && e == cudaSuccess; ++k)
-      e = launch_multi_step(s->d_slots, s->d_items, n_items, tc, s->stream, var, vcap);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = epoch_max_grid(tc, var, vcap, &per_sm);
+    if (e == cudaSuccess && per_sm <= 0) e = cudaErrorInvalidConfiguration;
+    const int grid = (int)std::min<uint64_t>(all_chunks, (uint64_t)std::max(per_sm, 1) * s->ctx->num_sms);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->d_end, s->h_end, S * sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_queue, 0, (size_t)total * sizeof(QEntry), s->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->d_queue, s->h_qinit, n_init * sizeof(QEntry), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_qctl, s->h_qctl, sizeof(QCtl), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->d_berr, s->h_berr, sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) {
+      BatchArgs A;
+      A.inst = s->d_slots;
+      A.queue = s->d_queue;
+      A.qctl = s->d_qctl;
+      A.err = s->d_berr;
+      A.timeout_ns = 20ull * 1000 * 1000 * 1000;  // 20 s per wait for work
+      e = launch_epoch(A, s->d_end, grid, tc, s->stream, var, vcap);
+    }
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s->h_hdr, s->d_hdr, S * sizeof(Header), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->h_berr, s->d_berr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess && *s->h_berr != 0u) {
+      server_fail_all(s, QPSO_ERR_TIMEOUT, "serving epoch: a bounded wait for work expired");
+      active.clear();
+      continue;
+    }
     if (e != cudaSuccess) {
       server_fail_all(s, QPSO_ERR_CUDA, cudaGetErrorString(e));
       active.clear();
@@ -1694,11 +1734,11 @@ void server_loop(qpso_server* s) {
     }
     std::lock_guard<std::mutex> g(s->mu);
     s->st.epochs++;
-    s->st.launches += K;
+    s->st.launches += 1;
     std::vector<int> still;
     for (int slot : active) {
       ServerReq& r = s->reqs[s->slot_req[slot]];
-      r.remaining -= K;
+      r.remaining -= ran[slot];
       if (r.remaining > 0) {
         still.push_back(slot);
         continue;
@@ -1733,9 +1773,7 @@ qpso_status qpso_server_start(qpso_context* ctx, const qpso_server_config* cfg, 
   s->cfg = *cfg;
   s->tc = ctx->batch;
   const uint32_t S = cfg->max_slots;
-  s->max_items = S * 65536u;  // upper bound of chunks: P <= 2^20 particles / ppb, capped below
-  s->max_items = std::min<uint64_t>(s->max_items, (uint64_t)S * ((1u << 20) / s->tc.ppb + 1));
-  s->max_items = std::min<uint32_t>(s->max_items, 1u << 22);
+  const size_t max_entries = (size_t)S * cfg->iters_per_epoch;
   cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   cudaMemPoolProps props = {};
   props.allocType = cudaMemAllocationTypePinned;
@@ -1748,12 +1786,18 @@ qpso_status qpso_server_start(qpso_context* ctx, const qpso_server_config* cfg, 
   }
   if (e == cudaSuccess) e = cudaMalloc(&s->d_slots, S * sizeof(Instance));
   if (e == cudaSuccess) e = cudaMalloc(&s->d_hdr, S * sizeof(Header));
-  if (e == cudaSuccess) e = cudaMalloc(&s->d_items, (size_t)s->max_items * sizeof(WorkItem));
   if (e == cudaSuccess) e = cudaMalloc(&s->d_prep, S * sizeof(PrepDesc));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_queue, max_entries * sizeof(QEntry));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_qctl, sizeof(QCtl));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_end, S * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_berr, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_slots, S * sizeof(Instance));
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_hdr, S * sizeof(Header));
-  if (e == cudaSuccess) e = cudaMallocHost(&s->h_items, (size_t)s->max_items * sizeof(WorkItem));
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_prep, S * sizeof(PrepDesc));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_qinit, S * sizeof(QEntry));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_qctl, sizeof(QCtl));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_end, S * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_berr, sizeof(uint32_t));
   size_t free_b = 0, total_b = 0;
   if (e == cudaSuccess) e = cudaMemGetInfo(&free_b, &total_b);
   if (e != cudaSuccess) {
@@ -1782,9 +1826,7 @@ qpso_status qpso_server_submit(qpso_server* s, const qpso_solve_desc* desc, uint
   TileConfig fit = s->tc;
   if (!shrink_cfg(fit, m->mlet_cap, s->ctx->smem_optin))
     return fail(s->ctx, QPSO_ERR_ARG, "the server's launch config cannot fit this mesh's vertex caches");
-  const uint32_t chunks = (desc->num_particles + s->tc.ppb - 1) / s->tc.ppb;
-  if (request_bytes(*desc, f->cam) > s->st.budget_bytes || chunks * (uint64_t)s->cfg.max_slots > s->max_items)
-    return QPSO_ERR_BUSY;
+  if (request_bytes(*desc, f->cam) > s->st.budget_bytes) return QPSO_ERR_BUSY;
   std::lock_guard<std::mutex> g(s->mu);
   if (s->stop) return QPSO_ERR_BUSY;
   ServerReq r;
@@ -1856,12 +1898,18 @@ qpso_status qpso_server_stop(qpso_server* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   cudaFree(s->d_slots);
   cudaFree(s->d_hdr);
-  cudaFree(s->d_items);
   cudaFree(s->d_prep);
+  cudaFree(s->d_queue);
+  cudaFree(s->d_qctl);
+  cudaFree(s->d_end);
+  cudaFree(s->d_berr);
   cudaFreeHost(s->h_slots);
   cudaFreeHost(s->h_hdr);
-  cudaFreeHost(s->h_items);
   cudaFreeHost(s->h_prep);
+  cudaFreeHost(s->h_qinit);
+  cudaFreeHost(s->h_qctl);
+  cudaFreeHost(s->h_end);
+  cudaFreeHost(s->h_berr);
   if (s->pool) cudaMemPoolDestroy(s->pool);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;

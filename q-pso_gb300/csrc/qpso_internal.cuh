@@ -55,12 +55,6 @@ struct TileConfig {
   int ppb;          // particles per work item
 };
 
-// Work item of the persistent batched kernel: one chunk of one instance.
-struct WorkItem {
-  uint32_t inst;
-  uint32_t chunk;
-};
-
 // Per-instance preparation job: mask the frame to the cluster and build
 // the summed-area table of observed pixels.
 struct PrepDesc {
@@ -123,8 +117,12 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
                                  cudaStream_t st);
 cudaError_t launch_queue_probe(QCtl* qctl, QEntry* queue, uint32_t* err, uint32_t grid,
                                unsigned long long timeout_ns, cudaStream_t st);
-cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
-                              const TileConfig& cfg, cudaStream_t st, int var, int vcap);
+// Serving epoch: the dataflow queue of the batched kernel over the active
+// requests (args.inst = the slot records), request i running its
+// iterations up to end_iter[i] (device array), one cooperative launch.
+cudaError_t epoch_max_grid(const TileConfig& cfg, int var, int vcap, int* blocks_per_sm);
+cudaError_t launch_epoch(const BatchArgs& args, const uint32_t* end_iter, int grid, const TileConfig& cfg,
+                         cudaStream_t st, int var, int vcap);
 cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* di, PrepDesc* dj,
                                 cudaStream_t st);
 cudaError_t launch_copy_flags(const uint32_t* src, uint32_t* dst, cudaStream_t st);

@@ -1174,25 +1174,6 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* 
   instance_epilogue(I, iter, ctl);
 }
 
-// Serving form: one launch advances every active request by one
-// iteration, each at its own iteration number (continuous batching: the
-// set of requests changes between launches).  CTA b runs work item b; the
-// CTA finishing an instance's last chunk updates its global best and
-// advances its iteration counter for the next launch.
-template <int kVar>
-__global__ void __launch_bounds__(kMaxThreads) qpso_multi_step_kernel(Instance* __restrict__ slots,
-                                                                      const WorkItem* __restrict__ items,
-                                                                      int tile_px, int vcap) {
-  extern __shared__ int4 dyn_smem[];
-  __shared__ SmemCtl ctl;
-  const WorkItem it = items[blockIdx.x];
-  Instance& I = slots[it.inst];
-  const uint32_t iter = __ldcg(&I.cur_iter);
-  process_item<kVar>(I, it.chunk, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
-  instance_epilogue(I, iter, ctl);
-  if (ctl.last && threadIdx.x == 0) I.cur_iter = iter + 1;
-}
-
 // Batched form: every iteration of every instance in one cooperative
 // launch, scheduled as a dataflow queue with no grid-wide barrier.  The
 // queue starts with iteration 0 of every instance (most expensive first);
@@ -1278,6 +1259,34 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, in
     process_item<kVar>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
     instance_epilogue(I, it, ctl);
     if (ctl.last && threadIdx.x == 0 && it + 1 < I.prm.iterations) append_queue_item(A, in, it + 1);
+  }
+}
+
+// Serving form: one cooperative launch per scheduling epoch runs the same
+// dataflow queue over the active requests (continuous batching: the set of
+// requests changes between epochs).  Request `in` runs its iterations
+// cur_iter .. end_iter[in] - 1: the queue starts with every request's
+// current iteration, and the CTA that completes one advances the request's
+// counter and appends its next iteration while it is below end_iter.
+template <int kVar>
+__global__ void __launch_bounds__(kMaxThreads) qpso_epoch_kernel(BatchArgs A, const uint32_t* __restrict__ end_iter,
+                                                                 int tile_px, int vcap) {
+  extern __shared__ int4 dyn_smem[];
+  __shared__ SmemCtl ctl;
+  __shared__ uint32_t q[4];  // claim result, instance, iteration, chunk
+  while (true) {
+    if (threadIdx.x == 0) q[0] = (uint32_t)claim_queue_item(A, q[1], q[2], q[3]);
+    __syncthreads();
+    const uint32_t state = q[0], in = q[1], it = q[2], chunk = q[3];
+    __syncthreads();
+    if (state != 0u) return;
+    Instance& I = A.inst[in];
+    process_item<kVar>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
+    instance_epilogue(I, it, ctl);
+    if (ctl.last && threadIdx.x == 0) {
+      I.cur_iter = it + 1;
+      if (it + 1 < end_iter[in]) append_queue_item(A, in, it + 1);
+    }
   }
 }
 
@@ -1820,15 +1829,31 @@ cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_
   return cudaGetLastError();
 }
 
-cudaError_t launch_multi_step(Instance* slots, const WorkItem* items, uint32_t n_items,
-                              const TileConfig& cfg, cudaStream_t st, int var, int vcap) {
-  if (n_items == 0) return cudaSuccess;
+cudaError_t epoch_max_grid(const TileConfig& cfg, int var, int vcap, int* blocks_per_sm) {
   const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
-  auto* k = var == 2 ? qpso_multi_step_kernel<2> : var == 1 ? qpso_multi_step_kernel<1> : qpso_multi_step_kernel<0>;
+  auto* k = var == 2 ? qpso_epoch_kernel<2> : var == 1 ? qpso_epoch_kernel<1> : qpso_epoch_kernel<0>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  k<<<n_items, cfg.threads, smem, st>>>(slots, items, cfg.tile_px, vcap);
-  return cudaGetLastError();
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, cfg.threads, smem);
+}
+
+cudaError_t launch_epoch(const BatchArgs& args, const uint32_t* end_iter, int grid, const TileConfig& cfg,
+                         cudaStream_t st, int var, int vcap) {
+  const size_t smem = fused_smem_bytes(cfg.threads, cfg.ppb, cfg.tile_px, vcap);
+  auto* k = var == 2 ? qpso_epoch_kernel<2> : var == 1 ? qpso_epoch_kernel<1> : qpso_epoch_kernel<0>;
+  cudaError_t e = ensure_smem(k, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(grid);
+  lc.blockDim = dim3(cfg.threads);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, k, args, end_iter, cfg.tile_px, vcap);
 }
 
 cudaError_t launch_noalloc_init(const Instance& I, const PrepDesc& J, Instance* di, PrepDesc* dj,

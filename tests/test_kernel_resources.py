@@ -16,7 +16,7 @@ CSRC = os.path.join(ROOT, "q-pso_gb300", "csrc")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
 # kernel (mangled-name stem) -> most spill-store bytes allowed in variant 0
-LIMITS = {"qpso_step_kernel": 16, "qpso_batch_kernel": 32, "qpso_multi_step_kernel": 16,
+LIMITS = {"qpso_step_kernel": 16, "qpso_batch_kernel": 32, "qpso_epoch_kernel": 32,
           "score_poses_mlet_kernel": 8}
 
 
