@@ -429,22 +429,50 @@ def reference_shape_ours(ctx, w, repeats: int = 3):
                              "best_fits": [float(r.fit) for r in rb]}}
 
 
-def accuracy_vs_ground_truth(ctx, w, descs, results):
+def accuracy_vs_ground_truth(ctx, w, descs, results, refine: bool = True):
     """How close the solved poses are to the synthetic scenes' true poses:
     median translation error (mm) and rotation error (degrees; symmetric
     procedural shapes make this an upper bound), and the fraction of solves
     whose best fitness is at most the true pose's own fitness (the swarm
-    found a pose the objective ranks at least as well as the truth)."""
-    t_err, r_err, le = [], [], 0
+    found a pose the objective ranks at least as well as the truth).  With
+    refine, the same after qpso_refine (EDGE raster, default search) of
+    every solved pose, beside the unchanged solve."""
+    import qpso
+
+    def errs(poses):
+        t_err, r_err = [], []
+        for s, pose in zip(w["solves"], poses):
+            gt = np.asarray(s["gt_pose"], np.float64)
+            pose = np.asarray(pose, np.float64)
+            t_err.append(1000.0 * float(np.linalg.norm(pose[:3] - gt[:3])))
+            dq = abs(float(np.dot(pose[3:], gt[3:])))
+            r_err.append(2.0 * float(np.degrees(np.arccos(min(1.0, dq)))))
+        return float(np.median(t_err)), float(np.median(r_err))
+
+    le = 0
     for s, d, r in zip(w["solves"], descs, results):
-        gt = np.asarray(s["gt_pose"], np.float32)
-        pose = np.asarray(r.pose[:], np.float64)
-        t_err.append(1000.0 * float(np.linalg.norm(pose[:3] - gt[:3])))
-        dq = abs(float(np.dot(pose[3:], gt[3:].astype(np.float64))))
-        r_err.append(2.0 * float(np.degrees(np.arccos(min(1.0, dq)))))
-        le += int(r.fit <= float(ctx.score_poses(d, gt[None])[0]))
-    return {"trans_mm_median": float(np.median(t_err)), "rot_deg_median": float(np.median(r_err)),
-            "fit_at_most_true_pose_fraction": le / len(results), "solves": len(results)}
+        le += int(r.fit <= float(ctx.score_poses(d, np.asarray(s["gt_pose"], np.float32)[None])[0]))
+    t_med, r_med = errs([r.pose[:] for r in results])
+    out = {"trans_mm_median": t_med, "rot_deg_median": r_med,
+           "fit_at_most_true_pose_fraction": le / len(results), "solves": len(results)}
+    if refine:
+        prm = qpso.refine_params()
+        poses, le_r = [], 0
+        t0 = time.perf_counter()
+        for s, d, r in zip(w["solves"], descs, results):
+            pose, fit = ctx.refine(d, np.array(r.pose[:], np.float32), prm)
+            poses.append(pose)
+            d_edge = qpso.SolveDesc.from_buffer_copy(d)
+            d_edge.raster_mode = qpso.RASTER_EDGE
+            le_r += int(fit <= float(ctx.score_poses(d_edge, np.asarray(s["gt_pose"], np.float32)[None])[0]))
+        dt = time.perf_counter() - t0
+        t_ref, r_ref = errs(poses)
+        out["refined"] = {"trans_mm_median": t_ref, "rot_deg_median": r_ref,
+                          "fit_at_most_true_pose_fraction": le_r / len(results),
+                          "ms_per_solve": 1000.0 * dt / len(results),
+                          "search": "qpso_refine: %d rounds x %d candidates, EDGE raster, steps %.3f m / %.2f rad"
+                                    % (prm.rounds, prm.candidates, prm.step_t, prm.step_rot)}
+    return out
 
 
 def run_reference(args, ws, rank):
@@ -532,6 +560,7 @@ def extra_c3(ctx, local, hbm: float, mhz: float):
            "plain": {"value": 1000.0 * n / ms_p, "unit": "solves/s", "ms_per_step": ms_p,
                      "launch": {"threads": plain_cfg[0], "tile_px": plain_cfg[1], "ppb": plain_cfg[2]}},
            "speedup_batched_vs_plain": ms_p / ms_b, "plain_batched_bit_identical": bool(same),
+           "accuracy_vs_ground_truth": accuracy_vs_ground_truth(ctx, w, descs, rb),
            "device_error_bits": int(max(r.flags for r in rb)),
            "roofline": {"kernel": "qpso_batch_kernel", "bound": "hbm", "achieved": achieved, "peak": hbm,
                         "unit": "GB/s", "frac": achieved / hbm, "bytes_per_launch": bytes_launch,
@@ -550,7 +579,7 @@ def extra_c3(ctx, local, hbm: float, mhz: float):
     return out
 
 
-def extra_c4(ctx, slots: int = 64, epoch_iters: int = 4, rates=(10.0, 30.0, 100.0), duration_s: float = 5.0):
+def extra_c4(ctx, slots: int = 64, epoch_iters: int = 10, rates=(25.0, 40.0, 50.0), duration_s: float = 5.0):
     """The serving config (C4) in the default run: Poisson arrivals at three
     rates for duration_s each (serving_sweep)."""
     import scene
@@ -560,6 +589,7 @@ def extra_c4(ctx, slots: int = 64, epoch_iters: int = 4, rates=(10.0, 30.0, 100.
     cfg, _ = ctx.autotune(pool[:16], batched=True, tune_iters=6)
     results, top, best = serving_sweep(ctx, pool, list(rates), duration_s, slots, epoch_iters,
                                        max_requests=400)
+    batched = batched_same_mix(ctx, pool)
     for f in fids:
         ctx.frame_release(f)
     for m in mids:
@@ -572,7 +602,7 @@ def extra_c4(ctx, slots: int = 64, epoch_iters: int = 4, rates=(10.0, 30.0, 100.
             "sustained_rate_req_s": top["rate_req_s"] if top else None,
             "sustained_solves_per_s": top["solves_per_s"] if top else None,
             "p50_ms": head["p50_ms"], "p99_ms": head["p99_ms"],
-            "saturated_solves_per_s": best["solves_per_s"], "sweep": results}
+            "saturated_solves_per_s": best["solves_per_s"], "batched_same_mix": batched, "sweep": results}
 
 
 def extra_seg(ctx, steps: int = 5):
@@ -852,6 +882,21 @@ def serving_sweep(ctx, pool, rates, duration_s: float, slots: int, epoch_iters: 
     return results, top, best
 
 
+def batched_same_mix(ctx, pool, n: int = 64, seed: int = 17):
+    """The batched path (qpso_solve_batch, one persistent launch) over n
+    requests drawn from the serving pool as the sweep draws them: the
+    throughput the serving loop's epochs are measured against."""
+    rng = np.random.default_rng(seed + 1)
+    picks = [pool[int(i)] for i in rng.integers(0, len(pool), n)]
+    ctx.solve_batch(picks)  # warm-up (graph capture)
+    ctx.scrub_l2(L2_SCRUB_BYTES)
+    ctx.timer_record(0)
+    ctx.solve_batch(picks)
+    ctx.timer_record(1)
+    ms = ctx.timer_elapsed_ms(0, 1)
+    return {"requests": n, "value": 1000.0 * n / ms, "unit": "solves/s", "ms": ms}
+
+
 def c4_pool(ctx, w):
     import qpso
     import scene
@@ -880,6 +925,7 @@ def run_serving(args, ws, rank, local):
     results, top, best = serving_sweep(ctx, pool, rates, args.duration, args.slots, args.epoch_iters,
                                        max_requests=args.max_requests)
     clocks = sampler.stop()
+    batched = batched_same_mix(ctx, pool)
     head = top or best
     line = {"metric": "pose solves/sec at sustained load with p50/p99 latency (serving)",
             "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": len(rates),
@@ -890,7 +936,8 @@ def run_serving(args, ws, rank, local):
                        "launch_batched": {"threads": cfg[0], "tile_px": cfg[1], "ppb": cfg[2]}},
             "sustained_rate_req_s": top["rate_req_s"] if top else None,
             "p50_ms": head["p50_ms"], "p99_ms": head["p99_ms"],
-            "saturated_solves_per_s": best["solves_per_s"], "sweep": results, "clocks": clocks}
+            "saturated_solves_per_s": best["solves_per_s"], "batched_same_mix": batched, "sweep": results,
+            "clocks": clocks}
     print(json.dumps(line))
     ctx.close()
 
@@ -1021,11 +1068,11 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="c2: skip the C3, C4 and segmentation measurements added to the line")
     ap.add_argument("--launch", default="", help="THREADS,TILE_PX,PPB for both paths instead of autotuning")
-    ap.add_argument("--rates", default="10,25,50,100,1000,20000", help="c4: arrival rates (req/s)")
+    ap.add_argument("--rates", default="25,40,50,100,1000,20000", help="c4: arrival rates (req/s)")
     ap.add_argument("--max-requests", type=int, default=400, help="c4: requests per rate at most")
     ap.add_argument("--duration", type=float, default=5.0, help="c4: seconds of arrivals per rate")
     ap.add_argument("--slots", type=int, default=64, help="c4: server slots")
-    ap.add_argument("--epoch-iters", type=int, default=4, help="c4: iterations per epoch")
+    ap.add_argument("--epoch-iters", type=int, default=10, help="c4: iterations a request advances per epoch")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.workload == "seg":

@@ -268,6 +268,32 @@ qpso_status qpso_score_poses_noalloc(const float *d_mesh_soa, uint32_t num_faces
                                      const float *d_poses, uint32_t n, float *d_fit_out,
                                      uint32_t *d_flags_out, void *stream);
 
+/* Local refinement of a solved pose (no counterpart in the reference, whose
+ * answer is the PSO's global best, main.cu:1736-1757).  A deterministic
+ * pattern search around pose_in: each round scores `candidates` poses with
+ * the solver's render and fitness in `raster_mode` (default
+ * QPSO_RASTER_EDGE, the rasteriser's real triangle coverage): a step of
+ * +-step_t (m) along each axis, a rotation of about +-step_rot (rad) about
+ * each axis, and the rest random within those steps (a splitmix64 stream
+ * seeded by desc->seed and desc->stream); the best candidate replaces the
+ * pose when its fitness is lower, else both steps halve.  Rotations use
+ * dq = (1, a/2) renormalised, so every float operation is +, -, *, / or
+ * sqrt: the oracle replays the search bit for bit.  desc names the mesh,
+ * frame and cluster; its PSO fields and raster_mode are not read.
+ * pose_out and *fit_out receive the refined pose and its fitness in
+ * raster_mode; the solve's own result, the reference-parity trajectory,
+ * is untouched. */
+typedef struct {
+    uint32_t rounds;          /* 24 */
+    uint32_t candidates;      /* 64, at least 12 (the axis steps) */
+    float step_t;             /* 0.01 m */
+    float step_rot;           /* 0.2 rad */
+    uint32_t raster_mode;     /* QPSO_RASTER_EDGE */
+} qpso_refine_params;
+void qpso_refine_params_init(qpso_refine_params *p);
+qpso_status qpso_refine(qpso_context *ctx, const qpso_solve_desc *desc, const qpso_refine_params *prm,
+                        const float pose_in[7], float pose_out[7], float *fit_out);
+
 /* Render one pose of a mesh with the solver's rasteriser (renderFixedPointAABB,
  * main.h:1306-1491) into a window [x0,x0+w) x [y0,y0+h) of the raster
  * domain (int32 mm, 60000 where nothing was drawn) and return the render

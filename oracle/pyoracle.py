@@ -609,3 +609,78 @@ def segment_rgbd(bgr: np.ndarray, depth: np.ndarray, sp: SegParams | None = None
     clusters = seg_clusters(labels, len(lists), inp, v8, fp)
     return {"h": h8, "s": s8, "v": v8, "gray": gray, "smoothed": smoothed, "inpainted": inp,
             "saliency": sal, "labels": labels, "n_sets": len(lists), "clusters": clusters}
+
+
+# ---- post-PSO refinement (the search of qpso_refine, replayed) ----
+
+_MASK64 = (1 << 64) - 1
+
+
+def _splitmix64(state: int):
+    state = (state + 0x9E3779B97F4A7C15) & _MASK64
+    z = state
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK64
+    return state, z ^ (z >> 31)
+
+
+def _uniform_pm1(state: int):
+    state, z = _splitmix64(state)
+    u = np.float32(z >> 40) * np.float32(5.9604644775390625e-8)
+    return state, np.float32(u * np.float32(2.0) - np.float32(1.0))
+
+
+def _rotate_small(q, hx, hy, hz):
+    f = np.float32
+    a0, a1, a2, a3 = f(1.0), f(hx), f(hy), f(hz)
+    b0, b1, b2, b3 = (f(v) for v in q)
+    r = [f(f(f(a0 * b0 - a1 * b1) - a2 * b2) - a3 * b3),
+         f(f(f(a0 * b1 + a1 * b0) + a2 * b3) - a3 * b2),
+         f(f(f(a0 * b2 - a1 * b3) + a2 * b0) + a3 * b1),
+         f(f(f(a0 * b3 + a1 * b2) - a2 * b1) + a3 * b0)]
+    n = np.sqrt(f(f(f(r[0] * r[0] + r[1] * r[1]) + r[2] * r[2]) + r[3] * r[3]))
+    sgn = f(-1.0) if r[0] < 0 else f(1.0)
+    return [f(sgn * f(x / n)) for x in r]
+
+
+def refine(mesh, num_faces, obs, cam: Camera, prm: Params, pose0, seed: int, stream: int, rounds: int = 24,
+           candidates: int = 64, step_t: float = 0.01, step_rot: float = 0.2, mode: int = RASTER_EDGE):
+    """The oracle's replay of qpso_refine: the same candidates, scored by
+    the oracle's render and fitness in `mode`.  Returns (pose, fitness)."""
+    f = np.float32
+
+    def fitness(p):
+        zbuf, box, _ = render(mesh, num_faces, np.array(p, np.float32), cam, mode=mode)
+        return f(score(zbuf, box, obs, cam, prm).fit)
+
+    pose = [f(v) for v in pose0[:3]] + _rotate_small(pose0[3:], 0.0, 0.0, 0.0)
+    fit = fitness(pose)
+    rng = (seed ^ (stream << 32) ^ 0x5245464E45) & _MASK64
+    st, sr = f(step_t), f(step_rot)
+    for _ in range(rounds):
+        cands = []
+        for i in range(candidates):
+            c = list(pose)
+            if i < 6:
+                c[i // 2] = f(c[i // 2] + (-st if i & 1 else st))
+            elif i < 12:
+                h = [f(0.0)] * 3
+                h[(i - 6) // 2] = f((-sr if i & 1 else sr) * f(0.5))
+                c[3:] = _rotate_small(c[3:], *h)
+            else:
+                for k in range(3):
+                    rng, u = _uniform_pm1(rng)
+                    c[k] = f(c[k] + f(u * st))
+                h = []
+                for k in range(3):
+                    rng, u = _uniform_pm1(rng)
+                    h.append(f(f(u * sr) * f(0.5)))
+                c[3:] = _rotate_small(c[3:], *h)
+            cands.append(c)
+        fits = [fitness(c) for c in cands]
+        j = int(np.argmin(fits))  # first minimum
+        if fits[j] < fit:
+            fit, pose = fits[j], cands[j]
+        else:
+            st, sr = f(st * f(0.5)), f(sr * f(0.5))
+    return np.array(pose, np.float32), fit

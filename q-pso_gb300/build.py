@@ -27,9 +27,11 @@ FLAGS = ["-O3", "--fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"
          "-I", INCLUDE, "-I", CSRC]
 UNITS = ["qpso_kernels.cu", "qpso_api.cu", "qpso_noalloc.cu", "qpso_segment.cu", "qpso_seg_front.cu",
          "ingest.cpp"]
-# qpso_segment.cu's host code computes float expressions that must round like
-# the reference's on every host (no fused multiply-add on Arm either)
+# the host code of these units computes float expressions that must round
+# like the oracle's (or the reference's) on every host: no fused
+# multiply-add on Arm either
 UNIT_FLAGS = {"qpso_segment.cu": ["-Xcompiler", "-ffp-contract=off"],
+              "qpso_api.cu": ["-Xcompiler", "-ffp-contract=off"],
               "qpso_seg_front.cu": ["-Xcompiler", "-ffp-contract=off"]}
 HEADERS = ["qpso_device.cuh", "qpso_internal.cuh", "qpso_checks.h", "meshlets.h"]
 

@@ -1007,6 +1007,109 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
   return QPSO_OK;
 }
 
+void qpso_refine_params_init(qpso_refine_params* p) {
+  if (!p) return;
+  p->rounds = 24;
+  p->candidates = 64;
+  p->step_t = 0.01f;
+  p->step_rot = 0.2f;
+  p->raster_mode = QPSO_RASTER_EDGE;
+}
+
+}  // extern "C"
+
+namespace {
+
+// splitmix64 (Steele, Lea and Flood; the public-domain generator Vigna
+// recommends for seeding): the refinement's random candidates
+uint64_t splitmix64(uint64_t& state) {
+  state += 0x9E3779B97F4A7C15ull;
+  uint64_t z = state;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// a uniform float in [-1, 1): 24 random bits, exact in float
+float uniform_pm1(uint64_t& state) {
+  const float u = (float)(splitmix64(state) >> 40) * 5.9604644775390625e-8f;  // 2^-24
+  return u * 2.0f - 1.0f;
+}
+
+// q <- normalise(dq * q), dq = (1, hx, hy, hz), then the top hemisphere
+void rotate_small(float q[4], float hx, float hy, float hz) {
+  const float a0 = 1.0f, a1 = hx, a2 = hy, a3 = hz;
+  const float b0 = q[0], b1 = q[1], b2 = q[2], b3 = q[3];
+  float r[4];
+  r[0] = a0 * b0 - a1 * b1 - a2 * b2 - a3 * b3;
+  r[1] = a0 * b1 + a1 * b0 + a2 * b3 - a3 * b2;
+  r[2] = a0 * b2 - a1 * b3 + a2 * b0 + a3 * b1;
+  r[3] = a0 * b3 + a1 * b2 - a2 * b1 + a3 * b0;
+  const float n = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
+  const float sgn = r[0] < 0.0f ? -1.0f : 1.0f;
+  for (int k = 0; k < 4; ++k) q[k] = sgn * (r[k] / n);
+}
+
+}  // namespace
+
+extern "C" {
+
+qpso_status qpso_refine(qpso_context* ctx, const qpso_solve_desc* desc, const qpso_refine_params* prm,
+                        const float pose_in[7], float pose_out[7], float* fit_out) {
+  if (!ctx || !desc || !prm || !pose_in || !pose_out || !fit_out) return fail(ctx, QPSO_ERR_ARG, "null argument");
+  if (prm->candidates < 12 || prm->candidates > 4096 || prm->rounds > 4096 || !(prm->step_t >= 0.0f) ||
+      !(prm->step_rot >= 0.0f) || !std::isfinite(prm->step_t) || !std::isfinite(prm->step_rot) ||
+      (prm->raster_mode != QPSO_RASTER_REF && prm->raster_mode != QPSO_RASTER_EDGE))
+    return fail(ctx, QPSO_ERR_ARG, "bad refinement parameters");
+  for (int k = 0; k < 7; ++k)
+    if (!std::isfinite(pose_in[k])) return fail(ctx, QPSO_ERR_ARG, "non-finite pose");
+  qpso_solve_desc d = *desc;
+  d.raster_mode = prm->raster_mode;
+  float pose[7];
+  for (int k = 0; k < 3; ++k) pose[k] = pose_in[k];
+  for (int k = 0; k < 4; ++k) pose[3 + k] = pose_in[3 + k];
+  rotate_small(pose + 3, 0.0f, 0.0f, 0.0f);  // normalised, top hemisphere
+  float fit = 0.0f;
+  qpso_status st = qpso_score_poses(ctx, &d, pose, 1, &fit);
+  if (st != QPSO_OK) return st;
+  const uint32_t K = prm->candidates;
+  std::vector<float> cand((size_t)K * 7), fits(K);
+  uint64_t rng = desc->seed ^ ((uint64_t)desc->stream << 32) ^ 0x5245464E45ull;
+  float step_t = prm->step_t, step_r = prm->step_rot;
+  for (uint32_t r = 0; r < prm->rounds; ++r) {
+    for (uint32_t i = 0; i < K; ++i) {
+      float* c = &cand[(size_t)i * 7];
+      for (int k = 0; k < 7; ++k) c[k] = pose[k];
+      if (i < 6) {
+        c[i / 2] = c[i / 2] + ((i & 1) ? -step_t : step_t);
+      } else if (i < 12) {
+        float h[3] = {0.0f, 0.0f, 0.0f};
+        h[(i - 6) / 2] = ((i & 1) ? -step_r : step_r) * 0.5f;
+        rotate_small(c + 3, h[0], h[1], h[2]);
+      } else {
+        for (int k = 0; k < 3; ++k) c[k] = c[k] + uniform_pm1(rng) * step_t;
+        float h[3];
+        for (int k = 0; k < 3; ++k) h[k] = uniform_pm1(rng) * step_r * 0.5f;
+        rotate_small(c + 3, h[0], h[1], h[2]);
+      }
+    }
+    if ((st = qpso_score_poses(ctx, &d, cand.data(), K, fits.data())) != QPSO_OK) return st;
+    uint32_t j = 0;
+    for (uint32_t i = 1; i < K; ++i)
+      if (fits[i] < fits[j]) j = i;
+    if (fits[j] < fit) {
+      fit = fits[j];
+      for (int k = 0; k < 7; ++k) pose[k] = cand[(size_t)j * 7 + k];
+    } else {
+      step_t = step_t * 0.5f;
+      step_r = step_r * 0.5f;
+    }
+  }
+  for (int k = 0; k < 7; ++k) pose_out[k] = pose[k];
+  *fit_out = fit;
+  return QPSO_OK;
+}
+
 qpso_status qpso_render(qpso_context* ctx, uint32_t mesh_id, const qpso_camera* cam,
                         const float pose[7], int32_t x0, int32_t y0, int32_t w, int32_t h,
                         int32_t* depth_out, int32_t box_out[4]) {

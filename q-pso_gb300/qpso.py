@@ -36,6 +36,7 @@ EXPORTS = [
     "qpso_obj_load", "qpso_image_u16_load", "qpso_seg_params_init", "qpso_segment_num_edges",
     "qpso_segment_edge_ends", "qpso_segment_gauss_mask", "qpso_segment_edges", "qpso_segment_planes",
     "qpso_seg_front_params_init", "qpso_segment_rgbd", "qpso_segment_clusters", "qpso_image_bgr8_load",
+    "qpso_refine_params_init", "qpso_refine",
 ]
 
 
@@ -122,6 +123,11 @@ class SegFrameOut(C.Structure):
     _fields_ = [("h", C.c_void_p), ("s", C.c_void_p), ("v", C.c_void_p), ("gray", C.c_void_p),
                 ("smoothed", C.c_void_p), ("inpainted", C.c_void_p), ("saliency", C.c_void_p),
                 ("edges", C.c_void_p)]
+
+
+class RefineParams(C.Structure):
+    _fields_ = [("rounds", C.c_uint32), ("candidates", C.c_uint32), ("step_t", C.c_float),
+                ("step_rot", C.c_float), ("raster_mode", C.c_uint32)]
 
 
 class QpsoError(RuntimeError):
@@ -219,7 +225,7 @@ def load_library(path: str = LIB_PATH):
         if fn not in ("qpso_version", "qpso_destroy", "qpso_last_error", "qpso_solve_desc_init",
                       "qpso_box_from_centroid", "qpso_host_alloc", "qpso_host_free",
                       "qpso_get_stream", "qpso_seg_params_init", "qpso_segment_num_edges",
-                      "qpso_seg_front_params_init"):
+                      "qpso_seg_front_params_init", "qpso_refine_params_init"):
             getattr(L, fn).restype = C.c_int32
     _lib = L
     return L
@@ -359,6 +365,16 @@ class Context:
         self._check(self.L.qpso_score_poses(self.h, C.byref(desc), p.ctypes.data, p.shape[0],
                                             out.ctypes.data))
         return out
+
+    def refine(self, desc: SolveDesc, pose, params: "RefineParams | None" = None):
+        """Local refinement of a pose (qpso_refine): (pose float32[7], fitness)."""
+        prm = params if params is not None else refine_params()
+        p = _f32(pose)
+        out = np.zeros(7, np.float32)
+        fit = C.c_float()
+        self._check(self.L.qpso_refine(self.h, C.byref(desc), C.byref(prm), p.ctypes.data, out.ctypes.data,
+                                       C.byref(fit)))
+        return out, fit.value
 
     def render(self, mesh_id: int, cam: Camera, pose, x0: int, y0: int, w: int, h: int):
         out = np.zeros((h, w), np.int32)
@@ -613,6 +629,15 @@ def seg_params(**kw) -> SegParams:
     """The reference main's segmentation constants, fields overridden by kw."""
     p = SegParams()
     load_library().qpso_seg_params_init(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def refine_params(**kw) -> RefineParams:
+    """The refinement's defaults (qpso_refine_params_init), overridden by kw."""
+    p = RefineParams()
+    load_library().qpso_refine_params_init(C.byref(p))
     for k, v in kw.items():
         setattr(p, k, v)
     return p
