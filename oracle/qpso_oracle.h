@@ -290,7 +290,9 @@ float qo_smooth_alfa(void);
 int32_t qo_depth_smooth(const uint16_t *d, int32_t W, int32_t H, float beta, float gamma,
                         uint16_t *out, uint8_t *c_out, float *r_out);
 void qo_resize_bilinear_u8(const uint8_t *src, int32_t sw, int32_t sh, uint8_t *dst, int32_t dw, int32_t dh);
-float qo_eikonal(int k1, float t1, int k2, float t2);
+float qo_eikonal2(float a, float b);
+/* arrival times of the masked pixels; Jacobi iterations used, or -1 */
+int32_t qo_telea_times(const uint8_t *mask, int32_t w, int32_t h, float *T);
 /* inpaints img where mask != 0 in place; returns the pixels filled */
 int32_t qo_telea(uint8_t *img, const uint8_t *mask, int32_t w, int32_t h, int32_t radius);
 /* small_out (optional, capacity (W/5 + 1) (H/5 + 1)): the shrunk 8-bit map after inpainting */

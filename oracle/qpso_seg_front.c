@@ -259,115 +259,36 @@ void qo_resize_bilinear_u8(const uint8_t *src, int32_t sw, int32_t sh, uint8_t *
     }
 }
 
-/* Telea's fast-marching inpainting (A. Telea, "An Image Inpainting
- * Technique Based on the Fast Marching Method", J. Graphics Tools 9(1),
- * 2004), as the reference calls it through cv::inpaint(INPAINT_TELEA) on
- * the 8-bit map.  Restated with these exact choices (DEVIATION, unpinned
- * against OpenCV's implementation):
- *   - flags: masked pixels INSIDE (T = 1e6), unmasked pixels with a masked
- *     4-neighbour BAND (T = 0), the rest KNOWN (T = 0);
- *   - the band is a priority queue ordered by (T, pixel index);
- *   - a popped pixel becomes KNOWN; each 4-neighbour n (up, left, down,
- *     right) that is not KNOWN gets T(n) = the minimum of the first-order
- *     upwind solutions over its four quadrants, from KNOWN neighbours only
- *     (|T1 - T2| >= 1: min + 1, else (T1 + T2 + sqrt(2 - (T1 - T2)^2)) / 2;
- *     one known neighbour: T + 1), and, when it was INSIDE, is inpainted
- *     (its own value not yet counted) and turns BAND:
- *   - inpaint(n): over every non-INSIDE pixel k != n with |n - k| <= radius
- *     (r = n - k): dir = |r . grad T(n)| / |r|, dst = 1 / |r|^2,
- *     lev = 1 / (1 + |T(k) - T(n)|), w = (dir dst) lev, value
- *     I(k) + grad I(k) . r; gradients by central differences over
- *     non-INSIDE neighbours, one-sided where one is missing, 0 where both
- *     are; the sums of w and w * value are accumulated in 32.32 fixed
- *     point (exact, order-free), and I(n) = round-half-even(sum / weights),
- *     saturated to 8 bits; with all weights 0, dir is taken as 1; with no
- *     usable neighbour, I(n) = 0. */
-typedef struct {
-    float t;
-    int32_t idx;
-} qo_hent;
-
-static int hless(qo_hent a, qo_hent b) { return a.t < b.t || (a.t == b.t && a.idx < b.idx); }
-
-typedef struct {
-    qo_hent *e;
-    int32_t *pos; /* heap slot of each pixel, -1 when absent */
-    int32_t n;
-} qo_heap;
-
-static void hswap(qo_heap *h, int32_t i, int32_t j)
+/* Telea's inpainting (A. Telea, "An Image Inpainting Technique Based on the
+ * Fast Marching Method", J. Graphics Tools 9(1), 2004), as the reference
+ * calls it through cv::inpaint(INPAINT_TELEA) on the 8-bit map, restated in
+ * an order that lets pixels at the same distance from the known region be
+ * filled together (DEVIATION, unpinned against OpenCV's implementation):
+ *   - arrival times T: 0 on known pixels, and on masked pixels the fixed
+ *     point of the first-order upwind update of |grad T| = 1 over the
+ *     4-neighbourhood (Jacobi iterations from +infinity: a = the smaller of
+ *     the left/right times, b = of the up/down times; |a - b| >= 1: the
+ *     smaller + 1, else (a + b + sqrt(2 - (a - b)^2)) / 2); the march's
+ *     own discretisation, without the march's order;
+ *   - masked pixels are filled in increasing T; a pixel at time L is
+ *     computed from the pixels with T < L only (the known ones and those
+ *     filled before), so all pixels at time L are independent;
+ *   - the value of pixel n: over every such pixel k != n with
+ *     |n - k| <= radius (r = n - k): dir = |r . grad T(n)| / |r|,
+ *     dst = 1 / |r|^2, lev = 1 / (1 + |T(k) - T(n)|), w = (dir dst) lev,
+ *     value I(k) + grad I(k) . r; grad T by central differences over the
+ *     finite neighbours, grad I over the neighbours with T < L (one-sided
+ *     where one is missing, 0 where both are); the sums of w and w * value
+ *     in 32.32 fixed point (exact, order-free); I(n) = round-half-even(sum /
+ *     weights), saturated to 8 bits; with all weights 0, dir is taken as 1;
+ *     with no usable pixel, 0;
+ *   - a masked pixel that no known pixel reaches (T infinite) stays 0. */
+float qo_eikonal2(float a, float b)
 {
-    qo_hent t = h->e[i];
-    h->e[i] = h->e[j];
-    h->e[j] = t;
-    h->pos[h->e[i].idx] = i;
-    h->pos[h->e[j].idx] = j;
-}
-
-static void hup(qo_heap *h, int32_t i)
-{
-    while (i > 0) {
-        const int32_t p = (i - 1) / 2;
-        if (!hless(h->e[i], h->e[p])) break;
-        hswap(h, i, p);
-        i = p;
-    }
-}
-
-static void hdown(qo_heap *h, int32_t i)
-{
-    for (;;) {
-        const int32_t l = 2 * i + 1, r = l + 1;
-        int32_t m = i;
-        if (l < h->n && hless(h->e[l], h->e[m])) m = l;
-        if (r < h->n && hless(h->e[r], h->e[m])) m = r;
-        if (m == i) break;
-        hswap(h, i, m);
-        i = m;
-    }
-}
-
-static void hset(qo_heap *h, int32_t idx, float t)
-{
-    int32_t i = h->pos[idx];
-    if (i < 0) {
-        i = h->n++;
-        h->e[i].idx = idx;
-        h->e[i].t = t;
-        h->pos[idx] = i;
-        hup(h, i);
-    } else {
-        const qo_hent old = h->e[i];
-        h->e[i].t = t;
-        if (hless(h->e[i], old))
-            hup(h, i);
-        else
-            hdown(h, i);
-    }
-}
-
-static qo_hent hpop(qo_heap *h)
-{
-    const qo_hent top = h->e[0];
-    hswap(h, 0, h->n - 1);
-    h->n--;
-    h->pos[top.idx] = -1;
-    if (h->n > 0) hdown(h, 0);
-    return top;
-}
-
-enum { QO_KNOWN = 0, QO_BAND = 1, QO_INSIDE = 2 };
-
-float qo_eikonal(int k1, float t1, int k2, float t2)
-{
-    if (k1 && k2) {
-        const float dt = t1 - t2;
-        if (fabsf(dt) >= 1.0f) return (t1 < t2 ? t1 : t2) + 1.0f;
-        return (t1 + t2 + sqrtf(2.0f - dt * dt)) * 0.5f;
-    }
-    if (k1) return t1 + 1.0f;
-    if (k2) return t2 + 1.0f;
-    return 1e6f;
+    if (a == INFINITY && b == INFINITY) return INFINITY;
+    const float d = a - b;
+    if (fabsf(d) >= 1.0f) return (a < b ? a : b) + 1.0f;
+    return (a + b + sqrtf(2.0f - d * d)) * 0.5f;
 }
 
 /* gradient of a field along one axis at a pixel, from its two neighbours
@@ -382,14 +303,16 @@ static float grad1(int km, float am, int kp, float ap, float a0)
 
 static const double kFix = 4294967296.0; /* 2^32 */
 
-static uint8_t telea_value(const uint8_t *img, const uint8_t *flag, const float *T, int32_t w, int32_t h,
-                           int32_t x, int32_t y, int32_t rad)
+/* the value of pixel (x, y) at arrival time L = T[p] */
+static uint8_t telea_value(const uint8_t *img, const float *T, int32_t w, int32_t h, int32_t x, int32_t y,
+                           int32_t rad)
 {
     const size_t p = (size_t)y * w + x;
-    const int kxm = x > 0 && flag[p - 1] != QO_INSIDE, kxp = x + 1 < w && flag[p + 1] != QO_INSIDE;
-    const int kym = y > 0 && flag[p - w] != QO_INSIDE, kyp = y + 1 < h && flag[p + w] != QO_INSIDE;
-    const float gtx = grad1(kxm, kxm ? T[p - 1] : 0.0f, kxp, kxp ? T[p + 1] : 0.0f, T[p]);
-    const float gty = grad1(kym, kym ? T[p - w] : 0.0f, kyp, kyp ? T[p + w] : 0.0f, T[p]);
+    const float L = T[p];
+    const int fxm = x > 0 && T[p - 1] != INFINITY, fxp = x + 1 < w && T[p + 1] != INFINITY;
+    const int fym = y > 0 && T[p - w] != INFINITY, fyp = y + 1 < h && T[p + w] != INFINITY;
+    const float gtx = grad1(fxm, fxm ? T[p - 1] : 0.0f, fxp, fxp ? T[p + 1] : 0.0f, L);
+    const float gty = grad1(fym, fym ? T[p - w] : 0.0f, fyp, fyp ? T[p + w] : 0.0f, L);
     for (int pass = 0; pass < 2; ++pass) {
         int64_t num = 0, den = 0;
         for (int32_t dy = -rad; dy <= rad; ++dy)
@@ -399,16 +322,16 @@ static uint8_t telea_value(const uint8_t *img, const uint8_t *flag, const float 
                 const int32_t kx = x + dx, ky = y + dy;
                 if (kx < 0 || kx >= w || ky < 0 || ky >= h) continue;
                 const size_t k = (size_t)ky * w + kx;
-                if (flag[k] == QO_INSIDE) continue;
+                if (!(T[k] < L)) continue;
                 const int32_t rx = -dx, ry = -dy;
                 const float len2 = (float)(rx * rx + ry * ry);
                 const float len = sqrtf(len2);
                 const float dir = pass == 0 ? fabsf((float)rx * gtx + (float)ry * gty) / len : 1.0f;
                 const float dst = 1.0f / len2;
-                const float lev = 1.0f / (1.0f + fabsf(T[k] - T[p]));
+                const float lev = 1.0f / (1.0f + fabsf(T[k] - L));
                 const float wt = (dir * dst) * lev;
-                const int ixm = kx > 0 && flag[k - 1] != QO_INSIDE, ixp = kx + 1 < w && flag[k + 1] != QO_INSIDE;
-                const int iym = ky > 0 && flag[k - w] != QO_INSIDE, iyp = ky + 1 < h && flag[k + w] != QO_INSIDE;
+                const int ixm = kx > 0 && T[k - 1] < L, ixp = kx + 1 < w && T[k + 1] < L;
+                const int iym = ky > 0 && T[k - w] < L, iyp = ky + 1 < h && T[k + w] < L;
                 const float a0 = (float)img[k];
                 const float gix = grad1(ixm, ixm ? (float)img[k - 1] : 0.0f, ixp, ixp ? (float)img[k + 1] : 0.0f, a0);
                 const float giy = grad1(iym, iym ? (float)img[k - w] : 0.0f, iyp, iyp ? (float)img[k + w] : 0.0f, a0);
@@ -424,71 +347,75 @@ static uint8_t telea_value(const uint8_t *img, const uint8_t *flag, const float 
     return 0;
 }
 
+/* arrival times of the masked pixels (T, w * h); returns the Jacobi
+ * iterations used, or -1 without convergence within 4 (w + h) + 8 */
+int32_t qo_telea_times(const uint8_t *mask, int32_t w, int32_t h, float *T)
+{
+    const size_t n = (size_t)w * h;
+    float *U = (float *)malloc(n * sizeof(float));
+    if (!U) return -1;
+    for (size_t i = 0; i < n; ++i) T[i] = mask[i] ? INFINITY : 0.0f;
+    const int32_t cap = 4 * (w + h) + 8;
+    int32_t it = 0;
+    for (;;) {
+        int changed = 0;
+        for (int32_t y = 0; y < h; ++y)
+            for (int32_t x = 0; x < w; ++x) {
+                const size_t p = (size_t)y * w + x;
+                if (!mask[p]) {
+                    U[p] = 0.0f;
+                    continue;
+                }
+                const float l = x > 0 ? T[p - 1] : INFINITY, r = x + 1 < w ? T[p + 1] : INFINITY;
+                const float u = y > 0 ? T[p - w] : INFINITY, d = y + 1 < h ? T[p + w] : INFINITY;
+                const float a = l < r ? l : r, b = u < d ? u : d;
+                U[p] = qo_eikonal2(a, b);
+                changed |= U[p] != T[p];
+            }
+        memcpy(T, U, n * sizeof(float));
+        ++it;
+        if (!changed) break;
+        if (it > cap) {
+            free(U);
+            return -1;
+        }
+    }
+    free(U);
+    return it;
+}
+
 int32_t qo_telea(uint8_t *img, const uint8_t *mask, int32_t w, int32_t h, int32_t radius)
 {
     if (w <= 0 || h <= 0 || radius < 1) return -1;
     const size_t n = (size_t)w * h;
-    uint8_t *flag = (uint8_t *)malloc(n);
     float *T = (float *)malloc(n * sizeof(float));
-    qo_heap hp;
-    hp.e = (qo_hent *)malloc(n * sizeof(qo_hent));
-    hp.pos = (int32_t *)malloc(n * sizeof(int32_t));
-    hp.n = 0;
-    if (!flag || !T || !hp.e || !hp.pos) {
-        free(flag); free(T); free(hp.e); free(hp.pos);
+    if (!T) return -1;
+    if (qo_telea_times(mask, w, h, T) < 0) {
+        free(T);
         return -1;
     }
-    for (size_t i = 0; i < n; ++i) {
-        flag[i] = mask[i] ? QO_INSIDE : QO_KNOWN;
-        T[i] = mask[i] ? 1e6f : 0.0f;
-        hp.pos[i] = -1;
-    }
-    for (int32_t y = 0; y < h; ++y)
-        for (int32_t x = 0; x < w; ++x) {
-            const size_t p = (size_t)y * w + x;
-            if (mask[p]) continue;
-            const int adj = (y > 0 && mask[p - w]) || (x > 0 && mask[p - 1]) || (y + 1 < h && mask[p + w]) ||
-                            (x + 1 < w && mask[p + 1]);
-            if (adj) {
-                flag[p] = QO_BAND;
-                hset(&hp, (int32_t)p, 0.0f);
-            }
-        }
+    for (size_t i = 0; i < n; ++i)
+        if (mask[i]) img[i] = 0;
     int32_t filled = 0;
-    while (hp.n > 0) {
-        const qo_hent top = hpop(&hp);
-        const int32_t p = top.idx;
-        flag[p] = QO_KNOWN;
-        const int32_t px = p % w, py = p / w;
-        const int32_t nx[4] = {px, px - 1, px, px + 1}, ny[4] = {py - 1, py, py + 1, py};
-        for (int j = 0; j < 4; ++j) {
-            const int32_t x = nx[j], y = ny[j];
-            if (x < 0 || x >= w || y < 0 || y >= h) continue;
-            const size_t q = (size_t)y * w + x;
-            if (flag[q] == QO_KNOWN) continue;
-            /* T from the KNOWN neighbours, quadrants (up,left) (down,left) (up,right) (down,right) */
-            const int ku = y > 0 && flag[q - w] == QO_KNOWN, kd = y + 1 < h && flag[q + w] == QO_KNOWN;
-            const int kl = x > 0 && flag[q - 1] == QO_KNOWN, kr = x + 1 < w && flag[q + 1] == QO_KNOWN;
-            const float tu = ku ? T[q - w] : 0.0f, td = kd ? T[q + w] : 0.0f;
-            const float tl = kl ? T[q - 1] : 0.0f, tr = kr ? T[q + 1] : 0.0f;
-            float t = qo_eikonal(ku, tu, kl, tl);
-            float t2 = qo_eikonal(kd, td, kl, tl);
-            if (t2 < t) t = t2;
-            t2 = qo_eikonal(ku, tu, kr, tr);
-            if (t2 < t) t = t2;
-            t2 = qo_eikonal(kd, td, kr, tr);
-            if (t2 < t) t = t2;
-            T[q] = t;
-            if (flag[q] == QO_INSIDE) {
-                /* inpainted while still INSIDE (its own value is not used), then BAND */
-                img[q] = telea_value(img, flag, T, w, h, x, y, radius);
-                flag[q] = QO_BAND;
-                ++filled;
+    float last = 0.0f;
+    for (;;) {
+        /* the next arrival time */
+        float L = INFINITY;
+        for (size_t i = 0; i < n; ++i)
+            if (mask[i] && T[i] > last && T[i] < L) L = T[i];
+        if (L == INFINITY) break;
+        /* its pixels read only pixels of smaller time: fill them in place */
+        for (int32_t y = 0; y < h; ++y)
+            for (int32_t x = 0; x < w; ++x) {
+                const size_t p = (size_t)y * w + x;
+                if (mask[p] && T[p] == L) {
+                    img[p] = telea_value(img, T, w, h, x, y, radius);
+                    ++filled;
+                }
             }
-            hset(&hp, (int32_t)q, t);
-        }
+        last = L;
     }
-    free(flag); free(T); free(hp.e); free(hp.pos);
+    free(T);
     return filled;
 }
 

@@ -292,49 +292,31 @@ __global__ void inpaint_shrink_kernel(const uint16_t* __restrict__ sm, const uin
   }
 }
 
-// Telea's fast-marching inpainting of the shrunk map's zero pixels, in one
-// CTA: thread 0 runs the band's priority queue, the whole CTA computes each
-// inpainted value (its weighted sum over the disc of `radius`, in 32.32
-// fixed point so that the sum does not depend on the order of terms).  The
-// state (flags, arrival times T, the map, the queue and every pixel's
-// queue slot) lives in shared memory when it fits, else in global memory.
-enum : uint8_t { kKnown = 0, kBand = 1, kInside = 2 };
-
+// Telea's inpainting of the shrunk map's zero pixels, by arrival time: the
+// times T are the fixed point of the upwind eikonal update (Jacobi
+// iterations), and the masked pixels are filled in increasing T, each from
+// the pixels of smaller T, so that every pixel at one time is independent:
+// the CTA finds the next time, lists its pixels, and each warp fills one
+// pixel (its lanes share the disc of `radius`; the sums are in 32.32 fixed
+// point, so they do not depend on the order of terms).  One CTA; the
+// state (times, their next iterate, the map, the list) lives in shared
+// memory when it fits, else in global memory.
 struct TeleaMem {
-  uint8_t* flag;
-  uint8_t* img;
   float* T;
-  float* ht;     // queue entries: arrival time
-  int32_t* hi;   // queue entries: pixel
-  int32_t* pos;  // queue slot of each pixel, -1 when absent
-  short2* off;   // disc offsets
+  float* U;
+  uint8_t* img;
+  int32_t* list;
+  short2* off;   // the disc's offsets, raster order
+  float* olen;   // |offset| and 1 / |offset|^2 (they depend on the offset only)
+  float* odst;
 };
 
-__device__ __forceinline__ bool tless(float ta, int32_t ia, float tb, int32_t ib) {
-  return ta < tb || (ta == tb && ia < ib);
-}
-
-// warp-wide minimum by (T, pixel index); lane 0 ends with it
-__device__ __forceinline__ void warp_argmin(float& t, int32_t& i) {
-  for (int s = 16; s > 0; s >>= 1) {
-    const float ot = __shfl_down_sync(0xffffffffu, t, s);
-    const int32_t oi = __shfl_down_sync(0xffffffffu, i, s);
-    if (tless(ot, oi, t, i)) {
-      t = ot;
-      i = oi;
-    }
-  }
-}
-
-__device__ __forceinline__ float eikonal(bool k1, float t1, bool k2, float t2) {
-  if (k1 && k2) {
-    const float dt = __fsub_rn(t1, t2);
-    if (fabsf(dt) >= 1.0f) return __fadd_rn(t1 < t2 ? t1 : t2, 1.0f);
-    return __fmul_rn(__fadd_rn(__fadd_rn(t1, t2), __fsqrt_rn(__fsub_rn(2.0f, __fmul_rn(dt, dt)))), 0.5f);
-  }
-  if (k1) return __fadd_rn(t1, 1.0f);
-  if (k2) return __fadd_rn(t2, 1.0f);
-  return 1e6f;
+__device__ __forceinline__ float eikonal2(float a, float b) {
+  const float inf = __int_as_float(0x7f800000);
+  if (a == inf && b == inf) return inf;
+  const float d = __fsub_rn(a, b);
+  if (fabsf(d) >= 1.0f) return __fadd_rn(a < b ? a : b, 1.0f);
+  return __fmul_rn(__fadd_rn(__fadd_rn(a, b), __fsqrt_rn(__fsub_rn(2.0f, __fmul_rn(d, d)))), 0.5f);
 }
 
 __device__ __forceinline__ float grad1(bool km, float am, bool kp, float ap, float a0) {
@@ -344,27 +326,25 @@ __device__ __forceinline__ float grad1(bool km, float am, bool kp, float ap, flo
   return 0.0f;
 }
 
-// Partial sums of one inpainted value over this thread's disc offsets.
-__device__ void telea_terms(const TeleaMem& m, int32_t w, int32_t h, int32_t x, int32_t y, float gtx, float gty,
-                            int n_off, bool unit_dir, long long& num, long long& den) {
-  const size_t p = (size_t)y * w + x;
-  const float tp = m.T[p];
-  for (int o = threadIdx.x; o < n_off; o += blockDim.x) {
+// This lane's partial sums of pixel (x, y)'s value over its share of the disc.
+__device__ void telea_terms(const TeleaMem& m, int32_t w, int32_t h, int32_t x, int32_t y, float L, float gtx,
+                            float gty, int n_off, bool unit_dir, long long& num, long long& den) {
+  for (int o = threadIdx.x & 31; o < n_off; o += 32) {
     const int32_t dx = m.off[o].x, dy = m.off[o].y;
     const int32_t kx = x + dx, ky = y + dy;
     if (kx < 0 || kx >= w || ky < 0 || ky >= h) continue;
     const size_t k = (size_t)ky * w + kx;
-    if (m.flag[k] == kInside) continue;
+    const float tk = m.T[k];
+    if (!(tk < L)) continue;
     const int32_t rx = -dx, ry = -dy;
-    const float len2 = (float)(rx * rx + ry * ry);
-    const float len = __fsqrt_rn(len2);
-    const float dir =
-        unit_dir ? 1.0f : __fdiv_rn(fabsf(__fadd_rn(__fmul_rn((float)rx, gtx), __fmul_rn((float)ry, gty))), len);
-    const float dst = __fdiv_rn(1.0f, len2);
-    const float lev = __fdiv_rn(1.0f, __fadd_rn(1.0f, fabsf(__fsub_rn(m.T[k], tp))));
+    const float dir = unit_dir ? 1.0f
+                               : __fdiv_rn(fabsf(__fadd_rn(__fmul_rn((float)rx, gtx), __fmul_rn((float)ry, gty))),
+                                           m.olen[o]);
+    const float dst = m.odst[o];
+    const float lev = __fdiv_rn(1.0f, __fadd_rn(1.0f, fabsf(__fsub_rn(tk, L))));
     const float wt = __fmul_rn(__fmul_rn(dir, dst), lev);
-    const bool ixm = kx > 0 && m.flag[k - 1] != kInside, ixp = kx + 1 < w && m.flag[k + 1] != kInside;
-    const bool iym = ky > 0 && m.flag[k - w] != kInside, iyp = ky + 1 < h && m.flag[k + w] != kInside;
+    const bool ixm = kx > 0 && m.T[k - 1] < L, ixp = kx + 1 < w && m.T[k + 1] < L;
+    const bool iym = ky > 0 && m.T[k - w] < L, iyp = ky + 1 < h && m.T[k + w] < L;
     const float a0 = (float)m.img[k];
     const float gix = grad1(ixm, ixm ? (float)m.img[k - 1] : 0.0f, ixp, ixp ? (float)m.img[k + 1] : 0.0f, a0);
     const float giy = grad1(iym, iym ? (float)m.img[k - w] : 0.0f, iyp, iyp ? (float)m.img[k + w] : 0.0f, a0);
@@ -376,227 +356,138 @@ __device__ void telea_terms(const TeleaMem& m, int32_t w, int32_t h, int32_t x, 
   }
 }
 
-__device__ void block_sum2(long long& a, long long& b, long long* red) {
-  for (int s = 16; s > 0; s >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, s);
-    b += __shfl_down_sync(0xffffffffu, b, s);
-  }
-  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    red[2 * wid] = a;
-    red[2 * wid + 1] = b;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    long long sa = 0, sb = 0;
-    for (int i = 0; i < nw; ++i) {
-      sa += red[2 * i];
-      sb += red[2 * i + 1];
-    }
-    red[64] = sa;
-    red[65] = sb;
-  }
-  __syncthreads();
-  a = red[64];
-  b = red[65];
-}
-
-__global__ void __launch_bounds__(512) telea_kernel(uint8_t* __restrict__ img_io, const uint32_t* misc,
-                                                     int32_t w, int32_t h, int32_t radius, int n_off,
-                                                     unsigned char* __restrict__ gmem, int use_smem) {
+__global__ void __launch_bounds__(1024) telea_kernel(uint8_t* __restrict__ img_io, const uint32_t* misc,
+                                                      int32_t w, int32_t h, int32_t radius, int n_off,
+                                                      unsigned char* __restrict__ gmem, int use_smem) {
   extern __shared__ __align__(16) unsigned char tsm[];
-  __shared__ long long red[66];
-  __shared__ int32_t s_q;
-  __shared__ float s_gtx, s_gty;
+  __shared__ uint32_t s_min[32];
+  __shared__ uint32_t s_L, s_cnt;
   if (misc[3] == misc[2]) return;  // flat depth: nothing is filled
   const size_t n = (size_t)w * h;
   unsigned char* base = use_smem ? tsm : gmem;
-  // layout: offsets | T | ht | hi | pos | flag | img
+  // layout: offsets | lengths | 1 / lengths^2 | T | U | list | img
   TeleaMem m;
   size_t o = 0;
+  const size_t ob = ((size_t)n_off * 4 + 15) & ~(size_t)15;
   m.off = reinterpret_cast<short2*>(base + o);
-  o += ((size_t)n_off * sizeof(short2) + 15) & ~(size_t)15;
+  m.olen = reinterpret_cast<float*>(base + o + ob);
+  m.odst = reinterpret_cast<float*>(base + o + 2 * ob);
+  o += 3 * ob;
   m.T = reinterpret_cast<float*>(base + o);
   o += (n * 4 + 15) & ~(size_t)15;
-  m.ht = reinterpret_cast<float*>(base + o);
+  m.U = reinterpret_cast<float*>(base + o);
   o += (n * 4 + 15) & ~(size_t)15;
-  m.hi = reinterpret_cast<int32_t*>(base + o);
+  m.list = reinterpret_cast<int32_t*>(base + o);
   o += (n * 4 + 15) & ~(size_t)15;
-  m.pos = reinterpret_cast<int32_t*>(base + o);
-  o += (n * 4 + 15) & ~(size_t)15;
-  m.flag = base + o;
-  o += (n + 15) & ~(size_t)15;
   m.img = base + o;
-  // disc offsets in raster order
-  if (threadIdx.x == 0) {
+  const float inf = __int_as_float(0x7f800000);
+  const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = T >> 5;
+  if (tid == 0) {  // disc offsets in raster order
     int k = 0;
     for (int32_t dy = -radius; dy <= radius; ++dy)
       for (int32_t dx = -radius; dx <= radius; ++dx)
         if ((dx || dy) && dx * dx + dy * dy <= radius * radius) m.off[k++] = make_short2((short)dx, (short)dy);
   }
-  for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+  __syncthreads();
+  for (int k = tid; k < n_off; k += T) {
+    const float len2 = (float)(m.off[k].x * m.off[k].x + m.off[k].y * m.off[k].y);
+    m.olen[k] = __fsqrt_rn(len2);
+    m.odst[k] = __fdiv_rn(1.0f, len2);
+  }
+  for (size_t i = tid; i < n; i += T) {
     const uint8_t v = img_io[i];
     m.img[i] = v;
-    m.flag[i] = v == 0 ? kInside : kKnown;
-    m.T[i] = v == 0 ? 1e6f : 0.0f;
-    m.pos[i] = -1;
+    m.T[i] = v == 0 ? inf : 0.0f;
   }
   __syncthreads();
-  // The initial band: known pixels with an unknown 4-neighbour, all at T = 0.
-  // Listed in pixel order they form a valid queue (equal times, increasing
-  // index), so each chunk of pixels is counted, then written at its offset.
-  __shared__ int32_t s_cnt[512 + 1];
-  int32_t hn = 0;  // queue length (thread 0)
-  {
-    const int T = blockDim.x;
-    const size_t chunk = (n + T - 1) / T;
-    const size_t b0 = threadIdx.x * chunk, b1 = b0 + chunk < n ? b0 + chunk : n;
-    auto is_band = [&](size_t p) {
-      if (m.flag[p] == kInside) return false;
-      const int32_t y = (int32_t)(p / w), x = (int32_t)(p - (size_t)y * w);
-      return (y > 0 && m.flag[p - w] == kInside) || (x > 0 && m.flag[p - 1] == kInside) ||
-             (y + 1 < h && m.flag[p + w] == kInside) || (x + 1 < w && m.flag[p + 1] == kInside);
-    };
-    int32_t c = 0;
-    for (size_t p = b0; p < b1; ++p) c += is_band(p);
-    s_cnt[threadIdx.x + 1] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      s_cnt[0] = 0;
-      for (int i = 1; i <= T; ++i) s_cnt[i] += s_cnt[i - 1];
-    }
-    __syncthreads();
-    int32_t at = s_cnt[threadIdx.x];
-    for (size_t p = b0; p < b1; ++p)
-      if (is_band(p)) {
-        m.ht[at] = 0.0f;
-        m.hi[at] = (int32_t)p;
-        m.pos[p] = at;
-        ++at;
+  // arrival times: Jacobi iterations of the upwind update to the fixed point
+  const int cap = 4 * (w + h) + 8;
+  bool converged = false;
+  for (int it = 0; it <= cap; ++it) {
+    int changed = 0;
+    for (size_t p = tid; p < n; p += T) {
+      float v = 0.0f;
+      if (m.img[p] == 0) {
+        const int32_t y = (int32_t)(p / w), x = (int32_t)(p - (size_t)y * w);
+        const float l = x > 0 ? m.T[p - 1] : inf, r = x + 1 < w ? m.T[p + 1] : inf;
+        const float u = y > 0 ? m.T[p - w] : inf, d = y + 1 < h ? m.T[p + w] : inf;
+        v = eikonal2(l < r ? l : r, u < d ? u : d);
+        changed |= v != m.T[p];
       }
-    __syncthreads();
-    for (size_t p = b0; p < b1; ++p)
-      if (m.pos[p] >= 0) m.flag[p] = kBand;
-    hn = s_cnt[T];
+      m.U[p] = v;
+    }
+    changed = __syncthreads_or(changed);
+    float* t = m.T;
+    m.T = m.U;
+    m.U = t;
+    if (!changed) {
+      converged = true;
+      break;
+    }
   }
-  // The band is an unordered list (ht/hi, s_B entries; pos: each pixel's
-  // slot).  Each step the whole CTA finds its first pixel by (T, pixel
-  // index) -- a total order, so the steps are those of any exact priority
-  // queue -- and thread 0 updates the list and the neighbours.
-  __shared__ float s_wt[32];
-  __shared__ int32_t s_wi[32];
-  __shared__ int32_t s_B;
-  if (threadIdx.x == 0) s_B = hn;
-  int32_t cur = -1, nb = 4;  // thread 0: the popped pixel and its next neighbour
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();
+  if (!converged) return;  // cannot happen: the iterates only fall (as the oracle, nothing is filled)
+  // the masked pixels, level by level in increasing arrival time; the map
+  // still holds 0 there, so a pixel is masked exactly when T > 0
+  float last = 0.0f;
   for (;;) {
-    const int32_t B = s_B;
-    if (B == 0) break;
-    float bt = __int_as_float(0x7f800000);
-    int32_t bi = 0x7fffffff;
-    for (int32_t i = threadIdx.x; i < B; i += blockDim.x) {
-      const float t = m.ht[i];
-      const int32_t x = m.hi[i];
-      if (tless(t, x, bt, bi)) {
-        bt = t;
-        bi = x;
-      }
+    uint32_t lo = 0x7f800000u;  // the next time (non-negative floats order as their bits)
+    for (size_t p = tid; p < n; p += T) {
+      const float t = m.T[p];
+      if (t > last) lo = min(lo, __float_as_uint(t));
     }
-    warp_argmin(bt, bi);
-    if (lane == 0) {
-      s_wt[wid] = bt;
-      s_wi[wid] = bi;
-    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    if (lane == 0) s_min[wid] = lo;
+    if (tid == 0) s_cnt = 0;
     __syncthreads();
     if (wid == 0) {
-      bt = lane < nw ? s_wt[lane] : __int_as_float(0x7f800000);
-      bi = lane < nw ? s_wi[lane] : 0x7fffffff;
-      warp_argmin(bt, bi);
-      if (lane == 0) {
-        cur = bi;
-        const int32_t slot = m.pos[cur], last = B - 1;
-        if (slot != last) {
-          m.ht[slot] = m.ht[last];
-          m.hi[slot] = m.hi[last];
-          m.pos[m.hi[slot]] = slot;
-        }
-        m.pos[cur] = -1;
-        s_B = last;
-        m.flag[cur] = kKnown;
-        nb = 0;
-      }
+      uint32_t v = lane < nw ? s_min[lane] : 0x7f800000u;
+      v = __reduce_min_sync(0xffffffffu, v);
+      if (lane == 0) s_L = v;
     }
-    // thread 0 walks the popped pixel's neighbours (up, left, down, right);
-    // each one that was INSIDE is inpainted by the whole CTA before the next
-    for (;;) {
-      if (threadIdx.x == 0) {
-        s_q = -1;
-        while (nb < 4) {
-          const int32_t px = cur % w, py = cur / w;
-          const int32_t j = nb++;
-          const int32_t x = j == 1 ? px - 1 : j == 3 ? px + 1 : px;
-          const int32_t y = j == 0 ? py - 1 : j == 2 ? py + 1 : py;
-          if (x < 0 || x >= w || y < 0 || y >= h) continue;
-          const size_t q = (size_t)y * w + x;
-          if (m.flag[q] == kKnown) continue;
-          const bool ku = y > 0 && m.flag[q - w] == kKnown, kd = y + 1 < h && m.flag[q + w] == kKnown;
-          const bool kl = x > 0 && m.flag[q - 1] == kKnown, kr = x + 1 < w && m.flag[q + 1] == kKnown;
-          const float tu = ku ? m.T[q - w] : 0.0f, td = kd ? m.T[q + w] : 0.0f;
-          const float tl = kl ? m.T[q - 1] : 0.0f, tr = kr ? m.T[q + 1] : 0.0f;
-          float t = eikonal(ku, tu, kl, tl);
-          float t2 = eikonal(kd, td, kl, tl);
-          if (t2 < t) t = t2;
-          t2 = eikonal(ku, tu, kr, tr);
-          if (t2 < t) t = t2;
-          t2 = eikonal(kd, td, kr, tr);
-          if (t2 < t) t = t2;
-          m.T[q] = t;
-          // into the band, or its time updated in place
-          if (m.pos[q] < 0) {
-            const int32_t slot = s_B++;
-            m.ht[slot] = t;
-            m.hi[slot] = (int32_t)q;
-            m.pos[q] = slot;
-          } else {
-            m.ht[m.pos[q]] = t;
-          }
-          if (m.flag[q] == kInside) {
-            // inpainted while still INSIDE (its own value is not used), then
-            // BAND; the arrival-time gradient at q over its non-INSIDE neighbours
-            const bool kxm = x > 0 && m.flag[q - 1] != kInside, kxp = x + 1 < w && m.flag[q + 1] != kInside;
-            const bool kym = y > 0 && m.flag[q - w] != kInside, kyp = y + 1 < h && m.flag[q + w] != kInside;
-            s_gtx = grad1(kxm, kxm ? m.T[q - 1] : 0.0f, kxp, kxp ? m.T[q + 1] : 0.0f, t);
-            s_gty = grad1(kym, kym ? m.T[q - w] : 0.0f, kyp, kyp ? m.T[q + w] : 0.0f, t);
-            s_q = (int32_t)q;
-            break;
-          }
-        }
-      }
-      __syncthreads();
-      const int32_t q = s_q;
-      if (q < 0) break;
+    __syncthreads();
+    const float L = __uint_as_float(s_L);
+    if (L == inf) break;
+    for (size_t p0 = (size_t)(tid & ~31); p0 < n; p0 += T) {  // whole warps: list the level's pixels
+      const size_t p = p0 + lane;
+      const bool on = p < n && m.T[p] == L;
+      const unsigned bal = __ballot_sync(0xffffffffu, on);
+      uint32_t at = 0;
+      if (lane == 0 && bal) at = atomicAdd(&s_cnt, (uint32_t)__popc(bal));
+      at = __shfl_sync(0xffffffffu, at, 0);
+      if (on) m.list[at + __popc(bal & ((1u << lane) - 1u))] = (int32_t)p;
+    }
+    __syncthreads();
+    const uint32_t cnt = s_cnt;
+    for (uint32_t i = wid; i < cnt; i += nw) {
+      const int32_t q = m.list[i];
       const int32_t qx = q % w, qy = q / w;
+      const bool fxm = qx > 0 && m.T[q - 1] != inf, fxp = qx + 1 < w && m.T[q + 1] != inf;
+      const bool fym = qy > 0 && m.T[q - w] != inf, fyp = qy + 1 < h && m.T[q + w] != inf;
+      const float gtx = grad1(fxm, fxm ? m.T[q - 1] : 0.0f, fxp, fxp ? m.T[q + 1] : 0.0f, L);
+      const float gty = grad1(fym, fym ? m.T[q - w] : 0.0f, fyp, fyp ? m.T[q + w] : 0.0f, L);
       uint8_t val = 0;
-      bool set = false;
-      for (int pass = 0; pass < 2 && !set; ++pass) {
+      for (int pass = 0; pass < 2; ++pass) {
         long long num = 0, den = 0;
-        telea_terms(m, w, h, qx, qy, s_gtx, s_gty, n_off, pass == 1, num, den);
-        block_sum2(num, den, red);
+        telea_terms(m, w, h, qx, qy, L, gtx, gty, n_off, pass == 1, num, den);
+        for (int sft = 16; sft > 0; sft >>= 1) {
+          num += __shfl_down_sync(0xffffffffu, num, sft);
+          den += __shfl_down_sync(0xffffffffu, den, sft);
+        }
+        den = __shfl_sync(0xffffffffu, den, 0);
+        num = __shfl_sync(0xffffffffu, num, 0);
         if (den > 0) {
           const double v = rint((double)num / (double)den);
           val = (uint8_t)(v < 0.0 ? 0.0 : v > 255.0 ? 255.0 : v);
-          set = true;
+          break;
         }
       }
-      if (threadIdx.x == 0) {
-        m.img[q] = val;
-        m.flag[q] = kBand;
-      }
-      __syncthreads();
+      // the level's own pixels are not read while it is filled (T < L only)
+      if (lane == 0) m.img[q] = val;
     }
+    __syncthreads();
+    last = L;
   }
-  for (size_t i = threadIdx.x; i < n; i += blockDim.x) img_io[i] = m.img[i];
+  for (size_t i = tid; i < n; i += T) img_io[i] = m.img[i];
 }
 
 // Grow the inpainted map back to full size where it is needed and fill the
@@ -881,7 +772,7 @@ int disc_count(int32_t radius) {
 size_t telea_bytes(int32_t sw, int32_t sh, int n_off) {
   const size_t n = (size_t)sw * sh;
   auto a16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
-  return a16((size_t)n_off * 4) + 4 * a16(n * 4) + a16(n) + a16(n);
+  return 3 * a16((size_t)n_off * 4) + 3 * a16(n * 4) + a16(n);
 }
 
 }  // namespace
@@ -995,7 +886,7 @@ cudaError_t seg_front_run(const SegFrontArgs& a, void* ws, int sms, size_t smem_
           cudaSuccess)
         return e;
     }
-    telea_kernel<<<1, 512, dyn, st>>>(d_small, d_misc, sw, sh, a.radius, n_off, d_telea, use_smem);
+    telea_kernel<<<1, 1024, dyn, st>>>(d_small, d_misc, sw, sh, a.radius, n_off, d_telea, use_smem);
   }
   inpaint_fill_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_sm, d_misc, d_small, a.inpainted_out, c, dims);
   // Canny saliency

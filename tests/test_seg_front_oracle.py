@@ -186,17 +186,32 @@ def test_telea_continues_a_ramp():
     assert np.abs(out[mask == 1].astype(int) - ramp[mask == 1].astype(int)).max() <= 3
 
 
-def test_eikonal_update():
-    assert po.lib().qo_eikonal  # exported
+def test_eikonal_update_and_arrival_times():
     import ctypes as C
 
-    f = po.lib().qo_eikonal
+    f = po.lib().qo_eikonal2
     f.restype = C.c_float
-    f.argtypes = [C.c_int, C.c_float, C.c_int, C.c_float]
-    assert f(1, 0.0, 1, 0.0) == np.float32((0.0 + 0.0 + math.sqrt(2.0)) / 2)
-    assert f(1, 0.0, 1, 1.5) == 1.0
-    assert f(1, 2.0, 0, 0.0) == 3.0
-    assert f(0, 0.0, 0, 0.0) == np.float32(1e6)
+    f.argtypes = [C.c_float, C.c_float]
+    assert f(0.0, 0.0) == np.float32((0.0 + 0.0 + math.sqrt(2.0)) / 2)
+    assert f(0.0, 1.5) == 1.0
+    assert f(2.0, float("inf")) == 3.0
+    assert f(float("inf"), float("inf")) == float("inf")
+    # a masked 5 x 5 square in a known frame: times grow inwards, symmetric
+    mask = np.zeros((9, 9), np.uint8)
+    mask[2:7, 2:7] = 1
+    T = np.zeros(mask.shape, np.float32)
+    g = po.lib().qo_telea_times
+    g.restype = C.c_int32
+    it = g(mask.ctypes.data_as(C.c_void_p), 9, 9, T.ctypes.data_as(C.c_void_p))
+    assert it > 0
+    assert (T[mask == 0] == 0).all()
+    np.testing.assert_array_equal(T, T.T)
+    np.testing.assert_array_equal(T, T[::-1, ::-1])
+    # the corner from two known neighbours; the edge from the known pixel
+    # and the edge pixels beside it (as the march computes them); growing inwards
+    assert T[2, 2] == np.float32(math.sqrt(2.0) / 2)
+    assert abs(T[2, 4] - 1.0) < 1e-3 and 1.9 < T[3, 4] < 2.0
+    assert T[2, 4] < T[3, 4] < T[4, 4]
 
 
 def _resize_np(src, dw, dh):
