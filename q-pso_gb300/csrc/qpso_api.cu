@@ -64,7 +64,7 @@ struct Header {  // per instance, 64 bytes: result + counters read back once
   uint32_t done;
   uint32_t err;
   unsigned long long stats[2];
-  uint32_t pad[2];
+  unsigned long long argkey;  // the iteration's smallest (fitness bits, particle) key; all ones between iterations
 };
 static_assert(sizeof(Header) == 64, "header layout");
 
@@ -388,10 +388,12 @@ void fill_meta(qpso_context* ctx, const Layout& L, const std::vector<const qpso_
     I.done = &dh->done;
     I.err = &dh->err;
     I.stats = dh->stats;
+    I.argkey = &dh->argkey;
     I.trace = trace ? reinterpret_cast<float*>(d + L.trace[i]) : nullptr;
     I.ppb = ppb;
     I.chunks = (s.num_particles + ppb - 1) / ppb;
     hh[i].gbest[0] = kBestInit;
+    hh[i].argkey = ~0ull;
     PrepDesc& p = hp[i];
     p.depth = f.depth;
     p.labels = (s.cluster_label >= 0) ? f.labels : nullptr;
@@ -920,11 +922,14 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
   if (!ctx->timers[0]) QPSO_CUDA(ctx, cudaEventCreate(&ctx->timers[0]));
   if (!ctx->timers[1]) QPSO_CUDA(ctx, cudaEventCreate(&ctx->timers[1]));
   const int threads[] = {128, 256, 512};
-  const int tiles[] = {4096, 8192, 16384, 32768, 49152};
   const int ppbs[] = {1, 2, 4};
   for (int th : threads)
-    for (int tp : tiles)
-      for (int pb : ppbs) {
+    for (int pb : ppbs) {
+      // fixed sizes, and the largest tile that keeps two CTAs on an SM
+      std::vector<int> tiles = {4096, 8192, 16384, 32768, 49152};
+      const int t2 = tile_for_occupancy(th, pb, vcap, 2, batched != 0, var);
+      if (t2 > 0 && std::find(tiles.begin(), tiles.end(), t2) == tiles.end()) tiles.push_back(t2);
+      for (int tp : tiles) {
         const qpso_launch_config c{th, tp, pb};
         if (!valid_cfg(c, ctx->smem_optin, vcap)) continue;
         const TileConfig tc{th, tp, pb};
@@ -958,6 +963,7 @@ qpso_status qpso_autotune(qpso_context* ctx, const qpso_solve_desc* descs, uint3
           win = tc;
         }
       }
+    }
   if (batched) ctx->batch = win; else ctx->plain = win;
   if (best) *best = qpso_launch_config{win.threads, win.tile_px, win.ppb};
   if (best_ms) *best_ms = win_ms;
@@ -1723,6 +1729,7 @@ void server_loop(qpso_server* s) {
         I.done = &dh->done;
         I.err = &dh->err;
         I.stats = dh->stats;
+        I.argkey = &dh->argkey;
         I.trace = nullptr;
         I.ppb = (uint32_t)s->tc.ppb;
         I.chunks = (uint32_t)((P + s->tc.ppb - 1) / s->tc.ppb);
@@ -1730,6 +1737,7 @@ void server_loop(qpso_server* s) {
         Header& hh = s->h_hdr[slot];
         std::memset(&hh, 0, sizeof(hh));
         hh.gbest[0] = kBestInit;
+        hh.argkey = ~0ull;
         PrepDesc& pj = s->h_prep[admitted.size()];
         pj.depth = f->depth;
         pj.labels = r.desc.cluster_label >= 0 ? f->labels : nullptr;

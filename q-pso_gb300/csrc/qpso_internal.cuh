@@ -42,6 +42,7 @@ struct Instance {
   uint32_t* done;           // CTAs finished in the current iteration
   uint32_t* err;            // error bits
   unsigned long long* stats;  // [0] raster pixel writes, [1] tile passes
+  unsigned long long* argkey;  // smallest (fitness bits << 32 | particle) of the iteration
   float* trace;             // optional [iterations][8] gbest after each iteration
   uint32_t chunks;          // CTAs (work items) per iteration
   uint32_t ppb;             // particles per work item
@@ -105,6 +106,7 @@ cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, co
 cudaError_t launch_batch(const BatchArgs& args, int grid, const TileConfig& cfg, cudaStream_t st, int var,
                          int vcap);
 cudaError_t batch_max_grid(const TileConfig& cfg, int var, int vcap, int* blocks_per_sm);
+int tile_for_occupancy(int threads, int ppb, int vcap, int per_sm, bool batched, int var);
 cudaError_t launch_score(const Instance* inst, const float* poses, uint32_t n, float* fit_out,
                          const TileConfig& cfg, int grid, cudaStream_t st);
 cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_t n, float* fit_out,

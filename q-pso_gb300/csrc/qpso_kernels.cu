@@ -1023,9 +1023,14 @@ __device__ __forceinline__ void render_score_mlets(const Instance& I, int np, co
 }
 
 // PSO step + render + score + personal best for one work item.
+// dep_wait: the plain kernel is launched as a programmatic dependent of
+// the previous iteration's launch, so its CTAs may start while that launch
+// still runs; they wait (griddepcontrol.wait) before the first read of what
+// it writes: the swarm state, the global best and the counters.  The mesh
+// and the instance record are written before the first launch.
 template <int kVar>
 __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, unsigned char* dyn,
-                             int tile_px, int vcap, SmemCtl& ctl) {
+                             int tile_px, int vcap, SmemCtl& ctl, bool dep_wait) {
   const int tid = threadIdx.x;
   const uint32_t P = I.prm.num_particles;
   const uint32_t p0 = chunk * I.ppb;
@@ -1044,6 +1049,7 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
         prefetch_l1(reinterpret_cast<const char*>(I.mlets) + (size_t)(i - box_lines) * 128u);
     }
   }
+  if (dep_wait) asm volatile("griddepcontrol.wait;" ::: "memory");
   if (tid < (int)np) {
     const uint32_t p = p0 + tid;
     float s[7], v[7];
@@ -1096,66 +1102,59 @@ size_t fused_smem_bytes(int threads, int ppb, int tile_px, int vcap) {
          (size_t)ppb * tile_px * 4;
 }
 
-// After a work item: the CTA that completes the instance's last chunk of the
-// iteration takes the first minimum of the fitness and updates the global
-// best (main.cu:1691-1704 and 826-852).
-__device__ void instance_epilogue(const Instance& I, uint32_t iter, SmemCtl& ctl) {
-  const int tid = threadIdx.x, T = blockDim.x;
-  if (tid == 0) {
-    __threadfence();
-    const uint32_t t = atomicAdd(I.done, 1u);
-    ctl.last = (t == I.chunks - 1) ? 1 : 0;
+// After a work item: every CTA folds its particles' (fitness, index) into
+// the instance's key with one 64-bit atomicMin, and the CTA that completes
+// the instance's last chunk of the iteration reads (and resets) the key and
+// updates the global best (main.cu:1691-1704 and 826-852).  The fitness is
+// never NaN and never -0 (a sum of non-negative terms, +inf for an empty
+// render), so its bits order as the values do, and the smallest key is the
+// first minimum that thrust::min_element returns.
+__device__ __forceinline__ unsigned long long fit_key(float f, uint32_t p) {
+  return ((unsigned long long)__float_as_uint(f) << 32) | p;
+}
+
+__device__ void instance_epilogue(const Instance& I, uint32_t chunk, uint32_t iter, SmemCtl& ctl) {
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    const uint32_t P = I.prm.num_particles;
+    const uint32_t p0 = chunk * I.ppb;
+    const uint32_t np = min(I.ppb, P - p0);
+    unsigned long long k = ~0ull;
+    if ((uint32_t)tid < np) k = fit_key(ctl.argv[tid], p0 + (uint32_t)tid);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, o);
+      k = ok < k ? ok : k;
+    }
+    if (tid == 0) {
+      atomicMin(I.argkey, k);
+      __threadfence();
+      const uint32_t t = atomicAdd(I.done, 1u);
+      ctl.last = (t == I.chunks - 1) ? 1 : 0;
+    }
   }
   __syncthreads();
   if (!ctl.last) return;
-  __threadfence();
-  const uint32_t P = I.prm.num_particles;
-  // the global best is read while the fitness loads are in flight
-  const float gf = tid == 0 ? __ldcg(I.gbest) : 0.0f;
-  float bv = __int_as_float(0x7f800000);
-  uint32_t bi = 0xffffffffu;
-  for (uint32_t p = tid; p < P; p += T) {
-    const float f = __ldcg(I.fit + p);
-    if (bi == 0xffffffffu || f < bv) {
-      bv = f;
-      bi = p;
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-    const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-    if (oi != 0xffffffffu && (bi == 0xffffffffu || ov < bv || (!(bv < ov) && oi < bi))) {
-      bv = ov;
-      bi = oi;
-    }
-  }
-  const int wid = tid >> 5, lane = tid & 31, nw = T >> 5;
-  if (lane == 0) {
-    ctl.argv[wid] = bv;
-    ctl.argi[wid] = bi;
-  }
-  __syncthreads();
   if (tid == 0) {
-    bv = ctl.argv[0];
-    bi = ctl.argi[0];
-    for (int i = 1; i < nw; ++i) {
-      const float ov = ctl.argv[i];
-      const uint32_t oi = ctl.argi[i];
-      if (oi != 0xffffffffu && (bi == 0xffffffffu || ov < bv || (!(bv < ov) && oi < bi))) {
-        bv = ov;
-        bi = oi;
-      }
-    }
-    if (bi != 0xffffffffu && bv < gf) {
-      I.gbest[0] = bv;
+    __threadfence();
+    const uint32_t P = I.prm.num_particles;
+    const unsigned long long key = atomicExch(I.argkey, ~0ull);  // read, and reset for the next iteration
+    float g[8];
 #pragma unroll
-      for (int d = 0; d < 7; ++d) I.gbest[1 + d] = __ldcg(I.pos + bi + (size_t)d * P);
+    for (int d = 0; d < 8; ++d) g[d] = __ldcg(I.gbest + d);
+    const uint32_t bi = (uint32_t)(key & 0xffffffffull);
+    const float bv = __uint_as_float((uint32_t)(key >> 32));
+    if (key != ~0ull && bv < g[0]) {
+      g[0] = bv;
+#pragma unroll
+      for (int d = 0; d < 7; ++d) g[1 + d] = __ldcg(I.pos + bi + (size_t)d * P);
+#pragma unroll
+      for (int d = 0; d < 8; ++d) I.gbest[d] = g[d];
     }
     if (I.trace) {
       float* tr = I.trace + (size_t)iter * 8;
 #pragma unroll
-      for (int d = 0; d < 8; ++d) tr[d] = __ldcg(I.gbest + d);
+      for (int d = 0; d < 8; ++d) tr[d] = g[d];
     }
     *I.done = 0u;
     __threadfence();
@@ -1170,8 +1169,11 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* 
   extern __shared__ int4 dyn_smem[];
   __shared__ SmemCtl ctl;
   const Instance& I = *inst;
-  process_item<kVar>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
-  instance_epilogue(I, iter, ctl);
+  // the next iteration's launch may place its CTAs now; they wait for this
+  // grid to complete before reading anything it writes
+  asm volatile("griddepcontrol.launch_dependents;");
+  process_item<kVar>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl, true);
+  instance_epilogue(I, blockIdx.x, iter, ctl);
 }
 
 // Batched form: every iteration of every instance in one cooperative
@@ -1256,8 +1258,8 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_batch_kernel(BatchArgs A, in
     __syncthreads();
     if (state != 0u) return;
     const Instance& I = A.inst[in];
-    process_item<kVar>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
-    instance_epilogue(I, it, ctl);
+    process_item<kVar>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl, false);
+    instance_epilogue(I, chunk, it, ctl);
     if (ctl.last && threadIdx.x == 0 && it + 1 < I.prm.iterations) append_queue_item(A, in, it + 1);
   }
 }
@@ -1281,8 +1283,8 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_epoch_kernel(BatchArgs A, co
     __syncthreads();
     if (state != 0u) return;
     Instance& I = A.inst[in];
-    process_item<kVar>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl);
-    instance_epilogue(I, it, ctl);
+    process_item<kVar>(I, chunk, it, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl, false);
+    instance_epilogue(I, chunk, it, ctl);
     if (ctl.last && threadIdx.x == 0) {
       I.cur_iter = it + 1;
       if (it + 1 < end_iter[in]) append_queue_item(A, in, it + 1);
@@ -1614,8 +1616,56 @@ cudaError_t launch_step(const Instance* inst, uint32_t iter, uint32_t chunks, co
   auto* k = var == 2 ? qpso_step_kernel<2> : var == 1 ? qpso_step_kernel<1> : qpso_step_kernel<0>;
   cudaError_t e = ensure_smem(k, smem);
   if (e != cudaSuccess) return e;
-  k<<<chunks, cfg.threads, smem, st>>>(inst, iter, cfg.tile_px, vcap);
-  return cudaGetLastError();
+  // a programmatic dependent of the previous launch in the stream (the
+  // kernel waits for it before touching its outputs)
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(chunks);
+  lc.blockDim = dim3(cfg.threads);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, k, inst, iter, cfg.tile_px, vcap);
+}
+
+// The largest tile (a multiple of 8 pixels) with which `per_sm` CTAs of the
+// fused kernel (plain or batched form) are resident on one SM, or 0: the
+// shared memory left per CTA, then checked with the occupancy calculator
+// (allocation granularity), stepping down 256 pixels at a time.  The
+// kernel's dynamic shared memory limit is only ever raised (ensure_smem).
+template <typename K>
+static int tile_for_occupancy_k(K kernel, int threads, int ppb, int vcap, int per_sm) {
+  int dev = 0, smem_sm = 0, reserved = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
+    return 0;
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 0;
+  const long per_cta = (long)smem_sm / per_sm - reserved - (long)fa.sharedSizeBytes;
+  const long rest = (long)fused_smem_bytes(threads, ppb, 0, vcap);
+  long tile = ((per_cta - rest) / (4L * ppb)) & ~7L;
+  for (int step = 0; step < 16 && tile >= 64; ++step, tile -= 256) {
+    const size_t dyn = fused_smem_bytes(threads, ppb, (int)tile, vcap);
+    if (ensure_smem(kernel, dyn) != cudaSuccess) continue;
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, threads, dyn) != cudaSuccess) return 0;
+    if (blocks >= per_sm) return (int)tile;
+  }
+  return 0;
+}
+
+int tile_for_occupancy(int threads, int ppb, int vcap, int per_sm, bool batched, int var) {
+  if (batched)
+    return var == 2   ? tile_for_occupancy_k(qpso_batch_kernel<2>, threads, ppb, vcap, per_sm)
+           : var == 1 ? tile_for_occupancy_k(qpso_batch_kernel<1>, threads, ppb, vcap, per_sm)
+                      : tile_for_occupancy_k(qpso_batch_kernel<0>, threads, ppb, vcap, per_sm);
+  return var == 2   ? tile_for_occupancy_k(qpso_step_kernel<2>, threads, ppb, vcap, per_sm)
+         : var == 1 ? tile_for_occupancy_k(qpso_step_kernel<1>, threads, ppb, vcap, per_sm)
+                    : tile_for_occupancy_k(qpso_step_kernel<0>, threads, ppb, vcap, per_sm);
 }
 
 cudaError_t batch_max_grid(const TileConfig& cfg, int var, int vcap, int* blocks_per_sm) {
