@@ -918,14 +918,18 @@ def run_serving(args, ws, rank, local):
     w, desc = load_workload("c4")
     ctx = qpso.Context(local)
     pool, _, _ = c4_pool(ctx, w)
-    cfg, _ = ctx.autotune(pool[:16], batched=True, tune_iters=6)
+    if args.launch:  # a fixed shape instead of the autotuner's choice
+        cfg = tuple(int(x) for x in args.launch.split(","))
+        ctx.set_launch_config(batch=cfg)
+    else:
+        cfg, _ = ctx.autotune(pool[:16], batched=True, tune_iters=6)
     rates = [float(r) for r in args.rates.split(",")]
     sampler = ClockSampler(local)
     sampler.start()
     results, top, best = serving_sweep(ctx, pool, rates, args.duration, args.slots, args.epoch_iters,
                                        max_requests=args.max_requests)
     clocks = sampler.stop()
-    batched = batched_same_mix(ctx, pool)
+    batched = None if args.no_extras else batched_same_mix(ctx, pool)
     head = top or best
     line = {"metric": "pose solves/sec at sustained load with p50/p99 latency (serving)",
             "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": len(rates),
@@ -1066,7 +1070,8 @@ def main():
     ap.add_argument("--no-ref-kernels", action="store_true",
                     help="skip the reference-shaped solve (1024 particles x 20 iterations)")
     ap.add_argument("--no-extras", action="store_true",
-                    help="c2: skip the C3, C4 and segmentation measurements added to the line")
+                    help="c2: skip the C3, C4 and segmentation measurements added to the line; "
+                         "c4: skip the batched run of the same mix")
     ap.add_argument("--launch", default="", help="THREADS,TILE_PX,PPB for both paths instead of autotuning")
     ap.add_argument("--rates", default="25,40,50,100,1000,20000", help="c4: arrival rates (req/s)")
     ap.add_argument("--max-requests", type=int, default=400, help="c4: requests per rate at most")
