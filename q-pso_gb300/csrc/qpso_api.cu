@@ -1501,6 +1501,10 @@ qpso_status qpso_segment_rgbd(qpso_context* ctx, const uint8_t* bgr, const uint1
     a.smoothed_host = planes->smoothed;
     a.edges_host = planes->edges;
   }
+  if ((st = ensure_segpin(ctx, seg_merge_pinned_bytes(W, H))) != QPSO_OK) return st;
+  uint32_t* front_err = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx->segpin.p) + 32);
+  *front_err = 0u;
+  a.err_pinned = front_err;
   QPSO_CUDA(ctx, seg_front_run(a, front_ws, ctx->num_sms, (size_t)ctx->smem_optin, ctx->stream));
   if (planes) {
     uint8_t* hp[3] = {planes->h, planes->s, planes->v};
@@ -1511,11 +1515,13 @@ qpso_status qpso_segment_rgbd(qpso_context* ctx, const uint8_t* bgr, const uint1
     if (planes->saliency)
       QPSO_CUDA(ctx, cudaMemcpyAsync(planes->saliency, d_sal, 4 * n, cudaMemcpyDeviceToHost, ctx->stream));
   }
-  if ((st = ensure_segpin(ctx, seg_merge_pinned_bytes(W, H))) != QPSO_OK) return st;
   uint32_t err = 0, ns = 0;
   QPSO_CUDA(ctx, seg_graph_merge(nullptr, nullptr, nullptr, W, H, mask, len, prm->kdv, prm->kdc, prm->kx, prm->ks,
                                  base, ctx->num_sms, ctx->stream, ctx->segpin.p, ctx->seg_ev, kSegChunks, prm->k,
                                  prm->min_size, labels, &ns, &err));
+  // the front's error word was copied before the graph stage, which has
+  // synchronised with the stream since
+  if (*front_err) return fail(ctx, QPSO_ERR_TIMEOUT, "segmentation: the inpainting fill's grid barrier timed out");
   if (err & 5u) return fail(ctx, QPSO_ERR_INTERNAL, "segmentation graph: index out of range");
   if (err & 2u) return fail(ctx, QPSO_ERR_ARG, "segmentation graph: NaN edge weight (flat inpainted depth?)");
   *n_sets = ns;

@@ -182,6 +182,7 @@ struct SegFrontArgs {
   uint8_t* gray_host;        // optional host copies
   uint16_t* smoothed_host;
   uint8_t* edges_host;
+  uint32_t* err_pinned;      // optional pinned word: nonzero when the inpainting fill's grid barrier expired
 };
 int seg_gauss_taps(int ksize, int32_t* taps);
 size_t seg_front_workspace_bytes(int32_t W, int32_t H, int32_t radius);

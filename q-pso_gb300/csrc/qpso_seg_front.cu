@@ -292,24 +292,20 @@ __global__ void inpaint_shrink_kernel(const uint16_t* __restrict__ sm, const uin
   }
 }
 
-// Telea's inpainting of the shrunk map's zero pixels, by arrival time: the
+// Telea's inpainting of the shrunk map's zero pixels, by arrival time.  The
 // times T are the fixed point of the upwind eikonal update (Jacobi
 // iterations), and the masked pixels are filled in increasing T, each from
-// the pixels of smaller T, so that every pixel at one time is independent:
-// the CTA finds the next time, lists its pixels, and each warp fills one
-// pixel (its lanes share the disc of `radius`; the sums are in 32.32 fixed
-// point, so they do not depend on the order of terms).  One CTA; the
-// state (times, their next iterate, the map, the list) lives in shared
-// memory when it fits, else in global memory.
-struct TeleaMem {
-  float* T;
-  float* U;
-  uint8_t* img;
-  int32_t* list;
-  short2* off;   // the disc's offsets, raster order
-  float* olen;   // |offset| and 1 / |offset|^2 (they depend on the offset only)
-  float* odst;
-};
+// the pixels of smaller T only, so every pixel of one time (a level) is
+// independent of the others.  Two kernels:
+//   telea_levels_kernel (one CTA): T, then the masked pixels grouped by
+//     level in increasing T: order[lvl[l] .. lvl[l + 1]) holds level l,
+//     ctrl[0] the number of levels;
+//   telea_fill_kernel (cooperative, one CTA per SM): the levels in turn,
+//     their pixels spread over the CTAs (a CTA per pixel, or a warp per
+//     pixel when a level has more pixels than CTAs), a grid barrier between
+//     levels.  A pixel's sums over the disc of `radius` are in 32.32 fixed
+//     point, so they do not depend on the order of terms.
+// State lives in shared memory when it fits, else in global memory.
 
 __device__ __forceinline__ float eikonal2(float a, float b) {
   const float inf = __int_as_float(0x7f800000);
@@ -326,78 +322,34 @@ __device__ __forceinline__ float grad1(bool km, float am, bool kp, float ap, flo
   return 0.0f;
 }
 
-// This lane's partial sums of pixel (x, y)'s value over its share of the disc.
-__device__ void telea_terms(const TeleaMem& m, int32_t w, int32_t h, int32_t x, int32_t y, float L, float gtx,
-                            float gty, int n_off, bool unit_dir, long long& num, long long& den) {
-  for (int o = threadIdx.x & 31; o < n_off; o += 32) {
-    const int32_t dx = m.off[o].x, dy = m.off[o].y;
-    const int32_t kx = x + dx, ky = y + dy;
-    if (kx < 0 || kx >= w || ky < 0 || ky >= h) continue;
-    const size_t k = (size_t)ky * w + kx;
-    const float tk = m.T[k];
-    if (!(tk < L)) continue;
-    const int32_t rx = -dx, ry = -dy;
-    const float dir = unit_dir ? 1.0f
-                               : __fdiv_rn(fabsf(__fadd_rn(__fmul_rn((float)rx, gtx), __fmul_rn((float)ry, gty))),
-                                           m.olen[o]);
-    const float dst = m.odst[o];
-    const float lev = __fdiv_rn(1.0f, __fadd_rn(1.0f, fabsf(__fsub_rn(tk, L))));
-    const float wt = __fmul_rn(__fmul_rn(dir, dst), lev);
-    const bool ixm = kx > 0 && m.T[k - 1] < L, ixp = kx + 1 < w && m.T[k + 1] < L;
-    const bool iym = ky > 0 && m.T[k - w] < L, iyp = ky + 1 < h && m.T[k + w] < L;
-    const float a0 = (float)m.img[k];
-    const float gix = grad1(ixm, ixm ? (float)m.img[k - 1] : 0.0f, ixp, ixp ? (float)m.img[k + 1] : 0.0f, a0);
-    const float giy = grad1(iym, iym ? (float)m.img[k - w] : 0.0f, iyp, iyp ? (float)m.img[k + w] : 0.0f, a0);
-    const float val = __fadd_rn(a0, __fadd_rn(__fmul_rn(gix, (float)rx), __fmul_rn(giy, (float)ry)));
-    // x * 2^32 is exact in float as in double, so these equal
-    // llrint((double)x * 2^32) without the (slow) double pipe
-    den += __float2ll_rn(__fmul_rn(wt, 4294967296.0f));
-    num += __float2ll_rn(__fmul_rn(__fmul_rn(wt, val), 4294967296.0f));
-  }
-}
+__host__ __device__ __forceinline__ size_t a16(size_t b) { return (b + 15) & ~(size_t)15; }
 
-__global__ void __launch_bounds__(1024) telea_kernel(uint8_t* __restrict__ img_io, const uint32_t* misc,
-                                                      int32_t w, int32_t h, int32_t radius, int n_off,
-                                                      unsigned char* __restrict__ gmem, int use_smem) {
+// ctrl words: [0] levels, [1] barrier arrivals, [2] barrier generation
+__global__ void __launch_bounds__(1024) telea_levels_kernel(const uint8_t* __restrict__ img_io, const uint32_t* misc,
+                                                             int32_t w, int32_t h, float* __restrict__ T_out,
+                                                             int32_t* __restrict__ order, int32_t* __restrict__ lvl,
+                                                             uint32_t* ctrl, unsigned char* __restrict__ gmem,
+                                                             int use_smem) {
   extern __shared__ __align__(16) unsigned char tsm[];
   __shared__ uint32_t s_min[32];
   __shared__ uint32_t s_L, s_cnt;
+  if (threadIdx.x == 0) {
+    ctrl[0] = 0u;
+    ctrl[1] = 0u;
+    ctrl[2] = 0u;
+  }
   if (misc[3] == misc[2]) return;  // flat depth: nothing is filled
   const size_t n = (size_t)w * h;
   unsigned char* base = use_smem ? tsm : gmem;
-  // layout: offsets | lengths | 1 / lengths^2 | T | U | list | img
-  TeleaMem m;
-  size_t o = 0;
-  const size_t ob = ((size_t)n_off * 4 + 15) & ~(size_t)15;
-  m.off = reinterpret_cast<short2*>(base + o);
-  m.olen = reinterpret_cast<float*>(base + o + ob);
-  m.odst = reinterpret_cast<float*>(base + o + 2 * ob);
-  o += 3 * ob;
-  m.T = reinterpret_cast<float*>(base + o);
-  o += (n * 4 + 15) & ~(size_t)15;
-  m.U = reinterpret_cast<float*>(base + o);
-  o += (n * 4 + 15) & ~(size_t)15;
-  m.list = reinterpret_cast<int32_t*>(base + o);
-  o += (n * 4 + 15) & ~(size_t)15;
-  m.img = base + o;
+  float* T = reinterpret_cast<float*>(base);
+  float* U = reinterpret_cast<float*>(base + a16(n * 4));
+  uint8_t* img = base + 2 * a16(n * 4);
   const float inf = __int_as_float(0x7f800000);
-  const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = T >> 5;
-  if (tid == 0) {  // disc offsets in raster order
-    int k = 0;
-    for (int32_t dy = -radius; dy <= radius; ++dy)
-      for (int32_t dx = -radius; dx <= radius; ++dx)
-        if ((dx || dy) && dx * dx + dy * dy <= radius * radius) m.off[k++] = make_short2((short)dx, (short)dy);
-  }
-  __syncthreads();
-  for (int k = tid; k < n_off; k += T) {
-    const float len2 = (float)(m.off[k].x * m.off[k].x + m.off[k].y * m.off[k].y);
-    m.olen[k] = __fsqrt_rn(len2);
-    m.odst[k] = __fdiv_rn(1.0f, len2);
-  }
-  for (size_t i = tid; i < n; i += T) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  for (size_t i = tid; i < n; i += nt) {
     const uint8_t v = img_io[i];
-    m.img[i] = v;
-    m.T[i] = v == 0 ? inf : 0.0f;
+    img[i] = v;
+    T[i] = v == 0 ? inf : 0.0f;
   }
   __syncthreads();
   // arrival times: Jacobi iterations of the upwind update to the fixed point
@@ -405,34 +357,35 @@ __global__ void __launch_bounds__(1024) telea_kernel(uint8_t* __restrict__ img_i
   bool converged = false;
   for (int it = 0; it <= cap; ++it) {
     int changed = 0;
-    for (size_t p = tid; p < n; p += T) {
+    for (size_t p = tid; p < n; p += nt) {
       float v = 0.0f;
-      if (m.img[p] == 0) {
+      if (img[p] == 0) {
         const int32_t y = (int32_t)(p / w), x = (int32_t)(p - (size_t)y * w);
-        const float l = x > 0 ? m.T[p - 1] : inf, r = x + 1 < w ? m.T[p + 1] : inf;
-        const float u = y > 0 ? m.T[p - w] : inf, d = y + 1 < h ? m.T[p + w] : inf;
+        const float l = x > 0 ? T[p - 1] : inf, r = x + 1 < w ? T[p + 1] : inf;
+        const float u = y > 0 ? T[p - w] : inf, d = y + 1 < h ? T[p + w] : inf;
         v = eikonal2(l < r ? l : r, u < d ? u : d);
-        changed |= v != m.T[p];
+        changed |= v != T[p];
       }
-      m.U[p] = v;
+      U[p] = v;
     }
     changed = __syncthreads_or(changed);
-    float* t = m.T;
-    m.T = m.U;
-    m.U = t;
+    float* t = T;
+    T = U;
+    U = t;
     if (!changed) {
       converged = true;
       break;
     }
   }
   if (!converged) return;  // cannot happen: the iterates only fall (as the oracle, nothing is filled)
-  // the masked pixels, level by level in increasing arrival time; the map
-  // still holds 0 there, so a pixel is masked exactly when T > 0
+  for (size_t i = tid; i < n; i += nt) T_out[i] = T[i];
+  // the levels: masked pixels (T > 0) grouped by T in increasing order
   float last = 0.0f;
+  uint32_t total = 0, nlev = 0;
   for (;;) {
     uint32_t lo = 0x7f800000u;  // the next time (non-negative floats order as their bits)
-    for (size_t p = tid; p < n; p += T) {
-      const float t = m.T[p];
+    for (size_t p = tid; p < n; p += nt) {
+      const float t = T[p];
       if (t > last) lo = min(lo, __float_as_uint(t));
     }
     lo = __reduce_min_sync(0xffffffffu, lo);
@@ -447,47 +400,247 @@ __global__ void __launch_bounds__(1024) telea_kernel(uint8_t* __restrict__ img_i
     __syncthreads();
     const float L = __uint_as_float(s_L);
     if (L == inf) break;
-    for (size_t p0 = (size_t)(tid & ~31); p0 < n; p0 += T) {  // whole warps: list the level's pixels
+    for (size_t p0 = (size_t)(tid & ~31); p0 < n; p0 += nt) {  // whole warps
       const size_t p = p0 + lane;
-      const bool on = p < n && m.T[p] == L;
+      const bool on = p < n && T[p] == L;
       const unsigned bal = __ballot_sync(0xffffffffu, on);
       uint32_t at = 0;
       if (lane == 0 && bal) at = atomicAdd(&s_cnt, (uint32_t)__popc(bal));
       at = __shfl_sync(0xffffffffu, at, 0);
-      if (on) m.list[at + __popc(bal & ((1u << lane) - 1u))] = (int32_t)p;
+      if (on) order[total + at + __popc(bal & ((1u << lane) - 1u))] = (int32_t)p;
     }
     __syncthreads();
-    const uint32_t cnt = s_cnt;
-    for (uint32_t i = wid; i < cnt; i += nw) {
-      const int32_t q = m.list[i];
-      const int32_t qx = q % w, qy = q / w;
-      const bool fxm = qx > 0 && m.T[q - 1] != inf, fxp = qx + 1 < w && m.T[q + 1] != inf;
-      const bool fym = qy > 0 && m.T[q - w] != inf, fyp = qy + 1 < h && m.T[q + w] != inf;
-      const float gtx = grad1(fxm, fxm ? m.T[q - 1] : 0.0f, fxp, fxp ? m.T[q + 1] : 0.0f, L);
-      const float gty = grad1(fym, fym ? m.T[q - w] : 0.0f, fyp, fyp ? m.T[q + w] : 0.0f, L);
-      uint8_t val = 0;
-      for (int pass = 0; pass < 2; ++pass) {
-        long long num = 0, den = 0;
-        telea_terms(m, w, h, qx, qy, L, gtx, gty, n_off, pass == 1, num, den);
-        for (int sft = 16; sft > 0; sft >>= 1) {
-          num += __shfl_down_sync(0xffffffffu, num, sft);
-          den += __shfl_down_sync(0xffffffffu, den, sft);
-        }
-        den = __shfl_sync(0xffffffffu, den, 0);
-        num = __shfl_sync(0xffffffffu, num, 0);
-        if (den > 0) {
-          const double v = rint((double)num / (double)den);
-          val = (uint8_t)(v < 0.0 ? 0.0 : v > 255.0 ? 255.0 : v);
+    if (tid == 0) lvl[nlev] = (int32_t)total;
+    total += s_cnt;
+    ++nlev;
+    last = L;
+    __syncthreads();  // s_cnt is read before the next level resets it
+  }
+  if (tid == 0) {
+    lvl[nlev] = (int32_t)total;
+    __threadfence();
+    ctrl[0] = nlev;
+  }
+}
+
+// Grid barrier of the cooperative fill kernel, with a limit: a wait longer
+// than one second sets misc[7] and returns false (every CTA then leaves).
+__device__ bool fill_barrier(uint32_t* ctrl, uint32_t* misc) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t* gen = ctrl + 2;
+    const uint32_t g = *gen;
+    __threadfence();
+    const uint32_t arrived = atomicAdd(ctrl + 1, 1u) + 1u;
+    int ok = 1;
+    if (arrived == gridDim.x) {
+      ctrl[1] = 0u;
+      __threadfence();
+      atomicExch(ctrl + 2, g + 1u);
+    } else {
+      unsigned long long t0;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      while (*gen == g) {
+        if (*(volatile uint32_t*)(misc + 7) != 0u) {
+          ok = 0;
           break;
         }
+        unsigned long long now;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+        if (now - t0 > 1000000000ull) {
+          atomicOr(misc + 7, 1u);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
       }
-      // the level's own pixels are not read while it is filled (T < L only)
-      if (lane == 0) m.img[q] = val;
     }
-    __syncthreads();
-    last = L;
+    __threadfence();
+    s_ok = ok;
   }
-  for (size_t i = tid; i < n; i += T) img_io[i] = m.img[i];
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// A lane's (or thread's) share of pixel q's sums: offsets o = first, first +
+// step, ... of the disc, those whose pixel has T < L.  The map is read from
+// shared memory (kSmem) or from L2 (other CTAs write it).
+template <bool kSmem>
+__device__ __forceinline__ void telea_terms(const float* __restrict__ T, const uint8_t* img, const short2* off,
+                                            const float* olen, const float* odst, int32_t w, int32_t h, int32_t x,
+                                            int32_t y, float L, float gtx, float gty, int n_off, int first, int step,
+                                            bool unit_dir, long long& num, long long& den) {
+  for (int o = first; o < n_off; o += step) {
+    const int32_t dx = off[o].x, dy = off[o].y;
+    const int32_t kx = x + dx, ky = y + dy;
+    if (kx < 0 || kx >= w || ky < 0 || ky >= h) continue;
+    const size_t k = (size_t)ky * w + kx;
+    const float tk = T[k];
+    if (!(tk < L)) continue;
+    const int32_t rx = -dx, ry = -dy;
+    const float dir = unit_dir ? 1.0f
+                               : __fdiv_rn(fabsf(__fadd_rn(__fmul_rn((float)rx, gtx), __fmul_rn((float)ry, gty))),
+                                           olen[o]);
+    const float lev = __fdiv_rn(1.0f, __fadd_rn(1.0f, fabsf(__fsub_rn(tk, L))));
+    const float wt = __fmul_rn(__fmul_rn(dir, odst[o]), lev);
+    const bool ixm = kx > 0 && T[k - 1] < L, ixp = kx + 1 < w && T[k + 1] < L;
+    const bool iym = ky > 0 && T[k - w] < L, iyp = ky + 1 < h && T[k + w] < L;
+    auto at = [&](size_t i) { return kSmem ? (float)img[i] : (float)__ldcg(img + i); };
+    const float a0 = at(k);
+    const float gix = grad1(ixm, ixm ? at(k - 1) : 0.0f, ixp, ixp ? at(k + 1) : 0.0f, a0);
+    const float giy = grad1(iym, iym ? at(k - w) : 0.0f, iyp, iyp ? at(k + w) : 0.0f, a0);
+    const float val = __fadd_rn(a0, __fadd_rn(__fmul_rn(gix, (float)rx), __fmul_rn(giy, (float)ry)));
+    // x * 2^32 is exact in float as in double, so these equal
+    // llrint((double)x * 2^32) without the (slow) double pipe
+    den += __float2ll_rn(__fmul_rn(wt, 4294967296.0f));
+    num += __float2ll_rn(__fmul_rn(__fmul_rn(wt, val), 4294967296.0f));
+  }
+}
+
+// T's gradient at pixel q (finite neighbours)
+__device__ __forceinline__ void telea_tgrad(const float* __restrict__ T, int32_t w, int32_t h, int32_t qx, int32_t qy,
+                                            float L, float& gtx, float& gty) {
+  const float inf = __int_as_float(0x7f800000);
+  const size_t q = (size_t)qy * w + qx;
+  const bool fxm = qx > 0 && T[q - 1] != inf, fxp = qx + 1 < w && T[q + 1] != inf;
+  const bool fym = qy > 0 && T[q - w] != inf, fyp = qy + 1 < h && T[q + w] != inf;
+  gtx = grad1(fxm, fxm ? T[q - 1] : 0.0f, fxp, fxp ? T[q + 1] : 0.0f, L);
+  gty = grad1(fym, fym ? T[q - w] : 0.0f, fyp, fyp ? T[q + w] : 0.0f, L);
+}
+
+__device__ __forceinline__ uint8_t telea_round(long long num, long long den) {
+  const double v = rint((double)num / (double)den);
+  return (uint8_t)(v < 0.0 ? 0.0 : v > 255.0 ? 255.0 : v);
+}
+
+template <bool kSmem>
+__global__ void __launch_bounds__(256) telea_fill_kernel(uint8_t* img_io, const float* __restrict__ Tg,
+                                                         const int32_t* __restrict__ order,
+                                                         const int32_t* __restrict__ lvl, uint32_t* ctrl,
+                                                         uint32_t* misc, int32_t w, int32_t h, int32_t radius,
+                                                         int n_off) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  __shared__ long long s_red[8][2];
+  __shared__ long long s_sum[2];
+  const uint32_t nlev = ctrl[0];
+  if (nlev == 0u) return;  // CTA-uniform
+  const size_t n = (size_t)w * h;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  // layout: offsets | lengths | 1 / lengths^2 [| T | map]
+  const size_t ob = a16((size_t)n_off * 4);
+  short2* off = reinterpret_cast<short2*>(fsm);
+  float* olen = reinterpret_cast<float*>(fsm + ob);
+  float* odst = reinterpret_cast<float*>(fsm + 2 * ob);
+  const float* T = Tg;
+  uint8_t* img = img_io;
+  if (kSmem) {
+    float* Ts = reinterpret_cast<float*>(fsm + 3 * ob);
+    uint8_t* ims = fsm + 3 * ob + a16(n * 4);
+    for (size_t i = tid; i < n; i += nt) {
+      Ts[i] = Tg[i];
+      ims[i] = __ldcg(img_io + i);
+    }
+    T = Ts;
+    img = ims;
+  }
+  if (tid == 0) {  // disc offsets in raster order
+    int k = 0;
+    for (int32_t dy = -radius; dy <= radius; ++dy)
+      for (int32_t dx = -radius; dx <= radius; ++dx)
+        if ((dx || dy) && dx * dx + dy * dy <= radius * radius) off[k++] = make_short2((short)dx, (short)dy);
+  }
+  __syncthreads();
+  for (int k = tid; k < n_off; k += nt) {
+    const float len2 = (float)(off[k].x * off[k].x + off[k].y * off[k].y);
+    olen[k] = __fsqrt_rn(len2);
+    odst[k] = __fdiv_rn(1.0f, len2);
+  }
+  __syncthreads();
+  const int G = (int)gridDim.x;
+  for (uint32_t l = 0; l < nlev; ++l) {
+    const int32_t s = lvl[l], e = lvl[l + 1];
+    const float L = Tg[order[s]];
+    if (e - s <= G) {  // a CTA per pixel
+      for (int32_t i = s + (int32_t)blockIdx.x; i < e; i += G) {
+        const int32_t q = order[i];
+        const int32_t qx = q % w, qy = q / w;
+        float gtx, gty;
+        telea_tgrad(T, w, h, qx, qy, L, gtx, gty);
+        uint8_t val = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+          long long num = 0, den = 0;
+          telea_terms<kSmem>(T, img, off, olen, odst, w, h, qx, qy, L, gtx, gty, n_off, tid, nt, pass == 1, num,
+                             den);
+          for (int sft = 16; sft > 0; sft >>= 1) {
+            num += __shfl_down_sync(0xffffffffu, num, sft);
+            den += __shfl_down_sync(0xffffffffu, den, sft);
+          }
+          if (lane == 0) {
+            s_red[wid][0] = num;
+            s_red[wid][1] = den;
+          }
+          __syncthreads();
+          if (tid == 0) {
+            long long tn = 0, td = 0;
+            for (int k = 0; k < nw; ++k) {
+              tn += s_red[k][0];
+              td += s_red[k][1];
+            }
+            s_sum[0] = tn;
+            s_sum[1] = td;
+          }
+          __syncthreads();
+          const long long tn = s_sum[0], td = s_sum[1];
+          __syncthreads();  // s_sum is rewritten by the next pass or pixel
+          if (td > 0) {
+            val = telea_round(tn, td);
+            break;
+          }
+        }
+        // the level's own pixels are not read while it is filled (T < L only)
+        if (tid == 0) {
+          img_io[q] = val;
+          if (kSmem) img[q] = val;
+        }
+      }
+    } else {  // a warp per pixel
+      for (int32_t i = s + (int32_t)blockIdx.x * nw + wid; i < e; i += G * nw) {
+        const int32_t q = order[i];
+        const int32_t qx = q % w, qy = q / w;
+        float gtx, gty;
+        telea_tgrad(T, w, h, qx, qy, L, gtx, gty);
+        uint8_t val = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+          long long num = 0, den = 0;
+          telea_terms<kSmem>(T, img, off, olen, odst, w, h, qx, qy, L, gtx, gty, n_off, lane, 32, pass == 1, num,
+                             den);
+          for (int sft = 16; sft > 0; sft >>= 1) {
+            num += __shfl_down_sync(0xffffffffu, num, sft);
+            den += __shfl_down_sync(0xffffffffu, den, sft);
+          }
+          den = __shfl_sync(0xffffffffu, den, 0);
+          num = __shfl_sync(0xffffffffu, num, 0);
+          if (den > 0) {
+            val = telea_round(num, den);
+            break;
+          }
+        }
+        if (lane == 0) {
+          img_io[q] = val;
+          if (kSmem) img[q] = val;
+        }
+      }
+    }
+    if (l + 1 == nlev) break;
+    if (!fill_barrier(ctrl, misc)) return;
+    if (kSmem)  // the level's values from the other CTAs (L2: not this SM's L1)
+      for (int32_t i = s + tid; i < e; i += nt) {
+        const int32_t q = order[i];
+        img[q] = __ldcg(img_io + q);
+      }
+    __syncthreads();
+  }
 }
 
 // Grow the inpainted map back to full size where it is needed and fill the
@@ -769,10 +922,16 @@ int disc_count(int32_t radius) {
   return k;
 }
 
-size_t telea_bytes(int32_t sw, int32_t sh, int n_off) {
-  const size_t n = (size_t)sw * sh;
-  auto a16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
-  return 3 * a16((size_t)n_off * 4) + 3 * a16(n * 4) + a16(n);
+// telea_levels_kernel's state (times, their next iterate, the map)
+size_t telea_levels_bytes(size_t n) { return 2 * a16(n * 4) + a16(n); }
+// telea_fill_kernel's shared memory: the disc, and with kSmem the times and map
+size_t telea_fill_bytes(size_t n, int n_off, bool smem) {
+  return 3 * a16((size_t)n_off * 4) + (smem ? a16(n * 4) + a16(n) : 0);
+}
+// global buffers: times, level order, level offsets, control words, and the
+// levels kernel's state when it does not fit in shared memory
+size_t telea_ws_bytes(size_t n) {
+  return al256(4 * n) + al256(4 * n) + al256(4 * (n + 1)) + al256(16) + al256(telea_levels_bytes(n));
 }
 
 }  // namespace
@@ -799,12 +958,13 @@ int seg_gauss_taps(int ksize, int32_t* taps) {
 }
 
 size_t seg_front_workspace_bytes(int32_t W, int32_t H, int32_t radius) {
+  (void)radius;  // the inpainting disc lives in shared memory
   const size_t n = (size_t)W * H, n1 = (size_t)(W + 1) * (H + 1);
   const int32_t sw = (int32_t)std::rint(W * 0.2), sh = (int32_t)std::rint(H * 0.2);
   return al256(3 * n) + al256(n) + al256(2 * n) + al256(n) + al256(4 * n) + al256(4 * n) + 2 * al256(4 * n) +
          2 * al256(4 * n1) + al256(2 * n) + al256((size_t)(sw > 0 ? sw : 1) * (sh > 0 ? sh : 1)) +
          al256(4 * n) + al256(4 * n) + al256(n) + al256(4 * n) + al256(n) + al256(n) + al256(64) +
-         al256(telea_bytes(sw > 0 ? sw : 1, sh > 0 ? sh : 1, disc_count(radius)));
+         al256(telea_ws_bytes((size_t)(sw > 0 ? sw : 1) * (sh > 0 ? sh : 1)));
 }
 
 cudaError_t seg_front_run(const SegFrontArgs& a, void* ws, int sms, size_t smem_optin, cudaStream_t st) {
@@ -837,7 +997,13 @@ cudaError_t seg_front_run(const SegFrontArgs& a, void* ws, int sms, size_t smem_
   uint8_t* d_mb = (uint8_t*)take(n);
   uint32_t* d_misc = (uint32_t*)take(64);
   const int n_off = disc_count(a.radius);
-  unsigned char* d_telea = (unsigned char*)take(telea_bytes(sw > 0 ? sw : 1, sh > 0 ? sh : 1, n_off));
+  const size_t ns = (size_t)(sw > 0 ? sw : 1) * (sh > 0 ? sh : 1);
+  unsigned char* d_telea = (unsigned char*)take(telea_ws_bytes(ns));
+  float* d_T = reinterpret_cast<float*>(d_telea);
+  int32_t* d_order = reinterpret_cast<int32_t*>(d_telea + al256(4 * ns));
+  int32_t* d_lvl = reinterpret_cast<int32_t*>(d_telea + 2 * al256(4 * ns));
+  uint32_t* d_ctrl = reinterpret_cast<uint32_t*>(d_telea + 2 * al256(4 * ns) + al256(4 * (ns + 1)));
+  unsigned char* d_lstate = d_telea + 2 * al256(4 * ns) + al256(4 * (ns + 1)) + al256(16);
 
   FrontConst c{};
   c.W = W;
@@ -877,16 +1043,40 @@ cudaError_t seg_front_run(const SegFrontArgs& a, void* ws, int sms, size_t smem_
   InpaintDims dims{sw, sh};
   if (sw >= 1 && sh >= 1) {
     inpaint_shrink_kernel<<<grid_of((size_t)sw * sh, T, sms), T, 0, st>>>(d_sm, d_misc, d_small, c, dims);
-    const size_t tb = telea_bytes(sw, sh, n_off);
-    // the kernel's static shared memory (reduction slots) must fit beside it
-    const int use_smem = tb + 1024 <= smem_optin ? 1 : 0;
-    const size_t dyn = use_smem ? tb : 0;
-    if (use_smem && dyn > 48 * 1024) {
-      if ((e = cudaFuncSetAttribute(telea_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn)) !=
-          cudaSuccess)
-        return e;
-    }
-    telea_kernel<<<1, 1024, dyn, st>>>(d_small, d_misc, sw, sh, a.radius, n_off, d_telea, use_smem);
+    // the levels (one CTA; its static shared memory must fit beside the state)
+    const size_t lb = telea_levels_bytes(ns);
+    const int lsm = lb + 1024 <= smem_optin ? 1 : 0;
+    if (lsm && lb > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(telea_levels_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lb)) !=
+            cudaSuccess)
+      return e;
+    telea_levels_kernel<<<1, 1024, lsm ? lb : 0, st>>>(d_small, d_misc, sw, sh, d_T, d_order, d_lvl, d_ctrl,
+                                                       d_lstate, lsm);
+    // the fill: one CTA per SM, all resident (cooperative launch)
+    const size_t fbs = telea_fill_bytes(ns, n_off, true);
+    const bool fsm = fbs + 2048 <= smem_optin;
+    void (*kf)(uint8_t*, const float*, const int32_t*, const int32_t*, uint32_t*, uint32_t*, int32_t, int32_t,
+               int32_t, int) = fsm ? telea_fill_kernel<true> : telea_fill_kernel<false>;
+    const size_t fdyn = fsm ? fbs : telea_fill_bytes(ns, n_off, false);
+    if (fdyn > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fdyn)) != cudaSuccess)
+      return e;
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kf, 256, fdyn)) != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)sms);
+    lc.blockDim = dim3(256);
+    lc.dynamicSmemBytes = fdyn;
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    if ((e = cudaLaunchKernelEx(&lc, kf, d_small, (const float*)d_T, (const int32_t*)d_order, (const int32_t*)d_lvl,
+                                d_ctrl, d_misc, sw, sh, a.radius, n_off)) != cudaSuccess)
+      return e;
   }
   inpaint_fill_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_sm, d_misc, d_small, a.inpainted_out, c, dims);
   // Canny saliency
@@ -907,6 +1097,9 @@ cudaError_t seg_front_run(const SegFrontArgs& a, void* ws, int sms, size_t smem_
       (e = cudaMemcpyAsync(a.smoothed_host, d_sm, 2 * n, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     return e;
   if (a.edges_host && (e = cudaMemcpyAsync(a.edges_host, d_mag, n, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  // misc[7]: the inpainting fill's grid barrier expired
+  if (a.err_pinned && (e = cudaMemcpyAsync(a.err_pinned, d_misc + 7, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     return e;
   return cudaSuccess;
 }
