@@ -415,7 +415,8 @@ struct SegGraphDev {
   float* w;          // weights in edge order
   int32_t* ea;
   int32_t* eb;
-  uint32_t* misc;    // [0] depth min, [1] depth max, [2] error bits
+  uint32_t* misc;    // [0] depth min, [1] depth max, [2] error bits, [3] zero-weight edges
+  float* tmp;        // 12 n bytes, free after the smoothing
 };
 
 // Upload (or take the inputs already in their slots), smooth, weigh and sort.
@@ -494,23 +495,107 @@ cudaError_t seg_graph_device(const uint8_t* hsv_host[3], const uint16_t* depth_h
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  *out = SegGraphDev{src, dst, d_w, d_ea, d_eb, d_misc};
+  *out = SegGraphDev{src, dst, d_w, d_ea, d_eb, d_misc, d_tmp};
   return cudaSuccess;
 }
 
-// The sorted edges packed for the host: (first end << 2 | direction) and the
-// weight, in sorted order.  Directions: 0 right, 1 down, 2 down-right,
-// 3 up-right (the second end is first + 1, W, W + 1, 1 - W).
+// The sorted edges from position `first` (*first_at when first_at is not
+// null) packed for the host: (first end << 2 | direction) and the weight,
+// in sorted order.  Directions: 0 right, 1 down, 2 down-right, 3 up-right
+// (the second end is first + 1, W, W + 1, 1 - W).
 __global__ void seg_pack_kernel(const uint64_t* __restrict__ sorted, const int32_t* __restrict__ ea,
                                 const int32_t* __restrict__ eb, const float* __restrict__ w, uint32_t E,
-                                int32_t W, uint32_t* __restrict__ pk, float* __restrict__ pw) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < E; i += (size_t)gridDim.x * blockDim.x) {
+                                int32_t W, const uint32_t* first_at, uint32_t* __restrict__ pk,
+                                float* __restrict__ pw) {
+  const uint32_t first = first_at ? *first_at : 0u;
+  for (size_t i = first + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < E;
+       i += (size_t)gridDim.x * blockDim.x) {
     const uint32_t e = (uint32_t)(sorted[i] & 0xFFFFFFFFull);
     const int32_t a = ea[e], d = eb[e] - a;
     const uint32_t code = d == 1 ? 0u : d == W ? 1u : d == W + 1 ? 2u : 3u;
-    pk[i] = ((uint32_t)a << 2) | code;
-    pw[i] = w[e];
+    pk[i - first] = ((uint32_t)a << 2) | code;
+    pw[i - first] = w[e];
   }
+}
+
+// ---- the zero-weight edges: connected components -------------------------
+//
+// segment_graph's pass starts with singletons whose threshold is k / 1.  The
+// sorted edges begin with the weight-0 ones, and with k >= 0 every set
+// admits weight 0 (k / |C| >= 0, and a set merged at weight 0 has threshold
+// 0 + k / |C|).  So the pass over them joins exactly the connected
+// components of the weight-0 edges, whatever their order, and leaves each
+// component with threshold k / |C| (its last join sets it at its final
+// size).  The GPU builds that forest; the host starts its pass after those
+// edges, and its small-component pass skips them too (their ends are in one
+// set from then on).
+
+// z = the number of weight-0 edges (sorted keys whose order bits are those
+// of +0), or 0 when k < 0
+__global__ void seg_zero_count_kernel(const uint64_t* __restrict__ sorted, uint32_t E, int enabled, uint32_t* z) {
+  const uint32_t zb = 0x80000000u;  // order bits of +0
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < E; i += (size_t)gridDim.x * blockDim.x) {
+    const bool here = (uint32_t)(sorted[i] >> 32) == zb;
+    const bool next = i + 1 < E && (uint32_t)(sorted[i + 1] >> 32) == zb;
+    if (enabled && here && !next) *z = (uint32_t)(i + 1);  // the one boundary
+  }
+}
+
+__global__ void seg_forest_init_kernel(int32_t* __restrict__ parent, int32_t* __restrict__ size, uint32_t n) {
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+    parent[v] = (int32_t)v;
+    size[v] = 0;
+  }
+}
+
+// root of x, halving the path (only non-root entries are rewritten here;
+// roots change only by the hooking CAS)
+__device__ __forceinline__ int32_t seg_root(volatile int32_t* parent, int32_t x) {
+  while (true) {
+    const int32_t p = parent[x];
+    if (p == x) return x;
+    const int32_t g = parent[p];
+    if (g != p) parent[x] = g;
+    x = p;
+  }
+}
+
+// join the ends of each weight-0 edge: the larger root is hooked under the
+// smaller by CAS (a failed CAS means another thread hooked it: retry from
+// its new root), so each component's root ends as its smallest pixel
+__global__ void seg_zero_link_kernel(const uint64_t* __restrict__ sorted, const int32_t* __restrict__ ea,
+                                     const int32_t* __restrict__ eb, const uint32_t* z, int32_t* parent) {
+  const uint32_t nz = *z;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nz; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t e = (uint32_t)(sorted[i] & 0xFFFFFFFFull);
+    int32_t a = ea[e], b = eb[e];
+    while (true) {
+      a = seg_root(parent, a);
+      b = seg_root(parent, b);
+      if (a == b) break;
+      if (a > b) {
+        const int32_t t = a;
+        a = b;
+        b = t;
+      }
+      if (atomicCAS(parent + b, b, a) == b) break;
+    }
+  }
+}
+
+__global__ void seg_forest_flatten_kernel(int32_t* parent, int32_t* __restrict__ size, uint32_t n) {
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+    const int32_t r = seg_root(parent, (int32_t)v);
+    parent[v] = r;
+    atomicAdd(size + r, 1);
+  }
+}
+
+// thresholds of the roots: 0 + k / |C| = k / |C| (singletons: k / 1)
+__global__ void seg_forest_thr_kernel(const int32_t* __restrict__ parent, const int32_t* __restrict__ size,
+                                      float k, uint32_t n, float* __restrict__ thr) {
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
+    thr[v] = parent[v] == (int32_t)v ? __fdiv_rn(k, (float)size[v]) : 0.0f;
 }
 
 }  // namespace
@@ -540,14 +625,49 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
   return cudaSuccess;
 }
 
-size_t seg_merge_pinned_bytes(int32_t W, int32_t H) { return 8 * (size_t)seg_num_edges(W, H) + 64; }
+// pinned layout: 64 bytes of words ([0] error bits, [1] zero-weight edges,
+// [8] the front stage's error word), the packed edges and their weights,
+// then the forest after the zero-weight edges: parent, size, threshold
+size_t seg_merge_pinned_bytes(int32_t W, int32_t H) {
+  return 64 + 8 * (size_t)seg_num_edges(W, H) + 12 * (size_t)W * H;
+}
 
-// The graph stage with the merge passes streamed: the GPU packs the sorted
-// edges (8 bytes each), they come back in n_chunks copies into pinned host
-// memory, and the host runs segment_graph's pass over each chunk as soon as
-// its copy has landed, reading the edges in order; then the small-component
-// pass and the labels.  Same partition and numbering as seg_merge over the
-// same sorted order.
+namespace {
+
+// The host's part of the merge, on the forest the GPU left after the
+// weight-0 edges (parent, size and threshold at the roots, in pinned
+// memory): segment_graph's pass over the remaining sorted edges, chunk by
+// chunk as their copies land, then the small-component pass, then labels
+// numbered by smallest pixel.  A threshold is only read at the current root
+// of its set, so the partition does not depend on the union rule.
+struct PinnedForest {
+  int32_t* parent;
+  int32_t* size;
+  float* thr;
+  int32_t find(int32_t x) {
+    while (parent[x] != x) {
+      parent[x] = parent[parent[x]];
+      x = parent[x];
+    }
+    return x;
+  }
+  int32_t join(int32_t a, int32_t b) {  // roots; returns the new root
+    if (size[a] < size[b]) std::swap(a, b);
+    parent[b] = a;
+    size[a] += size[b];
+    return a;
+  }
+};
+
+}  // namespace
+
+// The graph stage with the merge passes streamed: the GPU sorts the edges,
+// joins the weight-0 ones (their connected components), packs the rest
+// (8 bytes each), and they come back in n_chunks copies into pinned host
+// memory after the forest; the host runs segment_graph's pass over each
+// chunk as soon as its copy has landed, then the small-component pass and
+// the labels.  Same partition and numbering as seg_merge over the same
+// sorted order.
 cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
                             int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
                             float ks, void* ws, int sms, cudaStream_t st, void* pinned, const cudaEvent_t* ev,
@@ -558,52 +678,71 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
   SegGraphDev g;
   cudaError_t e = seg_graph_device(hsv_host, depth_host, sal_host, W, H, mask, len, kdv, kdc, kx, ks, ws, sms, st, &g);
   if (e != cudaSuccess) return e;
-  uint32_t* h_err = reinterpret_cast<uint32_t*>(pinned);
+  uint32_t* h_words = reinterpret_cast<uint32_t*>(pinned);
   uint32_t* h_pk = reinterpret_cast<uint32_t*>(static_cast<char*>(pinned) + 64);
   float* h_pw = reinterpret_cast<float*>(h_pk + E);
+  int32_t* h_par = reinterpret_cast<int32_t*>(h_pw + E);
+  int32_t* d_par = reinterpret_cast<int32_t*>(g.tmp);
+  int32_t* d_size = d_par + n;
+  float* d_thr = reinterpret_cast<float*>(d_size + n);
+  uint32_t* d_z = g.misc + 3;
+  // the forest after the weight-0 edges, and the remaining edges packed
   if (E > 0) {
-    uint32_t* d_pk = reinterpret_cast<uint32_t*>(g.spare);
-    float* d_pw = reinterpret_cast<float*>(d_pk + E);
-    seg_pack_kernel<<<grid_for(E, 256, sms), 256, 0, st>>>(g.sorted, g.ea, g.eb, g.w, (uint32_t)E, W, d_pk, d_pw);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(h_err, g.misc + 2, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-    for (int c = 0; c < n_chunks; ++c) {
-      const uint64_t c0 = E * c / n_chunks, c1 = E * (c + 1) / n_chunks;
-      if (c1 > c0) {
-        if ((e = cudaMemcpyAsync(h_pk + c0, d_pk + c0, 4 * (c1 - c0), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-          return e;
-        if ((e = cudaMemcpyAsync(h_pw + c0, d_pw + c0, 4 * (c1 - c0), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-          return e;
-      }
-      if ((e = cudaEventRecord(ev[c], st)) != cudaSuccess) return e;
-    }
+    seg_zero_count_kernel<<<grid_for(E, 256, sms), 256, 0, st>>>(g.sorted, (uint32_t)E, k >= 0.0f ? 1 : 0, d_z);
+    if ((e = cudaMemcpyAsync(h_words, g.misc + 2, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
+  }
+  seg_forest_init_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_size, n);
+  if (E > 0) seg_zero_link_kernel<<<grid_for(E, 256, sms), 256, 0, st>>>(g.sorted, g.ea, g.eb, d_z, d_par);
+  seg_forest_flatten_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_size, n);
+  seg_forest_thr_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_size, k, n, d_thr);
+  uint32_t* d_pk = reinterpret_cast<uint32_t*>(g.spare);
+  float* d_pw = reinterpret_cast<float*>(d_pk + E);
+  if (E > 0)
+    seg_pack_kernel<<<grid_for(E, 256, sms), 256, 0, st>>>(g.sorted, g.ea, g.eb, g.w, (uint32_t)E, W, d_z, d_pk,
+                                                           d_pw);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  uint64_t E2 = 0;  // edges after the weight-0 ones
+  if (E > 0) {
     if ((e = cudaEventSynchronize(ev[0])) != cudaSuccess) return e;
-    *err_host = *h_err;
-    if (*err_host) {  // let the caller report it; finish the copies first
+    *err_host = h_words[0];
+    if (*err_host) {  // let the caller report it; finish the work first
       if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
       return cudaSuccess;
     }
+    E2 = E - h_words[1];
   } else {
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     *err_host = 0;
   }
+  if ((e = cudaMemcpyAsync(h_par, d_par, 12 * (size_t)n, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  const int chunks = E2 > 0 ? n_chunks : 0;
+  for (int c = 0; c < chunks; ++c) {
+    const uint64_t c0 = E2 * c / n_chunks, c1 = E2 * (c + 1) / n_chunks;
+    if (c1 > c0) {
+      if ((e = cudaMemcpyAsync(h_pk + c0, d_pk + c0, 4 * (c1 - c0), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return e;
+      if ((e = cudaMemcpyAsync(h_pw + c0, d_pw + c0, 4 * (c1 - c0), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return e;
+    }
+    if ((e = cudaEventRecord(ev[c], st)) != cudaSuccess) return e;
+  }
+  if (chunks == 0 && (e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   const int32_t dstep[4] = {1, W, W + 1, 1 - W};
-  Forest f(n);
-  std::vector<float> thr(n, k / (float)1);  // THRESHOLD(1, k)
-  for (int c = 0; c < (E > 0 ? n_chunks : 0); ++c) {
-    const uint64_t c0 = E * c / n_chunks, c1 = E * (c + 1) / n_chunks;
-    if ((e = cudaEventSynchronize(ev[c])) != cudaSuccess) return e;
+  PinnedForest f{h_par, h_par + n, reinterpret_cast<float*>(h_par + 2 * (size_t)n)};
+  for (int c = 0; c < chunks; ++c) {
+    const uint64_t c0 = E2 * c / n_chunks, c1 = E2 * (c + 1) / n_chunks;
+    if ((e = cudaEventSynchronize(ev[c])) != cudaSuccess) return e;  // chunk 0's event follows the forest too
     for (uint64_t i = c0; i < c1; ++i) {
       const uint32_t pk = h_pk[i];
       const int32_t a0 = (int32_t)(pk >> 2), b0 = a0 + dstep[pk & 3u];
       const float we = h_pw[i];
       const int32_t a = f.find(a0), b = f.find(b0);
-      if (a == b || !(we <= thr[a] && we <= thr[b])) continue;
+      if (a == b || !(we <= f.thr[a] && we <= f.thr[b])) continue;
       const int32_t r = f.join(a, b);
-      thr[r] = we + k / (float)f.size[r];
+      f.thr[r] = we + k / (float)f.size[r];
     }
   }
-  for (uint64_t i = 0; i < E; ++i) {
+  for (uint64_t i = 0; i < E2; ++i) {
     const uint32_t pk = h_pk[i];
     const int32_t a0 = (int32_t)(pk >> 2), b0 = a0 + dstep[pk & 3u];
     const int32_t a = f.find(a0), b = f.find(b0);
