@@ -541,10 +541,17 @@ __global__ void seg_zero_count_kernel(const uint64_t* __restrict__ sorted, uint3
   }
 }
 
-__global__ void seg_forest_init_kernel(int32_t* __restrict__ parent, int32_t* __restrict__ size, uint32_t n) {
+// A set's size and threshold side by side (one cache line holds both, the
+// host reads them together).
+struct SetState {
+  int32_t size;
+  float thr;
+};
+
+__global__ void seg_forest_init_kernel(int32_t* __restrict__ parent, SetState* __restrict__ state, uint32_t n) {
   for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
     parent[v] = (int32_t)v;
-    size[v] = 0;
+    state[v].size = 0;
   }
 }
 
@@ -583,19 +590,19 @@ __global__ void seg_zero_link_kernel(const uint64_t* __restrict__ sorted, const 
   }
 }
 
-__global__ void seg_forest_flatten_kernel(int32_t* parent, int32_t* __restrict__ size, uint32_t n) {
+__global__ void seg_forest_flatten_kernel(int32_t* parent, SetState* __restrict__ state, uint32_t n) {
   for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
     const int32_t r = seg_root(parent, (int32_t)v);
     parent[v] = r;
-    atomicAdd(size + r, 1);
+    atomicAdd(&state[r].size, 1);
   }
 }
 
-// thresholds of the roots: 0 + k / |C| = k / |C| (singletons: k / 1)
-__global__ void seg_forest_thr_kernel(const int32_t* __restrict__ parent, const int32_t* __restrict__ size,
-                                      float k, uint32_t n, float* __restrict__ thr) {
+// the roots' thresholds: 0 + k / |C| = k / |C| (singletons: k / 1)
+__global__ void seg_forest_thr_kernel(const int32_t* __restrict__ parent, float k, uint32_t n,
+                                      SetState* __restrict__ state) {
   for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
-    thr[v] = parent[v] == (int32_t)v ? __fdiv_rn(k, (float)size[v]) : 0.0f;
+    state[v].thr = parent[v] == (int32_t)v ? __fdiv_rn(k, (float)state[v].size) : 0.0f;
 }
 
 }  // namespace
@@ -627,7 +634,7 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
 
 // pinned layout: 64 bytes of words ([0] error bits, [1] zero-weight edges,
 // [8] the front stage's error word), the packed edges and their weights,
-// then the forest after the zero-weight edges: parent, size, threshold
+// then the forest after the zero-weight edges: parent, (size, threshold)
 size_t seg_merge_pinned_bytes(int32_t W, int32_t H) {
   return 64 + 8 * (size_t)seg_num_edges(W, H) + 12 * (size_t)W * H;
 }
@@ -642,8 +649,7 @@ namespace {
 // of its set, so the partition does not depend on the union rule.
 struct PinnedForest {
   int32_t* parent;
-  int32_t* size;
-  float* thr;
+  SetState* st;
   int32_t find(int32_t x) {
     while (parent[x] != x) {
       parent[x] = parent[parent[x]];
@@ -652,12 +658,15 @@ struct PinnedForest {
     return x;
   }
   int32_t join(int32_t a, int32_t b) {  // roots; returns the new root
-    if (size[a] < size[b]) std::swap(a, b);
+    if (st[a].size < st[b].size) std::swap(a, b);
     parent[b] = a;
-    size[a] += size[b];
+    st[a].size += st[b].size;
     return a;
   }
 };
+
+// how far ahead (in edges) the host brings the ends' parent entries into cache
+constexpr uint64_t kMergePrefetch = 16;
 
 }  // namespace
 
@@ -682,9 +691,8 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
   uint32_t* h_pk = reinterpret_cast<uint32_t*>(static_cast<char*>(pinned) + 64);
   float* h_pw = reinterpret_cast<float*>(h_pk + E);
   int32_t* h_par = reinterpret_cast<int32_t*>(h_pw + E);
-  int32_t* d_par = reinterpret_cast<int32_t*>(g.tmp);
-  int32_t* d_size = d_par + n;
-  float* d_thr = reinterpret_cast<float*>(d_size + n);
+  int32_t* d_par = reinterpret_cast<int32_t*>(g.tmp);  // the 12 n bytes of scratch: parent, then (size, threshold)
+  SetState* d_state = reinterpret_cast<SetState*>(d_par + n);
   uint32_t* d_z = g.misc + 3;
   // the forest after the weight-0 edges, and the remaining edges packed
   if (E > 0) {
@@ -692,10 +700,10 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
     if ((e = cudaMemcpyAsync(h_words, g.misc + 2, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
   }
-  seg_forest_init_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_size, n);
+  seg_forest_init_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_state, n);
   if (E > 0) seg_zero_link_kernel<<<grid_for(E, 256, sms), 256, 0, st>>>(g.sorted, g.ea, g.eb, d_z, d_par);
-  seg_forest_flatten_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_size, n);
-  seg_forest_thr_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_size, k, n, d_thr);
+  seg_forest_flatten_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_state, n);
+  seg_forest_thr_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, k, n, d_state);
   uint32_t* d_pk = reinterpret_cast<uint32_t*>(g.spare);
   float* d_pw = reinterpret_cast<float*>(d_pk + E);
   if (E > 0)
@@ -714,6 +722,7 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
   } else {
     *err_host = 0;
   }
+  SetState* h_state = reinterpret_cast<SetState*>(h_par + n);
   if ((e = cudaMemcpyAsync(h_par, d_par, 12 * (size_t)n, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
   const int chunks = E2 > 0 ? n_chunks : 0;
   for (int c = 0; c < chunks; ++c) {
@@ -728,25 +737,31 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
   }
   if (chunks == 0 && (e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   const int32_t dstep[4] = {1, W, W + 1, 1 - W};
-  PinnedForest f{h_par, h_par + n, reinterpret_cast<float*>(h_par + 2 * (size_t)n)};
+  PinnedForest f{h_par, h_state};
   for (int c = 0; c < chunks; ++c) {
     const uint64_t c0 = E2 * c / n_chunks, c1 = E2 * (c + 1) / n_chunks;
     if ((e = cudaEventSynchronize(ev[c])) != cudaSuccess) return e;  // chunk 0's event follows the forest too
     for (uint64_t i = c0; i < c1; ++i) {
+      if (i + kMergePrefetch < c1) {  // within the chunk that has landed
+        const uint32_t q = h_pk[i + kMergePrefetch];
+        const int32_t qa = (int32_t)(q >> 2);
+        __builtin_prefetch(h_par + qa, 1);
+        __builtin_prefetch(h_par + qa + dstep[q & 3u], 1);
+      }
       const uint32_t pk = h_pk[i];
       const int32_t a0 = (int32_t)(pk >> 2), b0 = a0 + dstep[pk & 3u];
       const float we = h_pw[i];
       const int32_t a = f.find(a0), b = f.find(b0);
-      if (a == b || !(we <= f.thr[a] && we <= f.thr[b])) continue;
+      if (a == b || !(we <= f.st[a].thr && we <= f.st[b].thr)) continue;
       const int32_t r = f.join(a, b);
-      f.thr[r] = we + k / (float)f.size[r];
+      f.st[r].thr = we + k / (float)f.st[r].size;
     }
   }
   for (uint64_t i = 0; i < E2; ++i) {
     const uint32_t pk = h_pk[i];
     const int32_t a0 = (int32_t)(pk >> 2), b0 = a0 + dstep[pk & 3u];
     const int32_t a = f.find(a0), b = f.find(b0);
-    if (a != b && ((float)f.size[a] < min_size || (float)f.size[b] < min_size)) f.join(a, b);
+    if (a != b && ((float)f.st[a].size < min_size || (float)f.st[b].size < min_size)) f.join(a, b);
   }
   std::vector<int32_t> id(n, -1);
   uint32_t next = 0;
