@@ -207,28 +207,34 @@ __global__ void rs_hist_kernel(const uint64_t* __restrict__ keys, uint32_t n, in
   hist[(size_t)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
 }
 
-// exclusive prefix sum of a[0, total) in place, one block of 1024 threads
-__global__ void rs_scan_kernel(uint32_t* a, uint32_t total) {
-  __shared__ uint32_t part[1024];
-  const uint32_t per = (total + 1023u) / 1024u;
-  const uint32_t lo = threadIdx.x * per;
-  const uint32_t hi = lo + per < total ? lo + per : total;
+// Exclusive prefix sums of the histogram's digit rows (digit-major: row d
+// holds the counts of digit d in tiles 0 .. nblk - 1), one CTA of
+// kRsThreads per row, in place; row totals into tot[d].
+__global__ void rs_rowscan_kernel(uint32_t* hist, uint32_t nblk, uint32_t* tot) {
+  __shared__ uint32_t wsum[kRsThreads / 32];
+  uint32_t* row = hist + (size_t)blockIdx.x * nblk;
+  const uint32_t per = (nblk + kRsThreads - 1) / kRsThreads;
+  const uint32_t lo = threadIdx.x * per, hi = min(lo + per, nblk);
   uint32_t s = 0;
-  for (uint32_t i = lo; i < hi; ++i) s += a[i];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  for (uint32_t off = 1; off < 1024u; off <<= 1) {
-    const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
-    __syncthreads();
-    part[threadIdx.x] += v;
-    __syncthreads();
+  for (uint32_t i = lo; i < hi; ++i) s += row[i];
+  // exclusive scan of the threads' sums
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = s;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  uint32_t before = 0;
+  for (int w = 0; w < warp; ++w) before += wsum[w];
+  uint32_t run = before + x - s;
   for (uint32_t i = lo; i < hi; ++i) {
-    const uint32_t v = a[i];
-    a[i] = run;
+    const uint32_t v = row[i];
+    row[i] = run;
     run += v;
   }
+  if (threadIdx.x == kRsThreads - 1) tot[blockIdx.x] = before + x;
 }
 
 // Stable scatter of one block's tile: keys go out in tile order within each
@@ -236,11 +242,27 @@ __global__ void rs_scan_kernel(uint32_t* a, uint32_t total) {
 // digit's running position + the same digit's count in earlier warps of the
 // round + its rank among equal digits of its own warp.
 __global__ void rs_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* __restrict__ out, uint32_t n,
-                                  int shift, const uint32_t* __restrict__ offs, uint32_t nblk, uint32_t* err) {
+                                  int shift, const uint32_t* __restrict__ offs, const uint32_t* __restrict__ tot,
+                                  uint32_t nblk, uint32_t* err) {
   __shared__ uint32_t base[kRsThreads];
   __shared__ uint32_t wcnt[kRsThreads / 32][kRsThreads];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  base[threadIdx.x] = offs[(size_t)threadIdx.x * nblk + blockIdx.x];
+  {
+    // digit d's first position: the keys of smaller digits (exclusive scan
+    // of the row totals), then this tile's place in row d
+    const uint32_t t = tot[threadIdx.x];
+    uint32_t x = t;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wcnt[0][warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int w = 0; w < warp; ++w) before += wcnt[0][w];
+    base[threadIdx.x] = before + x - t + offs[(size_t)threadIdx.x * nblk + blockIdx.x];
+    __syncthreads();  // wcnt is cleared below
+  }
   const size_t tile = (size_t)blockIdx.x * kRsTile;
   for (int r = 0; r < kRsItems; ++r) {
     for (int w = 0; w < kRsThreads / 32; ++w) wcnt[w][threadIdx.x] = 0u;
@@ -392,7 +414,7 @@ size_t seg_workspace_bytes(int32_t W, int32_t H) {
   const size_t nblk = (size_t)((E + kRsTile - 1) / kRsTile);
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   return al(3 * n) + al(2 * n) + al(4 * n) + 2 * al(12 * n) + 2 * al(8 * E) + 3 * al(4 * E) +
-         al(4 * 256 * (nblk ? nblk : 1)) + al(16);
+         al(4 * 256 * (nblk ? nblk : 1)) + al(4 * 256) + al(16);
 }
 
 void seg_ws_inputs(void* ws, int32_t W, int32_t H, uint8_t** hsv, uint16_t** depth, float** sal) {
@@ -450,6 +472,8 @@ cudaError_t seg_graph_device(const uint8_t* hsv_host[3], const uint16_t* depth_h
   const uint32_t nblk = (uint32_t)((E + kRsTile - 1) / kRsTile);
   uint32_t* d_hist = (uint32_t*)p;
   p += al(4 * 256 * (nblk ? nblk : 1));
+  uint32_t* d_tot = (uint32_t*)p;
+  p += al(4 * 256);
   uint32_t* d_misc = (uint32_t*)p;
 
   cudaError_t e;
@@ -489,8 +513,9 @@ cudaError_t seg_graph_device(const uint8_t* hsv_host[3], const uint16_t* depth_h
     for (int shift = 0; shift < 64; shift += 8) {
       if (shift < 32 && shift >= idx_bits) continue;  // all keys share these digits
       rs_hist_kernel<<<nblk, kRsThreads, 0, st>>>(src, (uint32_t)E, shift, d_hist, nblk);
-      rs_scan_kernel<<<1, 1024, 0, st>>>(d_hist, 256u * nblk);
-      rs_scatter_kernel<<<nblk, kRsThreads, 0, st>>>(src, dst, (uint32_t)E, shift, d_hist, nblk, d_misc + 2);
+      rs_rowscan_kernel<<<kRsThreads, kRsThreads, 0, st>>>(d_hist, nblk, d_tot);
+      rs_scatter_kernel<<<nblk, kRsThreads, 0, st>>>(src, dst, (uint32_t)E, shift, d_hist, d_tot, nblk,
+                                                     d_misc + 2);
       std::swap(src, dst);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;

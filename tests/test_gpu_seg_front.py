@@ -13,8 +13,10 @@
   * the cluster records of PostSegmFilter (exact moments, same filter).
 
 Frames: the production-size C2 frame (8 objects), the 15-object frame of
-the stress configuration, and a small crop whose shrunk map is not a
-multiple of the sampling grid."""
+the stress configuration, a small crop whose shrunk map is not a multiple
+of the sampling grid, and the 15-object frame at twice the size (1280x960):
+its 256x192 shrunk map is too large for shared memory, so both inpainting
+kernels run from global memory."""
 import numpy as np
 import pytest
 
@@ -29,8 +31,11 @@ def _frames():
     w2 = scene.workload_c2()
     d2, _, rgb2 = w2["frames"][0]
     d5, _, rgb5 = scene.segmentation_frame_c5()
+    big = (np.ascontiguousarray(np.repeat(np.repeat(rgb5, 2, axis=0), 2, axis=1)),
+           np.ascontiguousarray(np.repeat(np.repeat(d5, 2, axis=0), 2, axis=1)))
     return {"c2": (rgb2, d2), "c5": (rgb5, d5),
-            "crop": (np.ascontiguousarray(rgb5[60:223, 90:338]), np.ascontiguousarray(d5[60:223, 90:338]))}
+            "crop": (np.ascontiguousarray(rgb5[60:223, 90:338]), np.ascontiguousarray(d5[60:223, 90:338])),
+            "big": big}
 
 
 FRAMES = _frames()
@@ -41,7 +46,7 @@ def _rec(c):
             c.nan_ratio, c.dark_ratio, tuple(c.eig), c.eccentricity, c.far, c.kept)
 
 
-@pytest.mark.parametrize("name", ["crop", "c2", "c5"])
+@pytest.mark.parametrize("name", ["crop", "c2", "c5", "big"])
 def test_front_stages_equal_the_oracle(gpu_ctx, name):
     bgr, depth = FRAMES[name]
     out = gpu_ctx.segment_rgbd(bgr, depth, planes=True)
