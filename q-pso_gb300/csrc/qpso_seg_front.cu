@@ -123,24 +123,43 @@ __global__ void smooth_cmap_kernel(const uint16_t* __restrict__ d, uint8_t* __re
   if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) atomicOr(misc, 1u);
 }
 
-// Horizontal distance to the nearest marked pixel of the row (kInf: none),
-// one thread per row, two sweeps.
+// Horizontal distance to the nearest marked pixel of the row (kInf: none):
+// min(x - L, R - x) with L the last marked pixel at or before x and R the
+// first at or after it.  One warp per row, 32 pixels at a time: L is a
+// running maximum (left to right), R a running minimum (right to left),
+// each a warp scan plus the carry from the previous 32.
 constexpr int32_t kInf = 0x3fffffff;
 
 __global__ void edt_rows_kernel(const uint8_t* __restrict__ cm, int32_t* __restrict__ g, FrontConst c) {
-  const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= c.H) return;
+  const int32_t r = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= c.H) return;  // whole warps
   const uint8_t* row = cm + (size_t)r * c.W;
   int32_t* gr = g + (size_t)r * c.W;
-  int32_t last = -kInf;
-  for (int32_t x = 0; x < c.W; ++x) {
-    if (row[x]) last = x;
-    gr[x] = last == -kInf ? kInf : x - last;
+  int32_t carry = -kInf;
+  for (int32_t x0 = 0; x0 < c.W; x0 += 32) {
+    const int32_t x = x0 + lane;
+    int32_t L = (x < c.W && row[x]) ? x : -kInf;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(0xffffffffu, L, o);
+      if (lane >= o) L = max(L, y);
+    }
+    L = max(L, carry);
+    carry = __shfl_sync(0xffffffffu, L, 31);
+    if (x < c.W) gr[x] = L == -kInf ? kInf : x - L;
   }
-  last = kInf;
-  for (int32_t x = c.W - 1; x >= 0; --x) {
-    if (row[x]) last = x;
-    if (last != kInf && last - x < gr[x]) gr[x] = last - x;
+  carry = kInf;
+  const int32_t last0 = ((c.W - 1) / 32) * 32;
+  for (int32_t x0 = last0; x0 >= 0; x0 -= 32) {
+    const int32_t x = x0 + lane;
+    int32_t R = (x < c.W && row[x]) ? x : kInf;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_down_sync(0xffffffffu, R, o);
+      if (lane + o < 32) R = min(R, y);
+    }
+    R = min(R, carry);
+    carry = __shfl_sync(0xffffffffu, R, 0);
+    if (x < c.W && R != kInf && R - x < gr[x]) gr[x] = R - x;
   }
 }
 
@@ -184,22 +203,59 @@ __global__ void smooth_radius_kernel(const uint16_t* __restrict__ d, const int32
 // Summed-area tables of ModDepth (float, the running row sum added to the
 // entry above, in that order) and of its zeros (int).  Rows: one thread per
 // row, sequential in x; columns: one thread per column, sequential in y.
+// Row prefix sums of the unmarked depths (float, in order) and of the zero
+// pixels.  One warp per row, 32 pixels at a time with an integer warp scan:
+// while the row's total stays at or below 2^24 every partial sum is an
+// integer that float holds exactly, so each in-order float addition is
+// exact and the integer prefix is the same value.  A row whose total
+// exceeds 2^24 is summed again in order by one lane.
 __global__ void integral_rows_kernel(const uint16_t* __restrict__ d, const uint8_t* __restrict__ cm,
                                      float* __restrict__ rs, int32_t* __restrict__ rz, FrontConst c) {
-  const int32_t y = blockIdx.x * blockDim.x + threadIdx.x;
-  if (y >= c.H) return;
-  float s = 0.0f;
-  int32_t z = 0;
-  for (int32_t x = 0; x < c.W; ++x) {
-    const size_t p = (size_t)y * c.W + x;
-    const uint16_t v = cm[p] ? 0 : d[p];
-    s = __fadd_rn(s, (float)v);
-    z += v == 0;
-    rs[p] = s;
-    rz[p] = z;
+  const int32_t y = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (y >= c.H) return;  // whole warps
+  const size_t row = (size_t)y * c.W;
+  unsigned long long cs = 0;  // carries: depth sum (checked against 2^24 below), zero count
+  int32_t cz = 0;
+  for (int32_t x0 = 0; x0 < c.W; x0 += 32) {
+    const int32_t x = x0 + lane;
+    unsigned long long v = 0;
+    int32_t z = 0;
+    if (x < c.W) {
+      v = cm[row + x] ? 0u : d[row + x];
+      z = v == 0u;
+    }
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long sv = __shfl_up_sync(0xffffffffu, v, o);
+      const int32_t sz = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) {
+        v += sv;
+        z += sz;
+      }
+    }
+    v += cs;
+    z += cz;
+    if (x < c.W) {
+      rs[row + x] = (float)v;
+      rz[row + x] = z;
+    }
+    cs = __shfl_sync(0xffffffffu, v, 31);
+    cz = __shfl_sync(0xffffffffu, z, 31);
+  }
+  __syncwarp();  // the lanes' stores before lane 0 rewrites the row
+  if (cs > (1ull << 24) && lane == 0) {  // rounding enters: the reference's order
+    float s = 0.0f;
+    for (int32_t x = 0; x < c.W; ++x) {
+      const uint16_t v = cm[row + x] ? 0 : d[row + x];
+      s = __fadd_rn(s, (float)v);
+      rs[row + x] = s;
+    }
   }
 }
 
+// Column prefix sums of the row sums, in order (float: here rounding
+// enters), one thread per column; the loads run eight rows ahead of the
+// additions.
 __global__ void integral_cols_kernel(const float* __restrict__ rs, const int32_t* __restrict__ rz,
                                      float* __restrict__ I, int32_t* __restrict__ N, FrontConst c) {
   const int32_t x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -209,13 +265,31 @@ __global__ void integral_cols_kernel(const float* __restrict__ rs, const int32_t
   int32_t za = 0;
   I[x] = 0.0f;
   N[x] = 0;
-  for (int32_t y = 0; y < c.H; ++y) {
-    if (x > 0) {
-      acc = __fadd_rn(acc, rs[(size_t)y * c.W + x - 1]);
-      za += rz[(size_t)y * c.W + x - 1];
+  for (int32_t y0 = 0; y0 < c.H; y0 += 8) {
+    float fv[8];
+    int32_t zv[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int32_t y = y0 + j;
+      fv[j] = 0.0f;
+      zv[j] = 0;
+      if (x > 0 && y < c.H) {
+        fv[j] = rs[(size_t)y * c.W + x - 1];
+        zv[j] = rz[(size_t)y * c.W + x - 1];
+      }
     }
-    I[(size_t)(y + 1) * s1 + x] = acc;
-    N[(size_t)(y + 1) * s1 + x] = za;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int32_t y = y0 + j;
+      if (y < c.H) {
+        if (x > 0) {
+          acc = __fadd_rn(acc, fv[j]);
+          za += zv[j];
+        }
+        I[(size_t)(y + 1) * s1 + x] = acc;
+        N[(size_t)(y + 1) * s1 + x] = za;
+      }
+    }
   }
 }
 
@@ -1033,9 +1107,9 @@ cudaError_t seg_front_run(const SegFrontArgs& a, void* ws, int sms, size_t smem_
   front_colour_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_bgr, n, a.hsv_out, d_gray);
   // depth smoothing
   smooth_cmap_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_raw, d_cm, d_misc, c);
-  edt_rows_kernel<<<(H + 127) / 128, 128, 0, st>>>(d_cm, d_g, c);
+  edt_rows_kernel<<<(H + 7) / 8, 256, 0, st>>>(d_cm, d_g, c);  // a warp per row
   smooth_radius_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_raw, d_g, d_misc, d_R, c);
-  integral_rows_kernel<<<(H + 127) / 128, 128, 0, st>>>(d_raw, d_cm, d_rs, d_rz, c);
+  integral_rows_kernel<<<(H + 7) / 8, 256, 0, st>>>(d_raw, d_cm, d_rs, d_rz, c);  // a warp per row
   integral_cols_kernel<<<(W + 1 + 127) / 128, 128, 0, st>>>(d_rs, d_rz, d_I, d_N, c);
   smooth_out_kernel<<<grid_of(n, T, sms), T, 0, st>>>(d_raw, d_R, d_I, d_N, d_sm, c);
   // inpainting

@@ -16,7 +16,9 @@ Frames: the production-size C2 frame (8 objects), the 15-object frame of
 the stress configuration, a small crop whose shrunk map is not a multiple
 of the sampling grid, and the 15-object frame at twice the size (1280x960):
 its 256x192 shrunk map is too large for shared memory, so both inpainting
-kernels run from global memory."""
+kernels run from global memory; and the 15-object frame's depth times 40
+(up to 65535 mm), whose row sums pass 2^24, where float rounding enters the
+summed-area tables."""
 import numpy as np
 import pytest
 
@@ -35,7 +37,8 @@ def _frames():
            np.ascontiguousarray(np.repeat(np.repeat(d5, 2, axis=0), 2, axis=1)))
     return {"c2": (rgb2, d2), "c5": (rgb5, d5),
             "crop": (np.ascontiguousarray(rgb5[60:223, 90:338]), np.ascontiguousarray(d5[60:223, 90:338])),
-            "big": big}
+            "big": big,
+            "far": (rgb5, np.ascontiguousarray(np.minimum(d5.astype(np.int64) * 40, 65535).astype(np.uint16)))}
 
 
 FRAMES = _frames()
@@ -46,7 +49,7 @@ def _rec(c):
             c.nan_ratio, c.dark_ratio, tuple(c.eig), c.eccentricity, c.far, c.kept)
 
 
-@pytest.mark.parametrize("name", ["crop", "c2", "c5", "big"])
+@pytest.mark.parametrize("name", ["crop", "c2", "c5", "big", "far"])
 def test_front_stages_equal_the_oracle(gpu_ctx, name):
     bgr, depth = FRAMES[name]
     out = gpu_ctx.segment_rgbd(bgr, depth, planes=True)
