@@ -91,6 +91,21 @@ __device__ __forceinline__ uint32_t sat_count(const int32_t* sat, int32_t w, int
   return (uint32_t)(a - b - c + d);
 }
 
+// The summed-area table's words that sat_count reads, brought into L1.
+__device__ __forceinline__ void sat_prefetch(const int32_t* sat, int32_t w, int32_t h, int64_t x0, int64_t x1,
+                                             int64_t y0, int64_t y1) {
+  x0 = x0 < 0 ? 0 : (x0 > w ? w : x0);
+  x1 = x1 < 0 ? 0 : (x1 > w ? w : x1);
+  y0 = y0 < 0 ? 0 : (y0 > h ? h : y0);
+  y1 = y1 < 0 ? 0 : (y1 > h ? h : y1);
+  if (x0 >= x1 || y0 >= y1) return;
+  const int64_t W1 = (int64_t)w + 1;
+  prefetch_l1(sat + y1 * W1 + x1);
+  prefetch_l1(sat + y0 * W1 + x1);
+  prefetch_l1(sat + y1 * W1 + x0);
+  prefetch_l1(sat + y0 * W1 + x0);
+}
+
 // Per-particle bookkeeping of the meshlet path.
 struct PartCtl {
   int32_t bound[4];                 // conservative pixel bound (domain-clipped)
@@ -480,6 +495,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
     pc.bound[2] = dy1;
     pc.bound[3] = dy0;
   }
+  if (tid == 0) ctl.maxpass = 1;
   if (cull_ok)
     for (int i = tid; i < np * (int)nm; i += T)
       mbox[(i / nm) * kCullCap + (i % nm)] = make_int4(kAabbInitMin, kAabbInitMax, kAabbInitMin, kAabbInitMax);
@@ -558,12 +574,7 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
     pc.box[3] = kAabbInitMax;
     pc.nR = pc.nNo = pc.nSegR = 0;
     pc.lo = pc.hi = 0;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    int mp = 1;
-    for (int k = 0; k < np; ++k) mp = max(mp, ctl.part[k].npass);
-    ctl.maxpass = mp;
+    atomicMax(&ctl.maxpass, pc.npass);
   }
   __syncthreads();
   const int maxpass = ctl.maxpass;
@@ -860,6 +871,21 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
       if (cull) __syncthreads();  // the list is rebuilt for the next chunk
     }
     __syncthreads();
+    // the render AABB is final after pass 0's items: one thread per particle
+    // (from the last warp) brings the fitness's summed-area words into L1
+    if (pass == 0 && tid >= T - np) {
+      const PartCtl& pc = ctl.part[T - 1 - tid];
+      const SolveParams& prm = I.prm;
+      const int32_t minX = min(pc.box[0], prm.cl_min_x), maxX = max(pc.box[1], prm.cl_max_x);
+      const int32_t minY = min(pc.box[2], prm.cl_min_y), maxY = max(pc.box[3], prm.cl_max_y);
+      const int64_t Ww = (int64_t)maxX - minX, Hh = (int64_t)maxY - minY;
+      if (Ww > 0 && Hh > 0) {
+        const int64_t pad = (1024 - (Ww * Hh) % 1024) % 1024;
+        const int64_t L = pad < Ww ? pad : Ww;
+        sat_prefetch(I.sat, W, H, minX, maxX, minY, maxY);
+        sat_prefetch(I.sat, W, H, minX, (int64_t)minX + L, maxY, (int64_t)maxY + 1);
+      }
+    }
     // 2e. scan every active particle's tile over its render AABB
     for (int k = 0; k < np; ++k) {
       PartCtl& pc = ctl.part[k];
