@@ -78,3 +78,41 @@ def test_segment_planes_refuses_nan_weights(gpu_ctx):
     h8, s8, v8, d, sal = frame("scene", 24, 32, 1)
     labels, n = gpu_ctx.segment_planes(h8, s8, v8, d, sal, qpso.seg_params(min_size=20.0))
     assert n >= 1 and labels.min() == 0 and labels.max() == n - 1
+
+
+def _streamed_vs_oracle(ctx, h8, s8, v8, d, sal, prm):
+    """Labels of the streamed merge (the GPU joins the weight-0 edges, the
+    host the rest) against the oracle's merge of the GPU's own weights."""
+    H, W = h8.shape
+    _, _, w = ctx.segment_planes(h8, s8, v8, d, sal, prm, weights=True)
+    labels, n = ctx.segment_planes(h8, s8, v8, d, sal, prm)
+    a, b = qpso.segment_edge_ends(W, H)
+    lists, ns, _ = po.segment_graph(H * W, po.edges_array(a, b, w), prm.k, prm.min_size, True)
+    assert n == ns
+    assert np.array_equal(labels.ravel(), _labels_from_lists(lists, H * W))
+    return w
+
+
+@pytest.mark.parametrize("k", [-0.001, 0.0, 0.005, 0.05])
+def test_streamed_merge_against_oracle(gpu_ctx, k):
+    """k < 0: no set admits weight 0 beyond its own, the GPU leaves
+    singletons and the host runs every edge; k >= 0: the weight-0 edges are
+    joined on the GPU first."""
+    h8, s8, v8, d, sal = frame("scene", 480, 640, 11)
+    w = _streamed_vs_oracle(gpu_ctx, h8, s8, v8, d, sal, qpso.seg_params(k=k, min_size=50.0))
+    assert (w == 0).mean() > 0.05  # the frame has a weight-0 run to join
+
+
+def test_streamed_merge_mostly_zero_weights(gpu_ctx):
+    """A frame of one colour with one brighter, raised block: nearly every
+    weight is 0, so the host is left a couple of hundred edges."""
+    H, W = 96, 128
+    h8 = np.full((H, W), 40, np.uint8)
+    s8 = np.full((H, W), 90, np.uint8)
+    v8 = np.full((H, W), 150, np.uint8)
+    v8[40:52, 60:80] = 210
+    d = np.full((H, W), 1000, np.uint16)
+    d[40:52, 60:80] = 1300
+    sal = np.zeros((H, W), np.float32)
+    w = _streamed_vs_oracle(gpu_ctx, h8, s8, v8, d, sal, qpso.seg_params(min_size=20.0))
+    assert 0 < (w > 0).sum() < 0.05 * len(w)
