@@ -623,6 +623,94 @@ __global__ void seg_forest_flatten_kernel(int32_t* parent, SetState* __restrict_
   }
 }
 
+// ---- the small-component pass's candidate edges -------------------------
+//
+// After segment_graph's pass, an edge can join its ends in the
+// small-component pass only if, at that pass's start, they lie in different
+// sets and one of them is smaller than min_size: sets only grow and only
+// merge, so every other edge finds its ends in one set, or both sets large,
+// whatever the pass did before it.  The GPU lists those edges in sorted
+// order from the forest the host's first pass left (uploaded), and the host
+// runs the pass over the list alone.
+
+constexpr int kCandThreads = 1024;
+
+__global__ void seg_forest_roots_kernel(int32_t* parent, uint32_t n) {
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
+    parent[v] = seg_root(parent, (int32_t)v);
+}
+
+__device__ __forceinline__ bool seg_is_candidate(uint32_t pk, int32_t W, const int32_t* __restrict__ root,
+                                                 const SetState* __restrict__ st, float min_size) {
+  const int32_t a0 = (int32_t)(pk >> 2);
+  const uint32_t d = pk & 3u;
+  const int32_t b0 = a0 + (d == 0u ? 1 : d == 1u ? W : d == 2u ? W + 1 : 1 - W);
+  const int32_t ra = root[a0], rb = root[b0];
+  return ra != rb && ((float)st[ra].size < min_size || (float)st[rb].size < min_size);
+}
+
+// candidates per block of kCandThreads packed edges
+__global__ void __launch_bounds__(kCandThreads) seg_cand_count_kernel(const uint32_t* __restrict__ pk, uint32_t E2,
+                                                                      int32_t W, const int32_t* __restrict__ root,
+                                                                      const SetState* __restrict__ st,
+                                                                      float min_size, uint32_t* __restrict__ blk) {
+  const size_t i = (size_t)blockIdx.x * kCandThreads + threadIdx.x;
+  const bool c = i < E2 && seg_is_candidate(pk[i], W, root, st, min_size);
+  const int cnt = __syncthreads_count(c);
+  if (threadIdx.x == 0) blk[blockIdx.x] = (uint32_t)cnt;
+}
+
+// exclusive prefix of the block counts, in place; the total into blk[nb]
+__global__ void __launch_bounds__(kCandThreads) seg_cand_scan_kernel(uint32_t* blk, uint32_t nb) {
+  __shared__ uint32_t part[kCandThreads];
+  const uint32_t per = (nb + kCandThreads - 1) / kCandThreads;
+  const uint32_t lo = threadIdx.x * per, hi = min(lo + per, nb);
+  uint32_t s = 0;
+  for (uint32_t i = lo; i < hi; ++i) s += blk[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 1; off < kCandThreads; off <<= 1) {
+    const uint32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  for (uint32_t i = lo; i < hi; ++i) {
+    const uint32_t v = blk[i];
+    blk[i] = run;
+    run += v;
+  }
+  if (threadIdx.x == kCandThreads - 1) blk[nb] = part[kCandThreads - 1];
+}
+
+// the candidates, in sorted order
+__global__ void __launch_bounds__(kCandThreads) seg_cand_scatter_kernel(const uint32_t* __restrict__ pk, uint32_t E2,
+                                                                        int32_t W, const int32_t* __restrict__ root,
+                                                                        const SetState* __restrict__ st,
+                                                                        float min_size, const uint32_t* __restrict__ blk,
+                                                                        uint32_t* __restrict__ out) {
+  __shared__ uint32_t wbase[kCandThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t i = (size_t)blockIdx.x * kCandThreads + threadIdx.x;
+  const uint32_t v = i < E2 ? pk[i] : 0u;
+  const bool c = i < E2 && seg_is_candidate(v, W, root, st, min_size);
+  const unsigned bal = __ballot_sync(0xffffffffu, c);
+  if (lane == 0) wbase[warp] = (uint32_t)__popc(bal);
+  __syncthreads();
+  if (warp == 0) {  // exclusive scan of the warps' counts
+    const uint32_t cnt = lane < kCandThreads / 32 ? wbase[lane] : 0u;
+    uint32_t x = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane < kCandThreads / 32) wbase[lane] = x - cnt;
+  }
+  __syncthreads();
+  if (c) out[blk[blockIdx.x] + wbase[warp] + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = v;
+}
+
 // the roots' thresholds: 0 + k / |C| = k / |C| (singletons: k / 1)
 __global__ void seg_forest_thr_kernel(const int32_t* __restrict__ parent, float k, uint32_t n,
                                       SetState* __restrict__ state) {
@@ -658,7 +746,8 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
 }
 
 // pinned layout: 64 bytes of words ([0] error bits, [1] zero-weight edges,
-// [8] the front stage's error word), the packed edges and their weights,
+// [2] small-pass candidates, [8] the front stage's error word), the packed
+// edges and their weights,
 // then the forest after the zero-weight edges: parent, (size, threshold)
 size_t seg_merge_pinned_bytes(int32_t W, int32_t H) {
   return 64 + 8 * (size_t)seg_num_edges(W, H) + 12 * (size_t)W * H;
@@ -783,8 +872,30 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
       f.st[r].thr = we + k / (float)f.st[r].size;
     }
   }
-  for (uint64_t i = 0; i < E2; ++i) {
-    if (i + kMergePrefetch < E2) {  // every chunk has landed by now
+  // the small-component pass over the candidate edges, which the GPU lists
+  // from the forest the first pass left
+  uint64_t nc = 0;  // candidates
+  if (E2 > 0) {
+    const uint32_t nb = (uint32_t)((E2 + kCandThreads - 1) / kCandThreads);
+    uint32_t* d_cand = reinterpret_cast<uint32_t*>(g.sorted);  // free after the packing: 8 E bytes
+    uint32_t* d_blk = d_cand + E;
+    if ((e = cudaMemcpyAsync(d_par, h_par, 12 * (size_t)n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    seg_forest_roots_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, n);
+    seg_cand_count_kernel<<<nb, kCandThreads, 0, st>>>(d_pk, (uint32_t)E2, W, d_par, d_state, min_size, d_blk);
+    seg_cand_scan_kernel<<<1, kCandThreads, 0, st>>>(d_blk, nb);
+    seg_cand_scatter_kernel<<<nb, kCandThreads, 0, st>>>(d_pk, (uint32_t)E2, W, d_par, d_state, min_size, d_blk,
+                                                          d_cand);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(h_words + 2, d_blk + nb, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    nc = h_words[2];
+    if (nc > E2) return cudaErrorUnknown;  // cannot happen: at most every edge
+    // the list lands where the packed edges were (the host is done with them)
+    if (nc > 0 && (e = cudaMemcpyAsync(h_pk, d_cand, 4 * nc, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  }
+  for (uint64_t i = 0; i < nc; ++i) {
+    if (i + kMergePrefetch < nc) {
       const uint32_t q = h_pk[i + kMergePrefetch];
       const int32_t qa = (int32_t)(q >> 2);
       __builtin_prefetch(h_par + qa);
