@@ -1347,7 +1347,7 @@ qpso_status qpso_segment_planes(qpso_context* ctx, const uint8_t* h, const uint8
     uint32_t err = 0;
     QPSO_CUDA(ctx, seg_graph_merge(hsv, depth_mm, saliency, W, H, mask, len, prm->kdv, prm->kdc, prm->kx, prm->ks,
                                    ctx->ws.p, ctx->num_sms, ctx->stream, ctx->segpin.p, ctx->seg_ev, kSegChunks,
-                                   prm->k, prm->min_size, labels, n_clusters, &err));
+                                   prm->k, prm->min_size, labels, n_clusters, &err, nullptr));
     if (err & 5u) return fail(ctx, QPSO_ERR_INTERNAL, "segmentation graph: index out of range");
     if (err & 2u)
       return fail(ctx, QPSO_ERR_ARG, "segmentation graph: NaN edge weight (depth range zero, or NaN saliency)");
@@ -1518,7 +1518,7 @@ qpso_status qpso_segment_rgbd(qpso_context* ctx, const uint8_t* bgr, const uint1
   uint32_t err = 0, ns = 0;
   QPSO_CUDA(ctx, seg_graph_merge(nullptr, nullptr, nullptr, W, H, mask, len, prm->kdv, prm->kdc, prm->kx, prm->ks,
                                  base, ctx->num_sms, ctx->stream, ctx->segpin.p, ctx->seg_ev, kSegChunks, prm->k,
-                                 prm->min_size, labels, &ns, &err));
+                                 prm->min_size, labels, &ns, &err, d_labels));
   // the front's error word was copied before the graph stage, which has
   // synchronised with the stream since
   if (*front_err) return fail(ctx, QPSO_ERR_TIMEOUT, "segmentation: the inpainting fill's grid barrier timed out");
@@ -1527,7 +1527,7 @@ qpso_status qpso_segment_rgbd(qpso_context* ctx, const uint8_t* bgr, const uint1
   *n_sets = ns;
   if ((size_t)ns * sizeof(SetMoments) > mom_bytes)
     return fail(ctx, QPSO_ERR_INTERNAL, "segmentation: more sets than the small-component merge allows");
-  QPSO_CUDA(ctx, cudaMemcpyAsync(d_labels, labels, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+  // the merge left the labels in d_labels as well
   return cluster_records(ctx, d_labels, d_depth, d_hsv + 2 * n, W, H, ns, d_mom, fp, 0, clusters, capacity,
                          n_clusters);
 }

@@ -197,13 +197,14 @@ cudaError_t launch_set_moments(const int32_t* labels, const uint16_t* inp, const
                                int32_t n_sets, SetMoments* acc, int sms, cudaStream_t st);
 // The graph stage with the merge passes streamed over packed sorted edges
 // copied back in n_chunks pieces (pinned: seg_merge_pinned_bytes; ev:
-// n_chunks events); labels numbered by smallest pixel.
+// n_chunks events); labels numbered by smallest pixel, into host memory
+// and, when labels_dev is not null, into that device buffer too.
 size_t seg_merge_pinned_bytes(int32_t W, int32_t H);
 cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_host, const float* sal_host,
                             int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
                             float ks, void* ws, int sms, cudaStream_t st, void* pinned, const cudaEvent_t* ev,
                             int n_chunks, float k, float min_size, int32_t* labels, uint32_t* n_sets,
-                            uint32_t* err_host);
+                            uint32_t* err_host, int32_t* labels_dev);
 // the graph stage's device input slots inside its workspace
 void seg_ws_inputs(void* ws, int32_t W, int32_t H, uint8_t** hsv, uint16_t** depth, float** sal);
 // PostSegmFilter's record of one set from its moments (host).

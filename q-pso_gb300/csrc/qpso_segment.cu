@@ -414,7 +414,7 @@ size_t seg_workspace_bytes(int32_t W, int32_t H) {
   const size_t nblk = (size_t)((E + kRsTile - 1) / kRsTile);
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   return al(3 * n) + al(2 * n) + al(4 * n) + 2 * al(12 * n) + 2 * al(8 * E) + 3 * al(4 * E) +
-         al(4 * 256 * (nblk ? nblk : 1)) + al(4 * 256) + al(16);
+         al(4 * 256 * (nblk ? nblk : 1)) + al(4 * 256) + al(16) + al(4 * n) + al(4 * (n / 1024 + 2));
 }
 
 void seg_ws_inputs(void* ws, int32_t W, int32_t H, uint8_t** hsv, uint16_t** depth, float** sal) {
@@ -439,6 +439,8 @@ struct SegGraphDev {
   int32_t* eb;
   uint32_t* misc;    // [0] depth min, [1] depth max, [2] error bits, [3] zero-weight edges
   float* tmp;        // 12 n bytes, free after the smoothing
+  int32_t* lab;      // n labels
+  uint32_t* lblk;    // the label numbering's block counts (n / 1024 + 2)
 };
 
 // Upload (or take the inputs already in their slots), smooth, weigh and sort.
@@ -475,6 +477,10 @@ cudaError_t seg_graph_device(const uint8_t* hsv_host[3], const uint16_t* depth_h
   uint32_t* d_tot = (uint32_t*)p;
   p += al(4 * 256);
   uint32_t* d_misc = (uint32_t*)p;
+  p += al(16);
+  int32_t* d_lab = (int32_t*)p;
+  p += al(4 * n);
+  uint32_t* d_lblk = (uint32_t*)p;
 
   cudaError_t e;
   if (hsv_host) {
@@ -520,7 +526,7 @@ cudaError_t seg_graph_device(const uint8_t* hsv_host[3], const uint16_t* depth_h
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  *out = SegGraphDev{src, dst, d_w, d_ea, d_eb, d_misc, d_tmp};
+  *out = SegGraphDev{src, dst, d_w, d_ea, d_eb, d_misc, d_tmp, d_lab, d_lblk};
   return cudaSuccess;
 }
 
@@ -711,6 +717,59 @@ __global__ void __launch_bounds__(kCandThreads) seg_cand_scatter_kernel(const ui
   if (c) out[blk[blockIdx.x] + wbase[warp] + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = v;
 }
 
+// ---- labels numbered by each set's smallest pixel (collectSets' order) ----
+
+__global__ void seg_minpix_init_kernel(int32_t* __restrict__ minpix, uint32_t n) {
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
+    minpix[v] = INT32_MAX;
+}
+
+__global__ void seg_minpix_kernel(const int32_t* __restrict__ root, int32_t* minpix, uint32_t n) {
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
+    atomicMin(minpix + root[v], (int32_t)v);
+}
+
+// first pixels (each set's smallest) per block of kCandThreads pixels
+__global__ void __launch_bounds__(kCandThreads) seg_first_count_kernel(const int32_t* __restrict__ root,
+                                                                       const int32_t* __restrict__ minpix,
+                                                                       uint32_t n, uint32_t* __restrict__ blk) {
+  const size_t v = (size_t)blockIdx.x * kCandThreads + threadIdx.x;
+  const bool f = v < n && minpix[root[v]] == (int32_t)v;
+  const int cnt = __syncthreads_count(f);
+  if (threadIdx.x == 0) blk[blockIdx.x] = (uint32_t)cnt;
+}
+
+// a set's number, at its first pixel: the first pixels before it
+__global__ void __launch_bounds__(kCandThreads) seg_first_number_kernel(const int32_t* __restrict__ root,
+                                                                        const int32_t* __restrict__ minpix,
+                                                                        uint32_t n, const uint32_t* __restrict__ blk,
+                                                                        int32_t* __restrict__ number) {
+  __shared__ uint32_t wbase[kCandThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t v = (size_t)blockIdx.x * kCandThreads + threadIdx.x;
+  const bool f = v < n && minpix[root[v]] == (int32_t)v;
+  const unsigned bal = __ballot_sync(0xffffffffu, f);
+  if (lane == 0) wbase[warp] = (uint32_t)__popc(bal);
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t cnt = lane < kCandThreads / 32 ? wbase[lane] : 0u;
+    uint32_t x = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane < kCandThreads / 32) wbase[lane] = x - cnt;
+  }
+  __syncthreads();
+  if (f) number[v] = (int32_t)(blk[blockIdx.x] + wbase[warp] + (uint32_t)__popc(bal & ((1u << lane) - 1u)));
+}
+
+__global__ void seg_labels_kernel(const int32_t* __restrict__ root, const int32_t* __restrict__ minpix,
+                                  const int32_t* __restrict__ number, uint32_t n, int32_t* __restrict__ labels) {
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
+    labels[v] = number[minpix[root[v]]];
+}
+
 // the roots' thresholds: 0 + k / |C| = k / |C| (singletons: k / 1)
 __global__ void seg_forest_thr_kernel(const int32_t* __restrict__ parent, float k, uint32_t n,
                                       SetState* __restrict__ state) {
@@ -746,8 +805,8 @@ cudaError_t seg_graph_sorted(const uint8_t* hsv_host[3], const uint16_t* depth_h
 }
 
 // pinned layout: 64 bytes of words ([0] error bits, [1] zero-weight edges,
-// [2] small-pass candidates, [8] the front stage's error word), the packed
-// edges and their weights,
+// [2] small-pass candidates, [3] sets, [8] the front stage's error word),
+// the packed edges and their weights,
 // then the forest after the zero-weight edges: parent, (size, threshold)
 size_t seg_merge_pinned_bytes(int32_t W, int32_t H) {
   return 64 + 8 * (size_t)seg_num_edges(W, H) + 12 * (size_t)W * H;
@@ -796,7 +855,7 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
                             int32_t W, int32_t H, const float* mask, int len, float kdv, float kdc, float kx,
                             float ks, void* ws, int sms, cudaStream_t st, void* pinned, const cudaEvent_t* ev,
                             int n_chunks, float k, float min_size, int32_t* labels, uint32_t* n_sets,
-                            uint32_t* err_host) {
+                            uint32_t* err_host, int32_t* labels_dev) {
   const uint64_t E = seg_num_edges(W, H);
   const uint32_t n = (uint32_t)((size_t)W * H);
   SegGraphDev g;
@@ -878,7 +937,9 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
   if (E2 > 0) {
     const uint32_t nb = (uint32_t)((E2 + kCandThreads - 1) / kCandThreads);
     uint32_t* d_cand = reinterpret_cast<uint32_t*>(g.sorted);  // free after the packing: 8 E bytes
-    uint32_t* d_blk = d_cand + E;
+    // the block counts (E2 / 1024 + 2 <= n words) in the labels' buffer,
+    // which the labels take only later
+    uint32_t* d_blk = reinterpret_cast<uint32_t*>(g.lab);
     if ((e = cudaMemcpyAsync(d_par, h_par, 12 * (size_t)n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
     seg_forest_roots_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, n);
     seg_cand_count_kernel<<<nb, kCandThreads, 0, st>>>(d_pk, (uint32_t)E2, W, d_par, d_state, min_size, d_blk);
@@ -906,14 +967,28 @@ cudaError_t seg_graph_merge(const uint8_t* hsv_host[3], const uint16_t* depth_ho
     const int32_t a = f.find(a0), b = f.find(b0);
     if (a != b && ((float)f.st[a].size < min_size || (float)f.st[b].size < min_size)) f.join(a, b);
   }
-  std::vector<int32_t> id(n, -1);
-  uint32_t next = 0;
-  for (uint32_t v = 0; v < n; ++v) {
-    const int32_t r = f.find((int32_t)v);
-    if (id[r] < 0) id[r] = (int32_t)next++;
-    labels[v] = id[r];
+  // the labels on the GPU, from the final forest: roots, each set's
+  // smallest pixel, the sets numbered in the order of those pixels
+  {
+    int32_t* d_minpix = reinterpret_cast<int32_t*>(d_state);  // the records' 8 n bytes are free now
+    int32_t* d_number = d_minpix + n;
+    int32_t* d_lab = labels_dev ? labels_dev : g.lab;
+    uint32_t* d_blk = g.lblk;
+    const uint32_t nb = (n + kCandThreads - 1) / kCandThreads;
+    if ((e = cudaMemcpyAsync(d_par, h_par, 4 * (size_t)n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    seg_forest_roots_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, n);
+    seg_minpix_init_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_minpix, n);
+    seg_minpix_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_minpix, n);
+    seg_first_count_kernel<<<nb, kCandThreads, 0, st>>>(d_par, d_minpix, n, d_blk);
+    seg_cand_scan_kernel<<<1, kCandThreads, 0, st>>>(d_blk, nb);
+    seg_first_number_kernel<<<nb, kCandThreads, 0, st>>>(d_par, d_minpix, n, d_blk, d_number);
+    seg_labels_kernel<<<grid_for(n, 256, sms), 256, 0, st>>>(d_par, d_minpix, d_number, n, d_lab);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(labels, d_lab, 4 * (size_t)n, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(h_words + 3, d_blk + nb, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    *n_sets = h_words[3];
   }
-  *n_sets = next;
   return cudaSuccess;
 }
 
