@@ -605,7 +605,7 @@ def extra_c4(ctx, slots: int = 64, epoch_iters: int = 10, rates=(25.0, 40.0, 50.
             "saturated_solves_per_s": best["solves_per_s"], "batched_same_mix": batched, "sweep": results}
 
 
-def extra_seg(ctx, steps: int = 5):
+def extra_seg(ctx, steps: int = 10, warmup: int = 3):
     """The segmentation in the default run: frames/s of qpso_segment_rgbd
     (GraphCannySeg<hsv>::run, colour image and raw depth on the host to the
     label map and the kept clusters on the host) on the stress
@@ -615,14 +615,16 @@ def extra_seg(ctx, steps: int = 5):
     import scene
 
     depth, _, bgr = scene.segmentation_frame_c5()
-    ctx.segment_rgbd(bgr, depth)
+    for _ in range(warmup):  # the first calls size the workspace and the pinned buffers
+        ctx.segment_rgbd(bgr, depth)
     t0 = time.perf_counter()
     for _ in range(steps):
         out = ctx.segment_rgbd(bgr, depth)
     dt = time.perf_counter() - t0
     frame = segmentation_frame(seed=11)
     prm = qpso.seg_params()
-    ctx.segment_planes(*frame, prm)
+    for _ in range(warmup):
+        ctx.segment_planes(*frame, prm)
     t1 = time.perf_counter()
     for _ in range(steps):
         ctx.segment_planes(*frame, prm)
