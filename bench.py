@@ -1047,9 +1047,10 @@ def run_segment(args, ws, rank, local):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": desc, "edges": int(E), "sets": int(out["n_sets"]),
                            "clusters_kept": len(out["clusters"]), "l2": "inputs uploaded every step"},
-                # per frame: 22 front-stage kernels, 26 graph-stage kernels (4 + 7 sort passes of 3
-                # for a 640x480 frame), 2 for the per-set moments
-                "edges_per_s": value * E, "clocks": clocks, "gpu_launches": args.steps * 50,
+                # per frame: 22 front-stage kernels, 26 graph-stage kernels (5 + 7 sort passes of 3
+                # for a 640x480 frame), 17 for the merge (the weight-0 forest and packing, the
+                # small-component candidates, the labels), 2 for the per-set moments
+                "edges_per_s": value * E, "clocks": clocks, "gpu_launches": args.steps * 67,
                 "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": int(H * W * 5),
                         "d2h_bytes_per_step": int(20 * E + 4 * H * W)}}
         if not args.no_cpu_baseline:

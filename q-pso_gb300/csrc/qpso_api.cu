@@ -767,7 +767,7 @@ qpso_status qpso_solve_traced(qpso_context* ctx, const qpso_solve_desc* desc, qp
   if (prof) {
     ctx->prof.step_launches += desc->iterations;
     ctx->prof.step_ms += event_pairs_ms(ctx, desc->iterations);
-    ctx->prof.prep_launches += 3;
+    ctx->prof.prep_launches += 2;
   }
   const Header& hd = *reinterpret_cast<const Header*>(h + L.hdr);
   read_result(hd, result);
@@ -887,7 +887,7 @@ qpso_status qpso_solve_batch(qpso_context* ctx, const qpso_solve_desc* descs, ui
     float t = 0.f;
     if (cudaEventElapsedTime(&t, ctx->gev[0], ctx->gev[1]) == cudaSuccess) ctx->prof.batch_ms += t;
     ctx->prof.batch_launches += 1;
-    ctx->prof.prep_launches += 3;
+    ctx->prof.prep_launches += 2;
   }
   const Header* hh = reinterpret_cast<const Header*>(h + L.hdr);
   bool bad = false;

@@ -1340,17 +1340,10 @@ __global__ void qpso_queue_probe_kernel(QCtl* qctl, QEntry* queue, uint32_t* err
 // Cluster-masked observed depth (main.cu:1548-1557 builds it from
 // GraphCannySeg's clusterDepth): depth where label == cluster, else 0.
 // blockIdx.y selects the preparation job.
-__global__ void mask_depth_kernel(const PrepDesc* __restrict__ jobs) {
-  const PrepDesc J = jobs[blockIdx.y];
-  const int32_t n = J.width * J.height;
-  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint16_t d = J.depth[i];
-    J.obs[i] = (J.labels == nullptr || J.labels[i] == J.label) ? d : (uint16_t)0;
-  }
-}
-
-// Summed-area table of (obs != 0): sat[y][x] = #{(i,j): i<y, j<x, obs!=0}.
-// Pass 1: one warp per row, inclusive scan of the row into sat[y+1][1..w].
+// The cluster-masked depth obs (depth where the label matches, else 0) and
+// the summed-area table of (obs != 0): sat[y][x] = #{(i,j): i<y, j<x,
+// obs!=0}.  Pass 1: one warp per row writes the row's obs and the inclusive
+// scan of its mask into sat[y+1][1..w].
 __global__ void sat_rows_kernel(const PrepDesc* __restrict__ jobs) {
   const PrepDesc J = jobs[blockIdx.y];
   const int32_t w = J.width, h = J.height;
@@ -1365,7 +1358,14 @@ __global__ void sat_rows_kernel(const PrepDesc* __restrict__ jobs) {
     if (lane == 0) out[0] = 0;
     for (int32_t x0 = 0; x0 < w; x0 += 32) {
       const int32_t x = x0 + lane;
-      int32_t v = (x < w && J.obs[(int64_t)y * w + x] != 0) ? 1 : 0;
+      int32_t v = 0;
+      if (x < w) {
+        const int64_t i = (int64_t)y * w + x;
+        const uint16_t d = J.depth[i];
+        const uint16_t o = (J.labels == nullptr || J.labels[i] == J.label) ? d : (uint16_t)0;
+        J.obs[i] = o;
+        v = o != 0 ? 1 : 0;
+      }
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int32_t t = __shfl_up_sync(0xffffffffu, v, o);
@@ -1377,25 +1377,33 @@ __global__ void sat_rows_kernel(const PrepDesc* __restrict__ jobs) {
   }
 }
 
-// Pass 2: one thread per column, running sum down the rows, 16 rows per
-// step so that the loads of a step are in flight together.
-__global__ void sat_cols_kernel(const PrepDesc* __restrict__ jobs) {
+// Pass 2: running sums down the columns.  A CTA takes 32 columns; its 8
+// warps split the rows into 8 segments: each thread sums its segment, the
+// segments' offsets come from shared memory, and each thread writes its
+// segment's running sums.  Integer sums, so the split changes nothing.
+constexpr int kSatSegs = 8;
+
+__global__ void __launch_bounds__(32 * kSatSegs) sat_cols_kernel(const PrepDesc* __restrict__ jobs) {
+  __shared__ int32_t seg_sum[kSatSegs][32];
   const PrepDesc J = jobs[blockIdx.y];
   const int32_t w = J.width, h = J.height;
   const int64_t W1 = (int64_t)w + 1;
-  for (int32_t x = blockIdx.x * blockDim.x + threadIdx.x; x <= w; x += gridDim.x * blockDim.x) {
-    int32_t run = 0;
-    int32_t* col = J.sat + x;
-    for (int32_t y0 = 1; y0 <= h; y0 += 16) {
-      int32_t v[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = (y0 + i <= h) ? col[(y0 + i) * W1] : 0;
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        run += v[i];
-        if (y0 + i <= h) col[(y0 + i) * W1] = run;
-      }
-    }
+  const int lane = threadIdx.x & 31, seg = threadIdx.x >> 5;
+  const int32_t x = blockIdx.x * 32 + lane;
+  const int32_t rows = (h + kSatSegs - 1) / kSatSegs;
+  const int32_t y0 = 1 + seg * rows, y1 = min(h, y0 + rows - 1);  // rows y0 .. y1 of sat
+  int32_t* col = J.sat + x;
+  int32_t s = 0;
+  if (x <= w)
+    for (int32_t y = y0; y <= y1; ++y) s += col[(int64_t)y * W1];
+  seg_sum[seg][lane] = s;
+  __syncthreads();
+  if (x > w) return;
+  int32_t run = 0;
+  for (int k = 0; k < seg; ++k) run += seg_sum[k][lane];
+  for (int32_t y = y0; y <= y1; ++y) {
+    run += col[(int64_t)y * W1];
+    col[(int64_t)y * W1] = run;
   }
 }
 
@@ -1621,13 +1629,10 @@ static cudaError_t ensure_smem(K kernel, size_t bytes) {
 
 cudaError_t launch_prep(const PrepDesc* jobs, int n, int max_w, int max_h, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  const int npx = max_w * max_h;
-  dim3 g1((npx + 255) / 256 < 512 ? (npx + 255) / 256 : 512, n);
-  mask_depth_kernel<<<g1, 256, 0, st>>>(jobs);
   dim3 g2((max_h * 32 + 255) / 256, n);
   sat_rows_kernel<<<g2, 256, 0, st>>>(jobs);
-  dim3 g3((max_w + 1 + 127) / 128, n);
-  sat_cols_kernel<<<g3, 128, 0, st>>>(jobs);
+  dim3 g3((max_w + 1 + 31) / 32, n);
+  sat_cols_kernel<<<g3, 32 * kSatSegs, 0, st>>>(jobs);
   return cudaGetLastError();
 }
 
