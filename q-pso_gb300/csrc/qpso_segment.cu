@@ -724,9 +724,18 @@ __global__ void seg_minpix_init_kernel(int32_t* __restrict__ minpix, uint32_t n)
     minpix[v] = INT32_MAX;
 }
 
+// each set's smallest pixel; a warp's lanes of one set leave the atomic to
+// the lowest of them (pixels rise with the lane), so a large set costs one
+// atomic per warp, not one per pixel
 __global__ void seg_minpix_kernel(const int32_t* __restrict__ root, int32_t* minpix, uint32_t n) {
-  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
-    atomicMin(minpix + root[v], (int32_t)v);
+  const int lane = threadIdx.x & 31;
+  for (size_t v0 = blockIdx.x * (size_t)blockDim.x + (threadIdx.x & ~31u); v0 < n;
+       v0 += (size_t)gridDim.x * blockDim.x) {  // whole warps
+    const size_t v = v0 + lane;
+    const int32_t r = v < n ? root[v] : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, r);
+    if (v < n && (peers & ((1u << lane) - 1u)) == 0u) atomicMin(minpix + r, (int32_t)v);
+  }
 }
 
 // first pixels (each set's smallest) per block of kCandThreads pixels
