@@ -605,6 +605,46 @@ def extra_c4(ctx, slots: int = 64, epoch_iters: int = 10, rates=(25.0, 40.0, 50.
             "saturated_solves_per_s": best["solves_per_s"], "batched_same_mix": batched, "sweep": results}
 
 
+def seg_throughput(local: int, bgr, depth, threads: int = 4, frames: int = 12) -> dict:
+    """Frames/s of qpso_segment_rgbd with `threads` host threads, each with
+    its own context (stream, workspaces, pinned buffers) on the same GPU,
+    each segmenting `frames` frames: the host merge passes of different
+    frames run on different cores while the GPUs' stages interleave.  The
+    latency of one frame is unchanged."""
+    import threading
+
+    import qpso
+
+    ctxs = [qpso.Context(local) for _ in range(threads)]
+    for c in ctxs:  # size every context's buffers first
+        for _ in range(2):
+            c.segment_rgbd(bgr, depth)
+    barrier = threading.Barrier(threads + 1)
+    errors = []
+
+    def work(c):
+        try:
+            barrier.wait()
+            for _ in range(frames):
+                c.segment_rgbd(bgr, depth)
+        except Exception as e:  # reported below
+            errors.append(e)
+    ts = [threading.Thread(target=work, args=(c,)) for c in ctxs]
+    for t in ts:
+        t.start()
+    barrier.wait()
+    t0 = time.perf_counter()
+    for t in ts:
+        t.join()
+    dt = time.perf_counter() - t0
+    for c in ctxs:
+        c.close()
+    if errors:
+        raise errors[0]
+    return {"value": threads * frames / dt, "unit": "frames/s", "threads": threads, "contexts": threads,
+            "frames_per_thread": frames}
+
+
 def extra_seg(ctx, steps: int = 10, warmup: int = 3):
     """The segmentation in the default run: frames/s of qpso_segment_rgbd
     (GraphCannySeg<hsv>::run, colour image and raw depth on the host to the
@@ -633,7 +673,8 @@ def extra_seg(ctx, steps: int = 10, warmup: int = 3):
                         "from host BGR and depth to host labels and kept clusters",
             "value": steps / dt, "unit": "frames/s", "ms_per_frame": dt * 1000.0 / steps,
             "sets": int(out["n_sets"]), "clusters_kept": len(out["clusters"]),
-            "graph_stage_only": {"value": steps / dt_g, "unit": "frames/s", "ms_per_frame": dt_g * 1000.0 / steps}}
+            "graph_stage_only": {"value": steps / dt_g, "unit": "frames/s", "ms_per_frame": dt_g * 1000.0 / steps},
+            "four_contexts": seg_throughput(ctx.device, bgr, depth)}
 
 
 def run_ours(args, ws, rank, local):
@@ -1053,6 +1094,7 @@ def run_segment(args, ws, rank, local):
                 "edges_per_s": value * E, "clocks": clocks, "gpu_launches": args.steps * 67,
                 "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": int(H * W * 5),
                         "d2h_bytes_per_step": int(20 * E + 4 * H * W)}}
+        line["four_contexts"] = seg_throughput(local, bgr, depth)
         if not args.no_cpu_baseline:
             v, n = _oracle_segment_rate(frame, 10.0)
             line["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",

@@ -262,6 +262,7 @@ class Context:
 
     def __init__(self, device: int = 0):
         self.L = load_library()
+        self.device = device
         self.h = C.c_void_p()
         st = self.L.qpso_create(device, C.byref(self.h))
         if st != OK:
