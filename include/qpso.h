@@ -284,10 +284,10 @@ qpso_status qpso_score_poses_noalloc(const float *d_mesh_soa, uint32_t num_faces
  * raster_mode; the solve's own result, the reference-parity trajectory,
  * is untouched. */
 typedef struct {
-    uint32_t rounds;          /* 24 */
-    uint32_t candidates;      /* 64, at least 12 (the axis steps) */
-    float step_t;             /* 0.01 m */
-    float step_rot;           /* 0.2 rad */
+    uint32_t rounds;          /* 32 */
+    uint32_t candidates;      /* 128, at least 12 (the axis steps) */
+    float step_t;             /* 0.03 m */
+    float step_rot;           /* 0.5 rad */
     uint32_t raster_mode;     /* QPSO_RASTER_EDGE */
 } qpso_refine_params;
 void qpso_refine_params_init(qpso_refine_params *p);

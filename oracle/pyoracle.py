@@ -643,8 +643,8 @@ def _rotate_small(q, hx, hy, hz):
     return [f(sgn * f(x / n)) for x in r]
 
 
-def refine(mesh, num_faces, obs, cam: Camera, prm: Params, pose0, seed: int, stream: int, rounds: int = 24,
-           candidates: int = 64, step_t: float = 0.01, step_rot: float = 0.2, mode: int = RASTER_EDGE):
+def refine(mesh, num_faces, obs, cam: Camera, prm: Params, pose0, seed: int, stream: int, rounds: int = 32,
+           candidates: int = 128, step_t: float = 0.03, step_rot: float = 0.5, mode: int = RASTER_EDGE):
     """The oracle's replay of qpso_refine: the same candidates, scored by
     the oracle's render and fitness in `mode`.  Returns (pose, fitness)."""
     f = np.float32

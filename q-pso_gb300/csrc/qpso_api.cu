@@ -1015,10 +1015,10 @@ qpso_status qpso_score_poses(qpso_context* ctx, const qpso_solve_desc* desc, con
 
 void qpso_refine_params_init(qpso_refine_params* p) {
   if (!p) return;
-  p->rounds = 24;
-  p->candidates = 64;
-  p->step_t = 0.01f;
-  p->step_rot = 0.2f;
+  p->rounds = 32;
+  p->candidates = 128;
+  p->step_t = 0.03f;
+  p->step_rot = 0.5f;
   p->raster_mode = QPSO_RASTER_EDGE;
 }
 
