@@ -16,12 +16,15 @@
 //      as a 64-bit key: the weight's order bits above the edge index;
 //   4. a least-significant-digit radix sort of the keys.  It is stable and
 //      the keys are distinct, so equal weights end in edge-index order.
-// Host: segment_graph's merge pass over the sorted edges
-// (GraphCannySeg.cpp:1301-1373), the small-component merge
-// (GraphCannySeg.cpp:1243-1248) and the numbering of the sets in the order
-// of their smallest pixel (collectSets, GraphCannySeg.cpp:305-352).  That
-// pass is a sequential union-find over about 4 edges per pixel, so it runs
-// on the CPU beside the GPU.
+// segment_graph's merge pass (GraphCannySeg.cpp:1301-1373) is a sequential
+// union-find over about 4 edges per pixel.  The GPU joins the weight-0
+// edges, which come first and whose result does not depend on their order
+// (connected components); the host runs the pass over the rest, streamed
+// as the copies land.  For the small-component merge
+// (GraphCannySeg.cpp:1243-1248) the GPU lists the edges that can still
+// join two sets and the host runs the merge over that list.  The GPU then
+// numbers the sets in the order of their smallest pixel (collectSets,
+// GraphCannySeg.cpp:305-352).
 //
 // This unit is compiled with -ffp-contract=off for its host code too: the
 // mask and the thresholds are float expressions that must round like the
