@@ -338,6 +338,15 @@ qpso_status qpso_image_u16_load(const char *path, uint16_t *out, uint64_t capaci
 qpso_status qpso_image_bgr8_load(const char *path, uint8_t *out, uint64_t capacity_px, uint32_t *width,
                                  uint32_t *height);
 
+/* A B, G, R image written as a baseline JPEG (ITU-T T.81; 4:4:4 YCbCr,
+ * the Annex K tables, quality 1..100 scaled as the IJG software does), the
+ * format of the cluster images the reference's main writes with
+ * cv::imwrite (main.cu:1262-1272, default quality 95).  QPSO_ERR_ARG for
+ * bad arguments (a side above 65535), QPSO_ERR_NOT_FOUND when the file
+ * cannot be written. */
+qpso_status qpso_image_jpeg_write(const char *path, const uint8_t *bgr, uint32_t width, uint32_t height,
+                                  int32_t quality);
+
 /* ---- serving: continuous batching of solve requests ----
  * No counterpart in the reference (one solve per process).  A scheduler
  * thread admits submitted requests into free slots while the slot count and

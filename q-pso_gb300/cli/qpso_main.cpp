@@ -12,6 +12,9 @@
 // (vecSegResult[N], main.cu:1253-1269), solves its pose on the GPU against
 // the cluster's inpainted depth and writes what the reference writes:
 //
+//   results/<color_image>-cluster<i>.jpg             each kept cluster's colours
+//                                                    (segmenting runs; cluster N
+//                                                    also as ./cluster.jpg)
 //   results/<color_image>-<cluster_idx>-bestpose.csv  fit,tx,ty,tz,q0,q1,q2,q3
 //                                                     (main.cu:1752-1757)
 //   results/<color_image>-<cluster_idx>-best.csv      the best pose's depth
@@ -23,6 +26,7 @@
 // depth) the clusters come from it instead, the raw depth is solved
 // against, and the colour image only names the outputs.  Uses only the C
 // ABI of libqpso_gb300.
+#include <algorithm>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
@@ -212,6 +216,29 @@ int main(int argc, char** argv) {
                           &n_cl, &planes) != QPSO_OK)
       return fail("segmentation");
     std::printf("disjoint sets %u\nclusters kept %u\n", n_sets, n_cl);
+    // the reference's cluster images (main.cu:1257-1272): the colour image
+    // inside each kept cluster, black elsewhere, as results/<rgb>-cluster<i>.jpg,
+    // and cluster N once more as cluster.jpg in the working directory
+    if (::mkdir(results.c_str(), 0755) != 0 && errno != EEXIST) {
+      qpso_destroy(ctx);
+      return die("mkdir", results);
+    }
+    std::vector<uint8_t> img((size_t)W * H * 3);
+    for (uint32_t i = 0; i < n_cl && i < cap; ++i) {
+      std::fill(img.begin(), img.end(), (uint8_t)0);
+      for (size_t p = 0; p < (size_t)W * H; ++p)
+        if (labels[p] == cl[i].label)
+          for (int c = 0; c < 3; ++c) img[3 * p + c] = bgr[3 * p + c];
+      const std::string name = results + "/" + base_name(rgb_path) + "-cluster" + std::to_string(i) + ".jpg";
+      if (qpso_image_jpeg_write(name.c_str(), img.data(), W, H, 95) != QPSO_OK) {
+        qpso_destroy(ctx);
+        return die("cannot write", name);
+      }
+      if ((int32_t)i == idx && qpso_image_jpeg_write("cluster.jpg", img.data(), W, H, 95) != QPSO_OK) {
+        qpso_destroy(ctx);
+        return die("cannot write", "cluster.jpg");
+      }
+    }
     if ((uint32_t)idx >= n_cl || idx >= (int32_t)cap) {
       qpso_destroy(ctx);
       return die("cluster_idx", std::to_string(idx) + " is beyond the " + std::to_string(n_cl) +

@@ -9,7 +9,9 @@
 //  * 16-bit (or 8-bit) greyscale PNG, the "640x480 png images" the
 //    reference's usage text names (README.md), decoded with this file's own
 //    inflate (RFC 1950/1951) and scanline unfiltering (PNG specification,
-//    section 9).
+//    section 9);
+// and one writer: baseline JPEG (ITU-T T.81), for the cluster images the
+// reference's main writes with cv::imwrite (main.cu:1262-1272).
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -469,6 +471,256 @@ qpso_status decode_accv(const std::vector<unsigned char>& f, std::vector<uint16_
   return QPSO_OK;
 }
 
+
+// ---- baseline JPEG writer (ITU-T T.81: sequential DCT, Huffman coding) ----
+//
+// 4:4:4 YCbCr (JFIF, ITU-T T.871), one 8x8 block per component per MCU,
+// edges padded by repeating the last row and column.  The quantisation
+// tables are the example tables of T.81 Annex K.1 scaled by quality as the
+// IJG software scales them (cv::imwrite's default is quality 95); the
+// Huffman tables are the typical tables of Annex K.3, written into the file.
+
+const uint8_t kJpegZig[64] = {0,  1,  8,  16, 9,  2,  3,  10, 17, 24, 32, 25, 18, 11, 4,  5,
+                              12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6,  7,  14, 21, 28,
+                              35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51,
+                              58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
+// Annex K.1, natural (row-major) order
+const uint8_t kJpegQLum[64] = {16, 11, 10, 16, 24,  40,  51,  61,  12, 12, 14, 19, 26,  58,  60,  55,
+                               14, 13, 16, 24, 40,  57,  69,  56,  14, 17, 22, 29, 51,  87,  80,  62,
+                               18, 22, 37, 56, 68,  109, 103, 77,  24, 35, 55, 64, 81,  104, 113, 92,
+                               49, 64, 78, 87, 103, 121, 120, 101, 72, 92, 95, 98, 112, 100, 103, 99};
+const uint8_t kJpegQChr[64] = {17, 18, 24, 47, 99, 99, 99, 99, 18, 21, 26, 66, 99, 99, 99, 99,
+                               24, 26, 56, 99, 99, 99, 99, 99, 47, 66, 99, 99, 99, 99, 99, 99,
+                               99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99,
+                               99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99};
+// Annex K.3: code lengths (BITS, 1..16) and symbols (HUFFVAL)
+const uint8_t kDcLumBits[16] = {0, 1, 5, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0};
+const uint8_t kDcChrBits[16] = {0, 3, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0};
+const uint8_t kDcVals[12] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11};
+const uint8_t kAcLumBits[16] = {0, 2, 1, 3, 3, 2, 4, 3, 5, 5, 4, 4, 0, 0, 1, 0x7d};
+const uint8_t kAcLumVals[162] = {
+    0x01, 0x02, 0x03, 0x00, 0x04, 0x11, 0x05, 0x12, 0x21, 0x31, 0x41, 0x06, 0x13, 0x51, 0x61, 0x07, 0x22, 0x71,
+    0x14, 0x32, 0x81, 0x91, 0xa1, 0x08, 0x23, 0x42, 0xb1, 0xc1, 0x15, 0x52, 0xd1, 0xf0, 0x24, 0x33, 0x62, 0x72,
+    0x82, 0x09, 0x0a, 0x16, 0x17, 0x18, 0x19, 0x1a, 0x25, 0x26, 0x27, 0x28, 0x29, 0x2a, 0x34, 0x35, 0x36, 0x37,
+    0x38, 0x39, 0x3a, 0x43, 0x44, 0x45, 0x46, 0x47, 0x48, 0x49, 0x4a, 0x53, 0x54, 0x55, 0x56, 0x57, 0x58, 0x59,
+    0x5a, 0x63, 0x64, 0x65, 0x66, 0x67, 0x68, 0x69, 0x6a, 0x73, 0x74, 0x75, 0x76, 0x77, 0x78, 0x79, 0x7a, 0x83,
+    0x84, 0x85, 0x86, 0x87, 0x88, 0x89, 0x8a, 0x92, 0x93, 0x94, 0x95, 0x96, 0x97, 0x98, 0x99, 0x9a, 0xa2, 0xa3,
+    0xa4, 0xa5, 0xa6, 0xa7, 0xa8, 0xa9, 0xaa, 0xb2, 0xb3, 0xb4, 0xb5, 0xb6, 0xb7, 0xb8, 0xb9, 0xba, 0xc2, 0xc3,
+    0xc4, 0xc5, 0xc6, 0xc7, 0xc8, 0xc9, 0xca, 0xd2, 0xd3, 0xd4, 0xd5, 0xd6, 0xd7, 0xd8, 0xd9, 0xda, 0xe1, 0xe2,
+    0xe3, 0xe4, 0xe5, 0xe6, 0xe7, 0xe8, 0xe9, 0xea, 0xf1, 0xf2, 0xf3, 0xf4, 0xf5, 0xf6, 0xf7, 0xf8, 0xf9, 0xfa};
+const uint8_t kAcChrBits[16] = {0, 2, 1, 2, 4, 4, 3, 4, 7, 5, 4, 4, 0, 1, 2, 0x77};
+const uint8_t kAcChrVals[162] = {
+    0x00, 0x01, 0x02, 0x03, 0x11, 0x04, 0x05, 0x21, 0x31, 0x06, 0x12, 0x41, 0x51, 0x07, 0x61, 0x71, 0x13, 0x22,
+    0x32, 0x81, 0x08, 0x14, 0x42, 0x91, 0xa1, 0xb1, 0xc1, 0x09, 0x23, 0x33, 0x52, 0xf0, 0x15, 0x62, 0x72, 0xd1,
+    0x0a, 0x16, 0x24, 0x34, 0xe1, 0x25, 0xf1, 0x17, 0x18, 0x19, 0x1a, 0x26, 0x27, 0x28, 0x29, 0x2a, 0x35, 0x36,
+    0x37, 0x38, 0x39, 0x3a, 0x43, 0x44, 0x45, 0x46, 0x47, 0x48, 0x49, 0x4a, 0x53, 0x54, 0x55, 0x56, 0x57, 0x58,
+    0x59, 0x5a, 0x63, 0x64, 0x65, 0x66, 0x67, 0x68, 0x69, 0x6a, 0x73, 0x74, 0x75, 0x76, 0x77, 0x78, 0x79, 0x7a,
+    0x82, 0x83, 0x84, 0x85, 0x86, 0x87, 0x88, 0x89, 0x8a, 0x92, 0x93, 0x94, 0x95, 0x96, 0x97, 0x98, 0x99, 0x9a,
+    0xa2, 0xa3, 0xa4, 0xa5, 0xa6, 0xa7, 0xa8, 0xa9, 0xaa, 0xb2, 0xb3, 0xb4, 0xb5, 0xb6, 0xb7, 0xb8, 0xb9, 0xba,
+    0xc2, 0xc3, 0xc4, 0xc5, 0xc6, 0xc7, 0xc8, 0xc9, 0xca, 0xd2, 0xd3, 0xd4, 0xd5, 0xd6, 0xd7, 0xd8, 0xd9, 0xda,
+    0xe2, 0xe3, 0xe4, 0xe5, 0xe6, 0xe7, 0xe8, 0xe9, 0xea, 0xf2, 0xf3, 0xf4, 0xf5, 0xf6, 0xf7, 0xf8, 0xf9, 0xfa};
+
+// the canonical code of a table (Annex C): code and length per symbol
+struct HuffCode {
+  uint16_t code[256];
+  uint8_t len[256];
+  bool ok;
+};
+
+HuffCode huff_codes(const uint8_t bits[16], const uint8_t* vals) {
+  HuffCode h;
+  std::memset(&h, 0, sizeof(h));
+  uint32_t code = 0;
+  int k = 0;
+  for (int l = 1; l <= 16; ++l) {
+    for (int i = 0; i < bits[l - 1]; ++i, ++k) {
+      h.code[vals[k]] = (uint16_t)code;
+      h.len[vals[k]] = (uint8_t)l;
+      ++code;
+    }
+    code <<= 1;
+  }
+  h.ok = true;
+  return h;
+}
+
+struct BitWriter {
+  std::vector<unsigned char>& out;
+  uint32_t acc = 0;
+  int n = 0;
+  explicit BitWriter(std::vector<unsigned char>& o) : out(o) {}
+  void put(uint32_t v, int len) {  // len <= 16
+    acc = (acc << len) | (v & ((1u << len) - 1u));
+    n += len;
+    while (n >= 8) {
+      const unsigned char b = (unsigned char)(acc >> (n - 8));
+      out.push_back(b);
+      if (b == 0xFF) out.push_back(0x00);  // byte stuffing
+      n -= 8;
+    }
+    acc &= (1u << n) - 1u;
+  }
+  void flush() {  // pad with 1-bits
+    if (n > 0) put((1u << (8 - n)) - 1u, 8 - n);
+  }
+};
+
+int bit_size(int v) {  // the magnitude category of v
+  v = v < 0 ? -v : v;
+  int s = 0;
+  while (v) {
+    ++s;
+    v >>= 1;
+  }
+  return s;
+}
+
+void put_u16(std::vector<unsigned char>& o, uint32_t v) {
+  o.push_back((unsigned char)(v >> 8));
+  o.push_back((unsigned char)v);
+}
+
+// forward DCT of one 8x8 block (level-shifted samples), separable, by the
+// definition: F(u,v) = 1/4 C(u) C(v) sum f(x,y) cos((2x+1)u pi/16) cos((2y+1)v pi/16)
+void fdct8x8(const double in[64], double out[64]) {
+  static double c[8][8];
+  static bool init = false;
+  if (!init) {
+    for (int u = 0; u < 8; ++u)
+      for (int x = 0; x < 8; ++x)
+        c[u][x] = (u == 0 ? std::sqrt(0.125) : 0.5) * std::cos((2 * x + 1) * u * 3.14159265358979323846 / 16.0);
+    init = true;
+  }
+  double t[64];
+  for (int y = 0; y < 8; ++y)
+    for (int u = 0; u < 8; ++u) {
+      double s = 0.0;
+      for (int x = 0; x < 8; ++x) s += c[u][x] * in[y * 8 + x];
+      t[y * 8 + u] = s;
+    }
+  for (int u = 0; u < 8; ++u)
+    for (int v = 0; v < 8; ++v) {
+      double s = 0.0;
+      for (int y = 0; y < 8; ++y) s += c[v][y] * t[y * 8 + u];
+      out[v * 8 + u] = s;
+    }
+}
+
+std::vector<unsigned char> encode_jpeg(const uint8_t* bgr, uint32_t w, uint32_t h, int quality) {
+  quality = quality < 1 ? 1 : quality > 100 ? 100 : quality;
+  const int scale = quality < 50 ? 5000 / quality : 200 - 2 * quality;
+  uint8_t q[2][64];
+  for (int i = 0; i < 64; ++i) {
+    int a = (kJpegQLum[i] * scale + 50) / 100, b = (kJpegQChr[i] * scale + 50) / 100;
+    q[0][i] = (uint8_t)(a < 1 ? 1 : a > 255 ? 255 : a);
+    q[1][i] = (uint8_t)(b < 1 ? 1 : b > 255 ? 255 : b);
+  }
+  const HuffCode dc[2] = {huff_codes(kDcLumBits, kDcVals), huff_codes(kDcChrBits, kDcVals)};
+  const HuffCode ac[2] = {huff_codes(kAcLumBits, kAcLumVals), huff_codes(kAcChrBits, kAcChrVals)};
+  std::vector<unsigned char> o;
+  o.reserve((size_t)w * h + 1024);
+  o.push_back(0xFF), o.push_back(0xD8);  // SOI
+  // APP0 JFIF 1.01, no density units, no thumbnail
+  o.push_back(0xFF), o.push_back(0xE0);
+  put_u16(o, 16);
+  const unsigned char jfif[] = {'J', 'F', 'I', 'F', 0, 1, 1, 0, 0, 1, 0, 1, 0, 0};
+  o.insert(o.end(), jfif, jfif + sizeof(jfif));
+  for (int t = 0; t < 2; ++t) {  // DQT, in zigzag order
+    o.push_back(0xFF), o.push_back(0xDB);
+    put_u16(o, 67);
+    o.push_back((unsigned char)t);
+    for (int k = 0; k < 64; ++k) o.push_back(q[t][kJpegZig[k]]);
+  }
+  o.push_back(0xFF), o.push_back(0xC0);  // SOF0
+  put_u16(o, 17);
+  o.push_back(8);
+  put_u16(o, h);
+  put_u16(o, w);
+  o.push_back(3);
+  for (int c = 0; c < 3; ++c) {
+    o.push_back((unsigned char)(c + 1));
+    o.push_back(0x11);
+    o.push_back(c == 0 ? 0 : 1);
+  }
+  struct Table {
+    int tc_th;
+    const uint8_t* bits;
+    const uint8_t* vals;
+    int n;
+  };
+  const Table tabs[4] = {{0x00, kDcLumBits, kDcVals, 12}, {0x10, kAcLumBits, kAcLumVals, 162},
+                         {0x01, kDcChrBits, kDcVals, 12}, {0x11, kAcChrBits, kAcChrVals, 162}};
+  for (const Table& t : tabs) {  // DHT
+    o.push_back(0xFF), o.push_back(0xC4);
+    put_u16(o, (uint32_t)(3 + 16 + t.n));
+    o.push_back((unsigned char)t.tc_th);
+    o.insert(o.end(), t.bits, t.bits + 16);
+    o.insert(o.end(), t.vals, t.vals + t.n);
+  }
+  o.push_back(0xFF), o.push_back(0xDA);  // SOS
+  put_u16(o, 12);
+  o.push_back(3);
+  for (int c = 0; c < 3; ++c) {
+    o.push_back((unsigned char)(c + 1));
+    o.push_back(c == 0 ? 0x00 : 0x11);
+  }
+  o.push_back(0), o.push_back(63), o.push_back(0);
+  BitWriter bw(o);
+  int pred[3] = {0, 0, 0};
+  double blk[64], coef[64];
+  for (uint32_t by = 0; by < h; by += 8)
+    for (uint32_t bx = 0; bx < w; bx += 8)
+      for (int c = 0; c < 3; ++c) {
+        for (int y = 0; y < 8; ++y)
+          for (int x = 0; x < 8; ++x) {
+            const uint32_t sy = by + y < h ? by + y : h - 1, sx = bx + x < w ? bx + x : w - 1;
+            const uint8_t* p = bgr + 3 * ((size_t)sy * w + sx);
+            const double B = p[0], G = p[1], R = p[2];
+            const double v = c == 0   ? 0.299 * R + 0.587 * G + 0.114 * B
+                             : c == 1 ? -0.168736 * R - 0.331264 * G + 0.5 * B + 128.0
+                                      : 0.5 * R - 0.418688 * G - 0.081312 * B + 128.0;
+            blk[y * 8 + x] = v - 128.0;
+          }
+        fdct8x8(blk, coef);
+        const int t = c == 0 ? 0 : 1;
+        int zz[64];
+        for (int k = 0; k < 64; ++k) {
+          const int i = kJpegZig[k];
+          zz[k] = (int)std::lround(coef[i] / q[t][i]);
+        }
+        // the tables code DC differences up to category 11 and AC values up
+        // to category 10: clamp (reached only near quality 100)
+        for (int k = 1; k < 64; ++k) zz[k] = zz[k] < -1023 ? -1023 : zz[k] > 1023 ? 1023 : zz[k];
+        // DC: the difference from the component's previous block
+        int diff = zz[0] - pred[c];
+        diff = diff < -2047 ? -2047 : diff > 2047 ? 2047 : diff;
+        pred[c] += diff;
+        const int s = bit_size(diff);
+        bw.put(dc[t].code[s], dc[t].len[s]);
+        if (s) bw.put((uint32_t)(diff < 0 ? diff - 1 : diff), s);
+        // AC: runs of zeros and magnitude categories
+        int run = 0;
+        for (int k = 1; k < 64; ++k) {
+          if (zz[k] == 0) {
+            ++run;
+            continue;
+          }
+          while (run > 15) {
+            bw.put(ac[t].code[0xF0], ac[t].len[0xF0]);
+            run -= 16;
+          }
+          const int sz = bit_size(zz[k]);
+          const int sym = (run << 4) | sz;
+          bw.put(ac[t].code[sym], ac[t].len[sym]);
+          bw.put((uint32_t)(zz[k] < 0 ? zz[k] - 1 : zz[k]), sz);
+          run = 0;
+        }
+        if (run > 0) bw.put(ac[t].code[0x00], ac[t].len[0x00]);  // end of block
+      }
+  bw.flush();
+  o.push_back(0xFF), o.push_back(0xD9);  // EOI
+  return o;
+}
 }  // namespace
 
 extern "C" {
@@ -525,6 +777,18 @@ qpso_status qpso_image_bgr8_load(const char* path, uint8_t* out, uint64_t capaci
   if ((uint64_t)w * h > capacity_px) return QPSO_ERR_ARG;
   std::memcpy(out, bgr.data(), bgr.size());
   return QPSO_OK;
+}
+
+qpso_status qpso_image_jpeg_write(const char* path, const uint8_t* bgr, uint32_t width, uint32_t height,
+                                  int32_t quality) {
+  if (!path || !bgr || width == 0 || height == 0 || width > 65535 || height > 65535 || quality < 1 ||
+      quality > 100)
+    return QPSO_ERR_ARG;
+  const std::vector<unsigned char> jpg = encode_jpeg(bgr, width, height, quality);
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return QPSO_ERR_NOT_FOUND;
+  const bool ok = std::fwrite(jpg.data(), 1, jpg.size(), fp) == jpg.size();
+  return (std::fclose(fp) == 0 && ok) ? QPSO_OK : QPSO_ERR_NOT_FOUND;
 }
 
 }  // extern "C"

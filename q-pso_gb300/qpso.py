@@ -36,6 +36,7 @@ EXPORTS = [
     "qpso_obj_load", "qpso_image_u16_load", "qpso_seg_params_init", "qpso_segment_num_edges",
     "qpso_segment_edge_ends", "qpso_segment_gauss_mask", "qpso_segment_edges", "qpso_segment_planes",
     "qpso_seg_front_params_init", "qpso_segment_rgbd", "qpso_segment_clusters", "qpso_image_bgr8_load",
+    "qpso_image_jpeg_write",
     "qpso_refine_params_init", "qpso_refine",
 ]
 
@@ -148,6 +149,7 @@ def load_library(path: str = LIB_PATH):
         raise RuntimeError("qpso CUDA library not built: %s (run __graft_entry__.build())" % path)
     L = C.CDLL(path)
     vp = C.c_void_p
+    L.qpso_version.argtypes = []
     L.qpso_version.restype = C.c_char_p
     L.qpso_create.argtypes = [C.c_int, C.POINTER(vp)]
     L.qpso_destroy.argtypes = [vp]
@@ -178,6 +180,9 @@ def load_library(path: str = LIB_PATH):
     L.qpso_obj_load.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]
     L.qpso_image_u16_load.argtypes = [C.c_char_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint32),
                                       C.POINTER(C.c_uint32)]
+    L.qpso_image_bgr8_load.argtypes = [C.c_char_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint32),
+                                       C.POINTER(C.c_uint32)]
+    L.qpso_image_jpeg_write.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]
     L.qpso_barrier_selftest.argtypes = [vp, C.c_uint64, C.POINTER(C.c_uint32)]
     L.qpso_frame_update.argtypes = [vp, C.c_uint32, C.c_void_p, C.c_void_p]
     L.qpso_host_alloc.argtypes = [C.c_uint64]
@@ -218,6 +223,10 @@ def load_library(path: str = LIB_PATH):
     L.qpso_segment_rgbd.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(SegParams),
                                     C.POINTER(SegFrontParams), C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p,
                                     C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(SegFrameOut)]
+    L.qpso_seg_front_params_init.argtypes = [C.POINTER(SegFrontParams)]
+    L.qpso_refine_params_init.argtypes = [C.POINTER(RefineParams)]
+    L.qpso_refine.argtypes = [vp, C.POINTER(SolveDesc), C.POINTER(RefineParams), C.c_void_p, C.c_void_p,
+                              C.POINTER(C.c_float)]
     L.qpso_segment_clusters.argtypes = [vp, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
                                         C.c_uint32, C.POINTER(SegFrontParams), C.c_int, C.c_void_p, C.c_uint32,
                                         C.POINTER(C.c_uint32)]
@@ -619,6 +628,15 @@ def image_bgr8_load(path: str) -> np.ndarray:
     _status(L.qpso_image_bgr8_load(path.encode(), out.ctypes.data, h.value * w.value, C.byref(w), C.byref(h)),
             path)
     return out
+
+
+def image_jpeg_write(path: str, bgr, quality: int = 95) -> None:
+    """uint8 (height, width, 3) B G R -> baseline JPEG file.  Host only."""
+    L = load_library()
+    a = np.ascontiguousarray(bgr, np.uint8)
+    if a.ndim != 3 or a.shape[2] != 3:
+        raise ValueError("expected (height, width, 3) uint8")
+    _status(L.qpso_image_jpeg_write(path.encode(), a.ctypes.data, a.shape[1], a.shape[0], int(quality)), path)
 
 
 def result_dict(r: Result) -> dict:

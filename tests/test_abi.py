@@ -34,6 +34,15 @@ def test_header_and_binding_agree():
     assert declared_functions() == sorted(qpso.EXPORTS)
 
 
+def test_every_binding_declares_its_argument_types(lib):
+    """Without argtypes ctypes passes a Python int as a C int, masking a
+    64-bit array address to its low 32 bits."""
+    import qpso
+
+    missing = [f for f in qpso.EXPORTS if getattr(lib, f).argtypes is None]
+    assert not missing, missing
+
+
 def test_every_declared_symbol_is_exported(lib):
     out = subprocess.run(["nm", "-D", "--defined-only", os.path.abspath(lib._name)],
                          capture_output=True, text=True, check=True).stdout

@@ -16,7 +16,7 @@ import pytest
 import qpso
 import scene
 from oracle import pyoracle as po
-from tests.test_ingest import CLI, write_accv, write_obj, write_png_gray
+from tests.test_ingest import CLI, _jpeg_decode, write_accv, write_obj, write_png_gray
 
 pytestmark = pytest.mark.gpu
 
@@ -188,12 +188,26 @@ def test_cli_segments_the_frame_itself(gpu_ctx, rgbd_files, colour):
     res_dir = d / ("res_" + colour.split(".")[1])
     cmd = [CLI, obj, str(d / colour), str(d / "depth.png"), str(n), "--particles", "32", "--iterations", "6",
            "--seed", "7", "--results", str(res_dir)]
-    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    run_dir = d / ("cwd_" + colour.split(".")[1])
+    run_dir.mkdir(exist_ok=True)
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=str(run_dir))
     assert r.returncode == 0, r.stderr
     assert "clusters kept" in r.stdout
 
     seg = gpu_ctx.segment_rgbd(bgr, depth, planes=True)
     c = seg["clusters"][n]
+    # one image per kept cluster (main.cu:1257-1263): the colour image inside
+    # the cluster, black elsewhere; cluster N again as ./cluster.jpg (main.cu:1272)
+    for i, ci in enumerate(seg["clusters"]):
+        got, _ = _jpeg_decode(open(str(res_dir / ("%s-cluster%d.jpg" % (colour, i))), "rb").read())
+        inside = seg["labels"] == ci.label
+        want = np.where(inside[..., None], bgr, 0).astype(np.float64)
+        assert got.shape == bgr.shape
+        mse = np.mean((got.astype(np.float64) - want) ** 2)
+        assert 10 * np.log10(255.0 ** 2 / max(mse, 1e-12)) > 30, (i, mse)
+    assert not (res_dir / ("%s-cluster%d.jpg" % (colour, len(seg["clusters"])))).exists()
+    assert open(str(run_dir / "cluster.jpg"), "rb").read() == \
+        open(str(res_dir / ("%s-cluster%d.jpg" % (colour, n))), "rb").read()
     soa, F = qpso.obj_load(obj)
     cam = qpso.Camera(0, 0, 0, 0, 640, 480, qpso.PROJ_REF_ACCV)
     mid = gpu_ctx.mesh_upload(soa, F)
@@ -222,6 +236,8 @@ def test_cli_segments_the_frame_itself(gpu_ctx, rgbd_files, colour):
 
 def test_cli_cluster_beyond_the_kept_ones(rgbd_files):
     d, _, _, obj, _ = rgbd_files
+    run_dir = d / "cwd_beyond"
+    run_dir.mkdir(exist_ok=True)
     r = subprocess.run([CLI, obj, str(d / "img_0007.png"), str(d / "depth.png"), "999", "--particles", "8",
-                        "--iterations", "1"], capture_output=True, text=True, timeout=300)
+                        "--iterations", "1"], capture_output=True, text=True, timeout=300, cwd=str(run_dir))
     assert r.returncode == 1 and "beyond" in r.stderr

@@ -313,3 +313,146 @@ def test_bad_colour_images_are_refused(tmp_path, data):
     with pytest.raises(qpso.QpsoError) as e:
         qpso.image_bgr8_load(p)
     assert e.value.status == qpso.ERR_ARG
+
+
+# ---- the JPEG writer (cluster images of the command line) -------------------
+
+_JPEG_ZIG = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48, 41, 34, 27, 20,
+                      13, 6, 7, 14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51, 58, 59,
+                      52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63])
+
+
+def _jpeg_decode(data: bytes):
+    """A baseline sequential JPEG decoder (ITU-T T.81, Annex F), enough for
+    the writer's files (4:4:4, one scan, no restart intervals): returns
+    (height, width, 3) B G R and the parsed tables."""
+    i, q, huff, comps, scan = 2, {}, {}, [], None
+    assert data[:2] == b"\xff\xd8"
+    while scan is None:
+        assert data[i] == 0xFF
+        marker, n = data[i + 1], int.from_bytes(data[i + 2:i + 4], "big")
+        seg = data[i + 4:i + 2 + n]
+        if marker == 0xDB:
+            q[seg[0] & 15] = np.frombuffer(seg[1:65], np.uint8).astype(np.int32)
+        elif marker == 0xC0:
+            h, w = int.from_bytes(seg[1:3], "big"), int.from_bytes(seg[3:5], "big")
+            comps = [(seg[6 + 3 * k], seg[7 + 3 * k], seg[8 + 3 * k]) for k in range(seg[5])]
+        elif marker == 0xC4:
+            j = 0
+            while j < len(seg):
+                tc_th, bits = seg[j], seg[j + 1:j + 17]
+                vals = seg[j + 17:j + 17 + sum(bits)]
+                codes, code, k = {}, 0, 0
+                for length in range(1, 17):
+                    for _ in range(bits[length - 1]):
+                        codes[(length, code)] = vals[k]
+                        k += 1
+                        code += 1
+                    code <<= 1
+                huff[tc_th] = (codes, bytes(vals))
+                j += 17 + sum(bits)
+        elif marker == 0xDA:
+            scan = {seg[1 + 2 * k]: seg[2 + 2 * k] for k in range(seg[0])}
+        i += 2 + n
+    # entropy-coded data up to EOI, stuffed zero bytes removed
+    end = data.index(b"\xff\xd9", i)
+    raw = data[i:end].replace(b"\xff\x00", b"\xff")
+    bits = np.unpackbits(np.frombuffer(raw, np.uint8))
+    pos = 0
+
+    def read(nb):
+        nonlocal pos
+        v = 0
+        for _ in range(nb):
+            v = (v << 1) | int(bits[pos])
+            pos += 1
+        return v
+
+    def symbol(codes):
+        code = 0
+        for length in range(1, 17):
+            code = (code << 1) | read(1)
+            if (length, code) in codes:
+                return codes[(length, code)]
+        raise AssertionError("no Huffman code matches")
+
+    def extend(v, s):
+        return v if s == 0 or v >= (1 << (s - 1)) else v - (1 << s) + 1
+
+    c8 = np.array([[(np.sqrt(0.125) if u == 0 else 0.5) * np.cos((2 * x + 1) * u * np.pi / 16) for x in range(8)]
+                   for u in range(8)])
+    planes = [np.zeros(((h + 7) // 8 * 8, (w + 7) // 8 * 8)) for _ in comps]
+    pred = [0] * len(comps)
+    for by in range(0, h, 8):
+        for bx in range(0, w, 8):
+            for ci, (cid, _hv, tq) in enumerate(comps):
+                td, ta = scan[cid] >> 4, scan[cid] & 15
+                zz = np.zeros(64)
+                s = symbol(huff[td][0])
+                pred[ci] += extend(read(s), s)
+                zz[0] = pred[ci]
+                k = 1
+                while k < 64:
+                    rs = symbol(huff[0x10 | ta][0])
+                    r, s = rs >> 4, rs & 15
+                    if s == 0:
+                        if r != 15:
+                            break
+                        k += 16
+                        continue
+                    k += r
+                    zz[k] = extend(read(s), s)
+                    k += 1
+                coef = np.zeros(64)
+                coef[_JPEG_ZIG] = zz * q[tq]
+                planes[ci][by:by + 8, bx:bx + 8] = c8.T @ coef.reshape(8, 8) @ c8 + 128.0
+    Y, Cb, Cr = (p[:h, :w] for p in planes)
+    R = Y + 1.402 * (Cr - 128)
+    G = Y - 0.344136 * (Cb - 128) - 0.714136 * (Cr - 128)
+    B = Y + 1.772 * (Cb - 128)
+    img = np.clip(np.rint(np.stack([B, G, R], -1)), 0, 255).astype(np.uint8)
+    return img, {"huff": huff, "q": q, "comps": comps, "size": (h, w)}
+
+
+def test_jpeg_writer_round_trip(tmp_path):
+    import qpso
+
+    H, W = 37, 53  # not multiples of 8: padded blocks
+    yy, xx = np.mgrid[0:H, 0:W]
+    bgr = np.stack([(xx * 4) % 256, (yy * 6) % 256, 128 + 60 * np.sin(xx / 5.0) * np.cos(yy / 7.0)], -1)
+    bgr = bgr.astype(np.uint8)
+    bgr[10:20, 20:30] = 0  # a black cut-out, as in a cluster image
+    p = str(tmp_path / "c.jpg")
+    qpso.image_jpeg_write(p, bgr, 95)
+    data = open(p, "rb").read()
+    assert data[:2] == b"\xff\xd8" and data[-2:] == b"\xff\xd9"
+    img, info = _jpeg_decode(data)
+    assert info["size"] == (H, W) and [c[1] for c in info["comps"]] == [0x11] * 3
+    # the Annex K tables: each AC table codes exactly EOB, ZRL and every
+    # (run, size) with size 1..10
+    want = {0x00, 0xF0} | {(r << 4) | s for r in range(16) for s in range(1, 11)}
+    for tc_th in (0x10, 0x11):
+        assert set(info["huff"][tc_th][1]) == want and len(info["huff"][tc_th][1]) == 162
+    err = img.astype(np.float64) - bgr
+    psnr = 10 * np.log10(255.0 ** 2 / np.mean(err ** 2))
+    assert psnr > 34.0, psnr
+
+
+def test_jpeg_writer_quality_and_arguments(tmp_path):
+    import qpso
+
+    rng = np.random.default_rng(2)
+    bgr = rng.integers(0, 256, (16, 24, 3), dtype=np.uint8)
+    sizes = []
+    for qual in (10, 50, 95, 100):
+        p = str(tmp_path / ("q%d.jpg" % qual))
+        qpso.image_jpeg_write(p, bgr, qual)
+        data = open(p, "rb").read()
+        img, _ = _jpeg_decode(data)
+        assert img.shape == bgr.shape
+        sizes.append(len(data))
+    assert sizes == sorted(sizes)  # higher quality, larger file
+    with pytest.raises(qpso.QpsoError):
+        qpso.image_jpeg_write(str(tmp_path / "x.jpg"), bgr, 0)
+    with pytest.raises(qpso.QpsoError):
+        qpso.image_jpeg_write(str(tmp_path / "no_such_dir" / "x.jpg"), bgr, 90)
