@@ -456,3 +456,26 @@ def test_jpeg_writer_quality_and_arguments(tmp_path):
         qpso.image_jpeg_write(str(tmp_path / "x.jpg"), bgr, 0)
     with pytest.raises(qpso.QpsoError):
         qpso.image_jpeg_write(str(tmp_path / "no_such_dir" / "x.jpg"), bgr, 90)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (8, 8), (9, 1), (480, 640)], ids=["1x1", "8x8", "9x1", "640x480"])
+def test_jpeg_writer_small_and_black_frames(tmp_path, shape):
+    """A single pixel, one exact block, a one-pixel column, and a full
+    black frame with one coloured patch (what a cluster image mostly is:
+    blocks that code as DC 0 and end-of-block)."""
+    import qpso
+
+    H, W = shape
+    bgr = np.zeros((H, W, 3), np.uint8)
+    bgr[: max(1, H // 8), : max(1, W // 8)] = (40, 200, 90)
+    p = str(tmp_path / "s.jpg")
+    qpso.image_jpeg_write(p, bgr, 95)
+    img, info = _jpeg_decode(open(p, "rb").read())
+    assert info["size"] == (H, W)
+    assert np.abs(img.astype(np.int32) - bgr).max() <= 24
+    # 8x8 blocks that hold no patch pixel are black in, and exactly black
+    # out: their level-shifted DC, -1024, is a multiple of quality 95's
+    # DC step (2), and every AC coefficient is 0
+    ph, pw = max(1, H // 8), max(1, W // 8)
+    by0, bx0 = (ph + 7) // 8 * 8, (pw + 7) // 8 * 8
+    assert not img[by0:].any() and not img[:, bx0:].any()
