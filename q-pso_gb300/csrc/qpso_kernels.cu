@@ -743,17 +743,28 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
                 if (n > kLaneRasterMax) {
                   big = true;
                 } else {
-                  const int32_t rx0 = xa - fs.minx;
+                  // edge values at the row's first pixel, one step per row;
+                  // REF mode folds the rounding bias 0xF of the depth
+                  // weights into them (exact: 32-bit wrapping sums), EDGE
+                  // mode tests their signs and adds it per pixel
+                  const int32_t rx0 = xa - fs.minx, ry0 = ya - fs.miny;
+                  const int32_t bias = kEdge ? 0 : 0xF;
+                  int32_t R2 = wadd(wsub(wadd(fs.cy2, wmul(ry0, fs.fdx23)), wmul(rx0, fs.fdy23)), bias);
+                  int32_t R3 = wadd(wsub(wadd(fs.cy3, wmul(ry0, fs.fdx31)), wmul(rx0, fs.fdy31)), bias);
+                  int32_t R1 = kEdge ? wsub(wadd(fs.cy1, wmul(ry0, fs.fdx12)), wmul(rx0, fs.fdy12)) : 1;
+                  int32_t* row = tile + (ya - y0) * cwp - x0;
                   for (int32_t y = ya; y < yb; ++y) {
-                    const int32_t ry = y - fs.miny;
-                    int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
-                    int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
-                    int32_t CX1 = kEdge ? wsub(wadd(fs.cy1, wmul(ry, fs.fdx12)), wmul(rx0, fs.fdy12)) : 1;
-                    int32_t* row = tile + (y - y0) * cwp - x0;
+                    int32_t CX2 = R2, CX3 = R3, CX1 = R1;
+                    // each pixel is one dependent chain (shift, convert,
+                    // depth, convert, atomic) linked to the next only by the
+                    // edge steps: eight in flight per lane in REF mode (EDGE
+                    // mode's inside tests would spill in the variants that
+                    // carry both modes)
+#pragma unroll (kEdge ? 1 : 8)
                     for (int32_t x = xa; x < xb; ++x) {
                       if (!kEdge || (CX1 > 0 && CX2 > 0 && CX3 > 0)) {
-                        const int32_t cx2 = wadd(CX2, 0xF) >> 8;
-                        const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+                        const int32_t cx2 = (kEdge ? wadd(CX2, 0xF) : CX2) >> 8;
+                        const int32_t cx3 = (kEdge ? wadd(CX3, 0xF) : CX3) >> 8;
                         float depth = fs.z1;
                         depth = depth + (float)cx2 * fs.z2;
                         depth = depth + (float)cx3 * fs.z3;
@@ -765,6 +776,10 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
                       CX3 = wsub(CX3, fs.fdy31);
                       if (kEdge) CX1 = wsub(CX1, fs.fdy12);
                     }
+                    R2 = wadd(R2, fs.fdx23);
+                    R3 = wadd(R3, fs.fdx31);
+                    if (kEdge) R1 = wadd(R1, fs.fdx12);
+                    row += cwp;
                   }
                 }
               }
@@ -776,8 +791,9 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
             bigmask &= bigmask - 1;
             const int32_t fminx = __shfl_sync(0xffffffffu, fs.minx, src);
             const int32_t fminy = __shfl_sync(0xffffffffu, fs.miny, src);
-            const int32_t cy2 = __shfl_sync(0xffffffffu, fs.cy2, src);
-            const int32_t cy3 = __shfl_sync(0xffffffffu, fs.cy3, src);
+            // REF mode: the rounding bias folded in, as in the lane path
+            const int32_t cy2 = wadd(__shfl_sync(0xffffffffu, fs.cy2, src), kEdge ? 0 : 0xF);
+            const int32_t cy3 = wadd(__shfl_sync(0xffffffffu, fs.cy3, src), kEdge ? 0 : 0xF);
             const int32_t fdx23 = __shfl_sync(0xffffffffu, fs.fdx23, src);
             const int32_t fdx31 = __shfl_sync(0xffffffffu, fs.fdx31, src);
             const int32_t fdy23 = __shfl_sync(0xffffffffu, fs.fdy23, src);
@@ -809,8 +825,8 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
                 if (!(CX1 > 0 && CX2 > 0 && CX3 > 0)) continue;
                 writes += 1ull;
               }
-              const int32_t cx2 = wadd(CX2, 0xF) >> 8;
-              const int32_t cx3 = wadd(CX3, 0xF) >> 8;
+              const int32_t cx2 = (kEdge ? wadd(CX2, 0xF) : CX2) >> 8;
+              const int32_t cx3 = (kEdge ? wadd(CX3, 0xF) : CX3) >> 8;
               float depth = z1;
               depth = depth + (float)cx2 * z2;
               depth = depth + (float)cx3 * z3;
@@ -944,15 +960,18 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
                 if (kk[j][e] == 0u) {
                   acc.nNo += 1;
                 } else {
-                  const int64_t d64 = wsub(zr[e], (int32_t)kk[j][e]);
-                  add128(acc.lo, acc.hi, (uint64_t)(d64 * d64));
-                  acc.nSegR += 1;
+                  // the wrapped 32-bit difference squared: its magnitude
+                  // times itself, one 32 x 32 -> 64-bit product
+                  const int32_t d = wsub(zr[e], (int32_t)kk[j][e]);
+                  const uint32_t ad = d < 0 ? 0u - (uint32_t)d : (uint32_t)d;
+                  add128(acc.lo, acc.hi, (uint64_t)ad * ad);
                 }
               }
             }
           }
         }
       }
+      acc.nSegR = acc.nR - acc.nNo;  // rendered pixels with an observation
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         acc.nR += __shfl_xor_sync(0xffffffffu, acc.nR, o);
