@@ -488,10 +488,12 @@ __device__ __forceinline__ int32_t wshl(int32_t a, int s) { return (int32_t)((ui
 // whether or not the face is culled.
 struct FaceSetup {
   int32_t minx, maxx, miny, maxy;
-  int32_t cy2, cy3;           // edge functions 2,3 at (minx, miny), 2^8 scale
+  int32_t c2, c3;             // edge functions 2,3 at pixel (0, 0), 2^8 scale: at pixel
+                              // (x, y) they are c + y fdx - x fdy (32-bit wrapping, as
+                              // the reference's row and column steps reach them)
   int32_t fdx23, fdx31;       // per-row steps
   int32_t fdy23, fdy31;       // per-column steps
-  int32_t cy1, fdx12, fdy12;  // edge function 1, set only for the EDGE raster mode
+  int32_t c1, fdx12, fdy12;   // edge function 1, set only for the EDGE raster mode
   float z1, z2, z3;           // z1 and the two depth gradients
   bool live;                  // front-facing with a non-empty rectangle
 };
@@ -519,15 +521,14 @@ __device__ __forceinline__ void setup_face_fixed(int32_t X1, int32_t Y1, float w
   int32_t C3 = wsub(wmul(DY31, X3), wmul(DX31, Y3));
   C2 = wadd(C2, (DY23 < 0 || (DY23 == 0 && DX23 > 0)) ? 1 : 0);
   C3 = wadd(C3, (DY31 < 0 || (DY31 == 0 && DX31 > 0)) ? 1 : 0);
-  const int32_t MINY = wshl(f.miny, 4), MINX = wshl(f.minx, 4);
-  f.cy2 = wsub(wadd(C2, wmul(DX23, MINY)), wmul(DY23, MINX));
-  f.cy3 = wsub(wadd(C3, wmul(DX31, MINY)), wmul(DY31, MINX));
+  f.c2 = C2;
+  f.c3 = C3;
   if (edge) {
     f.fdx12 = wshl(DX12, 4);
     f.fdy12 = wshl(DY12, 4);
     int32_t C1 = wsub(wmul(DY12, X1), wmul(DX12, Y1));
     C1 = wadd(C1, (DY12 < 0 || (DY12 == 0 && DX12 > 0)) ? 1 : 0);
-    f.cy1 = wsub(wadd(C1, wmul(DX12, MINY)), wmul(DY12, MINX));
+    f.c1 = C1;
   }
   f.z1 = w1;
   f.z2 = (w2 - w1) * rA;
@@ -552,9 +553,9 @@ constexpr uint32_t kRasterRef = 0, kRasterEdge = 1;
 // Depth written at pixel (minx+rx, miny+ry) of a live face (main.h:1432-1448):
 // every pixel of the rectangle is written (the inside mask of main.h:1440
 // is a 0/1 value whose sign bit the guard of main.h:1473 tests).
-__device__ __forceinline__ int32_t face_depth(const FaceSetup& f, int32_t rx, int32_t ry) {
-  const int32_t CX2 = wsub(wadd(f.cy2, wmul(ry, f.fdx23)), wmul(rx, f.fdy23));
-  const int32_t CX3 = wsub(wadd(f.cy3, wmul(ry, f.fdx31)), wmul(rx, f.fdy31));
+__device__ __forceinline__ int32_t face_depth(const FaceSetup& f, int32_t x, int32_t y) {
+  const int32_t CX2 = wsub(wadd(f.c2, wmul(y, f.fdx23)), wmul(x, f.fdy23));
+  const int32_t CX3 = wsub(wadd(f.c3, wmul(y, f.fdx31)), wmul(x, f.fdy31));
   const int32_t cx2 = wadd(CX2, 0xF) >> 8;
   const int32_t cx3 = wadd(CX3, 0xF) >> 8;
   float depth = f.z1;

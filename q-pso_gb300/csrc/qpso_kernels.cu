@@ -265,12 +265,10 @@ __device__ float render_score(const Instance& I, const float* s, int32_t* tile, 
       const int32_t ya = max(fs.miny, y0), yb = min(fs.maxy, y0 + thp);
       if (xa >= xb || ya >= yb) continue;
       if (!edge) acc.writes += (unsigned long long)(xb - xa) * (unsigned long long)(yb - ya);
-      const int32_t rx0 = xa - fs.minx;
       for (int32_t y = ya; y < yb; ++y) {
-        const int32_t ry = y - fs.miny;
-        int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx0, fs.fdy23));
-        int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx0, fs.fdy31));
-        int32_t CX1 = edge ? wsub(wadd(fs.cy1, wmul(ry, fs.fdx12)), wmul(rx0, fs.fdy12)) : 1;
+        int32_t CX2 = wsub(wadd(fs.c2, wmul(y, fs.fdx23)), wmul(xa, fs.fdy23));
+        int32_t CX3 = wsub(wadd(fs.c3, wmul(y, fs.fdx31)), wmul(xa, fs.fdy31));
+        int32_t CX1 = edge ? wsub(wadd(fs.c1, wmul(y, fs.fdx12)), wmul(xa, fs.fdy12)) : 1;
         int32_t* row = tile + (y - y0) * cwp - x0;
         for (int32_t x = xa; x < xb; ++x) {
           if (!edge || (CX1 > 0 && CX2 > 0 && CX3 > 0)) {
@@ -726,13 +724,6 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
             bminy = min(bminy, fs.miny);
             bmaxy = max(bmaxy, fs.maxy);
             if (fs.live) {
-              if (pass == 0) {
-                const int32_t ca = max(fs.minx, dx0), cb = min(fs.maxx, dx1);
-                const int32_t ra = max(fs.miny, dy0), rb = min(fs.maxy, dy1);
-                if (ca < cb && ra < rb &&
-                    (ca < pc.bound[0] || cb > pc.bound[1] || ra < pc.bound[2] || rb > pc.bound[3]))
-                  violation = true;
-              }
               xa = max(fs.minx, x0);
               xb = min(fs.maxx, x0 + cwp);
               ya = max(fs.miny, y0);
@@ -747,11 +738,10 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
                   // REF mode folds the rounding bias 0xF of the depth
                   // weights into them (exact: 32-bit wrapping sums), EDGE
                   // mode tests their signs and adds it per pixel
-                  const int32_t rx0 = xa - fs.minx, ry0 = ya - fs.miny;
                   const int32_t bias = kEdge ? 0 : 0xF;
-                  int32_t R2 = wadd(wsub(wadd(fs.cy2, wmul(ry0, fs.fdx23)), wmul(rx0, fs.fdy23)), bias);
-                  int32_t R3 = wadd(wsub(wadd(fs.cy3, wmul(ry0, fs.fdx31)), wmul(rx0, fs.fdy31)), bias);
-                  int32_t R1 = kEdge ? wsub(wadd(fs.cy1, wmul(ry0, fs.fdx12)), wmul(rx0, fs.fdy12)) : 1;
+                  int32_t R2 = wadd(wsub(wadd(fs.c2, wmul(ya, fs.fdx23)), wmul(xa, fs.fdy23)), bias);
+                  int32_t R3 = wadd(wsub(wadd(fs.c3, wmul(ya, fs.fdx31)), wmul(xa, fs.fdy31)), bias);
+                  int32_t R1 = kEdge ? wsub(wadd(fs.c1, wmul(ya, fs.fdx12)), wmul(xa, fs.fdy12)) : 1;
                   int32_t* row = tile + (ya - y0) * cwp - x0;
                   for (int32_t y = ya; y < yb; ++y) {
                     int32_t CX2 = R2, CX3 = R3, CX1 = R1;
@@ -789,11 +779,9 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
           while (bigmask) {
             const int src = __ffs(bigmask) - 1;
             bigmask &= bigmask - 1;
-            const int32_t fminx = __shfl_sync(0xffffffffu, fs.minx, src);
-            const int32_t fminy = __shfl_sync(0xffffffffu, fs.miny, src);
             // REF mode: the rounding bias folded in, as in the lane path
-            const int32_t cy2 = wadd(__shfl_sync(0xffffffffu, fs.cy2, src), kEdge ? 0 : 0xF);
-            const int32_t cy3 = wadd(__shfl_sync(0xffffffffu, fs.cy3, src), kEdge ? 0 : 0xF);
+            const int32_t c2 = wadd(__shfl_sync(0xffffffffu, fs.c2, src), kEdge ? 0 : 0xF);
+            const int32_t c3 = wadd(__shfl_sync(0xffffffffu, fs.c3, src), kEdge ? 0 : 0xF);
             const int32_t fdx23 = __shfl_sync(0xffffffffu, fs.fdx23, src);
             const int32_t fdx31 = __shfl_sync(0xffffffffu, fs.fdx31, src);
             const int32_t fdy23 = __shfl_sync(0xffffffffu, fs.fdy23, src);
@@ -805,9 +793,9 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
             const int32_t bxb = __shfl_sync(0xffffffffu, xb, src);
             const int32_t bya = __shfl_sync(0xffffffffu, ya, src);
             const int32_t byb = __shfl_sync(0xffffffffu, yb, src);
-            int32_t cy1 = 0, fdx12 = 0, fdy12 = 0;
+            int32_t c1 = 0, fdx12 = 0, fdy12 = 0;
             if (kEdge) {
-              cy1 = __shfl_sync(0xffffffffu, fs.cy1, src);
+              c1 = __shfl_sync(0xffffffffu, fs.c1, src);
               fdx12 = __shfl_sync(0xffffffffu, fs.fdx12, src);
               fdy12 = __shfl_sync(0xffffffffu, fs.fdy12, src);
             }
@@ -817,11 +805,10 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
             for (int32_t pix = lane; pix < n; pix += 32) {
               const int32_t r = small_div(pix, rw);
               const int32_t x = bxa + (pix - r * w), y = bya + r;
-              const int32_t ry = y - fminy, rx = x - fminx;
-              const int32_t CX2 = wsub(wadd(cy2, wmul(ry, fdx23)), wmul(rx, fdy23));
-              const int32_t CX3 = wsub(wadd(cy3, wmul(ry, fdx31)), wmul(rx, fdy31));
+              const int32_t CX2 = wsub(wadd(c2, wmul(y, fdx23)), wmul(x, fdy23));
+              const int32_t CX3 = wsub(wadd(c3, wmul(y, fdx31)), wmul(x, fdy31));
               if (kEdge) {
-                const int32_t CX1 = wsub(wadd(cy1, wmul(ry, fdx12)), wmul(rx, fdy12));
+                const int32_t CX1 = wsub(wadd(c1, wmul(y, fdx12)), wmul(x, fdy12));
                 if (!(CX1 > 0 && CX2 > 0 && CX3 > 0)) continue;
                 writes += 1ull;
               }
@@ -840,6 +827,32 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
           bmaxx = __reduce_max_sync(0xffffffffu, bmaxx);
           bminy = __reduce_min_sync(0xffffffffu, bminy);
           bmaxy = __reduce_max_sync(0xffffffffu, bmaxy);
+          // the bound must hold every live face's rectangle (clipped to the
+          // domain), or the band passes could miss pixels: the meshlet's
+          // union of rectangles, live faces or not, inside the bound
+          // settles it for all of them; otherwise (not met in practice: the
+          // bound holds the meshlet's projected box) face by face
+          {
+            const int32_t ux0 = max(bminx, dx0), ux1 = min(bmaxx, dx1);
+            const int32_t uy0 = max(bminy, dy0), uy1 = min(bmaxy, dy1);
+            if (ux0 < ux1 && uy0 < uy1 &&
+                (ux0 < pc.bound[0] || ux1 > pc.bound[1] || uy0 < pc.bound[2] || uy1 > pc.bound[3])) {
+              for (int f = lane; f < nf; f += 32) {
+                const uint32_t fi = __ldg(gf + f);
+                const int4 a = vc[fi & 1023u], bb = vc[(fi >> 10) & 1023u], c = vc[(fi >> 20) & 1023u];
+                FaceSetup fs;
+                setup_face_fixed(a.x, a.y, __int_as_float(a.z), bb.x, bb.y, __int_as_float(bb.z), c.x, c.y,
+                                 __int_as_float(c.z), fs, kEdge);
+                if (fs.live) {
+                  const int32_t ca = max(fs.minx, dx0), cb = min(fs.maxx, dx1);
+                  const int32_t ra = max(fs.miny, dy0), rb = min(fs.maxy, dy1);
+                  if (ca < cb && ra < rb &&
+                      (ca < pc.bound[0] || cb > pc.bound[1] || ra < pc.bound[2] || rb > pc.bound[3]))
+                    violation = true;
+                }
+              }
+            }
+          }
           if (lane == 0) {
             atomicMin(&pc.box[0], bminx);
             atomicMax(&pc.box[1], bmaxx);
@@ -1502,9 +1515,8 @@ __global__ void render_window_kernel(const Instance* __restrict__ inst, const fl
     const int32_t xa = max(max(fs.minx, x0), dx0), xb = min(min(fs.maxx, x0 + ww), dx1);
     const int32_t ya = max(max(fs.miny, y0), dy0), yb = min(min(fs.maxy, y0 + wh), dy1);
     for (int32_t y = ya; y < yb; ++y) {
-      const int32_t ry = y - fs.miny;
-      int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(xa - fs.minx, fs.fdy23));
-      int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(xa - fs.minx, fs.fdy31));
+      int32_t CX2 = wsub(wadd(fs.c2, wmul(y, fs.fdx23)), wmul(xa, fs.fdy23));
+      int32_t CX3 = wsub(wadd(fs.c3, wmul(y, fs.fdx31)), wmul(xa, fs.fdy31));
       for (int32_t x = xa; x < xb; ++x) {
         const int32_t cx2 = wadd(CX2, 0xF) >> 8;
         const int32_t cx3 = wadd(CX3, 0xF) >> 8;
@@ -1816,9 +1828,8 @@ __global__ void __launch_bounds__(256) host_render_kernel(const float* __restric
   for (int32_t pix = (int32_t)lane; pix < n; pix += 32) {
     const int32_t r = pix / w;
     const int32_t x = (int32_t)xa + (pix - r * w), y = (int32_t)ya + r;
-    const int32_t rx = wsub(x, fs.minx), ry = wsub(y, fs.miny);
-    const int32_t CX2 = wsub(wadd(fs.cy2, wmul(ry, fs.fdx23)), wmul(rx, fs.fdy23));
-    const int32_t CX3 = wsub(wadd(fs.cy3, wmul(ry, fs.fdx31)), wmul(rx, fs.fdy31));
+    const int32_t CX2 = wsub(wadd(fs.c2, wmul(y, fs.fdx23)), wmul(x, fs.fdy23));
+    const int32_t CX3 = wsub(wadd(fs.c3, wmul(y, fs.fdx31)), wmul(x, fs.fdy31));
     const int32_t cx2 = wadd(CX2, 0xF) >> 8;
     const int32_t cx3 = wadd(CX3, 0xF) >> 8;
     float d = fs.z1;
