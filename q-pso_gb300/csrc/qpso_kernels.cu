@@ -680,6 +680,9 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
           const uint32_t e = sm.live[item];
           k = (int)(e >> 28);
           m = e & 0x0fffffffu;
+        } else if (np == 1) {  // one particle per CTA: no division
+          k = 0;
+          m = item;
         } else {
           k = (int)(item / nm);
           m = item - (uint32_t)k * nm;
