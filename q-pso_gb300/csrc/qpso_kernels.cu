@@ -467,7 +467,7 @@ __device__ __forceinline__ bool box_rect(const float* pose, const Camera& cam, f
 // pass 0 records every meshlet's screen rectangle per particle when the
 // mesh has at most kCullCap meshlets; larger meshes project each meshlet's
 // object-space box instead (checked in pass 0 against the real rectangle).
-template <bool kEdge, bool kRefProj>
+template <bool kEdge, bool kRefProj, bool kFacePipe>
 __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSmem& sm, int tile_px,
                                         SmemCtl& ctl, float* fit_out) {
   const int tid = threadIdx.x, T = blockDim.x;
@@ -697,6 +697,11 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
         const float4* gv = reinterpret_cast<const float4*>(I.mlet_blob + h.off);
         const uint32_t* gf = reinterpret_cast<const uint32_t*>(I.mlet_blob + h.off + nv * 16);
         const float* pose = ctl.pose[k];
+        // kFacePipe: the lane's face words are loaded a round ahead, the
+        // first before the transform, so that their latency hides behind
+        // it (it costs the plain step kernel's default variant spills)
+        uint32_t fi_next = 0u;
+        if (kFacePipe) fi_next = lane < nf ? __ldg(gf + lane) : 0u;
         for (int v = lane; v < nv; v += 32) {
           const float4 qv = __ldg(gv + v);
           float u, vv, z;
@@ -714,11 +719,16 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
         // whole warp (set-up broadcast by shuffles, pixels strided over lanes)
         for (int base = 0; base < nf; base += 32) {
           const int f = base + lane;
+          uint32_t fi = 0u;
+          if (kFacePipe) {
+            fi = fi_next;
+            if (f + 32 < nf) fi_next = __ldg(gf + f + 32);
+          }
           FaceSetup fs;
           int32_t xa = 0, xb = 0, ya = 0, yb = 0;
           bool big = false;
           if (f < nf) {
-            const uint32_t fi = __ldg(gf + f);
+            if (!kFacePipe) fi = __ldg(gf + f);
             const int4 a = vc[fi & 1023u], bb = vc[(fi >> 10) & 1023u], c = vc[(fi >> 20) & 1023u];
             setup_face_fixed(a.x, a.y, __int_as_float(a.z), bb.x, bb.y, __int_as_float(bb.z), c.x, c.y,
                              __int_as_float(c.z), fs, kEdge);
@@ -1068,19 +1078,19 @@ __device__ void render_score_mlets_mode(const Instance& I, int np, const FusedSm
 //   kVar 0: REF raster, fp32 projection (the default);
 //   kVar 1: REF or EDGE raster, fp32 projection;
 //   kVar 2: either raster, either projection.
-template <int kVar>
+template <int kVar, bool kFacePipe = true>
 __device__ __forceinline__ void render_score_mlets(const Instance& I, int np, const FusedSmem& sm, int tile_px,
                                                    SmemCtl& ctl, float* fit_out) {
   const bool edge = kVar >= 1 && I.prm.raster_mode == kRasterEdge;
   const bool ref = kVar == 2 && I.cam.proj == kProjRefAccv;
   if (kVar == 2 && edge && ref)
-    render_score_mlets_mode<true, true>(I, np, sm, tile_px, ctl, fit_out);
+    render_score_mlets_mode<true, true, kFacePipe>(I, np, sm, tile_px, ctl, fit_out);
   else if (kVar == 2 && ref)
-    render_score_mlets_mode<false, true>(I, np, sm, tile_px, ctl, fit_out);
+    render_score_mlets_mode<false, true, kFacePipe>(I, np, sm, tile_px, ctl, fit_out);
   else if (kVar >= 1 && edge)
-    render_score_mlets_mode<true, false>(I, np, sm, tile_px, ctl, fit_out);
+    render_score_mlets_mode<true, false, kFacePipe>(I, np, sm, tile_px, ctl, fit_out);
   else
-    render_score_mlets_mode<false, false>(I, np, sm, tile_px, ctl, fit_out);
+    render_score_mlets_mode<false, false, kFacePipe>(I, np, sm, tile_px, ctl, fit_out);
 }
 
 // PSO step + render + score + personal best for one work item.
@@ -1089,7 +1099,7 @@ __device__ __forceinline__ void render_score_mlets(const Instance& I, int np, co
 // still runs; they wait (griddepcontrol.wait) before the first read of what
 // it writes: the swarm state, the global best and the counters.  The mesh
 // and the instance record are written before the first launch.
-template <int kVar>
+template <int kVar, bool kFacePipe = true>
 __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, unsigned char* dyn,
                              int tile_px, int vcap, SmemCtl& ctl, bool dep_wait) {
   const int tid = threadIdx.x;
@@ -1142,7 +1152,7 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
     }
   }
   __syncthreads();
-  render_score_mlets<kVar>(I, (int)np, carve_smem(dyn, (int)I.ppb, vcap), tile_px, ctl, ctl.argv);
+  render_score_mlets<kVar, kFacePipe>(I, (int)np, carve_smem(dyn, (int)I.ppb, vcap), tile_px, ctl, ctl.argv);
   if (tid < (int)np) {
     const uint32_t p = p0 + tid;
     const float fv = ctl.argv[tid];
@@ -1233,7 +1243,8 @@ __global__ void __launch_bounds__(kMaxThreads) qpso_step_kernel(const Instance* 
   // the next iteration's launch may place its CTAs now; they wait for this
   // grid to complete before reading anything it writes
   asm volatile("griddepcontrol.launch_dependents;");
-  process_item<kVar>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl, true);
+  process_item<kVar, kVar != 0>(I, blockIdx.x, iter, reinterpret_cast<unsigned char*>(dyn_smem), tile_px, vcap, ctl,
+                                true);
   instance_epilogue(I, blockIdx.x, iter, ctl);
 }
 
