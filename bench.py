@@ -743,7 +743,7 @@ def run_ours(args, ws, rank, local):
         ctx.set_launch_config(plain=plain_cfg, batch=batch_cfg)
     else:
         tune = descs[::max(1, len(descs) // 16)][:16]
-        tune_iters = 4 if args.workload == "c5" else 30
+        tune_iters = 20 if args.workload == "c5" else 30
         plain_cfg, _ = ctx.autotune(tune[::max(1, len(tune) // 4)][:4], batched=False, tune_iters=tune_iters)
         batch_cfg, _ = ctx.autotune(tune, batched=True, tune_iters=tune_iters)
 
