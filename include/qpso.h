@@ -282,7 +282,8 @@ qpso_status qpso_score_poses_noalloc(const float *d_mesh_soa, uint32_t num_faces
  * frame and cluster; its PSO fields and raster_mode are not read.
  * pose_out and *fit_out receive the refined pose and its fitness in
  * raster_mode; the solve's own result, the reference-parity trajectory,
- * is untouched. */
+ * is untouched.  The rounds run on the device, queued without waits; the
+ * call returns when the last one ends. */
 typedef struct {
     uint32_t rounds;          /* 32 */
     uint32_t candidates;      /* 128, at least 12 (the axis steps) */

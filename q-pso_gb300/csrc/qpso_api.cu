@@ -1026,36 +1026,6 @@ void qpso_refine_params_init(qpso_refine_params* p) {
 
 namespace {
 
-// splitmix64 (Steele, Lea and Flood; the public-domain generator Vigna
-// recommends for seeding): the refinement's random candidates
-uint64_t splitmix64(uint64_t& state) {
-  state += 0x9E3779B97F4A7C15ull;
-  uint64_t z = state;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-
-// a uniform float in [-1, 1): 24 random bits, exact in float
-float uniform_pm1(uint64_t& state) {
-  const float u = (float)(splitmix64(state) >> 40) * 5.9604644775390625e-8f;  // 2^-24
-  return u * 2.0f - 1.0f;
-}
-
-// q <- normalise(dq * q), dq = (1, hx, hy, hz), then the top hemisphere
-void rotate_small(float q[4], float hx, float hy, float hz) {
-  const float a0 = 1.0f, a1 = hx, a2 = hy, a3 = hz;
-  const float b0 = q[0], b1 = q[1], b2 = q[2], b3 = q[3];
-  float r[4];
-  r[0] = a0 * b0 - a1 * b1 - a2 * b2 - a3 * b3;
-  r[1] = a0 * b1 + a1 * b0 + a2 * b3 - a3 * b2;
-  r[2] = a0 * b2 - a1 * b3 + a2 * b0 + a3 * b1;
-  r[3] = a0 * b3 + a1 * b2 - a2 * b1 + a3 * b0;
-  const float n = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
-  const float sgn = r[0] < 0.0f ? -1.0f : 1.0f;
-  for (int k = 0; k < 4; ++k) q[k] = sgn * (r[k] / n);
-}
-
 }  // namespace
 
 extern "C" {
@@ -1071,48 +1041,67 @@ qpso_status qpso_refine(qpso_context* ctx, const qpso_solve_desc* desc, const qp
     if (!std::isfinite(pose_in[k])) return fail(ctx, QPSO_ERR_ARG, "non-finite pose");
   qpso_solve_desc d = *desc;
   d.raster_mode = prm->raster_mode;
-  float pose[7];
-  for (int k = 0; k < 3; ++k) pose[k] = pose_in[k];
-  for (int k = 0; k < 4; ++k) pose[3 + k] = pose_in[3 + k];
-  rotate_small(pose + 3, 0.0f, 0.0f, 0.0f);  // normalised, top hemisphere
-  float fit = 0.0f;
-  qpso_status st = qpso_score_poses(ctx, &d, pose, 1, &fit);
+  cudaSetDevice(ctx->device);
+  std::vector<const qpso_solve_desc*> ds;
+  std::vector<const MeshObj*> ms;
+  std::vector<const FrameObj*> fs;
+  qpso_status st = gather_descs(ctx, &d, 1, ds, ms, fs);
   if (st != QPSO_OK) return st;
+  // the whole search runs on the device: the instance and its summed-area
+  // table are prepared once, each round generates its candidates, scores
+  // them with the solver's render and fitness and keeps the best, and the
+  // host waits once at the end
   const uint32_t K = prm->candidates;
-  std::vector<float> cand((size_t)K * 7), fits(K);
-  uint64_t rng = desc->seed ^ ((uint64_t)desc->stream << 32) ^ 0x5245464E45ull;
-  float step_t = prm->step_t, step_r = prm->step_rot;
+  Layout L = make_layout(ds, fs, 0, false);
+  const size_t state_off = align_up(L.total, 256);
+  const size_t cand_off = align_up(state_off + sizeof(RefineState), 256);
+  const size_t fit_off = align_up(cand_off + (size_t)K * 7 * sizeof(float), 256);
+  const size_t total = align_up(fit_off + (size_t)K * sizeof(float), 256);
+  if ((st = ensure_ws(ctx, total)) != QPSO_OK) return st;
+  // the state's host copy sits after the metadata in the pinned buffer
+  const size_t hstate_off = align_up(std::max<size_t>(L.meta_end, L.hdr + sizeof(Header)), 256);
+  if ((st = ensure_pin(ctx, hstate_off + sizeof(RefineState))) != QPSO_OK) return st;
+  QPSO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  TileConfig cfg = ctx->plain;
+  const int vcap = launch_vcap(ms);
+  if ((st = fit_cfg(ctx, cfg, vcap)) != QPSO_OK) return st;
+  fill_meta(ctx, L, ds, ms, fs, (uint32_t)cfg.ppb, false);
+  char* dw = static_cast<char*>(ctx->ws.p);
+  char* hp = static_cast<char*>(ctx->pin.p);
+  RefineState* hs = reinterpret_cast<RefineState*>(hp + hstate_off);
+  std::memset(hs, 0, sizeof(RefineState));
+  for (int k = 0; k < 7; ++k) hs->pose[k] = pose_in[k];
+  rotate_small(hs->pose + 3, 0.0f, 0.0f, 0.0f);  // normalised, top hemisphere
+  hs->step_t = prm->step_t;
+  hs->step_r = prm->step_rot;
+  hs->K = K;
+  hs->rng_seed = desc->seed ^ ((uint64_t)desc->stream << 32) ^ 0x5245464E45ull;
+  RefineState* dst = reinterpret_cast<RefineState*>(dw + state_off);
+  float* dcand = reinterpret_cast<float*>(dw + cand_off);
+  float* dfit = reinterpret_cast<float*>(dw + fit_off);
+  const Instance* dinst = reinterpret_cast<const Instance*>(dw + L.inst);
+  const int var = kernel_variant(d, fs[0]->cam);
+  cudaStream_t s = ctx->stream;
+  QPSO_CUDA(ctx, cudaMemcpyAsync(dw, hp, L.meta_end, cudaMemcpyHostToDevice, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(dst, hs, sizeof(RefineState), cudaMemcpyHostToDevice, s));
+  QPSO_CUDA(ctx, launch_prep(reinterpret_cast<PrepDesc*>(dw + L.prep), 1, fs[0]->cam.width, fs[0]->cam.height,
+                             s));
+  // the starting pose's fitness, straight into the state
+  QPSO_CUDA(ctx, launch_score_mlets(dinst, dst->pose, 1, &dst->fit, cfg, 1, s, var, vcap));
+  const uint32_t groups = (K + cfg.ppb - 1) / cfg.ppb;
+  const int grid = (int)std::min<uint32_t>(groups, (uint32_t)ctx->num_sms * 4);
   for (uint32_t r = 0; r < prm->rounds; ++r) {
-    for (uint32_t i = 0; i < K; ++i) {
-      float* c = &cand[(size_t)i * 7];
-      for (int k = 0; k < 7; ++k) c[k] = pose[k];
-      if (i < 6) {
-        c[i / 2] = c[i / 2] + ((i & 1) ? -step_t : step_t);
-      } else if (i < 12) {
-        float h[3] = {0.0f, 0.0f, 0.0f};
-        h[(i - 6) / 2] = ((i & 1) ? -step_r : step_r) * 0.5f;
-        rotate_small(c + 3, h[0], h[1], h[2]);
-      } else {
-        for (int k = 0; k < 3; ++k) c[k] = c[k] + uniform_pm1(rng) * step_t;
-        float h[3];
-        for (int k = 0; k < 3; ++k) h[k] = uniform_pm1(rng) * step_r * 0.5f;
-        rotate_small(c + 3, h[0], h[1], h[2]);
-      }
-    }
-    if ((st = qpso_score_poses(ctx, &d, cand.data(), K, fits.data())) != QPSO_OK) return st;
-    uint32_t j = 0;
-    for (uint32_t i = 1; i < K; ++i)
-      if (fits[i] < fits[j]) j = i;
-    if (fits[j] < fit) {
-      fit = fits[j];
-      for (int k = 0; k < 7; ++k) pose[k] = cand[(size_t)j * 7 + k];
-    } else {
-      step_t = step_t * 0.5f;
-      step_r = step_r * 0.5f;
-    }
+    QPSO_CUDA(ctx, launch_refine_gen(dst, dcand, K, s));
+    QPSO_CUDA(ctx, launch_score_mlets(dinst, dcand, K, dfit, cfg, grid, s, var, vcap));
+    QPSO_CUDA(ctx, launch_refine_pick(dst, dcand, dfit, K, s));
   }
-  for (int k = 0; k < 7; ++k) pose_out[k] = pose[k];
-  *fit_out = fit;
+  QPSO_CUDA(ctx, cudaMemcpyAsync(hs, dst, sizeof(RefineState), cudaMemcpyDeviceToHost, s));
+  QPSO_CUDA(ctx, cudaMemcpyAsync(hp + L.hdr, dw + L.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
+  QPSO_CUDA(ctx, cudaStreamSynchronize(s));
+  const Header& hd = *reinterpret_cast<const Header*>(hp + L.hdr);
+  if (hd.err & kErrBound) return fail(ctx, QPSO_ERR_INTERNAL, "raster bound violated");
+  for (int k = 0; k < 7; ++k) pose_out[k] = hs->pose[k];
+  *fit_out = hs->fit;
   return QPSO_OK;
 }
 

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 
 #include "meshlets.h"
@@ -114,6 +115,74 @@ cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_
 // Dynamic shared memory of the fused kernels; vcap: vertex cache slots per
 // warp, the largest meshlet of the launch's meshes (meshlet_cap()).
 size_t fused_smem_bytes(int threads, int ppb, int tile_px, int vcap);
+// qpso_refine's pattern search, one copy for the host and the device: every
+// float operation is +, -, *, / or sqrt in a fixed order (the device build
+// contracts nothing, the host unit is compiled without contraction), so the
+// oracle replays it bit for bit.
+//
+// splitmix64 (Steele, Lea and Flood; the public-domain generator Vigna
+// recommends for seeding).  Draw n (0-based) of a stream seeded with s is
+// splitmix64_out(s + (n + 1) * kSplitmixGamma): any draw can be reached
+// directly.
+constexpr uint64_t kSplitmixGamma = 0x9E3779B97F4A7C15ull;
+__host__ __device__ inline uint64_t splitmix64_out(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+// a uniform float in [-1, 1): 24 random bits, exact in float
+__host__ __device__ inline float uniform_pm1(uint64_t& state) {
+  state += kSplitmixGamma;
+  const float u = (float)(splitmix64_out(state) >> 40) * 5.9604644775390625e-8f;  // 2^-24
+  return u * 2.0f - 1.0f;
+}
+// q <- normalise(dq * q), dq = (1, hx, hy, hz), then the top hemisphere
+__host__ __device__ inline void rotate_small(float q[4], float hx, float hy, float hz) {
+  const float a0 = 1.0f, a1 = hx, a2 = hy, a3 = hz;
+  const float b0 = q[0], b1 = q[1], b2 = q[2], b3 = q[3];
+  float r[4];
+  r[0] = a0 * b0 - a1 * b1 - a2 * b2 - a3 * b3;
+  r[1] = a0 * b1 + a1 * b0 + a2 * b3 - a3 * b2;
+  r[2] = a0 * b2 - a1 * b3 + a2 * b0 + a3 * b1;
+  r[3] = a0 * b3 + a1 * b2 - a2 * b1 + a3 * b0;
+  const float n = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
+  const float sgn = r[0] < 0.0f ? -1.0f : 1.0f;
+  for (int k = 0; k < 4; ++k) q[k] = sgn * (r[k] / n);
+}
+// Candidate i of a round (K per round): the pose stepped by +-step_t along
+// one axis (i < 6), rotated by about +-step_r about one axis (i < 12), or
+// moved at random within the steps, from draw `draw0` of the stream on.
+__host__ __device__ inline void refine_candidate(const float pose[7], uint32_t i, float step_t, float step_r,
+                                                 uint64_t rng_seed, uint64_t draw0, float c[7]) {
+  for (int k = 0; k < 7; ++k) c[k] = pose[k];
+  if (i < 6) {
+    c[i / 2] = c[i / 2] + ((i & 1) ? -step_t : step_t);
+  } else if (i < 12) {
+    float h[3] = {0.0f, 0.0f, 0.0f};
+    h[(i - 6) / 2] = ((i & 1) ? -step_r : step_r) * 0.5f;
+    rotate_small(c + 3, h[0], h[1], h[2]);
+  } else {
+    uint64_t state = rng_seed + draw0 * kSplitmixGamma;
+    for (int k = 0; k < 3; ++k) c[k] = c[k] + uniform_pm1(state) * step_t;
+    float h[3];
+    for (int k = 0; k < 3; ++k) h[k] = uniform_pm1(state) * step_r * 0.5f;
+    rotate_small(c + 3, h[0], h[1], h[2]);
+  }
+}
+// The search's state in device memory: the current pose, its fitness, the
+// two steps, the stream's seed and the round.
+struct RefineState {
+  float pose[7];
+  float fit;
+  float step_t, step_r;
+  uint32_t round, K;
+  uint64_t rng_seed;
+};
+// one round: K candidates around the state's pose; then the first smallest
+// fitness replaces the pose when it is lower, else both steps halve
+cudaError_t launch_refine_gen(const RefineState* st, float* cand, uint32_t K, cudaStream_t s);
+cudaError_t launch_refine_pick(RefineState* st, const float* cand, const float* fits, uint32_t K, cudaStream_t s);
+
 cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_t x0, int32_t y0,
                                  int32_t w, int32_t h, int32_t* out, int32_t* box, int threads,
                                  cudaStream_t st);

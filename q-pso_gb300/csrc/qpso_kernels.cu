@@ -1944,6 +1944,60 @@ cudaError_t launch_score_mlets(const Instance* inst, const float* poses, uint32_
   return cudaGetLastError();
 }
 
+// qpso_refine on the device: one thread per candidate of the round
+__global__ void refine_gen_kernel(const RefineState* __restrict__ st, float* __restrict__ cand, uint32_t K) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K) return;
+  float pose[7];
+  for (int k = 0; k < 7; ++k) pose[k] = st->pose[k];
+  // the stream's draws in the host order: 6 per random candidate, rounds
+  // one after another
+  const uint64_t draw0 = ((uint64_t)st->round * (K - 12u) + (i >= 12u ? i - 12u : 0u)) * 6u;
+  float c[7];
+  refine_candidate(pose, i, st->step_t, st->step_r, st->rng_seed, draw0, c);
+  for (int k = 0; k < 7; ++k) cand[(size_t)i * 7 + k] = c[k];
+}
+
+// The round's first smallest fitness (the fitness is never NaN and never
+// -0, so its bits order as its values do), then the state's update.
+__global__ void __launch_bounds__(1024) refine_pick_kernel(RefineState* __restrict__ st,
+                                                           const float* __restrict__ cand,
+                                                           const float* __restrict__ fits, uint32_t K) {
+  __shared__ unsigned long long best[32];
+  unsigned long long key = ~0ull;
+  for (uint32_t i = threadIdx.x; i < K; i += blockDim.x)
+    key = min(key, ((unsigned long long)__float_as_uint(fits[i]) << 32) | i);
+  for (int o = 16; o > 0; o >>= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
+  if ((threadIdx.x & 31) == 0) best[threadIdx.x >> 5] = key;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    key = threadIdx.x < (blockDim.x >> 5) ? best[threadIdx.x] : ~0ull;
+    for (int o = 16; o > 0; o >>= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
+    if (threadIdx.x == 0) {
+      const uint32_t j = (uint32_t)(key & 0xffffffffu);
+      const float fj = fits[j];
+      if (fj < st->fit) {
+        st->fit = fj;
+        for (int k = 0; k < 7; ++k) st->pose[k] = cand[(size_t)j * 7 + k];
+      } else {
+        st->step_t = st->step_t * 0.5f;
+        st->step_r = st->step_r * 0.5f;
+      }
+      st->round += 1;
+    }
+  }
+}
+
+cudaError_t launch_refine_gen(const RefineState* st, float* cand, uint32_t K, cudaStream_t s) {
+  refine_gen_kernel<<<(K + 127) / 128, 128, 0, s>>>(st, cand, K);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine_pick(RefineState* st, const float* cand, const float* fits, uint32_t K, cudaStream_t s) {
+  refine_pick_kernel<<<1, 1024, 0, s>>>(st, cand, fits, K);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_render_window(const Instance* inst, const float* pose, int32_t x0, int32_t y0,
                                  int32_t w, int32_t h, int32_t* out, int32_t* box, int threads,
                                  cudaStream_t st) {
