@@ -356,12 +356,10 @@ __device__ __forceinline__ void init_particle(const SolveParams& prm, uint32_t p
   v[kQ3] = prm.ang_lo + span * u[11];
 }
 
-// UpdateParticlesEquationKernel, main.cu:858-1060 (draw group `iter`).
-__device__ __forceinline__ void update_particle(const SolveParams& prm, uint32_t p, uint32_t iter,
-                                                float s[7], float v[7], const float b[7],
-                                                const float g[7]) {
-  float u[12];
-  draw_group(prm.seed, prm.stream, p, iter, u);
+// UpdateParticlesEquationKernel, main.cu:858-1060, with the iteration's 12
+// uniforms already drawn (draw group `iter`).
+__device__ __forceinline__ void update_particle_drawn(const SolveParams& prm, float s[7], float v[7],
+                                                      const float b[7], const float g[7], const float u[12]) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float r1 = prm.c1 * u[2 * d];
@@ -415,6 +413,14 @@ __device__ __forceinline__ void update_particle(const SolveParams& prm, uint32_t
 #pragma unroll
   for (int d = 0; d < 7; ++d) from[d] = s[d];
   kinematics(from, s, v);
+}
+
+__device__ __forceinline__ void update_particle(const SolveParams& prm, uint32_t p, uint32_t iter,
+                                                float s[7], float v[7], const float b[7],
+                                                const float g[7]) {
+  float u[12];
+  draw_group(prm.seed, prm.stream, p, iter, u);
+  update_particle_drawn(prm, s, v, b, g, u);
 }
 
 // ------------------------------------------------------------------------

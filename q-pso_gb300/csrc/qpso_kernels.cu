@@ -1120,6 +1120,14 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
         prefetch_l1(reinterpret_cast<const char*>(I.mlets) + (size_t)(i - box_lines) * 128u);
     }
   }
+  // the iteration's uniforms depend on nothing the previous launch writes:
+  // drawn while it finishes (the empty asm keeps them before the wait)
+  float u[12];
+  if (dep_wait && tid < (int)np && iter > 0) {
+    draw_group(I.prm.seed, I.prm.stream, p0 + tid, iter, u);
+    asm volatile("" ::"f"(u[0]), "f"(u[1]), "f"(u[2]), "f"(u[3]), "f"(u[4]), "f"(u[5]), "f"(u[6]), "f"(u[7]),
+                 "f"(u[8]), "f"(u[9]), "f"(u[10]), "f"(u[11]));
+  }
   if (dep_wait) asm volatile("griddepcontrol.wait;" ::: "memory");
   if (tid < (int)np) {
     const uint32_t p = p0 + tid;
@@ -1142,7 +1150,8 @@ __device__ void process_item(const Instance& I, uint32_t chunk, uint32_t iter, u
         b[d] = __ldcg(I.pbest + p + (size_t)d * P);
         g[d] = __ldcg(I.gbest + 1 + d);
       }
-      update_particle(I.prm, p, iter, s, v, b, g);
+      if (!dep_wait) draw_group(I.prm.seed, I.prm.stream, p, iter, u);
+      update_particle_drawn(I.prm, s, v, b, g, u);
     }
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
